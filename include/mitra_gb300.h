@@ -1,0 +1,291 @@
+/* SPDX-License-Identifier: MPL-2.0
+ *
+ * mitra_gb300.h - C ABI of the GB300 symmetry hot path.
+ *
+ * The entry points replace the six stage methods of the reference's
+ * `symmetry::Backend` (include/symmetry/pipeline.h:54-69 of deoksieze/Mitra_algo)
+ * for one mesh on one GPU: curvature, select, pairing, transformations,
+ * clustering and verification.  Every view points at HOST memory, exactly as
+ * the reference documents for its backends (pipeline.h:51-53): a call uploads
+ * what it needs, runs its sm_103a kernels and returns completed host results.
+ *
+ * Conventions
+ *  - Every function returns a sym_status.  On failure the message of the error
+ *    (the same text the reference throws, e.g. "Pair budget exceeded; ...") is
+ *    kept per thread and read with sym_last_error().
+ *  - Fixed-size outputs (features) are written to caller-owned buffers.
+ *    Variable-size outputs (selection, pairs, votes, clusters, verification)
+ *    are allocated by the library and released with the matching *_release.
+ *  - SoA columns, 32-bit vertex/face/pair/vote ids and 64-bit CSR offsets
+ *    follow include/symmetry/storage.h:14-16 of the reference.
+ *  - No exceptions, no C++ or torch types cross this boundary.
+ */
+#ifndef MITRA_GB300_H
+#define MITRA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef enum sym_status {
+  SYM_OK = 0,
+  SYM_INVALID_ARGUMENT = 1, /* reference: std::invalid_argument */
+  SYM_RUNTIME_ERROR = 2,    /* reference: std::runtime_error (budgets, ...) */
+  SYM_OVERFLOW = 3,         /* reference: std::overflow_error */
+  SYM_CUDA_ERROR = 4,       /* reference: runtime_error("CUDA: <msg>") */
+  SYM_NO_DEVICE = 5,        /* reference: "CUDA: no available device" */
+  SYM_DEVICE_TIMEOUT = 6    /* a bounded device-side wait gave up */
+} sym_status;
+
+/* Message of the last failing call made on the calling thread. */
+const char *sym_last_error(void);
+
+/* ------------------------------------------------------------ input views */
+typedef struct sym_points_view {
+  const double *x, *y, *z;
+  uint64_t count;
+} sym_points_view;
+
+typedef struct sym_faces_view { /* three index columns, reference Faces */
+  const int32_t *v0, *v1, *v2;
+  uint64_t count;
+} sym_faces_view;
+
+typedef struct sym_mesh_view { /* reference MeshView, storage.h:135-138 */
+  sym_points_view vertices;
+  sym_faces_view faces;
+} sym_mesh_view;
+
+typedef struct sym_csr_view { /* reference CsrView, storage.h:143-151 */
+  const uint64_t *offsets;
+  uint64_t rows; /* offsets has rows + 1 entries */
+  const int32_t *indices;
+} sym_csr_view;
+
+typedef struct sym_edge { /* reference Edge, pipeline.h:11-13 */
+  int32_t lo, hi, a, b, face0, face1;
+} sym_edge;
+
+typedef struct sym_topology_view { /* reference TopologyView, pipeline.h:14-20 */
+  sym_points_view normals, face_normals;
+  const double *weights;
+  uint64_t weight_count;
+  sym_csr_view neighbors, incident_faces;
+  const sym_edge *edges;
+  uint64_t edge_count;
+} sym_topology_view;
+
+typedef struct sym_features_view { /* reference FeaturesView, storage.h:196-205 */
+  sym_points_view normal, dmin, dmax;
+  const double *kmin, *kmax;
+  const uint8_t *valid;
+  uint64_t count;
+} sym_features_view;
+
+typedef struct sym_features_out { /* caller-owned, `count` rows each */
+  double *normal_x, *normal_y, *normal_z;
+  double *dmin_x, *dmin_y, *dmin_z;
+  double *dmax_x, *dmax_y, *dmax_z;
+  double *kmin, *kmax;
+  uint8_t *valid;
+  uint64_t count;
+} sym_features_out;
+
+typedef struct sym_pairs_view { /* reference PairsView, storage.h:231-235 */
+  const int32_t *a, *b;
+  uint64_t count;
+} sym_pairs_view;
+
+/* Vote kinds follow reference TransformKind (storage.h:296). */
+enum { SYM_RIGID = 0, SYM_REFLECTION = 1 };
+
+typedef struct sym_votes_view { /* reference VotesView, storage.h:305-330 */
+  const int32_t *pair;
+  const uint8_t *kind;
+  const double *rotation[9]; /* row-major 3x3 */
+  const double *translation[3];
+  const double *plane_normal[3];
+  const double *plane_offset;
+  const double *descriptor[12]; /* 4 used for reflections, 12 for rigid */
+  uint64_t count;
+} sym_votes_view;
+
+/* Same memory layout as the reference ClusterRecord (storage.h:365-370). */
+typedef struct sym_cluster_record {
+  uint8_t reflection;
+  double rotation[9];
+  double translation[3];
+  double plane_normal[3];
+  double plane_offset;
+} sym_cluster_record;
+
+typedef struct sym_clusters_view { /* reference ClustersView, storage.h:383-387 */
+  const sym_cluster_record *records;
+  uint64_t count;
+  const uint64_t *vote_offsets; /* count + 1 */
+  const int32_t *vote_indices;
+} sym_clusters_view;
+
+typedef struct sym_model_context { /* reference ModelContext, pipeline.h:30-33 */
+  double box_size;
+  double center[3];
+} sym_model_context;
+
+typedef struct sym_options { /* reference Options, options.h:5-12 */
+  double sample_ratio, prune, pair_threshold, bandwidth, verify_threshold;
+  int32_t smoothing, subdivide, max_iterations, max_clusters;
+  uint64_t seed, max_pairs, max_votes;
+  int32_t patching;
+} sym_options;
+
+/* The reference's defaults (options.h:6-11). */
+void sym_options_default(sym_options *out);
+
+/* std::mt19937_64 state: 312 words and the position, in the order libstdc++
+ * streams the engine (operator<< / operator>>).  The reference threads one
+ * engine through select() and clustering() (pipeline.h:60-66). */
+typedef struct sym_rng {
+  uint64_t words[312];
+  uint64_t index;
+} sym_rng;
+void sym_rng_seed(sym_rng *rng, uint64_t seed);
+uint64_t sym_rng_next(sym_rng *rng);
+
+/* ---------------------------------------------------- library-owned outputs */
+typedef struct sym_selection { /* reference Selection, pipeline.h:45-47 */
+  int32_t *sample;
+  uint64_t sample_count;
+  int32_t *pruned;
+  uint64_t pruned_count;
+  void *storage;
+} sym_selection;
+void sym_selection_release(sym_selection *s);
+
+typedef struct sym_pairs { /* reference Pairs, storage.h:236-250 */
+  int32_t *a, *b;
+  uint64_t count;
+  void *storage;
+} sym_pairs;
+void sym_pairs_release(sym_pairs *p);
+
+typedef struct sym_votes { /* reference Votes, storage.h:331-364 */
+  int32_t *pair;
+  uint8_t *kind;
+  double *rotation[9];
+  double *translation[3];
+  double *plane_normal[3];
+  double *plane_offset;
+  double *descriptor[12];
+  uint64_t count;
+  void *storage;
+} sym_votes;
+void sym_votes_release(sym_votes *v);
+
+typedef struct sym_clusters { /* reference ClusterOutput, pipeline.h:48-51 */
+  sym_cluster_record *records;
+  uint64_t count;
+  uint64_t *vote_offsets; /* count + 1 */
+  int32_t *vote_indices;
+  int32_t limited_iterations;
+  void *storage;
+} sym_clusters;
+void sym_clusters_release(sym_clusters *c);
+
+typedef struct sym_grouped_csr { /* reference GroupedCsr, storage.h:171-183 */
+  uint64_t *groups;      /* cluster_count + 1 row ranges */
+  uint64_t *offsets;     /* rows + 1 */
+  int32_t *indices;
+  uint64_t rows;
+} sym_grouped_csr;
+
+typedef struct sym_verification_result { /* reference Verification, storage.h:371-382 */
+  uint64_t cluster_count;
+  uint64_t *side_a_offsets, *side_b_offsets; /* cluster_count + 1 */
+  int32_t *side_a, *side_b;
+  sym_grouped_csr patches_a, patches_b;
+  double *coverage, *rms;
+  void *storage;
+} sym_verification_result;
+void sym_verification_release(sym_verification_result *v);
+
+/* ------------------------------------------------------------------ context */
+/* One context = one device, one stream, one growable device workspace and
+ * pinned staging buffers reused across calls.  A context is used by one
+ * thread at a time (the reference Backend methods are const but its CUDA
+ * backend keeps thread-local metrics: profile.cpp:23-24). */
+typedef struct sym_context sym_context;
+sym_status sym_context_create(int device, sym_context **out);
+void sym_context_destroy(sym_context *ctx);
+/* Name reported by Backend::name() for this backend. */
+const char *sym_backend_name(void);
+
+/* ---------------------------------------------------------- stage methods */
+/* Backend::curvature (pipeline.h:58; CPU reference src/cpu/curvature.cpp:14-79) */
+sym_status sym_curvature(sym_context *ctx, const sym_mesh_view *mesh,
+                         const sym_topology_view *topology,
+                         const sym_options *options,
+                         const sym_features_out *out);
+
+/* Backend::select (pipeline.h:59-60; src/cpu/selection.cpp:15-29).  Area-
+ * weighted sampling runs on the host with `rng` (src/core/sampling.cpp:5-24),
+ * the anisotropy prune and its stable compaction run on the GPU. */
+sym_status sym_select(sym_context *ctx, const sym_mesh_view *mesh,
+                      const sym_features_view *features, const double *weights,
+                      uint64_t weight_count, const sym_options *options,
+                      sym_rng *rng, sym_selection *out);
+
+/* Backend::pairing (pipeline.h:61-62; src/cpu/pairing.cpp:14-35) */
+sym_status sym_pairing(sym_context *ctx, const sym_mesh_view *mesh,
+                       const sym_features_view *features,
+                       const int32_t *selected, uint64_t selected_count,
+                       const sym_model_context *model,
+                       const sym_options *options, sym_pairs *out);
+
+/* Backend::transformations (pipeline.h:63-64; src/cpu/transformations.cpp:17-73) */
+sym_status sym_transformations(sym_context *ctx, const sym_mesh_view *mesh,
+                               const sym_features_view *features,
+                               const sym_pairs_view *pairs,
+                               const sym_model_context *model,
+                               const sym_options *options, sym_votes *out);
+
+/* Backend::clustering (pipeline.h:65-66; src/cpu/clustering.cpp:32-208) */
+sym_status sym_clustering(sym_context *ctx, const sym_votes_view *votes,
+                          const sym_model_context *model,
+                          const sym_options *options, sym_rng *rng,
+                          sym_clusters *out);
+
+/* Backend::verification (pipeline.h:67-68; src/cpu/verification.cpp:50-110) */
+sym_status sym_verification(sym_context *ctx, const sym_mesh_view *mesh,
+                            const sym_topology_view *topology,
+                            const sym_clusters_view *clusters,
+                            const sym_model_context *model,
+                            const sym_options *options,
+                            sym_verification_result *out);
+
+/* Test hook for the device point-triangle distance, like the reference's
+ * cuda_detail::triangle_distances (src/cuda/verification.cu:266-281).
+ * `queries` holds 12 doubles per query: p, a, b, c. */
+sym_status sym_triangle_distances(sym_context *ctx, const double *queries,
+                                  uint64_t count, double *out);
+
+/* --------------------------------------------------------------- metrics */
+/* Per-stage accounting, the fields of the reference CudaMetric
+ * (include/symmetry/cuda.h:7-13, src/cuda/profile.cpp). */
+typedef struct sym_metric {
+  char stage[32];
+  uint64_t h2d_bytes, d2h_bytes, peak_buffer_bytes, custom_launches;
+  double gpu_interval_ms, h2d_ms, d2h_ms, custom_kernel_ms;
+  int32_t all_buffers_released;
+} sym_metric;
+sym_status sym_set_profiling(sym_context *ctx, int enabled);
+/* Moves up to `capacity` collected metrics into `out`; returns how many. */
+uint64_t sym_take_metrics(sym_context *ctx, sym_metric *out, uint64_t capacity);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MITRA_GB300_H */

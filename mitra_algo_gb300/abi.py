@@ -1,0 +1,204 @@
+"""ctypes mirror of include/mitra_gb300.h and the loader of the CUDA library.
+
+The library is built in-tree (``mitra_algo_gb300/_lib/libmitra_gb300.so``) by
+``mitra_algo_gb300.build``.  Loading fails loudly when it is missing: there is
+no CPU fallback behind these entry points.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+LIB_DIR = Path(__file__).resolve().parent / "_lib"
+LIB_PATH = LIB_DIR / "libmitra_gb300.so"
+
+# sym_status
+OK, INVALID_ARGUMENT, RUNTIME_ERROR, OVERFLOW, CUDA_ERROR, NO_DEVICE, DEVICE_TIMEOUT = range(7)
+RIGID, REFLECTION = 0, 1
+
+_d = C.POINTER(C.c_double)
+_i = C.POINTER(C.c_int32)
+_u8 = C.POINTER(C.c_uint8)
+_u64 = C.POINTER(C.c_uint64)
+
+
+class PointsView(C.Structure):
+    _fields_ = [("x", _d), ("y", _d), ("z", _d), ("count", C.c_uint64)]
+
+
+class FacesView(C.Structure):
+    _fields_ = [("v0", _i), ("v1", _i), ("v2", _i), ("count", C.c_uint64)]
+
+
+class MeshView(C.Structure):
+    _fields_ = [("vertices", PointsView), ("faces", FacesView)]
+
+
+class CsrView(C.Structure):
+    _fields_ = [("offsets", _u64), ("rows", C.c_uint64), ("indices", _i)]
+
+
+class Edge(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("lo", "hi", "a", "b", "face0", "face1")]
+
+
+class TopologyView(C.Structure):
+    _fields_ = [("normals", PointsView), ("face_normals", PointsView),
+                ("weights", _d), ("weight_count", C.c_uint64),
+                ("neighbors", CsrView), ("incident_faces", CsrView),
+                ("edges", C.POINTER(Edge)), ("edge_count", C.c_uint64)]
+
+
+class FeaturesView(C.Structure):
+    _fields_ = [("normal", PointsView), ("dmin", PointsView), ("dmax", PointsView),
+                ("kmin", _d), ("kmax", _d), ("valid", _u8), ("count", C.c_uint64)]
+
+
+class FeaturesOut(C.Structure):
+    _fields_ = [(n, _d) for n in ("normal_x", "normal_y", "normal_z", "dmin_x", "dmin_y",
+                                  "dmin_z", "dmax_x", "dmax_y", "dmax_z", "kmin", "kmax")] + \
+               [("valid", _u8), ("count", C.c_uint64)]
+
+
+class PairsView(C.Structure):
+    _fields_ = [("a", _i), ("b", _i), ("count", C.c_uint64)]
+
+
+class VotesView(C.Structure):
+    _fields_ = [("pair", _i), ("kind", _u8), ("rotation", _d * 9), ("translation", _d * 3),
+                ("plane_normal", _d * 3), ("plane_offset", _d), ("descriptor", _d * 12),
+                ("count", C.c_uint64)]
+
+
+class ClusterRecord(C.Structure):
+    _fields_ = [("reflection", C.c_uint8), ("rotation", C.c_double * 9),
+                ("translation", C.c_double * 3), ("plane_normal", C.c_double * 3),
+                ("plane_offset", C.c_double)]
+
+
+class ClustersView(C.Structure):
+    _fields_ = [("records", C.POINTER(ClusterRecord)), ("count", C.c_uint64),
+                ("vote_offsets", _u64), ("vote_indices", _i)]
+
+
+class ModelContext(C.Structure):
+    _fields_ = [("box_size", C.c_double), ("center", C.c_double * 3)]
+
+
+class Options(C.Structure):
+    _fields_ = [("sample_ratio", C.c_double), ("prune", C.c_double),
+                ("pair_threshold", C.c_double), ("bandwidth", C.c_double),
+                ("verify_threshold", C.c_double), ("smoothing", C.c_int32),
+                ("subdivide", C.c_int32), ("max_iterations", C.c_int32),
+                ("max_clusters", C.c_int32), ("seed", C.c_uint64),
+                ("max_pairs", C.c_uint64), ("max_votes", C.c_uint64),
+                ("patching", C.c_int32)]
+
+
+class Rng(C.Structure):
+    _fields_ = [("words", C.c_uint64 * 312), ("index", C.c_uint64)]
+
+
+class Selection(C.Structure):
+    _fields_ = [("sample", _i), ("sample_count", C.c_uint64), ("pruned", _i),
+                ("pruned_count", C.c_uint64), ("storage", C.c_void_p)]
+
+
+class PairsOut(C.Structure):
+    _fields_ = [("a", _i), ("b", _i), ("count", C.c_uint64), ("storage", C.c_void_p)]
+
+
+class VotesOut(C.Structure):
+    _fields_ = [("pair", _i), ("kind", _u8), ("rotation", _d * 9), ("translation", _d * 3),
+                ("plane_normal", _d * 3), ("plane_offset", _d), ("descriptor", _d * 12),
+                ("count", C.c_uint64), ("storage", C.c_void_p)]
+
+
+class ClustersOut(C.Structure):
+    _fields_ = [("records", C.POINTER(ClusterRecord)), ("count", C.c_uint64),
+                ("vote_offsets", _u64), ("vote_indices", _i),
+                ("limited_iterations", C.c_int32), ("storage", C.c_void_p)]
+
+
+class GroupedCsr(C.Structure):
+    _fields_ = [("groups", _u64), ("offsets", _u64), ("indices", _i), ("rows", C.c_uint64)]
+
+
+class VerificationOut(C.Structure):
+    _fields_ = [("cluster_count", C.c_uint64), ("side_a_offsets", _u64),
+                ("side_b_offsets", _u64), ("side_a", _i), ("side_b", _i),
+                ("patches_a", GroupedCsr), ("patches_b", GroupedCsr),
+                ("coverage", _d), ("rms", _d), ("storage", C.c_void_p)]
+
+
+class Metric(C.Structure):
+    _fields_ = [("stage", C.c_char * 32), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("peak_buffer_bytes", C.c_uint64), ("custom_launches", C.c_uint64),
+                ("gpu_interval_ms", C.c_double), ("h2d_ms", C.c_double), ("d2h_ms", C.c_double),
+                ("custom_kernel_ms", C.c_double), ("all_buffers_released", C.c_int32)]
+
+
+P = C.POINTER
+# (name, restype, argtypes) of every entry point declared in include/mitra_gb300.h.
+PROTOTYPES = [
+    ("sym_last_error", C.c_char_p, []),
+    ("sym_options_default", None, [P(Options)]),
+    ("sym_rng_seed", None, [P(Rng), C.c_uint64]),
+    ("sym_rng_next", C.c_uint64, [P(Rng)]),
+    ("sym_selection_release", None, [P(Selection)]),
+    ("sym_pairs_release", None, [P(PairsOut)]),
+    ("sym_votes_release", None, [P(VotesOut)]),
+    ("sym_clusters_release", None, [P(ClustersOut)]),
+    ("sym_verification_release", None, [P(VerificationOut)]),
+    ("sym_context_create", C.c_int, [C.c_int, P(C.c_void_p)]),
+    ("sym_context_destroy", None, [C.c_void_p]),
+    ("sym_backend_name", C.c_char_p, []),
+    ("sym_curvature", C.c_int, [C.c_void_p, P(MeshView), P(TopologyView), P(Options), P(FeaturesOut)]),
+    ("sym_select", C.c_int, [C.c_void_p, P(MeshView), P(FeaturesView), _d, C.c_uint64,
+                             P(Options), P(Rng), P(Selection)]),
+    ("sym_pairing", C.c_int, [C.c_void_p, P(MeshView), P(FeaturesView), _i, C.c_uint64,
+                              P(ModelContext), P(Options), P(PairsOut)]),
+    ("sym_transformations", C.c_int, [C.c_void_p, P(MeshView), P(FeaturesView), P(PairsView),
+                                      P(ModelContext), P(Options), P(VotesOut)]),
+    ("sym_clustering", C.c_int, [C.c_void_p, P(VotesView), P(ModelContext), P(Options),
+                                 P(Rng), P(ClustersOut)]),
+    ("sym_verification", C.c_int, [C.c_void_p, P(MeshView), P(TopologyView), P(ClustersView),
+                                   P(ModelContext), P(Options), P(VerificationOut)]),
+    ("sym_triangle_distances", C.c_int, [C.c_void_p, _d, C.c_uint64, _d]),
+    ("sym_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
+    ("sym_take_metrics", C.c_uint64, [C.c_void_p, P(Metric), C.c_uint64]),
+]
+
+_LIB = None
+
+
+def declared_symbols():
+    """Names of the functions include/mitra_gb300.h declares."""
+    import re
+    header = Path(__file__).resolve().parents[1] / "include" / "mitra_gb300.h"
+    text = header.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sym_[a-z0-9_]+)\s*\(", text)))
+
+
+def bind(lib, prototypes=PROTOTYPES, prefix="sym_", rename=None):
+    for name, res, args in prototypes:
+        target = name if rename is None else rename(name)
+        fn = getattr(lib, target)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+def library():
+    """The CUDA library, loaded once.  Raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        path = Path(os.environ.get("MITRA_GB300_LIB", LIB_PATH))
+        if not path.exists():
+            raise RuntimeError(
+                f"{path} is missing: build the CUDA library first "
+                "(python -c 'import __graft_entry__ as g; g.build()')")
+        _LIB = bind(C.CDLL(str(path)))
+    return _LIB
