@@ -1,0 +1,204 @@
+"""Python mirror of the reference's ``Backend`` over the GB300 C ABI.
+
+``Gb300Backend`` has the six stage methods of the reference's
+``symmetry::Backend`` (deoksieze/Mitra_algo include/symmetry/pipeline.h:54-69)
+with the same argument meaning, host-owned results and error behaviour:
+``ValueError`` for the reference's ``std::invalid_argument``,
+``OverflowError`` for ``std::overflow_error`` and ``RuntimeError`` (message
+text included, e.g. "Pair budget exceeded; ...") for ``std::runtime_error``.
+Every method runs the hand-written sm_103a kernels of
+``_lib/libmitra_gb300.so``; there is no CPU fallback.  ``detect`` strings the
+stages together like the reference's ``detect()`` (src/core/pipeline.cpp).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .mesh import Prepared, prepare
+from .types import (ClusterOutput, Features, Mesh, ModelContext, Options, Pairs, Rng, Selection,
+                    Topology, Verification, Votes, clusters_from_c, pairs_from_c,
+                    selection_from_c, verification_from_c, votes_from_c)
+
+
+class DeviceTimeout(RuntimeError):
+    """A bounded device-side loop gave up (the kernel returned an error
+    status instead of spinning)."""
+
+
+def _raise(status: int):
+    msg = abi.library().sym_last_error().decode()
+    if status == abi.INVALID_ARGUMENT:
+        raise ValueError(msg)
+    if status == abi.OVERFLOW:
+        raise OverflowError(msg)
+    if status == abi.DEVICE_TIMEOUT:
+        raise DeviceTimeout(msg)
+    raise RuntimeError(msg)
+
+
+def _check(status: int):
+    if status != abi.OK:
+        _raise(status)
+
+
+class Gb300Backend:
+    """The GB300 backend: one device, one stream, one reusable workspace."""
+
+    def __init__(self, device: int = 0, profile: bool = False):
+        self._lib = abi.library()
+        ctx = C.c_void_p()
+        _check(self._lib.sym_context_create(device, C.byref(ctx)))
+        self._ctx = ctx
+        if profile:
+            _check(self._lib.sym_set_profiling(ctx, 1))
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._lib.sym_context_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def name(self) -> str:
+        return self._lib.sym_backend_name().decode()
+
+    # ----------------------------------------------------------- stages
+    def curvature(self, mesh: Mesh, topology: Topology, options: Options) -> Features:
+        f = Features.zeros(mesh.vertex_count)
+        _check(self._lib.sym_curvature(self._ctx, C.byref(mesh.view()), C.byref(topology.view()),
+                                       C.byref(options.to_c()), C.byref(f.out_view())))
+        return f
+
+    def select(self, mesh: Mesh, features: Features, weights, options: Options,
+               rng: Rng) -> Selection:
+        w = np.ascontiguousarray(weights, np.float64)
+        out = abi.Selection()
+        _check(self._lib.sym_select(self._ctx, C.byref(mesh.view()), C.byref(features.view()),
+                                    w.ctypes.data_as(C.POINTER(C.c_double)), w.size,
+                                    C.byref(options.to_c()), C.byref(rng.state), C.byref(out)))
+        try:
+            return selection_from_c(out)
+        finally:
+            self._lib.sym_selection_release(C.byref(out))
+
+    def pairing(self, mesh: Mesh, features: Features, selected, context: ModelContext,
+                options: Options) -> Pairs:
+        sel = np.ascontiguousarray(selected, np.int32)
+        out = abi.PairsOut()
+        _check(self._lib.sym_pairing(self._ctx, C.byref(mesh.view()), C.byref(features.view()),
+                                     sel.ctypes.data_as(C.POINTER(C.c_int32)), sel.size,
+                                     C.byref(context.to_c()), C.byref(options.to_c()),
+                                     C.byref(out)))
+        try:
+            return pairs_from_c(out)
+        finally:
+            self._lib.sym_pairs_release(C.byref(out))
+
+    def transformations(self, mesh: Mesh, features: Features, pairs: Pairs,
+                        context: ModelContext, options: Options) -> Votes:
+        out = abi.VotesOut()
+        _check(self._lib.sym_transformations(self._ctx, C.byref(mesh.view()),
+                                             C.byref(features.view()), C.byref(pairs.view()),
+                                             C.byref(context.to_c()), C.byref(options.to_c()),
+                                             C.byref(out)))
+        try:
+            return votes_from_c(out)
+        finally:
+            self._lib.sym_votes_release(C.byref(out))
+
+    def clustering(self, votes: Votes, context: ModelContext, options: Options,
+                   rng: Rng) -> ClusterOutput:
+        out = abi.ClustersOut()
+        _check(self._lib.sym_clustering(self._ctx, C.byref(votes.view()), C.byref(context.to_c()),
+                                        C.byref(options.to_c()), C.byref(rng.state),
+                                        C.byref(out)))
+        try:
+            return clusters_from_c(out)
+        finally:
+            self._lib.sym_clusters_release(C.byref(out))
+
+    def verification(self, mesh: Mesh, topology: Topology, clusters: ClusterOutput,
+                     context: ModelContext, options: Options) -> Verification:
+        view, keep = clusters.view()
+        out = abi.VerificationOut()
+        _check(self._lib.sym_verification(self._ctx, C.byref(mesh.view()),
+                                          C.byref(topology.view()), C.byref(view),
+                                          C.byref(context.to_c()), C.byref(options.to_c()),
+                                          C.byref(out)))
+        del keep
+        try:
+            return verification_from_c(out)
+        finally:
+            self._lib.sym_verification_release(C.byref(out))
+
+    def triangle_distances(self, queries) -> np.ndarray:
+        q = np.ascontiguousarray(queries, np.float64).reshape(-1)
+        n = q.size // 12
+        out = np.zeros(n)
+        _check(self._lib.sym_triangle_distances(self._ctx, q.ctypes.data_as(C.POINTER(C.c_double)),
+                                                n, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def take_metrics(self):
+        buf = (abi.Metric * 64)()
+        n = self._lib.sym_take_metrics(self._ctx, buf, 64)
+        return [{f: (getattr(buf[i], f).decode() if f == "stage" else getattr(buf[i], f))
+                 for f, _ in abi.Metric._fields_} for i in range(n)]
+
+
+@dataclass
+class Result:
+    """Reference ``Result`` (pipeline.h:72-81)."""
+    prepared: Prepared
+    options: Options
+    features: Features = None
+    sample: np.ndarray = None
+    pruned: np.ndarray = None
+    pairs: Pairs = None
+    votes: Votes = None
+    clusters: ClusterOutput = None
+    verification: Verification = None
+    timings: list = field(default_factory=list)
+
+
+def detect(mesh: Mesh, options: Options, backend, progress=None) -> Result:
+    """Reference ``detect`` (src/core/pipeline.cpp:5-52): prepare, then the six
+    stages in order with one RNG threaded through select and clustering."""
+    clock = time.perf_counter()
+    p = prepare(mesh, options)
+    r = Result(p, options)
+
+    def timed(stage):
+        nonlocal clock
+        now = time.perf_counter()
+        r.timings.append((stage, (now - clock) * 1e3))
+        if progress:
+            progress(stage, r.timings[-1][1])
+        clock = now
+
+    rng = Rng(options.seed, getattr(backend, "_lib", None))
+    timed("prepare")
+    r.features = backend.curvature(p.mesh, p.topology, options)
+    timed("curvature")
+    s = backend.select(p.mesh, r.features, p.topology.weights, options, rng)
+    r.sample, r.pruned = s.sample, s.pruned
+    timed("sample_prune")
+    r.pairs = backend.pairing(p.mesh, r.features, r.pruned, p.context, options)
+    timed("pairing")
+    r.votes = backend.transformations(p.mesh, r.features, r.pairs, p.context, options)
+    timed("transformation")
+    r.clusters = backend.clustering(r.votes, p.context, options, rng)
+    timed("mean_shift")
+    if options.patching:
+        r.verification = backend.verification(p.mesh, p.topology, r.clusters, p.context, options)
+    timed("verification")
+    return r

@@ -1,0 +1,421 @@
+// SPDX-License-Identifier: MPL-2.0
+// Stage (c): mean-shift clustering in transformation space, reference
+// semantics (Epanechnikov weights, 4-D reflection / 12-D rigid descriptors,
+// random seeding until every vote is visited).
+//
+// Reference: src/cpu/clustering.cpp:32-208 (driver + evaluator),
+// src/cuda/clustering.cu (the existing GPU path: one block per trajectory,
+// launched thousands of times from the host driver).
+//
+// GB300 design.  A trajectory is a pure function of its seed vote (the
+// reference evaluator only reads the seed descriptor and the vote set), so:
+//   1. one launch runs the trajectory of EVERY vote as a seed, a warp per
+//      seed, and records its final mean, its converged/exhausted flags and
+//      its support as a bitmask over same-kind votes;
+//   2. the host replays the reference driver verbatim (RNG draw per seed,
+//      visited set, merge test, budgets) on those results - no device round
+//      trip per trajectory;
+//   3. one launch re-runs only the trajectories the driver used and adds
+//      each member's per-iteration hit into its cluster's support counts;
+//      one launch picks each vote's winning cluster (largest count, first
+//      cluster on ties).
+// Distances and weights are the reference's FP64 expressions in its order
+// (no FMA contraction), so membership decisions match; the weighted sums use
+// a fixed warp-butterfly order (deterministic, within an ulp-level of the
+// reference's serial sum).
+#include "common.cuh"
+#include "primitives.cuh"
+#include "rng.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace sym {
+namespace {
+
+constexpr double kExhausted = 1e-14;  // clustering.cpp:15,169
+
+__global__ void split_kinds(const uint8_t *kind, uint64_t q, uint8_t *is_refl, uint8_t *is_rigid) {
+  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= q) return;
+  is_refl[i] = kind[i] == SYM_REFLECTION;
+  is_rigid[i] = kind[i] != SYM_REFLECTION;
+}
+
+// AoS descriptors of one kind: out[j*D + k] = lanes[k][ids[j]].
+template <int D>
+__global__ void gather_desc(const double *lanes, uint64_t q, const int32_t *ids, uint64_t n,
+                            double *out) {
+  uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int32_t v = ids[j];
+  for (int k = 0; k < D; ++k) out[j * D + k] = lanes[uint64_t(k) * q + v];
+}
+
+template <int D>
+struct Traj {
+  double mean[D];
+  bool converged, exhausted;
+};
+
+// One trajectory per warp.  RECORD: write the support bitmask row; else add
+// every member hit to counts[cluster * n + j].
+template <int D, bool RECORD>
+__global__ void __launch_bounds__(128) trajectories(const double *desc, uint64_t n,
+                                                    const int32_t *seeds, const int32_t *cluster,
+                                                    uint64_t nseeds, double h2, int max_iter,
+                                                    double *final_mean, uint8_t *flags,
+                                                    uint32_t *support, uint64_t words,
+                                                    uint32_t *counts) {
+  uint64_t si = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (si >= nseeds) return;
+  int32_t s = seeds[si];
+  uint64_t crow = RECORD ? 0 : uint64_t(cluster[si]) * n;
+  double mean[D];
+  for (int k = 0; k < D; ++k) mean[k] = desc[uint64_t(s) * D + k];
+  bool converged = false, exhausted = false;
+  const double stop = 1e-6 * h2;
+  for (int it = 0; it < max_iter; ++it) {
+    double wt = 0, ws[D];
+    for (int k = 0; k < D; ++k) ws[k] = 0;
+    for (uint64_t base = 0; base < n; base += 32) {
+      uint64_t j = base + lane;
+      bool in = false;
+      if (j < n) {
+        double x[D], dist = 0;
+        for (int k = 0; k < D; ++k) {
+          x[k] = desc[j * D + k];
+          double d = mean[k] - x[k];
+          dist += d * d;
+        }
+        if (dist < h2) {
+          in = true;
+          double w = 1 - dist / h2;
+          wt += w;
+          for (int k = 0; k < D; ++k) ws[k] += w * x[k];
+        }
+      }
+      if (RECORD) {
+        unsigned bits = __ballot_sync(0xffffffffu, in);
+        if (lane == 0 && bits) support[si * words + base / 32] |= bits;
+      } else if (in) {
+        atomicAdd(&counts[crow + j], 1u);
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      wt += __shfl_xor_sync(0xffffffffu, wt, o);
+      for (int k = 0; k < D; ++k) ws[k] += __shfl_xor_sync(0xffffffffu, ws[k], o);
+    }
+    if (wt <= kExhausted) {
+      exhausted = true;
+      break;
+    }
+    double movement = 0;
+    for (int k = 0; k < D; ++k) {
+      double next = ws[k] / wt;
+      double d = mean[k] - next;
+      movement += d * d;
+      mean[k] = next;
+    }
+    if (movement < stop) {
+      converged = true;
+      break;
+    }
+  }
+  if (RECORD && lane == 0) {
+    for (int k = 0; k < D; ++k) final_mean[si * D + k] = mean[k];
+    flags[si] = uint8_t((converged ? 1 : 0) | (exhausted ? 2 : 0));
+  }
+}
+
+// Winner per vote: the cluster (in creation order) with the largest count,
+// the first one on ties; -1 if no cluster counted the vote.
+__global__ void winners(const uint32_t *counts, uint64_t nclusters, uint64_t n,
+                        const int32_t *cluster_id, int32_t *winner) {
+  uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  uint32_t best = 0;
+  int32_t w = -1;
+  for (uint64_t c = 0; c < nclusters; ++c) {
+    uint32_t v = counts[c * n + j];
+    if (v > best) best = v, w = cluster_id[c];
+  }
+  winner[j] = w;
+}
+
+struct KindData {
+  int dim = 0;
+  uint64_t n = 0, words = 0;
+  std::vector<int32_t> ids;          // global vote id of each local index
+  double *desc = nullptr;            // device AoS
+  std::vector<double> mean;          // n x dim final means
+  std::vector<uint8_t> flags;        // bit0 converged, bit1 exhausted
+  std::vector<uint32_t> support;     // n x words
+};
+
+template <int D>
+void run_all_seeds(Call &call, KindData &k, double h2, int max_iter) {
+  if (!k.n) return;
+  cudaStream_t st = call.stream();
+  k.words = (k.n + 31) / 32;
+  int32_t *seeds = call.alloc<int32_t>(k.n);
+  std::vector<int32_t> iota(k.n);
+  for (uint64_t i = 0; i < k.n; ++i) iota[i] = int32_t(i);
+  call.h2d(seeds, iota.data(), k.n * 4);
+  double *mean = call.alloc<double>(k.n * D);
+  uint8_t *flags = call.alloc<uint8_t>(k.n);
+  uint32_t *support = call.alloc<uint32_t>(k.n * k.words);
+  SYM_CUDA(cudaMemsetAsync(support, 0, k.n * k.words * 4, st));
+  unsigned blocks = unsigned((k.n * 32 + 127) / 128);
+  trajectories<D, true><<<blocks, 128, 0, st>>>(k.desc, k.n, seeds, nullptr, k.n, h2, max_iter,
+                                                mean, flags, support, k.words, nullptr);
+  check_launch();
+  call.launched();
+  k.mean.resize(k.n * D);
+  k.flags.resize(k.n);
+  k.support.resize(k.n * k.words);
+  call.d2h(k.mean.data(), mean, k.n * D * 8);
+  call.d2h(k.flags.data(), flags, k.n);
+  call.d2h(k.support.data(), support, k.n * k.words * 4);
+}
+
+struct Center {
+  double v[12];
+  int kind;                    // index into kinds[]
+  std::vector<uint32_t> keys;  // union of supports, kind-local bitmask
+  uint64_t key_count = 0;
+  std::vector<int32_t> seeds;  // kind-local seeds merged into this cluster
+};
+
+uint64_t popcount_row(const uint32_t *row, uint64_t words) {
+  uint64_t c = 0;
+  for (uint64_t w = 0; w < words; ++w) c += __builtin_popcount(row[w]);
+  return c;
+}
+
+template <int D>
+void count_members(Call &call, KindData &k, const std::vector<Center> &centers, int kind_index,
+                   double h2, int max_iter, std::vector<int32_t> &winner_global) {
+  std::vector<int32_t> seeds, cluster, cluster_ids;
+  for (size_t c = 0; c < centers.size(); ++c) {
+    if (centers[c].kind != kind_index) continue;
+    int32_t local = int32_t(cluster_ids.size());
+    cluster_ids.push_back(int32_t(c));
+    for (int32_t s : centers[c].seeds) seeds.push_back(s), cluster.push_back(local);
+  }
+  if (seeds.empty()) return;
+  uint64_t nc = cluster_ids.size();
+  cudaStream_t st = call.stream();
+  uint64_t cells = nc * k.n;
+  uint32_t *counts = call.alloc<uint32_t>(cells);
+  SYM_CUDA(cudaMemsetAsync(counts, 0, cells * 4, st));
+  int32_t *dseeds = call.upload(seeds.data(), seeds.size());
+  int32_t *dcluster = call.upload(cluster.data(), cluster.size());
+  int32_t *dids = call.upload(cluster_ids.data(), nc);
+  unsigned blocks = unsigned((seeds.size() * 32 + 127) / 128);
+  trajectories<D, false><<<blocks, 128, 0, st>>>(k.desc, k.n, dseeds, dcluster, seeds.size(), h2,
+                                                 max_iter, nullptr, nullptr, nullptr, 0, counts);
+  check_launch();
+  int32_t *win = call.alloc<int32_t>(k.n);
+  winners<<<blocks_for(k.n), kThreads, 0, st>>>(counts, nc, k.n, dids, win);
+  check_launch();
+  call.launched(2);
+  std::vector<int32_t> local(k.n);
+  call.d2h(local.data(), win, k.n * 4);
+  call.sync();
+  for (uint64_t j = 0; j < k.n; ++j) winner_global[k.ids[j]] = local[j];
+}
+
+double desc_d2(const double *a, const double *b, int dim) {
+  double s = 0;
+  for (int i = 0; i < dim; ++i) {
+    double d = a[i] - b[i];
+    s += d * d;
+  }
+  return s;
+}
+
+}  // namespace
+
+void clustering_host(Call &call, const sym_votes_view &votes, const sym_model_context &ctx,
+                     const sym_options &o, sym_rng *rng, sym_clusters &out,
+                     void *(*allocate)(size_t)) {
+  const uint64_t q = votes.count;
+  const double h = o.bandwidth, h2 = h * h;
+  if (o.max_iterations < 1) fail(SYM_INVALID_ARGUMENT, "Invalid parameter range; see --help");
+  KindData kinds[2];  // 0: reflection (4-D), 1: rigid (12-D)
+  kinds[0].dim = 4, kinds[1].dim = 12;
+  std::vector<uint8_t> kind_of(q);
+  std::vector<int32_t> local_of(q);
+  for (uint64_t i = 0; i < q; ++i) {
+    int k = votes.kind[i] == SYM_REFLECTION ? 0 : 1;
+    kind_of[i] = uint8_t(k);
+    local_of[i] = int32_t(kinds[k].ids.size());
+    kinds[k].ids.push_back(int32_t(i));
+  }
+  for (auto &k : kinds) k.n = k.ids.size();
+  if (q) {
+    double *lanes = call.alloc<double>(12 * q);
+    for (int k = 0; k < 12; ++k) call.h2d(lanes + uint64_t(k) * q, votes.descriptor[k], q * 8);
+    for (int t = 0; t < 2; ++t) {
+      KindData &k = kinds[t];
+      if (!k.n) continue;
+      int32_t *ids = call.upload(k.ids.data(), k.n);
+      k.desc = call.alloc<double>(k.n * k.dim);
+      if (k.dim == 4)
+        gather_desc<4><<<blocks_for(k.n), kThreads, 0, call.stream()>>>(lanes, q, ids, k.n, k.desc);
+      else
+        gather_desc<12><<<blocks_for(k.n), kThreads, 0, call.stream()>>>(lanes, q, ids, k.n, k.desc);
+      check_launch();
+      call.launched();
+    }
+    run_all_seeds<4>(call, kinds[0], h2, o.max_iterations);
+    run_all_seeds<12>(call, kinds[1], h2, o.max_iterations);
+    call.sync();
+  }
+
+  // ---- the reference driver (clustering.cpp:44-96), replayed on the host
+  auto engine = load_rng(rng);
+  std::vector<uint64_t> visited((q + 63) / 64, 0);
+  uint64_t unvisited = q, support_entries = 0;
+  int limited = 0;
+  std::vector<Center> centers;
+  auto visit = [&](uint64_t i) {
+    uint64_t &w = visited[i >> 6];
+    uint64_t bit = 1ull << (i & 63);
+    if (!(w & bit)) w |= bit, --unvisited;
+  };
+  while (unvisited) {
+    uint64_t r = engine() % unvisited;
+    uint64_t seed = 0;
+    for (uint64_t w = 0;; ++w) {  // r-th unvisited vote, ascending
+      uint64_t free_bits = ~visited[w];
+      if ((w + 1) * 64 > q) free_bits &= (q % 64 ? (1ull << (q % 64)) - 1 : ~0ull);
+      uint64_t c = __builtin_popcountll(free_bits);
+      if (r < c) {
+        for (; r; --r) free_bits &= free_bits - 1;
+        seed = w * 64 + __builtin_ctzll(free_bits);
+        break;
+      }
+      r -= c;
+    }
+    int t = kind_of[seed];
+    KindData &k = kinds[t];
+    uint64_t s = uint64_t(local_of[seed]);
+    const uint32_t *row = &k.support[s * k.words];
+    for (uint64_t w = 0; w < k.words; ++w)
+      for (uint32_t m = row[w]; m; m &= m - 1) visit(uint64_t(k.ids[w * 32 + __builtin_ctz(m)]));
+    bool converged = k.flags[s] & 1, exhausted = k.flags[s] & 2;
+    if (exhausted) visit(seed);
+    if (!converged) ++limited;
+    const double *mean = &k.mean[s * k.dim];
+    uint64_t size = popcount_row(row, k.words);
+    int merge = -1;
+    for (size_t c = 0; c < centers.size(); ++c)
+      if (centers[c].kind == t && desc_d2(mean, centers[c].v, k.dim) < h2 / 4) {
+        merge = int(c);
+        break;
+      }
+    if (merge < 0) {
+      Center c;
+      for (int i = 0; i < 12; ++i) c.v[i] = i < k.dim ? mean[i] : 0;
+      c.kind = t;
+      c.keys.assign(row, row + k.words);
+      c.key_count = size;
+      c.seeds.push_back(int32_t(s));
+      support_entries += size;
+      centers.push_back(std::move(c));
+    } else {
+      Center &c = centers[merge];
+      double old = double(c.key_count), now = double(size);
+      if (old + now > 0)
+        for (int i = 0; i < k.dim; ++i) c.v[i] = (old * c.v[i] + now * mean[i]) / (old + now);
+      uint64_t before = c.key_count;
+      for (uint64_t w = 0; w < k.words; ++w) c.keys[w] |= row[w];
+      c.key_count = popcount_row(c.keys.data(), k.words);
+      c.seeds.push_back(int32_t(s));
+      support_entries += c.key_count - before;
+    }
+    if (support_entries > 5000000)
+      fail(SYM_RUNTIME_ERROR, "Mean-shift support budget exceeded; lower --sample-ratio");
+    if (centers.size() > 20000)
+      fail(SYM_RUNTIME_ERROR, "Too many mean-shift modes; increase --bandwidth or lower --sample-ratio");
+  }
+  store_rng(engine, rng);
+
+  // ---- support counts and winners (clustering.cpp:97-108) on the GPU
+  std::vector<int32_t> winner(q, -1);
+  count_members<4>(call, kinds[0], centers, 0, h2, o.max_iterations, winner);
+  count_members<12>(call, kinds[1], centers, 1, h2, o.max_iterations, winner);
+  std::vector<std::vector<int32_t>> members(centers.size());
+  for (uint64_t i = 0; i < q; ++i)
+    if (winner[i] >= 0) members[winner[i]].push_back(int32_t(i));
+
+  // ---- decode (clustering.cpp:109-141), stable sort, truncate
+  struct Row {
+    sym_cluster_record rec;
+    std::vector<int32_t> votes;
+  };
+  std::vector<Row> rows;
+  D3 origin{ctx.center[0], ctx.center[1], ctx.center[2]};
+  for (size_t c = 0; c < centers.size(); ++c) {
+    if (members[c].empty()) continue;
+    Row row{};
+    row.rec.reflection = centers[c].kind == 0;
+    row.votes = std::move(members[c]);
+    const double *d = centers[c].v;
+    if (row.rec.reflection) {
+      D3 n{d[0], d[1], d[2]};
+      double length = norm(n);
+      D3 pn = unit(n);
+      double offset = d[3] * ctx.box_size / length - dot(pn, origin);
+      M3 r = mirror(pn);
+      D3 t = pn * (-2 * offset);
+      for (int i = 0; i < 9; ++i) row.rec.rotation[i] = r.m[i];
+      row.rec.translation[0] = t.x, row.rec.translation[1] = t.y, row.rec.translation[2] = t.z;
+      row.rec.plane_normal[0] = pn.x, row.rec.plane_normal[1] = pn.y, row.rec.plane_normal[2] = pn.z;
+      row.rec.plane_offset = offset;
+    } else {
+      M3 m;
+      for (int i = 0; i < 9; ++i) m.m[i] = d[i] * 2;
+      D3 c0{m.m[0], m.m[3], m.m[6]}, c1{m.m[1], m.m[4], m.m[7]};
+      D3 a = unit(c0), b = unit(c1 - a * dot(a, c1));
+      if (norm(a) < 0.5 || norm(b) < 0.5) {
+        int32_t first = row.votes[0];
+        for (int i = 0; i < 9; ++i) m.m[i] = votes.rotation[i][first];
+      } else {
+        m = columns(a, b, cross(a, b));
+      }
+      D3 t{d[9], d[10], d[11]};
+      D3 tr = t * ctx.box_size + origin - mul(m, origin);
+      for (int i = 0; i < 9; ++i) row.rec.rotation[i] = m.m[i];
+      row.rec.translation[0] = tr.x, row.rec.translation[1] = tr.y, row.rec.translation[2] = tr.z;
+    }
+    rows.push_back(std::move(row));
+  }
+  std::stable_sort(rows.begin(), rows.end(),
+                   [](const Row &a, const Row &b) { return a.votes.size() > b.votes.size(); });
+  if (rows.size() > size_t(o.max_clusters)) rows.resize(o.max_clusters);
+  uint64_t total = 0;
+  for (auto &r : rows) total += r.votes.size();
+  size_t nrec = rows.size();
+  size_t bytes = nrec * sizeof(sym_cluster_record) + (nrec + 1) * 8 + total * 4 + 64;
+  char *block = static_cast<char *>(allocate(bytes));
+  if (!block) fail(SYM_RUNTIME_ERROR, "host allocation failed");
+  out.storage = block;
+  out.records = reinterpret_cast<sym_cluster_record *>(block);
+  out.vote_offsets = reinterpret_cast<uint64_t *>(block + nrec * sizeof(sym_cluster_record));
+  out.vote_indices = reinterpret_cast<int32_t *>(out.vote_offsets + nrec + 1);
+  out.count = nrec;
+  out.limited_iterations = limited;
+  out.vote_offsets[0] = 0;
+  for (size_t c = 0; c < nrec; ++c) {
+    out.records[c] = rows[c].rec;
+    std::copy(rows[c].votes.begin(), rows[c].votes.end(), out.vote_indices + out.vote_offsets[c]);
+    out.vote_offsets[c + 1] = out.vote_offsets[c] + rows[c].votes.size();
+  }
+}
+
+}  // namespace sym

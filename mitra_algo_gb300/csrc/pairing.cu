@@ -1,0 +1,347 @@
+// SPDX-License-Identifier: MPL-2.0
+// Stage (b), first half: anisotropy prune of the host sample and curvature
+// pair voting candidates.
+//
+// Reference: src/cpu/selection.cpp:15-29, src/cpu/pairing.cpp:14-35 (CPU);
+// src/cuda/backend.cu:21-31,128-339 (existing GPU path).
+//
+// Pairing on GB300:
+//  1. gather the pruned samples (ordinal order) and radix-sort ordinals by
+//     their kmin key;
+//  2. rebuild the sample SoA in key order, so every source's candidate window
+//     is one contiguous, coalesced range;
+//  3. bound each source's window with a conservative kmin radius derived
+//     from the acceptance test (|dk| <= t M implies M_b <= M_a / (1 - t'));
+//  4. count accepted targets per source (one CTA per source), scan, check
+//     the budget, then fill: a shared-memory bitmask over target ordinals
+//     turns the key-ordered window back into the reference's nested-loop
+//     order (source ordinal, then target ordinal) with no segmented sort.
+// The acceptance test is the reference's FP64 expression, evaluated in the
+// same order without FMA contraction, so the pair set is bit-exact.
+#include "common.cuh"
+#include "primitives.cuh"
+#include "rng.hpp"
+
+#include <cmath>
+#include <limits>
+
+namespace sym {
+namespace {
+
+__global__ void prune_kernel(const int32_t *sample, uint64_t count, const double *kmin,
+                             const double *kmax, const uint8_t *valid, double threshold,
+                             uint8_t *flags) {
+  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  int32_t v = sample[i];
+  double a = kmin[v], b = kmax[v];
+  double maximum = fabs(a) < fabs(b) ? fabs(b) : fabs(a);
+  flags[i] = valid[v] && maximum > 1e-10 && fabs(a - b) / maximum > threshold;
+}
+
+// Samples in ordinal order + validation + sort keys.
+__global__ void gather_samples(const int32_t *selected, uint64_t s, const double *xyz,
+                               uint64_t nv, const double *kmin, const double *kmax,
+                               uint64_t *keys, int32_t *ordinals, int *status) {
+  uint64_t a = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (a >= s) return;
+  int32_t v = selected[a];
+  ordinals[a] = int32_t(a);
+  if (v < 0 || uint64_t(v) >= nv) {
+    atomicExch(status, DS_INDEX_RANGE);
+    keys[a] = 0;
+    return;
+  }
+  double k0 = kmin[v], k1 = kmax[v];
+  if (!isfinite(k0) || !isfinite(k1) || !isfinite(xyz[v]) || !isfinite(xyz[nv + v]) ||
+      !isfinite(xyz[2 * nv + v]))
+    atomicExch(status, DS_NONFINITE);
+  keys[a] = orderable_key(k0);
+}
+
+struct SortedSamples {  // SoA in kmin-key order
+  int32_t *ordinal;
+  double *kmin, *kmax, *x, *y, *z;
+};
+
+__global__ void build_sorted(const int32_t *sorted_ord, const int32_t *selected, uint64_t s,
+                             const double *xyz, uint64_t nv, const double *kmin,
+                             const double *kmax, SortedSamples out) {
+  uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= s) return;
+  int32_t a = sorted_ord[k];
+  int32_t v = selected[a];
+  out.ordinal[k] = a;
+  out.kmin[k] = kmin[v];
+  out.kmax[k] = kmax[v];
+  out.x[k] = xyz[v];
+  out.y[k] = xyz[nv + v];
+  out.z[k] = xyz[2 * nv + v];
+}
+
+__device__ uint64_t lower_bound_key(const uint64_t *keys, uint64_t n, uint64_t key, bool upper) {
+  uint64_t first = 0;
+  while (n) {
+    uint64_t half = n / 2, mid = first + half;
+    if (keys[mid] < key || (upper && keys[mid] == key)) {
+      first = mid + 1;
+      n -= half + 1;
+    } else {
+      n = half;
+    }
+  }
+  return first;
+}
+
+// Per ordinal: own data and the key-order window [lo, hi) holding every
+// possible partner.
+__global__ void windows(const int32_t *selected, uint64_t s, const double *kmin,
+                        const double *kmax, const uint64_t *sorted_keys, double t,
+                        uint64_t *lo, uint64_t *hi) {
+  uint64_t a = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (a >= s) return;
+  int32_t v = selected[a];
+  double k0 = kmin[v], k1 = kmax[v];
+  const double u = 1.1102230246251565e-16;  // 2^-53
+  double ts = t * (1 + 8 * u) + 4 * u;       // t(1+u)/(1-u) rounded up, with slack
+  uint64_t l = 0, h = s;
+  if (ts < 1) {
+    double m = fmax(fmax(fabs(k0), fabs(k1)), 1e-10);
+    double r = ts * m / (1 - ts);
+    r = r * (1 + 16 * u);
+    double pad = 64 * u * (fabs(k0) + r);
+    double low = k0 - r - pad, high = k0 + r + pad;
+    l = lower_bound_key(sorted_keys, s, orderable_key(low), false);
+    h = lower_bound_key(sorted_keys, s, orderable_key(high), true);
+  }
+  lo[a] = l;
+  hi[a] = h;
+}
+
+// The reference's acceptance test (pairing.cpp:22-28) for ordinals a < b.
+__device__ __forceinline__ bool accept(double pa0, double pa1, D3 pp, double qb0, double qb1,
+                                       D3 qp, double t, double min_dist) {
+  double m = fmax(fmax(fmax(fmax(fabs(pa0), fabs(pa1)), fabs(qb0)), fabs(qb1)), 1e-10);
+  double tol = t * m;
+  if (fabs(pa0 - qb0) > tol || fabs(pa1 - qb1) > tol) return false;
+  return !(norm(pp - qp) < min_dist);
+}
+
+__device__ unsigned block_sum(unsigned v) {
+  __shared__ unsigned warp_sum[32];
+  for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) warp_sum[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned total = 0;
+  if (threadIdx.x < 32) {
+    total = threadIdx.x < (blockDim.x >> 5) ? warp_sum[threadIdx.x] : 0;
+    for (int o = 16; o; o >>= 1) total += __shfl_down_sync(0xffffffffu, total, o);
+  }
+  return total;  // valid in thread 0
+}
+
+__global__ void count_pairs(const int32_t *selected, uint64_t s, const double *xyz, uint64_t nv,
+                            const double *kmin, const double *kmax, SortedSamples srt,
+                            const uint64_t *lo, const uint64_t *hi, double t, double min_dist,
+                            uint64_t *counts) {
+  uint64_t a = blockIdx.x;
+  int32_t v = selected[a];
+  double a0 = kmin[v], a1 = kmax[v];
+  D3 ap = {xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  unsigned c = 0;
+  for (uint64_t k = lo[a] + threadIdx.x; k < hi[a]; k += blockDim.x) {
+    int32_t b = srt.ordinal[k];
+    if (uint64_t(b) <= a) continue;
+    c += accept(a0, a1, ap, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t, min_dist);
+  }
+  unsigned total = block_sum(c);
+  if (threadIdx.x == 0) counts[a] = total;
+}
+
+constexpr int kFillThreads = 256;
+constexpr int kChunkWords = 8192;  // 262,144 target ordinals per pass (32 KiB)
+
+__global__ void fill_pairs(const int32_t *selected, uint64_t s, const double *xyz, uint64_t nv,
+                           const double *kmin, const double *kmax, SortedSamples srt,
+                           const uint64_t *lo, const uint64_t *hi, const uint64_t *offsets,
+                           double t, double min_dist, int32_t *out_a, int32_t *out_b) {
+  __shared__ unsigned bits[kChunkWords];
+  __shared__ unsigned warp_tot[kFillThreads / 32];
+  uint64_t a = blockIdx.x;
+  int32_t v = selected[a];
+  double a0 = kmin[v], a1 = kmax[v];
+  D3 ap = {xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  uint64_t out = offsets[a];
+  const uint64_t end_out = offsets[a + 1];
+  if (out == end_out) return;
+  const uint64_t base = (a + 1) & ~uint64_t(31);
+  const uint64_t chunk_bits = uint64_t(kChunkWords) * 32;
+  for (uint64_t cb = base; cb < s; cb += chunk_bits) {
+    uint64_t ce = min(s, cb + chunk_bits);
+    unsigned words = unsigned((ce - cb + 31) / 32);
+    for (unsigned w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
+    __syncthreads();
+    for (uint64_t k = lo[a] + threadIdx.x; k < hi[a]; k += blockDim.x) {
+      int32_t b = srt.ordinal[k];
+      if (uint64_t(b) <= a || uint64_t(b) < cb || uint64_t(b) >= ce) continue;
+      if (accept(a0, a1, ap, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t,
+                 min_dist)) {
+        uint64_t bit = uint64_t(b) - cb;
+        atomicOr(&bits[bit >> 5], 1u << (bit & 31));
+      }
+    }
+    __syncthreads();
+    // Each thread owns a contiguous run of words; prefix of popcounts.
+    unsigned per = (words + blockDim.x - 1) / blockDim.x;
+    unsigned w0 = threadIdx.x * per, w1 = min(words, w0 + per);
+    unsigned mine = 0;
+    for (unsigned w = w0; w < w1; ++w) mine += __popc(bits[w]);
+    unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned incl = mine;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= unsigned(o)) incl += y;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    unsigned before = 0, total = 0;
+    for (unsigned w = 0; w < blockDim.x / 32; ++w) {
+      if (w < warp) before += warp_tot[w];
+      total += warp_tot[w];
+    }
+    uint64_t pos = out + before + incl - mine;
+    for (unsigned w = w0; w < w1; ++w) {
+      unsigned m = bits[w];
+      while (m) {
+        unsigned bit = __ffs(m) - 1;
+        m &= m - 1;
+        uint64_t b = cb + uint64_t(w) * 32 + bit;
+        if (pos < end_out) {
+          out_a[pos] = v;
+          out_b[pos] = selected[b];
+        }
+        ++pos;
+      }
+    }
+    out += total;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+void prune_device(Call &call, const int32_t *sample, uint64_t count, const double *kmin,
+                  const double *kmax, const uint8_t *valid, double prune, int32_t *pruned,
+                  uint64_t *pruned_count) {
+  uint8_t *flags = call.alloc<uint8_t>(count);
+  if (count) {
+    prune_kernel<<<blocks_for(count), kThreads, 0, call.stream()>>>(sample, count, kmin, kmax,
+                                                                     valid, 1 - prune, flags);
+    check_launch();
+    call.launched();
+  }
+  compact_values(call, flags, sample, count, pruned, pruned_count);
+}
+
+void select_host(Call &call, const sym_mesh_view &m, const sym_features_view &f,
+                 const double *weights, uint64_t weight_count, const sym_options &o,
+                 sym_rng *rng, std::vector<int32_t> &sample, std::vector<int32_t> &pruned) {
+  if (weight_count != m.vertices.count || f.count != weight_count)
+    fail(SYM_INVALID_ARGUMENT, "SoA component lengths differ");
+  auto engine = load_rng(rng);
+  sample = sample_vertices(weights, weight_count, o.sample_ratio, engine);
+  store_rng(engine, rng);
+  pruned.clear();
+  uint64_t n = weight_count, count = sample.size();
+  if (!count) return;
+  double *kmin = call.upload(f.kmin, n);
+  double *kmax = call.upload(f.kmax, n);
+  uint8_t *valid = call.upload(f.valid, n);
+  int32_t *dsample = call.upload(sample.data(), count);
+  int32_t *dpruned = call.alloc<int32_t>(count);
+  uint64_t *dcount = call.alloc<uint64_t>(1);
+  prune_device(call, dsample, count, kmin, kmax, valid, o.prune, dpruned, dcount);
+  uint64_t kept = 0;
+  call.d2h(&kept, dcount, 8);
+  call.sync();
+  pruned.resize(kept);
+  call.d2h(pruned.data(), dpruned, kept * 4);
+  call.sync();
+}
+
+// Device-resident pairing.  `selected` (s ordinals), `xyz` (3 x nv),
+// kmin/kmax (nv) are device pointers.  Returns the pair count; out_a/out_b
+// are allocated from the workspace.
+uint64_t pairing_device(Call &call, const int32_t *selected, uint64_t s, const double *xyz,
+                        uint64_t nv, const double *kmin, const double *kmax, double t,
+                        double box, uint64_t max_pairs, int32_t **out_a, int32_t **out_b) {
+  cudaStream_t st = call.stream();
+  *out_a = *out_b = nullptr;
+  if (s < 2) return 0;
+  uint64_t *keys = call.alloc<uint64_t>(s), *sorted_keys = call.alloc<uint64_t>(s);
+  int32_t *ord = call.alloc<int32_t>(s), *sorted_ord = call.alloc<int32_t>(s);
+  gather_samples<<<blocks_for(s), kThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, keys, ord,
+                                                     call.status());
+  check_launch();
+  call.check_status("pairing");
+  radix_sort_pairs(call, keys, ord, sorted_keys, sorted_ord, s, 64);
+  SortedSamples srt{call.alloc<int32_t>(s), call.alloc<double>(s), call.alloc<double>(s),
+                    call.alloc<double>(s), call.alloc<double>(s), call.alloc<double>(s)};
+  build_sorted<<<blocks_for(s), kThreads, 0, st>>>(sorted_ord, selected, s, xyz, nv, kmin, kmax, srt);
+  check_launch();
+  uint64_t *lo = call.alloc<uint64_t>(s), *hi = call.alloc<uint64_t>(s);
+  windows<<<blocks_for(s), kThreads, 0, st>>>(selected, s, kmin, kmax, sorted_keys, t, lo, hi);
+  check_launch();
+  uint64_t *counts = call.alloc<uint64_t>(s), *offsets = call.alloc<uint64_t>(s + 1);
+  double min_dist = 0.03 * box;
+  count_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo, hi,
+                                                    t, min_dist, counts);
+  check_launch();
+  exclusive_scan(call, counts, offsets, s);
+  call.launched(4);
+  uint64_t total = 0;
+  call.d2h(&total, offsets + s, 8);
+  call.sync();
+  if (total > max_pairs || total > uint64_t(std::numeric_limits<int32_t>::max()))
+    fail(SYM_RUNTIME_ERROR, "Pair budget exceeded; lower --sample-ratio or tighten --pair-threshold");
+  if (!total) return 0;
+  *out_a = call.alloc<int32_t>(total);
+  *out_b = call.alloc<int32_t>(total);
+  fill_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo, hi,
+                                                   offsets, t, min_dist, *out_a, *out_b);
+  check_launch();
+  call.launched();
+  return total;
+}
+
+void pairing_host(Call &call, const sym_mesh_view &m, const sym_features_view &f,
+                  const int32_t *selected, uint64_t s, const sym_model_context &ctx,
+                  const sym_options &o, std::vector<int32_t> &a, std::vector<int32_t> &b) {
+  a.clear();
+  b.clear();
+  if (s < 2) return;
+  if (f.count != m.vertices.count) fail(SYM_INVALID_ARGUMENT, "SoA component lengths differ");
+  if (s > uint64_t(std::numeric_limits<int32_t>::max()))
+    fail(SYM_OVERFLOW, "selected ordinals exceed int32 range");
+  if (!(ctx.box_size > 0) || !std::isfinite(ctx.box_size) ||
+      !(o.pair_threshold > 0 && o.pair_threshold <= 1))
+    fail(SYM_INVALID_ARGUMENT,
+         "pairing requires positive finite box size and threshold in (0,1]");
+  uint64_t nv = m.vertices.count;
+  double *xyz = upload_points(call, m.vertices);
+  double *kmin = call.upload(f.kmin, nv);
+  double *kmax = call.upload(f.kmax, nv);
+  int32_t *sel = call.upload(selected, s);
+  int32_t *da, *db;
+  uint64_t total = pairing_device(call, sel, s, xyz, nv, kmin, kmax, o.pair_threshold,
+                                  ctx.box_size, o.max_pairs, &da, &db);
+  a.resize(total);
+  b.resize(total);
+  if (total) {
+    call.d2h(a.data(), da, total * 4);
+    call.d2h(b.data(), db, total * 4);
+  }
+  call.check_status("pairing");
+}
+
+}  // namespace sym
