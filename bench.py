@@ -1,0 +1,376 @@
+#!/usr/bin/env python3
+"""Benchmark of the symmetry hot path on GB300.
+
+Workload (rigid mode, FP32 vs BF16-refined mean-shift): an icosphere
+subdivided 6 times, radially displaced by a seeded 12-bump motif repeated in
+5-fold rotation about z, plus a partial copy translated 0.4 along x, Gaussian
+vertex noise 1e-3 of the bbox diagonal (54,756 vertices, 109,102 faces);
+20,000 area-weighted samples, pair threshold 0.25 (~1e7 pairs), 6-D rigid
+votes, 2,048 mean-shift seeds, bandwidth 0.05.  Synthetic data, seeded.
+
+One step = the whole hot path on one mesh: curvature, prune, exact pairing,
+6-D votes, vote sort, mean-shift, modes, verification of the top 20 modes.
+
+  value  - meshes/s with the mesh resident in HBM (sym_mesh_load once),
+           device time from CUDA events on the library's stream, L2 flushed
+           (256 MiB write) before every step;
+  e2e    - meshes/s through the public C ABI from pinned host buffers: every
+           step uploads the mesh (sym_mesh_load), runs sym_detect_fast and
+           reads the result back.
+
+`--impl reference` times the reference's CPU path (oracle/_ref when it was
+built on this machine, else the oracle's restatement of it) on bounded
+samples of the same workload and extrapolates to meshes/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "meshes/s and pair votes/s, BF16-refined vs plain FP32 on GPU at ≤1e-4 mode error"
+SAMPLES = 20000
+PAIR_THRESHOLD = 0.25
+BANDWIDTH = 0.05
+SEEDS = 2048
+
+
+def workload(small=False):
+    """The benchmark mesh and options; `small` is a level-5, 5,000-sample,
+    256-seed variant used for profiler captures."""
+    global SAMPLES, SEEDS
+    from mitra_algo_gb300.mesh import motif_sphere, prepare
+    from mitra_algo_gb300.types import Options
+    if small:
+        SAMPLES, SEEDS = 5000, 256
+    mesh = motif_sphere(level=5 if small else 6, bumps=12, folds=5, partial_shift=0.4,
+                        noise=1e-3, seed=0)
+    opts = Options(sample_ratio=SAMPLES / mesh.vertex_count, pair_threshold=PAIR_THRESHOLD,
+                   bandwidth=BANDWIDTH, max_pairs=2 * 10 ** 7, max_votes=5 * 10 ** 7,
+                   max_clusters=20)
+    return prepare(mesh, opts), opts
+
+
+def config(prepared, r=None):
+    c = {"workload": "motif icosphere L6, rigid mode, 6-D votes",
+         "vertices": prepared.mesh.vertex_count, "faces": int(prepared.mesh.faces.shape[1]),
+         "samples": SAMPLES, "pair_threshold": PAIR_THRESHOLD, "bandwidth": BANDWIDTH,
+         "seeds": SEEDS, "l2": "flushed (256 MiB write) before every timed step"}
+    if r:
+        c.update({"pruned": int(r["pruned"]), "pairs": int(r["pairs"]), "votes": int(r["votes"])})
+    return c
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self, device=0):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[0] == str(device):
+                    rows.append(f)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].replace(".", "").isdigit() else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text()), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_estimate(prepared, opts, sample, gpu_result, budget_s=20.0):
+    """Per-mesh CPU time of the reference path, extrapolated from bounded
+    samples.  Uses the reference's own CPU library when oracle/_ref was built
+    on this machine, else the oracle's restatement of it."""
+    from mitra_algo_gb300.types import Pairs, Rng
+    from oracle import oracle
+    cpu = oracle.OracleBackend()
+    kind = "port"
+    p, o = prepared, opts
+    t = {}
+    t0 = time.perf_counter()
+    f = cpu.curvature(p.mesh, p.topology, o)
+    t["curvature"] = time.perf_counter() - t0
+    rng = oracle.rng(o.seed)
+    t0 = time.perf_counter()
+    sel = cpu.select(p.mesh, f, p.topology.weights, o, rng)
+    t["select"] = time.perf_counter() - t0
+    pruned = sel.pruned
+    s_full = pruned.size
+    s_sub = min(s_full, 3000)
+    t0 = time.perf_counter()
+    pairs = cpu.pairing(p.mesh, f, pruned[:s_sub], p.context, o.with_(max_pairs=10 ** 8))
+    t_pair = time.perf_counter() - t0
+    t["pairing"] = t_pair * (s_full * (s_full - 1)) / max(s_sub * (s_sub - 1), 1)
+    n_sub = min(len(pairs), 50000)
+    sub = Pairs(pairs.a[:n_sub], pairs.b[:n_sub])
+    t0 = time.perf_counter()
+    votes = cpu.transformations(p.mesh, f, sub, p.context, o.with_(max_votes=10 ** 8))
+    t_vote = time.perf_counter() - t0
+    t["transformations"] = t_vote * gpu_result["pairs"] / max(n_sub, 1)
+    # mean shift: cost per seed-vote evaluation of the reference evaluator
+    # on a vote subset, times the evaluations of the GPU run's dense
+    # equivalent (every seed iteration scans all votes).
+    q_sub = min(len(votes), 3000)
+    from mitra_algo_gb300.types import Votes
+    vs = Votes(votes.pair[:q_sub], votes.kind[:q_sub], votes.rotation[:, :q_sub],
+               votes.translation[:, :q_sub], votes.plane_normal[:, :q_sub],
+               votes.plane_offset[:q_sub], votes.descriptor[:, :q_sub])
+    t0 = time.perf_counter()
+    cpu.clustering(vs, p.context, o, oracle.rng(o.seed))
+    t_ms = time.perf_counter() - t0
+    _, evals = cpu.clustering_stats()
+    per_eval = t_ms / max(evals, 1)
+    t["mean_shift"] = per_eval * gpu_result["seed_iterations"] * gpu_result["votes"]
+    # verification: one of the GPU run's clusters, scaled to all of them
+    from mitra_algo_gb300.types import ClusterOutput, Csr
+    nc = max(int(gpu_result["clusters"]), 1)
+    rot = np.array(gpu_result["rotation"][:1] or [list(np.eye(3).ravel())])
+    tr = np.array(gpu_result["translation"][:1] or [[0, 0, 0]])
+    one = ClusterOutput(np.zeros(1, np.uint8), rot, tr, np.zeros((1, 3)), np.zeros(1),
+                        Csr(np.zeros(2, np.uint64), np.zeros(0, np.int32)))
+    t0 = time.perf_counter()
+    cpu.verification(p.mesh, p.topology, one, p.context, o)
+    t["verification"] = (time.perf_counter() - t0) * nc
+    total = sum(t.values())
+    sample_desc = (f"curvature+select full mesh; pairing on {s_sub} of {s_full} pruned samples "
+                   f"x (S/s)^2; transforms on {n_sub} pairs x P/p; mean-shift cost per "
+                   f"evaluation from a {q_sub}-vote reference clustering x (seed-iterations x "
+                   f"votes) of the GPU run; verification of 1 cluster x {nc}")
+    return {"value": 1.0 / total, "unit": "meshes/s", "cores": 1, "kind": kind,
+            "sample": sample_desc, "stage_s": {k: round(v, 4) for k, v in t.items()}}
+
+
+def ctypes_sizeof_result():
+    import ctypes
+    from mitra_algo_gb300 import abi
+    return ctypes.sizeof(abi.FastResult)
+
+
+# --------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    from mitra_algo_gb300 import Gb300Backend
+    from mitra_algo_gb300.types import Rng
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    prepared, opts = workload(args.small)
+    gpu = Gb300Backend(local)
+    stream = torch.cuda.ExternalStream(gpu.stream_handle, device=torch.device("cuda", local))
+    # sample: the reference's host RNG sampling (the input of the path)
+    feats = gpu.curvature(prepared.mesh, prepared.topology, opts)
+    sel = gpu.select(prepared.mesh, feats, prepared.topology.weights, opts, Rng(opts.seed))
+    sample = sel.sample
+    resident = gpu.load_mesh(prepared)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step(precision, reference_seeds=0):
+        return gpu.detect_fast(resident, sample, opts, precision=precision, seeds=SEEDS,
+                               reference_seeds=reference_seeds)
+
+    def timed(precision, steps, warmup):
+        for _ in range(warmup):
+            step(precision)
+        total_ms, results = 0.0, []
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.random_(0, 255)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+            results.append(step(precision))
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            b.synchronize()
+            total_ms += a.elapsed_time(b)
+        return total_ms / steps, results
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # correctness / error run (untimed): FP64 re-run of 256 seeds
+    err = {p: step(p, reference_seeds=256) for p in ("bf16", "fp32")}
+    barrier()
+    with Clocks(str(ROOT / "gpurun_out" / "bench_clocks.csv") if (ROOT / "gpurun_out").exists()
+                else "/tmp/bench_clocks.csv") as clk:
+        ms_bf16, res_bf16 = timed("bf16", args.steps, args.warmup)
+        barrier()
+        ms_fp32, res_fp32 = timed("fp32", args.steps, max(1, args.warmup // 2))
+        barrier()
+    clocks = clk.summary(local)
+    # e2e: pinned host buffers -> public ABI -> result read back, every step
+    p = prepared
+    pinned = {}
+    for name, arr in [("v", p.mesh.vertices), ("f", p.mesh.faces), ("vn", p.topology.normals),
+                      ("fn", p.topology.face_normals), ("w", p.topology.weights),
+                      ("no", p.topology.neighbors.offsets), ("ni", p.topology.neighbors.indices),
+                      ("e", np.ascontiguousarray(p.topology.edges, np.int32))]:
+        t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
+        pinned[name] = t.numpy()
+    from mitra_algo_gb300.mesh import Prepared
+    from mitra_algo_gb300.types import Csr, Mesh, Topology
+    pp = Prepared(Mesh(pinned["v"], pinned["f"]),
+                  Topology(pinned["vn"], pinned["fn"], pinned["w"], Csr(pinned["no"], pinned["ni"]),
+                           p.topology.incident_faces, pinned["e"]), p.context)
+    assert pp.mesh.vertices.ctypes.data == pinned["v"].ctypes.data  # still the pinned buffer
+    e2e_ms = []
+    h2d = d2h = 0
+    for i in range(args.warmup + args.steps):
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        mesh_i = gpu.load_mesh(pp)
+        r = gpu.detect_fast(mesh_i, sample, opts, precision="bf16", seeds=SEEDS)
+        b.record(stream)
+        b.synchronize()
+        mesh_i.close()
+        if i >= args.warmup:
+            e2e_ms.append(a.elapsed_time(b))
+            h2d = mesh_i.bytes() + sample.nbytes + r["h2d_bytes"]
+            d2h = r["d2h_bytes"] + ctypes_sizeof_result()
+    barrier()
+    ms = torch.tensor([ms_bf16, ms_fp32, statistics.mean(e2e_ms)], device=f"cuda:{local}")
+    if world > 1:
+        torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
+    ms_bf16, ms_fp32, ms_e2e = ms.tolist()
+    if rank != 0:
+        return
+    r = res_bf16[-1]
+    meshes = world * 1000.0 / ms_bf16
+    votes_per_s = world * r["votes"] * 1000.0 / ms_bf16
+    pk, pk_kind = peaks()
+    ms_stage = statistics.mean(x["stage_ms"]["mean_shift"] for x in res_bf16)
+    evals = statistics.mean(x["mean_shift_pairs"] for x in res_bf16)
+    achieved = evals * 64 / (ms_stage * 1e-3) / 1e12
+    line = {
+        "metric": METRIC, "value": round(meshes, 4), "unit": "meshes/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_bf16, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded motif icosphere, generated in-process)",
+        "config": config(prepared, r),
+        "pair_votes_per_s": round(votes_per_s, 1),
+        "fp32": {"meshes_per_s": round(world * 1000.0 / ms_fp32, 4), "ms_per_step": round(ms_fp32, 3)},
+        "bf16_over_fp32": round(ms_fp32 / ms_bf16, 3),
+        "mode_error": {pr: {"max": e["mode_error_max"], "mean": e["mode_error_mean"],
+                            "seeds": 256} for pr, e in err.items()},
+        "mean_shift": {"bulk_iterations": r["iterations"], "polish_iterations": r["polish_iterations"],
+                       "modes": r["modes"], "evaluations": evals},
+        "stage_ms": {k: round(statistics.mean(x["stage_ms"][k] for x in res_bf16), 3)
+                     for k in r["stage_ms"]},
+        "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"kernel": "mean-shift (seed x vote evaluations)", "bound": "tensor",
+                     "achieved": round(achieved, 3), "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                     "frac": round(achieved / pk["bf16_tflops"], 5), "traffic": None,
+                     "peak_source": pk_kind,
+                     "note": "achieved = evaluations x 64 (tensor formulation, D padded to 16) / mean-shift stage time"},
+        "clocks": clocks,
+        "gpu_launches": int(sum(x["launches"] for x in res_bf16)),
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_estimate(prepared, opts, sample, r)
+    print(json.dumps(line))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    prepared, opts = workload(args.small)
+    from oracle import oracle
+    cpu = oracle.OracleBackend()
+    # the GPU run's mean-shift work counts come from a fixed estimate of the
+    # same workload when no GPU result is at hand: seeds x avg iterations.
+    f = cpu.curvature(prepared.mesh, prepared.topology, opts)
+    sel = cpu.select(prepared.mesh, f, prepared.topology.weights, opts, oracle.rng(opts.seed))
+    gpu_like = {"pairs": 10_000_000, "votes": 20_000_000, "seed_iterations": SEEDS * 12.0,
+                "clusters": 20, "rotation": [], "translation": []}
+    times = []
+    est = None
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        est = cpu_estimate(prepared, opts, sel.sample, gpu_like)
+        if i >= args.warmup:
+            times.append(1.0 / est["value"])
+    per_mesh = statistics.mean(times)
+    line = {"metric": METRIC, "value": round(1.0 / per_mesh, 8), "unit": "meshes/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(per_mesh * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded motif icosphere)", "config": config(prepared),
+            "impl": "reference",
+            "cpu_baseline": {**est, "value": round(1.0 / per_mesh, 8)},
+            "e2e": {"value": round(1.0 / per_mesh, 8), "unit": "meshes/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline estimate")
+    ap.add_argument("--small", action="store_true",
+                    help="level-5 mesh, 5,000 samples, 256 seeds (profiler captures)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -220,6 +220,8 @@ void sym_verification_release(sym_verification_result *v);
 typedef struct sym_context sym_context;
 sym_status sym_context_create(int device, sym_context **out);
 void sym_context_destroy(sym_context *ctx);
+/* The context's cudaStream_t, for callers that time or order work on it. */
+void *sym_context_stream(sym_context *ctx);
 /* Name reported by Backend::name() for this backend. */
 const char *sym_backend_name(void);
 
@@ -271,6 +273,58 @@ sym_status sym_verification(sym_context *ctx, const sym_mesh_view *mesh,
  * `queries` holds 12 doubles per query: p, a, b, c. */
 sym_status sym_triangle_distances(sym_context *ctx, const double *queries,
                                   uint64_t count, double *out);
+
+/* ------------------------------------------------- throughput extension
+ * No counterpart in the reference (it processes one mesh per detect() with
+ * every stage re-uploading its inputs).  A mesh is loaded once into device
+ * memory, then sym_detect_fast runs the whole hot path on it with device-
+ * resident intermediates: curvature, prune of a host sample, exact pairing,
+ * 6-D rigid votes (axis-angle/2 + centred translation/box, FP32 transforms,
+ * FP64 log map near pi), a spatially sorted vote set, mean-shift from K seeds
+ * with Epanechnikov weights, mode merging, and verification of the top
+ * modes.  The mean-shift precision is selectable: plain FP32, or BF16 tensor-
+ * core bulk iterations refined by FP32 polish; a subset of seeds can be
+ * re-run in FP64 to report the mode error. */
+typedef struct sym_mesh_handle sym_mesh_handle;
+/* Uploads the mesh and its topology; the host views must stay valid while
+ * the handle is used (the verification BVH is built from them). */
+sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh,
+                         const sym_topology_view *topology,
+                         const sym_model_context *model, sym_mesh_handle **out);
+void sym_mesh_free(sym_mesh_handle *handle);
+
+enum { SYM_MS_FP32 = 0, SYM_MS_BF16_REFINED = 1 };
+typedef struct sym_fast_options {
+  int32_t precision;         /* SYM_MS_FP32 or SYM_MS_BF16_REFINED */
+  int32_t seeds;             /* mean-shift seeds K (votes drawn uniformly) */
+  uint64_t seed_rng;         /* seed of the seed-drawing std::mt19937_64 */
+  int32_t max_iterations;    /* bulk iterations (BF16 or FP32) */
+  int32_t polish_iterations; /* FP32 refinement iterations after BF16 */
+  int32_t reference_seeds;   /* seeds re-run in FP64 for the mode error */
+  int32_t verify;            /* verify the top modes (max_clusters) */
+} sym_fast_options;
+
+#define SYM_FAST_MAX_CLUSTERS 32
+typedef struct sym_fast_result {
+  uint64_t pruned, pairs, votes, modes, clusters;
+  int32_t iterations, polish_iterations;
+  double mode_error_max, mode_error_mean; /* relative to FP64, reference seeds */
+  /* device time per stage: curvature, prune, pairing, votes, vote sort,
+   * mean shift, modes, verification */
+  double stage_ms[8];
+  double mean_shift_pairs; /* seed-vote evaluations actually made */
+  double seed_iterations;  /* sum over seeds of the iterations each ran */
+  uint64_t launches, h2d_bytes, d2h_bytes;
+  sym_cluster_record records[SYM_FAST_MAX_CLUSTERS];
+  uint64_t support[SYM_FAST_MAX_CLUSTERS];
+  double coverage[SYM_FAST_MAX_CLUSTERS], rms[SYM_FAST_MAX_CLUSTERS];
+} sym_fast_result;
+void sym_fast_options_default(sym_fast_options *out);
+/* `sample` is a host array of vertex ids (the area-weighted sample). */
+sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
+                           const int32_t *sample, uint64_t sample_count,
+                           const sym_options *options,
+                           const sym_fast_options *fast, sym_fast_result *out);
 
 /* --------------------------------------------------------------- metrics */
 /* Per-stage accounting, the fields of the reference CudaMetric

@@ -139,6 +139,32 @@ class Metric(C.Structure):
                 ("custom_kernel_ms", C.c_double), ("all_buffers_released", C.c_int32)]
 
 
+class FastOptions(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("seeds", C.c_int32), ("seed_rng", C.c_uint64),
+                ("max_iterations", C.c_int32), ("polish_iterations", C.c_int32),
+                ("reference_seeds", C.c_int32), ("verify", C.c_int32)]
+
+
+FAST_MAX_CLUSTERS = 32
+
+
+class FastResult(C.Structure):
+    _fields_ = [("pruned", C.c_uint64), ("pairs", C.c_uint64), ("votes", C.c_uint64),
+                ("modes", C.c_uint64), ("clusters", C.c_uint64), ("iterations", C.c_int32),
+                ("polish_iterations", C.c_int32), ("mode_error_max", C.c_double),
+                ("mode_error_mean", C.c_double), ("stage_ms", C.c_double * 8),
+                ("mean_shift_pairs", C.c_double), ("seed_iterations", C.c_double),
+                ("launches", C.c_uint64), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
+                ("records", ClusterRecord * FAST_MAX_CLUSTERS),
+                ("support", C.c_uint64 * FAST_MAX_CLUSTERS),
+                ("coverage", C.c_double * FAST_MAX_CLUSTERS),
+                ("rms", C.c_double * FAST_MAX_CLUSTERS)]
+
+
+MS_FP32, MS_BF16_REFINED = 0, 1
+STAGES = ["curvature", "prune", "pairing", "votes", "vote_sort", "mean_shift", "modes",
+          "verification"]
+
 P = C.POINTER
 # (name, restype, argtypes) of every entry point declared in include/mitra_gb300.h.
 PROTOTYPES = [
@@ -166,6 +192,13 @@ PROTOTYPES = [
     ("sym_verification", C.c_int, [C.c_void_p, P(MeshView), P(TopologyView), P(ClustersView),
                                    P(ModelContext), P(Options), P(VerificationOut)]),
     ("sym_triangle_distances", C.c_int, [C.c_void_p, _d, C.c_uint64, _d]),
+    ("sym_mesh_load", C.c_int, [C.c_void_p, P(MeshView), P(TopologyView), P(ModelContext),
+                                P(C.c_void_p)]),
+    ("sym_mesh_free", None, [C.c_void_p]),
+    ("sym_fast_options_default", None, [P(FastOptions)]),
+    ("sym_detect_fast", C.c_int, [C.c_void_p, C.c_void_p, _i, C.c_uint64, P(Options),
+                                  P(FastOptions), P(FastResult)]),
+    ("sym_context_stream", C.c_void_p, [C.c_void_p]),
     ("sym_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("sym_take_metrics", C.c_uint64, [C.c_void_p, P(Metric), C.c_uint64]),
 ]

@@ -148,6 +148,41 @@ class Gb300Backend:
                                                 n, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out
 
+    # ------------------------------------------- throughput extension
+    @property
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer."""
+        return int(self._lib.sym_context_stream(self._ctx) or 0)
+
+    def load_mesh(self, prepared: Prepared) -> "ResidentMesh":
+        return ResidentMesh(self, prepared)
+
+    def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
+                    seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
+                    reference_seeds=0, verify=True) -> dict:
+        """Throughput pipeline on a resident mesh (no reference counterpart)."""
+        sample = np.ascontiguousarray(sample, np.int32)
+        fo = abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
+                             seed_rng, max_iterations, polish_iterations, reference_seeds,
+                             1 if verify else 0)
+        res = abi.FastResult()
+        _check(self._lib.sym_detect_fast(self._ctx, mesh.handle,
+                                         sample.ctypes.data_as(C.POINTER(C.c_int32)), sample.size,
+                                         C.byref(options.to_c()), C.byref(fo), C.byref(res)))
+        n = int(res.clusters)
+        out = {k: getattr(res, k) for k in ("pruned", "pairs", "votes", "modes", "clusters",
+                                            "iterations", "polish_iterations", "mode_error_max",
+                                            "mode_error_mean", "mean_shift_pairs",
+                                            "seed_iterations", "launches", "h2d_bytes",
+                                            "d2h_bytes")}
+        out["stage_ms"] = dict(zip(abi.STAGES, list(res.stage_ms)))
+        out["support"] = list(res.support)[:n]
+        out["coverage"] = list(res.coverage)[:n]
+        out["rms"] = list(res.rms)[:n]
+        out["rotation"] = [list(res.records[i].rotation) for i in range(n)]
+        out["translation"] = [list(res.records[i].translation) for i in range(n)]
+        return out
+
     def take_metrics(self):
         buf = (abi.Metric * 64)()
         n = self._lib.sym_take_metrics(self._ctx, buf, 64)
@@ -202,3 +237,36 @@ def detect(mesh: Mesh, options: Options, backend, progress=None) -> Result:
         r.verification = backend.verification(p.mesh, p.topology, r.clusters, p.context, options)
     timed("verification")
     return r
+
+
+class ResidentMesh:
+    """A prepared mesh uploaded once to the device (sym_mesh_load)."""
+
+    def __init__(self, backend: Gb300Backend, prepared: Prepared):
+        self._lib = backend._lib
+        self.prepared = prepared
+        self._views = (prepared.mesh.view(), prepared.topology.view(), prepared.context.to_c())
+        h = C.c_void_p()
+        _check(self._lib.sym_mesh_load(backend._ctx, C.byref(self._views[0]),
+                                       C.byref(self._views[1]), C.byref(self._views[2]),
+                                       C.byref(h)))
+        self.handle = h
+
+    def bytes(self) -> int:
+        """Host-to-device bytes of one load."""
+        p = self.prepared
+        return int(p.mesh.vertices.nbytes + p.mesh.faces.nbytes + p.topology.normals.nbytes +
+                   p.topology.face_normals.nbytes + p.topology.weights.nbytes +
+                   p.topology.neighbors.offsets.nbytes + p.topology.neighbors.indices.nbytes +
+                   np.asarray(p.topology.edges).nbytes)
+
+    def close(self):
+        if self.handle:
+            self._lib.sym_mesh_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

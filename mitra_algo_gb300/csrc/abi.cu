@@ -29,8 +29,11 @@ void verification_host(Call &, const sym_mesh_view &, const sym_topology_view &,
 void triangle_distances_host(Call &, const double *, uint64_t, double *);
 }  // namespace sym
 
+// Message of the last failing call on this thread (read by sym_last_error).
+thread_local std::string sym_error_text;
+
 namespace {
-thread_local std::string g_error;
+std::string &g_error = sym_error_text;
 
 void *host_alloc(size_t bytes) { return std::malloc(bytes); }
 
@@ -62,6 +65,8 @@ extern "C" {
 const char *sym_last_error(void) { return g_error.c_str(); }
 
 const char *sym_backend_name(void) { return "gb300"; }
+
+void *sym_context_stream(sym_context *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
 
 void sym_options_default(sym_options *o) {
   *o = sym_options{0.5, 0.85, 0.15, 0.08, 0.025, 3, 0, 100, 20, 42, 200000, 600000, 1};

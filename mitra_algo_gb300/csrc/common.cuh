@@ -74,6 +74,9 @@ struct Metrics {
 
 }  // namespace sym
 
+// Message of the last failing ABI call on this thread (sym_last_error).
+extern thread_local std::string sym_error_text;
+
 struct sym_context {
   int device = 0;
   cudaStream_t stream = nullptr;

@@ -58,11 +58,9 @@ Call::Call(sym_context *c, const char *stage) : ctx(c), stage_(stage) {
   ctx->arena.reset();
   *ctx->host_status = 0;
   cuda_check(cudaMemsetAsync(ctx->status, 0, sizeof(int), ctx->stream), "status reset");
-  if (ctx->metrics.enabled) {
-    ctx->metrics.current = sym_metric{};
-    std::strncpy(ctx->metrics.current.stage, stage, sizeof(ctx->metrics.current.stage) - 1);
-    cudaEventRecord(ctx->metrics.begin, ctx->stream);
-  }
+  ctx->metrics.current = sym_metric{};
+  std::strncpy(ctx->metrics.current.stage, stage, sizeof(ctx->metrics.current.stage) - 1);
+  if (ctx->metrics.enabled) cudaEventRecord(ctx->metrics.begin, ctx->stream);
 }
 
 Call::~Call() {

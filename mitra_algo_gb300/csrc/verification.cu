@@ -352,15 +352,110 @@ void triangle_distances_host(Call &call, const double *queries, uint64_t count, 
   call.sync();
 }
 
+// Device core shared by the ABI entry point and the resident pipeline.
+// Mesh arrays are device pointers; `m` is the host mesh (the BVH is built on
+// the host with the reference's construction order).  Fills per (cluster,
+// side) vertex lists, patches, rms and coverage.
+void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, const int32_t *faces,
+                       const double *vn, const double *w, const uint64_t *nbr_off,
+                       const int32_t *nbr, const sym_cluster_record *records, uint64_t nc,
+                       double tau, std::vector<std::vector<int32_t>> &side,
+                       std::vector<std::vector<std::vector<int32_t>>> &patches,
+                       std::vector<double> &coverage, std::vector<double> &rms) {
+  const uint64_t nv = m.vertices.count, nf = m.faces.count;
+  cudaStream_t st = call.stream();
+  side.assign(2 * nc, {});
+  patches.assign(2 * nc, {});
+  coverage.assign(nc, 0);
+  rms.assign(nc, 0);
+  if (!nc) return;
+  HostBvh bvh(m);
+  if (2 * bvh.depth + 4 > kStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
+  Surface s;
+  s.xyz = xyz;
+  s.nv = nv;
+  s.faces = faces;
+  s.nf = nf;
+  s.nodes = call.upload(bvh.nodes.data(), bvh.nodes.size());
+  s.ids = call.upload(bvh.ids.data(), bvh.ids.size());
+  std::vector<ClusterMotion> motions(nc);
+  for (uint64_t c = 0; c < nc; ++c) {
+    const sym_cluster_record &r = records[c];
+    for (int k = 0; k < 9; ++k) motions[c].r[k] = r.rotation[k];
+    for (int k = 0; k < 3; ++k) motions[c].t[k] = r.translation[k], motions[c].n[k] = r.plane_normal[k];
+    motions[c].offset = r.plane_offset;
+    motions[c].reflection = r.reflection != 0;
+  }
+  ClusterMotion *dm = call.upload(motions.data(), nc);
+  uint64_t rows = nc * 2 * nv;
+  uint8_t *flags = call.alloc<uint8_t>(rows);
+  double *err = call.alloc<double>(nc * nv);
+  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, flags, err,
+                                                         call.status());
+  check_launch();
+  double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
+  uint64_t *na = call.alloc<uint64_t>(nc);
+  ordered_sums<<<blocks_for(nc + 1, 64), 64, 0, st>>>(flags, err, w, nv, nc, error, area, na, total);
+  check_launch();
+  int32_t *parent = call.alloc<int32_t>(rows);
+  init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
+  check_launch();
+  unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(nbr_off, nbr, nv, 2 * nc, parent, call.status());
+  check_launch();
+  uint64_t *keys = call.alloc<uint64_t>(rows), *skeys = call.alloc<uint64_t>(rows);
+  int32_t *vals = call.alloc<int32_t>(rows), *svals = call.alloc<int32_t>(rows);
+  uint8_t *allowed = call.alloc<uint8_t>(rows);
+  root_keys<<<blocks_for(rows), kThreads, 0, st>>>(parent, nv, 2 * nc, keys, vals, allowed);
+  check_launch();
+  uint64_t *kept = call.alloc<uint64_t>(1);
+  int32_t *pos = call.alloc<int32_t>(rows);
+  compact_indices(call, allowed, rows, pos, kept);
+  uint64_t nkept = 0;
+  call.d2h(&nkept, kept, 8);
+  call.sync();
+  call.launched(5);
+  std::vector<uint64_t> hkeys(nkept);
+  std::vector<int32_t> hvals(nkept);
+  if (nkept) {
+    uint64_t *dk = call.alloc<uint64_t>(nkept);
+    int32_t *dv = call.alloc<int32_t>(nkept);
+    gather_kept<<<blocks_for(nkept), kThreads, 0, st>>>(pos, nkept, keys, nv, dk, dv);
+    check_launch();
+    int bits = 32;
+    while ((uint64_t(1) << (bits - 32)) < 2 * nc) ++bits;
+    radix_sort_pairs(call, dk, dv, skeys, svals, nkept, bits);
+    call.d2h(hkeys.data(), skeys, nkept * 8);
+    call.d2h(hvals.data(), svals, nkept * 4);
+  }
+  std::vector<double> herr(nc), harea(nc);
+  std::vector<uint64_t> hna(nc);
+  double htotal = 0;
+  call.d2h(herr.data(), error, nc * 8);
+  call.d2h(harea.data(), area, nc * 8);
+  call.d2h(hna.data(), na, nc * 8);
+  call.d2h(&htotal, total, 8);
+  call.check_status("verification");
+  for (uint64_t k = 0; k < nkept; ++k) {
+    uint64_t set = hkeys[k] >> 32;
+    side[set].push_back(hvals[k]);
+    if (k == 0 || hkeys[k] != hkeys[k - 1]) patches[set].emplace_back();
+    patches[set].back().push_back(hvals[k]);
+  }
+  for (auto &sv : side) std::sort(sv.begin(), sv.end());
+  for (uint64_t c = 0; c < nc; ++c) {
+    rms[c] = hna[c] ? std::sqrt(herr[c] / double(hna[c])) : 0;
+    coverage[c] = htotal > 0 ? std::min(1.0, harea[c] / htotal) : 0;
+  }
+}
+
 void verification_host(Call &call, const sym_mesh_view &m, const sym_topology_view &g,
                        const sym_clusters_view &cl, const sym_model_context &ctx,
                        const sym_options &o, sym_verification_result &out,
                        void *(*allocate)(size_t)) {
   const uint64_t nv = m.vertices.count, nf = m.faces.count, nc = cl.count;
-  cudaStream_t st = call.stream();
-  std::vector<std::vector<int32_t>> side(2 * nc);
-  std::vector<std::vector<std::vector<int32_t>>> patches(2 * nc);
-  std::vector<double> coverage(nc, 0), rms(nc, 0);
+  std::vector<std::vector<int32_t>> side;
+  std::vector<std::vector<std::vector<int32_t>>> patches;
+  std::vector<double> coverage, rms;
   if (nc) {
     if (!nv || !nf) fail(SYM_INVALID_ARGUMENT, "verification requires a nonempty surface");
     if (g.normals.count != nv || g.weight_count != nv || g.neighbors.rows != nv)
@@ -371,91 +466,18 @@ void verification_host(Call &call, const sym_mesh_view &m, const sym_topology_vi
           uint64_t(m.faces.v0[f]) >= nv || uint64_t(m.faces.v1[f]) >= nv ||
           uint64_t(m.faces.v2[f]) >= nv)
         fail(SYM_INVALID_ARGUMENT, "Face index out of range");
-    HostBvh bvh(m);
-    if (2 * bvh.depth + 4 > kStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
-    Surface s;
-    s.xyz = upload_points(call, m.vertices);
-    s.nv = nv;
-    s.faces = upload_faces(call, m.faces);
-    s.nf = nf;
-    s.nodes = call.upload(bvh.nodes.data(), bvh.nodes.size());
-    s.ids = call.upload(bvh.ids.data(), bvh.ids.size());
+    double *xyz = upload_points(call, m.vertices);
+    int32_t *faces = upload_faces(call, m.faces);
     double *vn = upload_points(call, g.normals);
     double *w = call.upload(g.weights, nv);
     uint64_t nbr_count = g.neighbors.offsets[nv];
     uint64_t *nbr_off = call.upload(g.neighbors.offsets, nv + 1);
     int32_t *nbr = call.upload(g.neighbors.indices, nbr_count);
-    std::vector<ClusterMotion> motions(nc);
-    for (uint64_t c = 0; c < nc; ++c) {
-      const sym_cluster_record &r = cl.records[c];
-      for (int k = 0; k < 9; ++k) motions[c].r[k] = r.rotation[k];
-      for (int k = 0; k < 3; ++k) motions[c].t[k] = r.translation[k], motions[c].n[k] = r.plane_normal[k];
-      motions[c].offset = r.plane_offset;
-      motions[c].reflection = r.reflection != 0;
-    }
-    ClusterMotion *dm = call.upload(motions.data(), nc);
-    uint64_t rows = nc * 2 * nv;
-    uint8_t *flags = call.alloc<uint8_t>(rows);
-    double *err = call.alloc<double>(nc * nv);
-    double tau = o.verify_threshold * ctx.box_size;
-    verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, flags, err,
-                                                           call.status());
-    check_launch();
-    double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
-    uint64_t *na = call.alloc<uint64_t>(nc);
-    ordered_sums<<<blocks_for(nc + 1, 64), 64, 0, st>>>(flags, err, w, nv, nc, error, area, na, total);
-    check_launch();
-    // patches: union-find per (cluster, side)
-    int32_t *parent = call.alloc<int32_t>(rows);
-    init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
-    check_launch();
-    unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(nbr_off, nbr, nv, 2 * nc, parent, call.status());
-    check_launch();
-    uint64_t *keys = call.alloc<uint64_t>(rows), *skeys = call.alloc<uint64_t>(rows);
-    int32_t *vals = call.alloc<int32_t>(rows), *svals = call.alloc<int32_t>(rows);
-    uint8_t *allowed = call.alloc<uint8_t>(rows);
-    root_keys<<<blocks_for(rows), kThreads, 0, st>>>(parent, nv, 2 * nc, keys, vals, allowed);
-    check_launch();
-    // keep allowed entries only (order preserved), then sort by (set, root)
-    uint64_t *kept = call.alloc<uint64_t>(1);
-    int32_t *pos = call.alloc<int32_t>(rows);
-    compact_indices(call, allowed, rows, pos, kept);
-    uint64_t nkept = 0;
-    call.d2h(&nkept, kept, 8);
-    call.sync();
-    call.launched(5);
-    std::vector<uint64_t> hkeys(nkept);
-    std::vector<int32_t> hvals(nkept);
-    if (nkept) {
-      uint64_t *dk = call.alloc<uint64_t>(nkept);
-      int32_t *dv = call.alloc<int32_t>(nkept);
-      gather_kept<<<blocks_for(nkept), kThreads, 0, st>>>(pos, nkept, keys, nv, dk, dv);
-      check_launch();
-      int bits = 32;
-      while ((uint64_t(1) << (bits - 32)) < 2 * nc) ++bits;
-      radix_sort_pairs(call, dk, dv, skeys, svals, nkept, bits);
-      call.d2h(hkeys.data(), skeys, nkept * 8);
-      call.d2h(hvals.data(), svals, nkept * 4);
-    }
-    std::vector<double> herr(nc), harea(nc);
-    std::vector<uint64_t> hna(nc);
-    double htotal = 0;
-    call.d2h(herr.data(), error, nc * 8);
-    call.d2h(harea.data(), area, nc * 8);
-    call.d2h(hna.data(), na, nc * 8);
-    call.d2h(&htotal, total, 8);
-    call.check_status("verification");
-    for (uint64_t k = 0; k < nkept; ++k) {
-      uint64_t set = hkeys[k] >> 32;
-      side[set].push_back(hvals[k]);
-      if (k == 0 || hkeys[k] != hkeys[k - 1]) patches[set].emplace_back();
-      patches[set].back().push_back(hvals[k]);
-    }
-    for (auto &sv : side) std::sort(sv.begin(), sv.end());
-    for (uint64_t c = 0; c < nc; ++c) {
-      rms[c] = hna[c] ? std::sqrt(herr[c] / double(hna[c])) : 0;
-      coverage[c] = htotal > 0 ? std::min(1.0, harea[c] / htotal) : 0;
-    }
+    verification_core(call, m, xyz, faces, vn, w, nbr_off, nbr, cl.records, nc,
+                      o.verify_threshold * ctx.box_size, side, patches, coverage, rms);
+  } else {
+    side.assign(0, {});
+    patches.assign(0, {});
   }
   uint64_t na = 0, nb = 0, ra = 0, rb = 0;
   for (uint64_t c = 0; c < nc; ++c) {
