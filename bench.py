@@ -362,9 +362,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline estimate")
+    ap.add_argument("--bandwidth", type=float, default=None, help="override the bandwidth")
     ap.add_argument("--small", action="store_true",
                     help="level-5 mesh, 5,000 samples, 256 seeds (profiler captures)")
     args = ap.parse_args()
+    if args.bandwidth:
+        global BANDWIDTH
+        BANDWIDTH = args.bandwidth
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
         run_reference(args)

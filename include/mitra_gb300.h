@@ -326,6 +326,28 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
                            const sym_options *options,
                            const sym_fast_options *fast, sym_fast_result *out);
 
+/* The mean-shift kernels of sym_detect_fast on their own (no reference
+ * counterpart): K seeds over Q 6-D votes (host, q x 6 doubles), seeds are
+ * vote indices.  Writes the K final means (k x 6), each seed's state (0 still
+ * moving, 1 converged, 2 exhausted) and the bulk / polish iteration counts.
+ * `precision`: SYM_MS_FP32, SYM_MS_BF16_REFINED, or SYM_MS_FP64 (the FP64
+ * form used to measure mode errors). */
+enum { SYM_MS_FP64 = 2 };
+sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q,
+                          const int64_t *seeds, uint64_t k, double bandwidth,
+                          int32_t precision, int32_t max_iterations,
+                          int32_t polish_iterations, double *means_out,
+                          uint8_t *state_out, int32_t *iterations_out);
+
+/* Test hook for the tensor-core path of the BF16 mean-shift: one tile of
+ * D = A1 . B1^T (128x128, K=16) and ACC = A2 . B2^T (128x16, K=128) from
+ * row-major BF16 inputs (a1, b1: 128 x 16; a2: 128 x 128; b2: 16 x 128), run
+ * through the kernel's shared-memory layouts, TMA bulk copy, tcgen05.mma and
+ * TMEM loads.  d_out: 128 x 128 floats, acc_out: 128 x 16 floats. */
+sym_status sym_tc_selftest(sym_context *ctx, const uint16_t *a1, const uint16_t *b1,
+                           const uint16_t *a2, const uint16_t *b2, float *d_out,
+                           float *acc_out);
+
 /* --------------------------------------------------------------- metrics */
 /* Per-stage accounting, the fields of the reference CudaMetric
  * (include/symmetry/cuda.h:7-13, src/cuda/profile.cpp). */

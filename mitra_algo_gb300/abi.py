@@ -21,6 +21,7 @@ _d = C.POINTER(C.c_double)
 _i = C.POINTER(C.c_int32)
 _u8 = C.POINTER(C.c_uint8)
 _u64 = C.POINTER(C.c_uint64)
+_f = C.POINTER(C.c_float)
 
 
 class PointsView(C.Structure):
@@ -161,7 +162,7 @@ class FastResult(C.Structure):
                 ("rms", C.c_double * FAST_MAX_CLUSTERS)]
 
 
-MS_FP32, MS_BF16_REFINED = 0, 1
+MS_FP32, MS_BF16_REFINED, MS_FP64 = 0, 1, 2
 STAGES = ["curvature", "prune", "pairing", "votes", "vote_sort", "mean_shift", "modes",
           "verification"]
 
@@ -199,6 +200,10 @@ PROTOTYPES = [
     ("sym_detect_fast", C.c_int, [C.c_void_p, C.c_void_p, _i, C.c_uint64, P(Options),
                                   P(FastOptions), P(FastResult)]),
     ("sym_context_stream", C.c_void_p, [C.c_void_p]),
+    ("sym_meanshift6", C.c_int, [C.c_void_p, _d, C.c_uint64, P(C.c_int64), C.c_uint64, C.c_double,
+                                 C.c_int32, C.c_int32, C.c_int32, _d, _u8, P(C.c_int32)]),
+    ("sym_tc_selftest", C.c_int, [C.c_void_p, P(C.c_uint16), P(C.c_uint16), P(C.c_uint16),
+                                  P(C.c_uint16), _f, _f]),
     ("sym_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("sym_take_metrics", C.c_uint64, [C.c_void_p, P(Metric), C.c_uint64]),
 ]

@@ -183,6 +183,38 @@ class Gb300Backend:
         out["translation"] = [list(res.records[i].translation) for i in range(n)]
         return out
 
+    def meanshift6(self, votes, seeds, bandwidth, precision="fp32", max_iterations=100,
+                   polish_iterations=100):
+        """Mean-shift of the seed votes over 6-D votes (q x 6); returns the
+        final means (k x 6), per-seed state and the (bulk, polish) iteration
+        counts.  precision: "fp32", "bf16" (BF16 bulk + FP32 polish) or
+        "fp64"."""
+        v = np.ascontiguousarray(votes, np.float64).reshape(-1, 6)
+        s = np.ascontiguousarray(seeds, np.int64)
+        means = np.zeros((s.size, 6))
+        state = np.zeros(s.size, np.uint8)
+        iters = (C.c_int32 * 2)()
+        code = {"fp32": abi.MS_FP32, "bf16": abi.MS_BF16_REFINED, "fp64": abi.MS_FP64}[precision]
+        _check(self._lib.sym_meanshift6(self._ctx, v.ctypes.data_as(C.POINTER(C.c_double)),
+                                        v.shape[0], s.ctypes.data_as(C.POINTER(C.c_int64)), s.size,
+                                        bandwidth, code, max_iterations, polish_iterations,
+                                        means.ctypes.data_as(C.POINTER(C.c_double)),
+                                        state.ctypes.data_as(C.POINTER(C.c_uint8)), iters))
+        return means, state, (iters[0], iters[1])
+
+    def tc_selftest(self, a1, b1, a2, b2):
+        """Tensor-core path check: returns (A1 . B1^T, A2 . B2^T) computed by
+        tcgen05 from BF16 bit patterns (uint16 arrays 128x16, 128x16, 128x128,
+        16x128)."""
+        arrs = [np.ascontiguousarray(x, np.uint16) for x in (a1, b1, a2, b2)]
+        d = np.zeros((128, 128), np.float32)
+        acc = np.zeros((128, 16), np.float32)
+        p16 = C.POINTER(C.c_uint16)
+        _check(self._lib.sym_tc_selftest(self._ctx, *[x.ctypes.data_as(p16) for x in arrs],
+                                         d.ctypes.data_as(C.POINTER(C.c_float)),
+                                         acc.ctypes.data_as(C.POINTER(C.c_float))))
+        return d, acc
+
     def take_metrics(self):
         buf = (abi.Metric * 64)()
         n = self._lib.sym_take_metrics(self._ctx, buf, 64)

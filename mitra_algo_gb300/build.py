@@ -23,7 +23,7 @@ LIB = OUT / "libmitra_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units that keep FMA contraction (throughput kernels that are
 # not required to round like the reference's FP64 CPU code).
-FAST_UNITS = {"resident.cu", "meanshift_tc.cu"}
+FAST_UNITS = {"resident.cu", "meanshift_fast.cu", "meanshift_tc.cu"}
 
 
 def nvcc() -> str:

@@ -1,0 +1,436 @@
+// SPDX-License-Identifier: MPL-2.0
+// SIMT mean-shift (FP32 and FP64) over a Morton-chunked 6-D vote set.
+#include "meanshift_fast.cuh"
+#include "primitives.cuh"
+
+#include <algorithm>
+#include <cmath>
+
+namespace sym {
+namespace {
+
+// ------------------------------------------------------------ vote sort
+__global__ void box_partials(const float *desc, uint64_t q, float *partial) {
+  __shared__ float lo[6][256], hi[6][256];
+  float l[6], h[6];
+  for (int k = 0; k < 6; ++k) l[k] = INFINITY, h[k] = -INFINITY;
+  for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < q;
+       v += uint64_t(gridDim.x) * blockDim.x)
+    for (int k = 0; k < 6; ++k) {
+      float x = desc[v * 8 + k];
+      l[k] = fminf(l[k], x), h[k] = fmaxf(h[k], x);
+    }
+  for (int k = 0; k < 6; ++k) lo[k][threadIdx.x] = l[k], hi[k][threadIdx.x] = h[k];
+  __syncthreads();
+  for (int s = 128; s; s >>= 1) {
+    if (threadIdx.x < s)
+      for (int k = 0; k < 6; ++k) {
+        lo[k][threadIdx.x] = fminf(lo[k][threadIdx.x], lo[k][threadIdx.x + s]);
+        hi[k][threadIdx.x] = fmaxf(hi[k][threadIdx.x], hi[k][threadIdx.x + s]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k)
+      partial[blockIdx.x * 12 + k] = lo[k][0], partial[blockIdx.x * 12 + 6 + k] = hi[k][0];
+}
+
+__global__ void box_final(const float *partial, int n, float *box) {
+  int k = threadIdx.x;
+  if (k >= 12) return;
+  float v = k < 6 ? INFINITY : -INFINITY;
+  for (int i = 0; i < n; ++i) v = k < 6 ? fminf(v, partial[i * 12 + k]) : fmaxf(v, partial[i * 12 + k]);
+  box[k] = v;
+}
+
+__device__ __forceinline__ uint64_t morton6(const float *x, const float *box) {
+  uint64_t key = 0;
+  for (int k = 0; k < 6; ++k) {
+    float lo = box[k], span = box[6 + k] - lo;
+    float t = span > 0 ? (x[k] - lo) / span : 0.f;
+    uint64_t cell = uint64_t(min(1023, max(0, int(t * 1024.f))));
+    for (int b = 0; b < 10; ++b) key |= ((cell >> b) & 1ull) << (6 * b + k);
+  }
+  return key;
+}
+
+__global__ void morton_keys(const float *desc, uint64_t q, const float *box, uint64_t *keys,
+                            int32_t *idx) {
+  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= q) return;
+  keys[v] = morton6(desc + v * 8, box);
+  idx[v] = int32_t(v);
+}
+
+template <typename T>
+__global__ void permute(const T *src, const int32_t *order, uint64_t q, T *dst) {
+  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= q) return;
+  uint64_t from = uint64_t(uint32_t(order[v]));
+  for (int k = 0; k < 8; ++k) dst[v * 8 + k] = src[from * 8 + k];
+}
+
+__global__ void invert(const int32_t *order, uint64_t q, int32_t *rank) {
+  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v < q) rank[order[v]] = int32_t(v);
+}
+
+// One warp per chunk: [lo0..lo5, hi0..hi5].
+__global__ void chunk_boxes(const float *desc, uint64_t q, uint64_t nchunks, float *cbox) {
+  uint64_t c = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (c >= nchunks) return;
+  float l[6], h[6];
+  for (int k = 0; k < 6; ++k) l[k] = INFINITY, h[k] = -INFINITY;
+  for (int j = lane; j < kChunk; j += 32) {
+    uint64_t v = c * kChunk + j;
+    if (v >= q) break;
+    for (int k = 0; k < 6; ++k) {
+      float x = desc[v * 8 + k];
+      l[k] = fminf(l[k], x), h[k] = fmaxf(h[k], x);
+    }
+  }
+  for (int o = 16; o; o >>= 1)
+    for (int k = 0; k < 6; ++k) {
+      l[k] = fminf(l[k], __shfl_xor_sync(0xffffffffu, l[k], o));
+      h[k] = fmaxf(h[k], __shfl_xor_sync(0xffffffffu, h[k], o));
+    }
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k) cbox[c * 12 + k] = l[k], cbox[c * 12 + 6 + k] = h[k];
+}
+
+// ------------------------------------------------------------ mean shift
+__device__ __forceinline__ float box_gap2(const float *a_lo, const float *a_hi, const float *b) {
+  float g = 0;
+  for (int k = 0; k < 6; ++k) {
+    float d = fmaxf(fmaxf(b[k] - a_hi[k], a_lo[k] - b[6 + k]), 0.f);
+    g += d * d;
+  }
+  return g;
+}
+
+// One block = one tile of up to kChunk active seeds (ids[tile*kChunk + t])
+// x one split of the chunk range.  Each thread accumulates, for its seed,
+// sum w x and sum w over the votes of the chunks its tile cannot skip.
+// COUNT: count the votes within the bandwidth instead.
+template <typename T, bool COUNT>
+__global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cbox, uint64_t nchunks,
+                                                  uint64_t q, const T *means, const int32_t *ids,
+                                                  uint64_t nactive, T h2, float skip_gap2,
+                                                  uint64_t chunks_per_split, T *partial,
+                                                  unsigned long long *evals) {
+  __shared__ T xs[kChunk * 8];
+  __shared__ float tlo[6][4], thi[6][4];
+  uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x, split = blockIdx.y;
+  uint64_t slots = uint64_t(gridDim.x) * kChunk;
+  bool live = slot < nactive;
+  int32_t seed = live ? ids[slot] : 0;
+  T m[6];
+  for (int d = 0; d < 6; ++d) m[d] = live ? means[uint64_t(seed) * 8 + d] : T(0);
+  float lo[6], hi[6];
+  for (int d = 0; d < 6; ++d) {
+    lo[d] = live ? float(m[d]) : INFINITY;
+    hi[d] = live ? float(m[d]) : -INFINITY;
+  }
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o; o >>= 1)
+    for (int d = 0; d < 6; ++d) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+  if (lane == 0)
+    for (int d = 0; d < 6; ++d) tlo[d][warp] = lo[d], thi[d][warp] = hi[d];
+  __syncthreads();
+  for (int d = 0; d < 6; ++d) {
+    lo[d] = fminf(fminf(tlo[d][0], tlo[d][1]), fminf(tlo[d][2], tlo[d][3]));
+    hi[d] = fmaxf(fmaxf(thi[d][0], thi[d][1]), fmaxf(thi[d][2], thi[d][3]));
+  }
+  T acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  uint64_t c0 = split * chunks_per_split;
+  uint64_t c1 = c0 + chunks_per_split < nchunks ? c0 + chunks_per_split : nchunks;
+  unsigned long long done = 0;
+  for (uint64_t c = c0; c < c1; ++c) {
+    if (box_gap2(lo, hi, cbox + c * 12) > skip_gap2) continue;
+    __syncthreads();
+    uint64_t v = c * kChunk + threadIdx.x;
+    for (int d = 0; d < 8; ++d) xs[threadIdx.x * 8 + d] = v < q ? desc[v * 8 + d] : T(1e30);
+    __syncthreads();
+    uint64_t rest = q - c * kChunk;
+    int n = rest < uint64_t(kChunk) ? int(rest) : kChunk;
+    done += n;
+    for (int j = 0; j < n; ++j) {
+      T d2 = 0;
+#pragma unroll
+      for (int d = 0; d < 6; ++d) {
+        T e = m[d] - xs[j * 8 + d];
+        d2 += e * e;
+      }
+      if (d2 < h2) {
+        if (COUNT) {
+          acc[6] += T(1);
+        } else {
+          T w = T(1) - d2 / h2;
+#pragma unroll
+          for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
+          acc[6] += w;
+        }
+      }
+    }
+  }
+  for (int d = 0; d < 7; ++d) partial[(split * slots + slot) * 8 + d] = acc[d];
+  if (threadIdx.x == 0 && done && evals) atomicAdd(evals, done * (unsigned long long)kChunk);
+}
+
+// Sum of the splits (fixed order) then the Epanechnikov mean-shift step and
+// the reference's stopping rules: exhausted when the weight is <= 1e-14,
+// converged when the squared movement is < 1e-6 h^2.
+template <typename T>
+__global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t slots,
+                          const int32_t *ids, uint64_t nactive, T h2, uint8_t *state) {
+  uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (slot >= nactive) return;
+  int32_t s = ids[slot];
+  T acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint64_t p = 0; p < splits; ++p)
+    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * slots + slot) * 8 + d];
+  if (acc[6] <= T(1e-14)) {
+    state[s] = 2;
+    return;
+  }
+  T move = 0;
+  for (int d = 0; d < 6; ++d) {
+    T nx = acc[d] / acc[6];
+    T e = means[uint64_t(s) * 8 + d] - nx;
+    move += e * e;
+    means[uint64_t(s) * 8 + d] = nx;
+  }
+  if (move < T(1e-6) * h2) state[s] = 1;
+}
+
+constexpr int kRetile = 2048;  // seeds sorted in one block (static shared memory)
+
+// Active seeds (state 0) in seed order, then sorted by the Morton key of
+// their current mean (ties by seed id) when k <= kRetile.
+template <typename T>
+__global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *state, uint64_t k,
+                                               const float *box, int32_t *ids, unsigned *nactive) {
+  __shared__ unsigned long long keys[kRetile];
+  __shared__ int32_t vals[kRetile];
+  __shared__ unsigned warp_tot[32];
+  __shared__ unsigned base_s;
+  if (threadIdx.x == 0) base_s = 0;
+  __syncthreads();
+  bool sort = k <= kRetile;
+  for (uint64_t at = 0; at < k; at += blockDim.x) {
+    uint64_t s = at + threadIdx.x;
+    bool act = s < k && state[s] == 0;
+    unsigned bal = __ballot_sync(0xffffffffu, act);
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_tot[warp] = __popc(bal);
+    __syncthreads();
+    unsigned before = 0, total = 0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+      if (w < warp) before += warp_tot[w];
+      total += warp_tot[w];
+    }
+    unsigned pos = base_s + before + __popc(bal & ((1u << lane) - 1));
+    if (act) {
+      if (sort) {
+        float x[6];
+        for (int d = 0; d < 6; ++d) x[d] = float(means[s * 8 + d]);
+        keys[pos] = morton6(x, box);
+        vals[pos] = int32_t(s);
+      } else {
+        ids[pos] = int32_t(s);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base_s += total;
+    __syncthreads();
+  }
+  unsigned n = base_s;
+  if (sort) {
+    unsigned p2 = 1;
+    while (p2 < n) p2 <<= 1;
+    for (unsigned i = n + threadIdx.x; i < p2; i += blockDim.x) keys[i] = ~0ull, vals[i] = 0x7fffffff;
+    __syncthreads();
+    for (unsigned size = 2; size <= p2; size <<= 1)
+      for (unsigned stride = size >> 1; stride; stride >>= 1) {
+        for (unsigned i = threadIdx.x; i < p2; i += blockDim.x) {
+          unsigned j = i ^ stride;
+          if (j > i) {
+            bool up = (i & size) == 0;
+            bool gt = keys[i] > keys[j] || (keys[i] == keys[j] && vals[i] > vals[j]);
+            if (gt == up) {
+              unsigned long long tk = keys[i];
+              keys[i] = keys[j], keys[j] = tk;
+              int32_t tv = vals[i];
+              vals[i] = vals[j], vals[j] = tv;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) ids[i] = vals[i];
+  }
+  if (threadIdx.x == 0) *nactive = n;
+}
+
+template <typename T>
+__global__ void gather_seeds(const T *desc, const int64_t *pos, uint64_t k, T *means) {
+  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  for (int d = 0; d < 8; ++d) means[i * 8 + d] = desc[uint64_t(pos[i]) * 8 + d];
+}
+
+__global__ void sum_counts(const float *partial, uint64_t splits, uint64_t slots, const int32_t *ids,
+                           uint64_t n, unsigned long long *counts) {
+  uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (slot >= n) return;
+  unsigned long long c = 0;
+  for (uint64_t p = 0; p < splits; ++p) c += (unsigned long long)partial[(p * slots + slot) * 8 + 6];
+  counts[ids[slot]] = c;
+}
+
+struct Grid {
+  uint64_t tiles, splits, cps, slots;
+};
+
+Grid grid_for(uint64_t nactive, uint64_t nchunks) {
+  Grid g;
+  g.tiles = (nactive + kChunk - 1) / kChunk;
+  uint64_t want = (64 * 152 + g.tiles - 1) / g.tiles;
+  g.splits = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, want));
+  g.cps = (nchunks + g.splits - 1) / g.splits;
+  g.splits = (nchunks + g.cps - 1) / g.cps;
+  g.slots = g.tiles * kChunk;
+  return g;
+}
+
+template <typename T>
+int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *state, uint64_t k,
+               double h2, int max_iter, double *seed_iterations, unsigned long long *evals) {
+  cudaStream_t st = call.stream();
+  int32_t *ids = call.alloc<int32_t>(k);
+  unsigned *nact = call.alloc<unsigned>(1);
+  // partial capacity: splits x slots is at most ~64*152*kChunk (+ one tile)
+  uint64_t cap = (64 * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
+  T *partial = call.alloc<T>(cap * 8);
+  float gap = float(std::sqrt(h2)) + 1e-6f;
+  int it = 0;
+  for (; it < max_iter; ++it) {
+    retile<T><<<1, 1024, 0, st>>>(means, state, k, v.gbox, ids, nact);
+    check_launch();
+    unsigned n = 0;
+    SYM_CUDA(cudaMemcpyAsync(&n, nact, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    call.sync();
+    call.launched();
+    if (!n) break;
+    if (seed_iterations) *seed_iterations += n;
+    Grid g = grid_for(n, v.nchunks);
+    if (g.splits * g.slots > cap) fail(SYM_RUNTIME_ERROR, "mean-shift partial buffer too small");
+    ms_tile<T, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
+        desc, v.cbox, v.nchunks, v.q, means, ids, n, T(h2), gap * gap, g.cps, partial, evals);
+    check_launch();
+    ms_update<T><<<blocks_for(n), kThreads, 0, st>>>(means, partial, g.splits, g.slots, ids, n,
+                                                     T(h2), state);
+    check_launch();
+    call.launched(2);
+  }
+  return it;
+}
+
+}  // namespace
+
+VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_raw, uint64_t q) {
+  cudaStream_t st = call.stream();
+  VoteSet v;
+  v.q = q;
+  v.nchunks = (q + kChunk - 1) / kChunk;
+  const int kBoxBlocks = 256;
+  float *bpart = call.alloc<float>(kBoxBlocks * 12);
+  v.gbox = call.alloc<float>(12);
+  box_partials<<<kBoxBlocks, 256, 0, st>>>(desc_raw, q, bpart);
+  check_launch();
+  box_final<<<1, 32, 0, st>>>(bpart, kBoxBlocks, v.gbox);
+  check_launch();
+  uint64_t *keys = call.alloc<uint64_t>(q), *skeys = call.alloc<uint64_t>(q);
+  int32_t *idx = call.alloc<int32_t>(q);
+  v.order = call.alloc<int32_t>(q);
+  v.rank = call.alloc<int32_t>(q);
+  morton_keys<<<blocks_for(q), kThreads, 0, st>>>(desc_raw, q, v.gbox, keys, idx);
+  check_launch();
+  radix_sort_pairs(call, keys, idx, skeys, v.order, q, 60);
+  invert<<<blocks_for(q), kThreads, 0, st>>>(v.order, q, v.rank);
+  check_launch();
+  v.desc = call.alloc<float>(q * 8);
+  permute<float><<<blocks_for(q), kThreads, 0, st>>>(desc_raw, v.order, q, v.desc);
+  check_launch();
+  if (desc64_raw) {
+    v.desc64 = call.alloc<double>(q * 8);
+    permute<double><<<blocks_for(q), kThreads, 0, st>>>(desc64_raw, v.order, q, v.desc64);
+    check_launch();
+  }
+  v.cbox = call.alloc<float>(v.nchunks * 12);
+  chunk_boxes<<<blocks_for(v.nchunks * 32), kThreads, 0, st>>>(v.desc, q, v.nchunks, v.cbox);
+  check_launch();
+  call.launched(desc64_raw ? 8 : 7);
+  return v;
+}
+
+void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, float *means) {
+  gather_seeds<float><<<blocks_for(k), kThreads, 0, call.stream()>>>(v.desc, seed_rank, k, means);
+  check_launch();
+  call.launched();
+}
+
+void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, double *means) {
+  gather_seeds<double><<<blocks_for(k), kThreads, 0, call.stream()>>>(v.desc64, seed_rank, k, means);
+  check_launch();
+  call.launched();
+}
+
+int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k, double h2,
+          int max_iter, double *seed_iterations, unsigned long long *evals) {
+  return shift_impl<float>(call, v, v.desc, means, state, k, h2, max_iter, seed_iterations, evals);
+}
+
+int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,
+          int max_iter, double *seed_iterations, unsigned long long *evals) {
+  return shift_impl<double>(call, v, v.desc64, means, state, k, h2, max_iter, seed_iterations, evals);
+}
+
+unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
+                      uint64_t k, int32_t *ids) {
+  unsigned *nact = call.alloc<unsigned>(1);
+  retile<float><<<1, 1024, 0, call.stream()>>>(means, state, k, v.gbox, ids, nact);
+  check_launch();
+  call.launched();
+  unsigned n = 0;
+  SYM_CUDA(cudaMemcpyAsync(&n, nact, sizeof(unsigned), cudaMemcpyDeviceToHost, call.stream()));
+  call.sync();
+  return n;
+}
+
+void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm, double h2,
+                  unsigned long long *counts) {
+  if (!nm) return;
+  cudaStream_t st = call.stream();
+  uint8_t *state = call.alloc<uint8_t>(nm);
+  SYM_CUDA(cudaMemsetAsync(state, 0, nm, st));
+  int32_t *ids = call.alloc<int32_t>(nm);
+  unsigned *nact = call.alloc<unsigned>(1);
+  retile<float><<<1, 1024, 0, st>>>(points, state, nm, v.gbox, ids, nact);
+  check_launch();
+  Grid g = grid_for(nm, v.nchunks);
+  float *partial = call.alloc<float>(g.splits * g.slots * 8);
+  float gap = float(std::sqrt(h2)) + 1e-6f;
+  ms_tile<float, true><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
+      v.desc, v.cbox, v.nchunks, v.q, points, ids, nm, float(h2), gap * gap, g.cps, partial, nullptr);
+  check_launch();
+  sum_counts<<<blocks_for(nm), kThreads, 0, st>>>(partial, g.splits, g.slots, ids, nm, counts);
+  check_launch();
+  call.launched(3);
+}
+
+}  // namespace sym

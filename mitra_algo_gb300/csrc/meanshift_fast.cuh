@@ -1,0 +1,53 @@
+// SPDX-License-Identifier: MPL-2.0
+// Mean-shift of K seeds over a large set of 6-D votes (throughput path, no
+// reference counterpart beyond the Epanechnikov update and the stopping
+// rules of src/cpu/clustering.cpp:156-208).
+//
+// Votes are stored 8 values per vote (6 coordinates, |x|^2, padding), sorted
+// along a 6-D Morton curve and cut into chunks of kChunk votes with bounding
+// boxes.  Seeds are processed in tiles of kChunk active seeds re-sorted along
+// the same curve every iteration; a (tile, chunk) pair whose boxes are more
+// than the bandwidth apart is skipped, which is exact for Epanechnikov
+// weights (they vanish beyond the bandwidth).
+#pragma once
+#include "common.cuh"
+
+namespace sym {
+
+constexpr int kChunk = 128;  // votes per chunk = seeds per tile
+
+struct VoteSet {
+  uint64_t q = 0, nchunks = 0;
+  float *desc = nullptr;      // q x 8, Morton order
+  double *desc64 = nullptr;   // q x 8, same order (only when requested)
+  float *cbox = nullptr;      // nchunks x 12: lo[6], hi[6]
+  float *gbox = nullptr;      // 12: box of all votes
+  int32_t *order = nullptr;   // sorted position -> original vote
+  int32_t *rank = nullptr;    // original vote -> sorted position
+};
+
+// Sorts raw votes (q x 8; desc64_raw may be null) into a VoteSet.
+VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_raw, uint64_t q);
+
+// Seeds: sorted positions of the seed votes -> initial means (k x 8).
+void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, float *means);
+void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, double *means);
+
+// Iterates until every seed converged/exhausted or max_iter; state[k] in/out
+// (0 moving, 1 converged, 2 exhausted).  Adds the seed-iterations to
+// *seed_iterations and seed-vote evaluations to *evals (device counter).
+int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k, double h2,
+          int max_iter, double *seed_iterations, unsigned long long *evals);
+int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,
+          int max_iter, double *seed_iterations, unsigned long long *evals);
+
+// Active seeds (state 0), Morton-sorted by position when k <= 2048; returns
+// their number (synchronises).
+unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
+                      uint64_t k, int32_t *ids);
+
+// Number of votes within the bandwidth of each of `nm` points (nm x 8).
+void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm, double h2,
+                  unsigned long long *counts);
+
+}  // namespace sym

@@ -1,10 +1,603 @@
 // SPDX-License-Identifier: MPL-2.0
-// BF16 tensor-core mean-shift bulk iterations (tcgen05 + TMEM).
-#include "common.cuh"
+// BF16 tensor-core mean-shift bulk iterations on sm_103a (tcgen05 + TMEM).
+//
+// Flash-style: per (tile of 128 seeds, chunk of 128 votes)
+//   MMA1  D[128x128] = S'[128x16] . X'[128x16]^T      (seed-vote dot products)
+//   epilogue: tcgen05.ld D, w = max(0, 1 - (|s'|^2 + |x'|^2 - 2 s'.x') / h^2)
+//             (Epanechnikov), written as BF16 into shared memory
+//   MMA2  ACC[128x16] += W[128x128] . X'[128x16]        (weighted sums)
+// S' and X' are centred on the chunk's centre c (X' once per vote set, S' per
+// chunk), which keeps |s'|, |x'| small so the expanded distance does not lose
+// its digits in BF16; sum w x = ACC + c sum w, with sum w kept in FP32.
+// Votes are pre-arranged per chunk in the canonical no-swizzle K-major
+// core-matrix layout (8 rows x 16 bytes per core matrix), so one TMA bulk copy
+// (cp.async.bulk + mbarrier complete_tx) stages a chunk.  Accumulators live
+// in TMEM (256 columns per CTA: D at 0..127, ACC at 128..143).  Every
+// mbarrier wait is bounded; on timeout the CTA records a status, drains and
+// frees its TMEM.
+#include "meanshift_fast.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
 
 namespace sym {
-bool meanshift_bf16_bulk(Call &, const float *, const float *, uint64_t, uint64_t, float *,
-                         uint8_t *, uint64_t, float, int, int *, double *) {
+namespace {
+
+// --------------------------------------------------------------- PTX glue
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+// Bounded wait: false when the barrier phase never completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
+
+__device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, uint32_t bytes,
+                                              uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// Whole warp: allocate `cols` TMEM columns, address written to shared memory.
+__device__ __forceinline__ void tmem_alloc(uint32_t *dst, uint32_t cols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                   smem_u32(dst)),
+               "r"(cols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t cols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols)
+               : "memory");
+}
+
+// Shared-memory matrix descriptor (sm_100 family): start address, leading
+// (K-direction core-matrix) byte offset, stride (M/N-direction 8-row group)
+// byte offset, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(const void *p, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t(smem_u32(p)) >> 4) & 0x3FFFull;
+  d |= uint64_t((lbo >> 4) & 0x3FFFu) << 16;
+  d |= uint64_t((sbo >> 4) & 0x3FFFu) << 32;
+  d |= uint64_t(1) << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::f16: F32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ------------------------------------------------------------- layouts
+// Canonical no-swizzle K-major tile of 16-bit elements: core matrices of 8
+// rows x 8 elements (16 bytes per row), `lbo` bytes between K-adjacent core
+// matrices, `sbo` bytes between row groups.
+__host__ __device__ constexpr uint32_t kmajor_offset(uint32_t row, uint32_t k, uint32_t lbo,
+                                                     uint32_t sbo) {
+  return (row / 8) * sbo + (k / 8) * lbo + (row % 8) * 16 + (k % 8) * 2;
+}
+
+// Chunk image: B1 (X' as 128 votes x 16 features, LBO 128, SBO 256), B2 (X'^T
+// as 16 features x 128 votes, LBO 128, SBO 2048), |x'|^2 (128 floats).
+constexpr uint32_t kB1Bytes = 4096, kB2Bytes = 4096, kXXBytes = 512;
+constexpr uint32_t kImage = kB1Bytes + kB2Bytes + kXXBytes;  // 8704, 16-byte multiple
+
+__global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, const float *cbox,
+                             uint8_t *images, float *centers) {
+  uint64_t c = blockIdx.x;
+  int t = threadIdx.x;  // vote in chunk
+  if (c >= nchunks) return;
+  const float *b = cbox + c * 12;
+  float cen[6];
+  for (int d = 0; d < 6; ++d) cen[d] = 0.5f * (b[d] + b[6 + d]);
+  if (t < 6) centers[c * 8 + t] = cen[t];
+  if (t >= 6 && t < 8) centers[c * 8 + t] = 0.f;
+  uint64_t v = c * kChunk + t;
+  uint8_t *img = images + c * kImage;
+  __nv_bfloat16 *b1 = reinterpret_cast<__nv_bfloat16 *>(img);
+  __nv_bfloat16 *b2 = reinterpret_cast<__nv_bfloat16 *>(img + kB1Bytes);
+  float *xx = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes);
+  float n2 = 0;
+  for (int k = 0; k < 16; ++k) {
+    float x = 0;
+    if (k < 6 && v < q) x = desc[v * 8 + k] - cen[k];
+    __nv_bfloat16 h = __float2bfloat16_rn(x);
+    float r = __bfloat162float(h);
+    n2 += r * r;
+    b1[kmajor_offset(t, k, 128, 256) / 2] = h;
+    b2[kmajor_offset(k, t, 128, 2048) / 2] = h;
+  }
+  xx[t] = v < q ? n2 : 1e30f;  // padding votes sit infinitely far away
+}
+
+struct TcArgs {
+  const uint8_t *images;
+  const float *centers;  // nchunks x 8
+  const float *cbox;     // nchunks x 12
+  uint64_t nchunks;
+  const float *means;    // k x 8
+  const int32_t *ids;
+  uint64_t nactive;
+  float inv_h2, skip_gap2;
+  uint64_t chunks_per_split;
+  float *partial;        // splits x slots x 8
+  unsigned long long *evals;
+  int *status;
+};
+
+// Dynamic shared memory layout (bytes).
+constexpr uint32_t kOffA1 = 0, kOffA2 = 4096, kOffStage = 4096 + 32768;
+constexpr uint32_t kOffBars = kOffStage + 2 * kImage;  // 54272
+constexpr uint32_t kOffMisc = kOffBars + 64;
+constexpr uint32_t kOffRed = kOffMisc + 64;            // 128 rows x 8 floats
+constexpr uint32_t kSmemUsed = kOffRed + 128 * 8 * 4;
+static_assert(kSmemUsed <= 100 * 1024, "shared memory plan exceeds the request");
+// Two CTAs per SM: their 2 x 256 TMEM columns fill the SM's 512 exactly.
+constexpr uint32_t kSmemRequest = 100 * 1024;
+constexpr uint32_t kTmemCols = 256, kColD = 0, kColAcc = 128;
+
+__device__ __forceinline__ float box_gap2_tc(const float *lo, const float *hi, const float *b) {
+  float g = 0;
+  for (int k = 0; k < 6; ++k) {
+    float d = fmaxf(fmaxf(b[k] - hi[k], lo[k] - b[6 + k]), 0.f);
+    g += d * d;
+  }
+  return g;
+}
+
+__global__ void __launch_bounds__(256, 2) ms_tile_tc(TcArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t *A1 = smem + kOffA1, *A2 = smem + kOffA2;
+  uint8_t *stage[2] = {smem + kOffStage, smem + kOffStage + kImage};
+  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + kOffBars);  // [2]
+  uint64_t *bar_mma1 = bar_load + 2, *bar_mma2 = bar_load + 3;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kOffMisc);
+  float *tile_box = reinterpret_cast<float *>(smem + kOffMisc + 16);  // written by warp 0: 12
+  float *red = reinterpret_cast<float *>(smem + kOffRed);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wg = warp >> 2, quad = warp & 3, row = quad * 32 + lane;
+  const uint64_t slot = uint64_t(blockIdx.x) * kChunk + row, split = blockIdx.y;
+  const uint64_t slots = uint64_t(gridDim.x) * kChunk;
+  const bool live = slot < a.nactive;
+  float m[6];
+  {
+    int32_t seed = live ? a.ids[slot] : 0;
+    for (int d = 0; d < 6; ++d) m[d] = live ? a.means[uint64_t(seed) * 8 + d] : 0.f;
+  }
+  // tile box over live seeds (warpgroup 0 covers every row once)
+  if (wg == 0) {
+    float lo[6], hi[6];
+    for (int d = 0; d < 6; ++d) lo[d] = live ? m[d] : INFINITY, hi[d] = live ? m[d] : -INFINITY;
+    for (int o = 16; o; o >>= 1)
+      for (int d = 0; d < 6; ++d) {
+        lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+        hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+      }
+    if (lane == 0)
+      for (int d = 0; d < 6; ++d) red[quad * 12 + d] = lo[d], red[quad * 12 + 6 + d] = hi[d];
+  }
+  if (tid == 0) {
+    mbar_init(&bar_load[0], 1);
+    mbar_init(&bar_load[1], 1);
+    mbar_init(bar_mma1, 1);
+    mbar_init(bar_mma2, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+  __syncthreads();
+  if (tid < 12) {
+    float v = red[tid];
+    for (int qd = 1; qd < 4; ++qd) v = tid < 6 ? fminf(v, red[qd * 12 + tid]) : fmaxf(v, red[qd * 12 + tid]);
+    tile_box[tid] = v;
+  }
+  tc_fence_after();
+  __syncthreads();
+  const uint32_t tmem = *tmem_slot;
+  float tlo[6], thi[6];
+  for (int d = 0; d < 6; ++d) tlo[d] = tile_box[d], thi[d] = tile_box[6 + d];
+
+  const uint64_t c0 = split * a.chunks_per_split;
+  const uint64_t c1 = c0 + a.chunks_per_split < a.nchunks ? c0 + a.chunks_per_split : a.nchunks;
+  auto next_needed = [&](uint64_t c) {
+    while (c < c1 && box_gap2_tc(tlo, thi, a.cbox + c * 12) > a.skip_gap2) ++c;
+    return c;
+  };
+  const float inv_h2 = a.inv_h2, two_inv_h2 = 2.f * a.inv_h2;
+  float sumw = 0, corr[6] = {0, 0, 0, 0, 0, 0};
+  bool ok = true;
+  uint64_t processed = 0;
+  uint64_t c = next_needed(c0);
+  // issued[b] / consumed[b]: loads issued into / waited on buffer b
+  uint32_t issued[2] = {0, 0}, consumed[2] = {0, 0}, mma_issued = 0, mma_done = 0;
+  if (tid == 0 && c < c1) {
+    mbar_expect_tx(&bar_load[0], kImage);
+    tma_bulk_load(stage[0], a.images + c * kImage, kImage, &bar_load[0]);
+  }
+  if (c < c1) issued[0] = 1;
+  uint32_t i = 0;
+  for (; c < c1 && ok; ++i) {
+    const uint32_t buf = i & 1;
+    const uint64_t cn = next_needed(c + 1);
+    if (tid == 0 && cn < c1) {  // prefetch the next needed chunk
+      mbar_expect_tx(&bar_load[buf ^ 1], kImage);
+      tma_bulk_load(stage[buf ^ 1], a.images + cn * kImage, kImage, &bar_load[buf ^ 1]);
+    }
+    if (cn < c1) ++issued[buf ^ 1];
+    // A1: this tile's seeds centred on the chunk, BF16, 16 features
+    const float *cen = a.centers + c * 8;
+    float sp[6], ss = 0;
+    for (int d = 0; d < 6; ++d) {
+      float r = __bfloat162float(__float2bfloat16_rn(m[d] - cen[d]));
+      sp[d] = r;
+      ss += r * r;
+    }
+    if (wg == 0) {
+      __align__(16) __nv_bfloat16 h[16];
+      for (int k = 0; k < 16; ++k) h[k] = __float2bfloat16_rn(k < 6 ? sp[k] : 0.f);
+      *reinterpret_cast<uint4 *>(A1 + kmajor_offset(row, 0, 128, 256)) = *reinterpret_cast<uint4 *>(&h[0]);
+      *reinterpret_cast<uint4 *>(A1 + kmajor_offset(row, 8, 128, 256)) = *reinterpret_cast<uint4 *>(&h[8]);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (!__syncthreads_and(mbar_wait(&bar_load[buf], (i >> 1) & 1))) {
+      ok = false;
+      break;
+    }
+    ++consumed[buf];
+    if (tid == 0) {
+      mma_bf16(tmem + kColD, smem_desc(A1, 128, 256), smem_desc(stage[buf], 128, 256),
+               idesc_bf16(128, 128), 0);
+      mma_commit(bar_mma1);
+    }
+    ++mma_issued;
+    if (!__syncthreads_and(mbar_wait(bar_mma1, i & 1))) {
+      ok = false;
+      break;
+    }
+    tc_fence_after();
+    // epilogue: 64 columns of this thread's row
+    const float *xx = reinterpret_cast<const float *>(stage[buf] + kB1Bytes + kB2Bytes);
+    const float rowc = 1.f - ss * inv_h2;
+    float sw = 0;
+    for (int half = 0; half < 2; ++half) {
+      const uint32_t col = 64 * wg + 32 * half;
+      float dot[32];
+      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kColD + col, dot);
+      __align__(16) __nv_bfloat16 w[32];
+      for (int j = 0; j < 32; ++j) {
+        float t = fmaf(dot[j], two_inv_h2, fmaf(xx[col + j], -inv_h2, rowc));
+        float wj = fmaxf(t, 0.f);
+        sw += wj;
+        w[j] = __float2bfloat16_rn(wj);
+      }
+      for (int kb = 0; kb < 4; ++kb)
+        *reinterpret_cast<uint4 *>(A2 + kmajor_offset(row, col + 8 * kb, 128, 2048)) =
+            *reinterpret_cast<uint4 *>(&w[8 * kb]);
+    }
+    sumw += sw;
+    for (int d = 0; d < 6; ++d) corr[d] = fmaf(cen[d], sw, corr[d]);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+      for (uint32_t s = 0; s < 8; ++s)
+        mma_bf16(tmem + kColAcc, smem_desc(A2 + s * 256, 128, 2048),
+                 smem_desc(stage[buf] + kB1Bytes + s * 256, 128, 2048), idesc_bf16(128, 16),
+                 (processed > 0 || s > 0) ? 1u : 0u);
+      mma_commit(bar_mma2);
+    }
+    ++mma_issued;
+    if (!__syncthreads_and(mbar_wait(bar_mma2, i & 1))) {
+      ok = false;
+      break;
+    }
+    mma_done = mma_issued;
+    tc_fence_after();
+    ++processed;
+    c = cn;
+  }
+  if (!ok && tid == 0) {
+    // Drain: wait (bounded) for every copy and MMA still in flight before
+    // the shared memory and TMEM of this CTA are released.
+    for (uint32_t b = 0; b < 2; ++b)
+      for (uint32_t n = consumed[b]; n < issued[b]; ++n) mbar_wait(&bar_load[b], n & 1);
+    if (mma_issued > mma_done) {
+      mbar_wait(bar_mma1, (mma_done / 2) & 1);
+      mbar_wait(bar_mma2, (mma_done / 2) & 1);
+    }
+  }
+  // combine: warpgroup 1 hands its FP32 parts to warpgroup 0
+  __syncthreads();
+  if (wg == 1) {
+    red[row * 8 + 6] = sumw;
+    for (int d = 0; d < 6; ++d) red[row * 8 + d] = corr[d];
+  }
+  __syncthreads();
+  if (wg == 0) {
+    float acc[32];
+    if (processed && ok) {
+      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kColAcc, acc);
+    } else {
+      for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+    }
+    float *out = a.partial + (split * slots + slot) * 8;
+    for (int d = 0; d < 6; ++d) out[d] = acc[d] + corr[d] + red[row * 8 + d];
+    out[6] = sumw + red[row * 8 + 6];
+    out[7] = 0.f;
+  }
+  if (tid == 0) {
+    if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
+    if (processed && a.evals) atomicAdd(a.evals, processed * (unsigned long long)(kChunk * kChunk));
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+// ------------------------------------------------------ tensor self-test
+// One tile: D = A1 . B1^T (128 x 128 x 16) and ACC = A2 . B2^T (128 x 16 x
+// 128) from row-major BF16 inputs, through the same layouts, TMA, MMA and
+// TMEM path as ms_tile_tc.
+__global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, const __nv_bfloat16 *b1,
+                                                      const __nv_bfloat16 *a2, const __nv_bfloat16 *b2,
+                                                      uint8_t *scratch, float *d_out, float *acc_out,
+                                                      int *status) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t *A1 = smem + kOffA1, *A2 = smem + kOffA2, *S = smem + kOffStage;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBars);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kOffMisc);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, quad = warp & 3, wg = warp >> 2;
+  const int row = quad * 32 + lane;
+  // stage B1 | B2 in global scratch in the canonical layout, then TMA it in
+  if (tid < 128) {
+    __nv_bfloat16 *g1 = reinterpret_cast<__nv_bfloat16 *>(scratch);
+    __nv_bfloat16 *g2 = reinterpret_cast<__nv_bfloat16 *>(scratch + kB1Bytes);
+    for (int k = 0; k < 16; ++k) {
+      g1[kmajor_offset(tid, k, 128, 256) / 2] = b1[tid * 16 + k];
+      g2[kmajor_offset(k, tid, 128, 2048) / 2] = b2[k * 128 + tid];
+    }
+    __nv_bfloat16 *s1 = reinterpret_cast<__nv_bfloat16 *>(A1);
+    __nv_bfloat16 *s2 = reinterpret_cast<__nv_bfloat16 *>(A2);
+    for (int k = 0; k < 16; ++k) s1[kmajor_offset(tid, k, 128, 256) / 2] = a1[tid * 16 + k];
+    for (int k = 0; k < 128; ++k) s2[kmajor_offset(tid, k, 128, 2048) / 2] = a2[tid * 128 + k];
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+  __threadfence();
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+  if (tid == 0) {
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    mbar_expect_tx(&bar[0], kB1Bytes + kB2Bytes);
+    tma_bulk_load(S, scratch, kB1Bytes + kB2Bytes, &bar[0]);
+  }
+  ok = __syncthreads_and(mbar_wait(&bar[0], 0));
+  if (ok && tid == 0) {
+    mma_bf16(tmem + kColD, smem_desc(A1, 128, 256), smem_desc(S, 128, 256), idesc_bf16(128, 128), 0);
+    for (uint32_t s = 0; s < 8; ++s)
+      mma_bf16(tmem + kColAcc, smem_desc(A2 + s * 256, 128, 2048),
+               smem_desc(S + kB1Bytes + s * 256, 128, 2048), idesc_bf16(128, 16), s > 0);
+    mma_commit(&bar[1]);
+  }
+  if (ok) ok = __syncthreads_and(mbar_wait(&bar[1], 0));
+  tc_fence_after();
+  if (ok) {
+    for (int half = 0; half < 2; ++half) {
+      float v[32];
+      uint32_t col = 64 * wg + 32 * half;
+      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kColD + col, v);
+      for (int j = 0; j < 32; ++j) d_out[row * 128 + col + j] = v[j];
+    }
+    if (wg == 0) {
+      float v[32];
+      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kColAcc, v);
+      for (int j = 0; j < 16; ++j) acc_out[row * 16 + j] = v[j];
+    }
+  }
+  if (!ok && tid == 0) atomicExch(status, DS_SPIN_LIMIT);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+__global__ void ms_update_bulk(float *means, const float *partial, uint64_t splits, uint64_t slots,
+                               const int32_t *ids, uint64_t nactive, float h2, float stop,
+                               uint8_t *state) {
+  uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (slot >= nactive) return;
+  int32_t s = ids[slot];
+  float acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint64_t p = 0; p < splits; ++p)
+    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * slots + slot) * 8 + d];
+  if (acc[6] <= 1e-14f) {
+    state[s] = 2;
+    return;
+  }
+  float move = 0;
+  for (int d = 0; d < 6; ++d) {
+    float nx = acc[d] / acc[6];
+    float e = means[uint64_t(s) * 8 + d] - nx;
+    move += e * e;
+    means[uint64_t(s) * 8 + d] = nx;
+  }
+  if (move < stop * h2) state[s] = 1;
+}
+
+}  // namespace
+
+// Active-seed list as in the SIMT path (meanshift_fast.cu).
+unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
+                      uint64_t k, int32_t *ids);
+
+bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
+                         double h2, int max_iter, int *iterations, double *evaluations) {
+  *iterations = 0;
+  *evaluations = 0;
+  if (!k || !v.q) return false;
+  cudaStream_t st = call.stream();
+  static bool configured = false;
+  if (!configured) {
+    SYM_CUDA(cudaFuncSetAttribute(ms_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemRequest));
+    configured = true;
+  }
+  uint8_t *images = call.alloc<uint8_t>(v.nchunks * kImage);
+  float *centers = call.alloc<float>(v.nchunks * 8);
+  build_images<<<unsigned(v.nchunks), kChunk, 0, st>>>(v.desc, v.q, v.nchunks, v.cbox, images,
+                                                       centers);
+  check_launch();
+  int32_t *ids = call.alloc<int32_t>(k);
+  uint64_t cap = (64 * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
+  float *partial = call.alloc<float>(cap * 8);
+  unsigned long long *evals = call.alloc<unsigned long long>(1);
+  SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
+  float gap = float(std::sqrt(h2)) + 1e-6f;
+  call.launched();
+  int it = 0;
+  for (; it < max_iter; ++it) {
+    unsigned n = active_seeds(call, v, means, state, k, ids);
+    if (!n) break;
+    uint64_t tiles = (n + kChunk - 1) / kChunk;
+    uint64_t want = (2 * 152 + tiles - 1) / tiles;
+    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(v.nchunks, want));
+    uint64_t cps = (v.nchunks + splits - 1) / splits;
+    splits = (v.nchunks + cps - 1) / cps;
+    uint64_t slots = tiles * kChunk;
+    if (splits * slots > cap) fail(SYM_RUNTIME_ERROR, "tensor mean-shift partial buffer too small");
+    TcArgs args{images, centers, v.cbox, v.nchunks, means, ids, n, float(1.0 / h2), gap * gap,
+                cps, partial, evals, call.status()};
+    ms_tile_tc<<<dim3(unsigned(tiles), unsigned(splits)), 256, kSmemRequest, st>>>(args);
+    check_launch();
+    ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, splits, slots, ids, n,
+                                                       float(h2), 1e-4f, state);
+    check_launch();
+    call.launched(2);
+  }
+  call.check_status("mean_shift (tensor)");
+  unsigned long long ev = 0;
+  call.d2h(&ev, evals, 8);
+  call.sync();
+  *iterations = it;
+  *evaluations = double(ev);
+  return true;
+}
+
+void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,
+                      const uint16_t *b2, float *d_out, float *acc_out) {
+  static bool configured = false;
+  if (!configured) {
+    SYM_CUDA(cudaFuncSetAttribute(tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemRequest));
+    configured = true;
+  }
+  auto up = [&](const uint16_t *p, size_t n) {
+    return reinterpret_cast<const __nv_bfloat16 *>(call.upload(p, n));
+  };
+  const __nv_bfloat16 *da1 = up(a1, 128 * 16), *db1 = up(b1, 128 * 16), *da2 = up(a2, 128 * 128),
+                      *db2 = up(b2, 16 * 128);
+  uint8_t *scratch = call.alloc<uint8_t>(kB1Bytes + kB2Bytes);
+  float *dd = call.alloc<float>(128 * 128), *dacc = call.alloc<float>(128 * 16);
+  tc_selftest<<<1, 256, kSmemRequest, call.stream()>>>(da1, db1, da2, db2, scratch, dd, dacc,
+                                                       call.status());
+  check_launch();
+  call.launched();
+  call.d2h(d_out, dd, 128 * 128 * 4);
+  call.d2h(acc_out, dacc, 128 * 16 * 4);
+  call.check_status("tensor self-test");
+}
+
 }  // namespace sym

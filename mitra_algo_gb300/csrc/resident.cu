@@ -15,11 +15,13 @@
 // in FP32; a subset of seeds re-runs in FP64 to measure the mode error.
 #include "common.cuh"
 #include "primitives.cuh"
+#include "meanshift_fast.cuh"
 #include "rng.hpp"
 
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <map>
 #include <vector>
 
 namespace sym {
@@ -38,9 +40,10 @@ void verification_core(Call &, const sym_mesh_view &, const double *, const int3
                        std::vector<double> &);
 // BF16 tensor-core bulk iterations (meanshift_tc.cu); returns false when the
 // tensor path cannot run this problem (the caller then stays in FP32).
-bool meanshift_bf16_bulk(Call &call, const float *desc, const float *cbox, uint64_t nchunks,
-                         uint64_t q, float *means, uint8_t *state, uint64_t k, float h2,
-                         int max_iter, int *iterations, double *evaluations);
+bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
+                         double h2, int max_iter, int *iterations, double *evaluations);
+void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,
+                      const uint16_t *b2, float *d_out, float *acc_out);
 }  // namespace sym
 
 struct sym_mesh_handle {
@@ -57,8 +60,6 @@ struct sym_mesh_handle {
 };
 
 namespace sym {
-
-constexpr int kChunk = 128;  // votes per chunk = seeds per tile
 
 // --------------------------------------------------------------- 6-D votes
 // Rotation log map: axis-angle w with |w| = theta in [0, pi].  Near pi the
@@ -137,293 +138,24 @@ __global__ void votes6(const double *pos, const double *nrm, const double *dmn, 
   }
 }
 
-// ------------------------------------------------------ sort into chunks
-__global__ void box_partials(const float *desc, uint64_t q, float *partial) {
-  __shared__ float lo[6][256], hi[6][256];
-  float l[6], h[6];
-  for (int k = 0; k < 6; ++k) l[k] = INFINITY, h[k] = -INFINITY;
-  for (uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; v < q;
-       v += uint64_t(gridDim.x) * blockDim.x)
-    for (int k = 0; k < 6; ++k) {
-      float x = desc[v * 8 + k];
-      l[k] = fminf(l[k], x), h[k] = fmaxf(h[k], x);
-    }
-  for (int k = 0; k < 6; ++k) lo[k][threadIdx.x] = l[k], hi[k][threadIdx.x] = h[k];
-  __syncthreads();
-  for (int s = 128; s; s >>= 1) {
-    if (threadIdx.x < s)
-      for (int k = 0; k < 6; ++k) {
-        lo[k][threadIdx.x] = fminf(lo[k][threadIdx.x], lo[k][threadIdx.x + s]);
-        hi[k][threadIdx.x] = fmaxf(hi[k][threadIdx.x], hi[k][threadIdx.x + s]);
-      }
-    __syncthreads();
+// K distinct vote indices drawn uniformly (Floyd's algorithm), ascending.
+std::vector<int64_t> draw_seeds(uint64_t q, uint64_t k, uint64_t seed) {
+  std::mt19937_64 rng(seed);
+  std::vector<int64_t> pool;
+  std::vector<char> taken(q, 0);
+  for (uint64_t j = q - k; j < q; ++j) {
+    uint64_t t = rng() % (j + 1);
+    uint64_t pick = taken[t] ? j : t;
+    pool.push_back(int64_t(pick));
+    taken[pick] = 1;
   }
-  if (threadIdx.x == 0)
-    for (int k = 0; k < 6; ++k) partial[blockIdx.x * 12 + k] = lo[k][0], partial[blockIdx.x * 12 + 6 + k] = hi[k][0];
+  std::sort(pool.begin(), pool.end());
+  return pool;
 }
 
-__global__ void box_final(const float *partial, int n, float *box) {
-  int k = threadIdx.x;
-  if (k >= 12) return;
-  float v = k < 6 ? INFINITY : -INFINITY;
-  for (int i = 0; i < n; ++i) v = k < 6 ? fminf(v, partial[i * 12 + k]) : fmaxf(v, partial[i * 12 + k]);
-  box[k] = v;
-}
-
-__device__ __forceinline__ uint64_t spread6(uint64_t x) {  // 10 bits -> every 6th bit
-  uint64_t r = 0;
-  for (int b = 0; b < 10; ++b) r |= ((x >> b) & 1ull) << (6 * b);
-  return r;
-}
-
-__global__ void morton_keys(const float *desc, uint64_t q, const float *box, uint64_t *keys,
-                            int32_t *idx) {
-  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (v >= q) return;
-  uint64_t key = 0;
-  for (int k = 0; k < 6; ++k) {
-    float lo = box[k], span = box[6 + k] - lo;
-    float t = span > 0 ? (desc[v * 8 + k] - lo) / span : 0.f;
-    int cell = min(1023, max(0, int(t * 1024.f)));
-    key |= spread6(uint64_t(cell)) << k;
-  }
-  keys[v] = key;
-  idx[v] = int32_t(v);
-}
-
-template <typename T>
-__global__ void permute(const T *src, const int32_t *order, uint64_t q, T *dst) {
-  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (v >= q) return;
-  uint64_t from = uint64_t(uint32_t(order[v]));
-  for (int k = 0; k < 8; ++k) dst[v * 8 + k] = src[from * 8 + k];
-}
-
-// One warp per chunk: [lo0..lo5, hi0..hi5].
-__global__ void chunk_boxes(const float *desc, uint64_t q, uint64_t nchunks, float *cbox) {
-  uint64_t c = (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (c >= nchunks) return;
-  float l[6], h[6];
-  for (int k = 0; k < 6; ++k) l[k] = INFINITY, h[k] = -INFINITY;
-  for (int j = lane; j < kChunk; j += 32) {
-    uint64_t v = c * kChunk + j;
-    if (v >= q) break;
-    for (int k = 0; k < 6; ++k) {
-      float x = desc[v * 8 + k];
-      l[k] = fminf(l[k], x), h[k] = fmaxf(h[k], x);
-    }
-  }
-  for (int o = 16; o; o >>= 1)
-    for (int k = 0; k < 6; ++k) {
-      l[k] = fminf(l[k], __shfl_xor_sync(0xffffffffu, l[k], o));
-      h[k] = fmaxf(h[k], __shfl_xor_sync(0xffffffffu, h[k], o));
-    }
-  if (lane == 0)
-    for (int k = 0; k < 6; ++k) cbox[c * 12 + k] = l[k], cbox[c * 12 + 6 + k] = h[k];
-}
-
-// --------------------------------------------------------------- mean shift
-// Squared gap between two boxes, widened by `slack` per side.
-__device__ __forceinline__ float box_gap2(const float *a_lo, const float *a_hi, const float *b) {
-  float g = 0;
-  for (int k = 0; k < 6; ++k) {
-    float d = fmaxf(fmaxf(b[k] - a_hi[k], a_lo[k] - b[6 + k]), 0.f);
-    g += d * d;
-  }
-  return g;
-}
-
-// One block = one tile of 128 seeds x one split of the chunk range.  The
-// tile's box (over its active seeds) skips chunks that cannot contribute.
-template <typename T>
-__global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cbox, uint64_t nchunks,
-                                                  uint64_t q, const T *means, const uint8_t *state,
-                                                  const uint8_t *tile_active, uint64_t k, T h2,
-                                                  float skip_gap2, uint64_t chunks_per_split,
-                                                  T *partial, unsigned long long *evals) {
-  __shared__ T xs[kChunk * 8];
-  __shared__ float tlo[6][4], thi[6][4];
-  uint64_t tile = blockIdx.x, split = blockIdx.y;
-  if (!tile_active[tile]) return;
-  uint64_t seed = tile * kChunk + threadIdx.x;
-  bool live = seed < k && state[seed] == 0;
-  T m[6];
-  for (int d = 0; d < 6; ++d) m[d] = seed < k ? means[seed * 8 + d] : T(0);
-  float lo[6], hi[6];
-  for (int d = 0; d < 6; ++d) {
-    lo[d] = live ? float(m[d]) : INFINITY;
-    hi[d] = live ? float(m[d]) : -INFINITY;
-  }
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int o = 16; o; o >>= 1)
-    for (int d = 0; d < 6; ++d) {
-      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
-    }
-  if (lane == 0)
-    for (int d = 0; d < 6; ++d) tlo[d][warp] = lo[d], thi[d][warp] = hi[d];
-  __syncthreads();
-  for (int d = 0; d < 6; ++d) {
-    lo[d] = fminf(fminf(tlo[d][0], tlo[d][1]), fminf(tlo[d][2], tlo[d][3]));
-    hi[d] = fmaxf(fmaxf(thi[d][0], thi[d][1]), fmaxf(thi[d][2], thi[d][3]));
-  }
-  T acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  uint64_t c0 = split * chunks_per_split, c1 = min(nchunks, c0 + chunks_per_split);
-  unsigned long long done = 0;
-  for (uint64_t c = c0; c < c1; ++c) {
-    if (box_gap2(lo, hi, cbox + c * 12) > skip_gap2) continue;
-    __syncthreads();
-    uint64_t v = c * kChunk + threadIdx.x;
-    for (int d = 0; d < 8; ++d) xs[threadIdx.x * 8 + d] = v < q ? desc[v * 8 + d] : T(1e30);
-    __syncthreads();
-    uint64_t rest = q - c * kChunk;
-    int n = rest < uint64_t(kChunk) ? int(rest) : kChunk;
-    done += n;
-    for (int j = 0; j < n; ++j) {
-      T d2 = 0;
-#pragma unroll
-      for (int d = 0; d < 6; ++d) {
-        T e = m[d] - xs[j * 8 + d];
-        d2 += e * e;
-      }
-      if (d2 < h2) {
-        T w = T(1) - d2 / h2;
-#pragma unroll
-        for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
-        acc[6] += w;
-      }
-    }
-  }
-  if (seed < k)
-    for (int d = 0; d < 7; ++d) partial[(split * k + seed) * 8 + d] = acc[d];
-  if (threadIdx.x == 0 && done) atomicAdd(evals, done * kChunk);
-}
-
-// Sum the splits (fixed order), move the seed, test convergence like the
-// reference (movement < 1e-6 h^2, exhausted when the weight is <= 1e-14).
-template <typename T>
-__global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t k, T h2,
-                          uint8_t *state, const uint8_t *tile_active, uint8_t *tile_next,
-                          unsigned *active) {
-  uint64_t s = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (s >= k || state[s] || !tile_active[s / kChunk]) return;
-  T acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (uint64_t p = 0; p < splits; ++p)
-    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * k + s) * 8 + d];
-  if (acc[6] <= T(1e-14)) {
-    state[s] = 2;
-    return;
-  }
-  T move = 0;
-  for (int d = 0; d < 6; ++d) {
-    T nx = acc[d] / acc[6];
-    T e = means[s * 8 + d] - nx;
-    move += e * e;
-    means[s * 8 + d] = nx;
-  }
-  if (move < T(1e-6) * h2) {
-    state[s] = 1;
-    return;
-  }
-  tile_next[s / kChunk] = 1;
-  atomicAdd(active, 1u);
-}
-
-// Votes within the bandwidth of each mode (one block per chunk).
-__global__ void mode_support(const float *desc, const float *cbox, uint64_t nchunks, uint64_t q,
-                             const float *modes, uint64_t nm, float h2, float skip_gap2,
-                             unsigned long long *support) {
-  uint64_t c = blockIdx.x;
-  uint64_t v = c * kChunk + threadIdx.x;
-  float x[6];
-  for (int d = 0; d < 6; ++d) x[d] = v < q ? desc[v * 8 + d] : 1e30f;
-  const float *b = cbox + c * 12;
-  for (uint64_t m = 0; m < nm; ++m) {
-    const float *mm = modes + m * 8;
-    if (box_gap2(mm, mm, b) > skip_gap2) continue;
-    float d2 = 0;
-    for (int d = 0; d < 6; ++d) {
-      float e = mm[d] - x[d];
-      d2 += e * e;
-    }
-    unsigned hit = __ballot_sync(0xffffffffu, v < q && d2 < h2);
-    if ((threadIdx.x & 31) == 0 && hit) atomicAdd(&support[m], (unsigned long long)__popc(hit));
-  }
-}
-
-template <typename T>
-struct Shift {
-  T *means;
-  uint8_t *state, *tile_active, *tile_next;
-  T *partial;
-  unsigned *active;
-};
-
-// Runs FP32/FP64 iterations until every seed stops or `max_iter` is hit.
-template <typename T>
-int run_shift(Call &call, const T *desc, const float *cbox, uint64_t nchunks, uint64_t q,
-              Shift<T> &s, uint64_t k, double h2, int max_iter, unsigned long long *evals,
-              double *seed_iterations = nullptr) {
-  cudaStream_t st = call.stream();
-  uint64_t tiles = (k + kChunk - 1) / kChunk;
-  uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, (64 * 152 + tiles - 1) / tiles));
-  uint64_t cps = (nchunks + splits - 1) / splits;
-  splits = (nchunks + cps - 1) / cps;
-  float gap = float(std::sqrt(h2)) + 1e-6f;
-  int it = 0;
-  unsigned live = unsigned(k);
-  for (; it < max_iter; ++it) {
-    if (seed_iterations) *seed_iterations += live;
-    ms_tile<T><<<dim3(unsigned(tiles), unsigned(splits)), kChunk, 0, st>>>(
-        desc, cbox, nchunks, q, s.means, s.state, s.tile_active, k, T(h2), gap * gap, cps,
-        s.partial, evals);
-    check_launch();
-    SYM_CUDA(cudaMemsetAsync(s.tile_next, 0, tiles, st));
-    SYM_CUDA(cudaMemsetAsync(s.active, 0, sizeof(unsigned), st));
-    ms_update<T><<<blocks_for(k), kThreads, 0, st>>>(s.means, s.partial, splits, k, T(h2), s.state,
-                                                     s.tile_active, s.tile_next, s.active);
-    check_launch();
-    call.launched(2);
-    SYM_CUDA(cudaMemcpyAsync(s.tile_active, s.tile_next, tiles, cudaMemcpyDeviceToDevice, st));
-    unsigned active = 0;
-    SYM_CUDA(cudaMemcpyAsync(&active, s.active, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-    call.sync();
-    live = active;
-    if (!active) {
-      ++it;
-      break;
-    }
-  }
-  return it;
-}
-
-template <typename T>
-__global__ void gather_seeds(const T *desc, const int64_t *pos, uint64_t k, T *means) {
+__global__ void ranks_of(const int32_t *rank, const int64_t *seeds, uint64_t k, int64_t *out) {
   uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= k) return;
-  for (int d = 0; d < 8; ++d) means[i * 8 + d] = desc[uint64_t(pos[i]) * 8 + d];
-}
-
-template <typename T>
-Shift<T> make_shift(Call &call, uint64_t k, uint64_t nchunks, const T *desc,
-                    const std::vector<int64_t> &seed_pos) {
-  Shift<T> s;
-  uint64_t tiles = (k + kChunk - 1) / kChunk;
-  uint64_t splits_max = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, (64 * 152 + tiles - 1) / tiles)) + 1;
-  s.means = call.alloc<T>(k * 8);
-  s.state = call.alloc<uint8_t>(k);
-  s.tile_active = call.alloc<uint8_t>(tiles);
-  s.tile_next = call.alloc<uint8_t>(tiles);
-  s.partial = call.alloc<T>(splits_max * k * 8);
-  s.active = call.alloc<unsigned>(1);
-  SYM_CUDA(cudaMemsetAsync(s.state, 0, k, call.stream()));
-  SYM_CUDA(cudaMemsetAsync(s.tile_active, 1, tiles, call.stream()));
-  int64_t *pos = call.upload(seed_pos.data(), k);
-  gather_seeds<T><<<blocks_for(k), kThreads, 0, call.stream()>>>(desc, pos, k, s.means);
-  check_launch();
-  call.launched();
-  return s;
+  if (i < k) out[i] = rank[seeds[i]];
 }
 
 // Rodrigues: R = exp([w]x).
@@ -523,71 +255,30 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   call.launched(want64 ? 2 : 1);
   clock.mark(4);
   // ---- Morton sort into chunks
-  const int kBoxBlocks = 256;
-  float *bpart = call.alloc<float>(kBoxBlocks * 12), *gbox = call.alloc<float>(12);
-  box_partials<<<kBoxBlocks, 256, 0, st>>>(desc_raw, q, bpart);
-  check_launch();
-  box_final<<<1, 32, 0, st>>>(bpart, kBoxBlocks, gbox);
-  check_launch();
-  uint64_t *keys = call.alloc<uint64_t>(q), *skeys = call.alloc<uint64_t>(q);
-  int32_t *idx = call.alloc<int32_t>(q), *order = call.alloc<int32_t>(q);
-  morton_keys<<<blocks_for(q), kThreads, 0, st>>>(desc_raw, q, gbox, keys, idx);
-  check_launch();
-  radix_sort_pairs(call, keys, idx, skeys, order, q, 60);
-  float *desc = call.alloc<float>(q * 8);
-  permute<float><<<blocks_for(q), kThreads, 0, st>>>(desc_raw, order, q, desc);
-  check_launch();
-  double *desc64 = nullptr;
-  if (want64) {
-    desc64 = call.alloc<double>(q * 8);
-    permute<double><<<blocks_for(q), kThreads, 0, st>>>(desc64_raw, order, q, desc64);
-    check_launch();
-  }
-  uint64_t nchunks = (q + kChunk - 1) / kChunk;
-  float *cbox = call.alloc<float>(nchunks * 12);
-  chunk_boxes<<<blocks_for(nchunks * 32), kThreads, 0, st>>>(desc, q, nchunks, cbox);
-  check_launch();
-  call.launched(want64 ? 6 : 5);
+  VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q);
   clock.mark(5);
-  // ---- (c) mean shift from K seeds (uniform draw, in sorted vote order)
+  // ---- (c) mean shift from K seeds (uniform draw of distinct votes)
   uint64_t k = std::min<uint64_t>(uint64_t(std::max(fo.seeds, 1)), q);
-  std::mt19937_64 rng(fo.seed_rng);
-  std::vector<int64_t> seed_pos;
-  {
-    std::vector<int64_t> pool;  // Floyd's sampling of k distinct positions
-    std::vector<char> taken;
-    if (q <= (1u << 26)) taken.assign(q, 0);
-    for (uint64_t j = q - k; j < q; ++j) {
-      uint64_t t = rng() % (j + 1);
-      bool dup = taken.empty() ? std::find(pool.begin(), pool.end(), int64_t(t)) != pool.end() : taken[t];
-      uint64_t pick = dup ? j : t;
-      pool.push_back(int64_t(pick));
-      if (!taken.empty()) taken[pick] = 1;
-    }
-    std::sort(pool.begin(), pool.end());
-    seed_pos = pool;
-  }
+  std::vector<int64_t> seeds = draw_seeds(q, k, fo.seed_rng);
+  int64_t *dseeds = call.upload(seeds.data(), k);
+  int64_t *seed_rank = call.alloc<int64_t>(k);
+  ranks_of<<<blocks_for(k), kThreads, 0, st>>>(vs.rank, dseeds, k, seed_rank);
+  check_launch();
   const double h2 = o.bandwidth * o.bandwidth;
   unsigned long long *evals = call.alloc<unsigned long long>(1);
   SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
-  Shift<float> s32 = make_shift<float>(call, k, nchunks, desc, seed_pos);
+  float *m32 = call.alloc<float>(k * 8);
+  uint8_t *st32 = call.alloc<uint8_t>(k);
+  SYM_CUDA(cudaMemsetAsync(st32, 0, k, st));
+  init_means(call, vs, seed_rank, k, m32);
   int bulk = 0, polish = 0;
-  double bf16_evals = 0;
-  if (fo.precision == SYM_MS_BF16_REFINED) {
-    if (meanshift_bf16_bulk(call, desc, cbox, nchunks, q, s32.means, s32.state, k, float(h2),
-                            fo.max_iterations, &bulk, &bf16_evals)) {
-      // polish: every seed restarts in FP32 from its BF16 mode
-      SYM_CUDA(cudaMemsetAsync(s32.state, 0, k, st));
-      SYM_CUDA(cudaMemsetAsync(s32.tile_active, 1, (k + kChunk - 1) / kChunk, st));
-      polish = run_shift<float>(call, desc, cbox, nchunks, q, s32, k, h2, fo.polish_iterations, evals,
-                                &r.seed_iterations);
-    } else {
-      bulk = run_shift<float>(call, desc, cbox, nchunks, q, s32, k, h2, fo.max_iterations, evals,
-                              &r.seed_iterations);
-    }
+  double tc_evals = 0;
+  if (fo.precision == SYM_MS_BF16_REFINED &&
+      meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals)) {
+    SYM_CUDA(cudaMemsetAsync(st32, 0, k, st));  // polish every seed in FP32
+    polish = shift(call, vs, m32, st32, k, h2, fo.polish_iterations, &r.seed_iterations, evals);
   } else {
-    bulk = run_shift<float>(call, desc, cbox, nchunks, q, s32, k, h2, fo.max_iterations, evals,
-                            &r.seed_iterations);
+    bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, &r.seed_iterations, evals);
   }
   r.iterations = bulk;
   r.polish_iterations = polish;
@@ -595,65 +286,77 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   call.d2h(&ev, evals, 8);
   std::vector<float> means(k * 8);
   std::vector<uint8_t> state(k);
-  call.d2h(means.data(), s32.means, k * 8 * 4);
-  call.d2h(state.data(), s32.state, k);
+  call.d2h(means.data(), m32, k * 8 * 4);
+  call.d2h(state.data(), st32, k);
   call.sync();
-  r.mean_shift_pairs = double(ev) + bf16_evals;
+  r.mean_shift_pairs = double(ev) + tc_evals;
   r.h2d_bytes = call.ctx->metrics.current.h2d_bytes;
   r.d2h_bytes = call.ctx->metrics.current.d2h_bytes;
   clock.mark(6);
   // ---- FP64 reference on the first seeds (mode error)
   if (want64) {
     uint64_t k64 = std::min<uint64_t>(k, uint64_t(fo.reference_seeds));
-    std::vector<int64_t> sp(seed_pos.begin(), seed_pos.begin() + k64);
-    Shift<double> s64 = make_shift<double>(call, k64, nchunks, desc64, sp);
-    unsigned long long *ev64 = call.alloc<unsigned long long>(1);
-    run_shift<double>(call, desc64, cbox, nchunks, q, s64, k64, h2, 1000, ev64);
-    std::vector<double> m64(k64 * 8);
-    std::vector<uint8_t> st64(k64);
-    call.d2h(m64.data(), s64.means, k64 * 8 * 8);
-    call.d2h(st64.data(), s64.state, k64);
+    double *m64 = call.alloc<double>(k64 * 8);
+    uint8_t *st64 = call.alloc<uint8_t>(k64);
+    SYM_CUDA(cudaMemsetAsync(st64, 0, k64, st));
+    init_means(call, vs, seed_rank, k64, m64);
+    shift(call, vs, m64, st64, k64, h2, 1000, nullptr, nullptr);
+    std::vector<double> hm(k64 * 8);
+    call.d2h(hm.data(), m64, k64 * 8 * 8);
     call.sync();
     double emax = 0, esum = 0;
-    uint64_t n = 0;
     for (uint64_t i = 0; i < k64; ++i) {
       double num = 0, den = 0;
       for (int d = 0; d < 6; ++d) {
-        double e = double(means[i * 8 + d]) - m64[i * 8 + d];
-        num += e * e, den += m64[i * 8 + d] * m64[i * 8 + d];
+        double e = double(means[i * 8 + d]) - hm[i * 8 + d];
+        num += e * e, den += hm[i * 8 + d] * hm[i * 8 + d];
       }
       double rel = std::sqrt(num) / std::max(std::sqrt(den), 1e-300);
-      emax = std::max(emax, rel), esum += rel, ++n;
+      emax = std::max(emax, rel), esum += rel;
     }
     r.mode_error_max = emax;
-    r.mode_error_mean = n ? esum / n : 0;
+    r.mode_error_mean = k64 ? esum / k64 : 0;
   }
   clock.mark(7);
   // ---- modes: greedy merge (h^2/4, first mode wins) + support
+  // Greedy merge in seed order: a seed joins the earliest-created mode within
+  // h/2 (squared distance < h^2/4).  Candidates come from a window of the
+  // modes sorted by their first coordinate.
   std::vector<double> mode_pos;
   std::vector<uint64_t> mode_seeds;
+  std::multimap<double, uint64_t> by_x;
+  const double half = 0.5 * std::sqrt(h2) * (1 + 1e-12);
   for (uint64_t i = 0; i < k; ++i) {
     if (state[i] == 2) continue;  // exhausted
-    int hit = -1;
-    for (size_t m = 0; m < mode_seeds.size(); ++m) {
+    double x0 = means[i * 8];
+    int64_t hit = -1;
+    for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
+      uint64_t m = it->second;
+      if (hit >= 0 && int64_t(m) > hit) continue;
       double d2 = 0;
       for (int d = 0; d < 6; ++d) {
         double e = double(means[i * 8 + d]) - mode_pos[m * 6 + d];
         d2 += e * e;
       }
-      if (d2 < h2 / 4) {
-        hit = int(m);
-        break;
-      }
+      if (d2 < h2 / 4) hit = int64_t(m);
     }
     if (hit < 0) {
       for (int d = 0; d < 6; ++d) mode_pos.push_back(means[i * 8 + d]);
       mode_seeds.push_back(1);
+      by_x.emplace(mode_pos[(mode_seeds.size() - 1) * 6], mode_seeds.size() - 1);
     } else {
       double n = double(mode_seeds[hit]);
+      double old_x = mode_pos[hit * 6];
       for (int d = 0; d < 6; ++d)
         mode_pos[hit * 6 + d] = (n * mode_pos[hit * 6 + d] + means[i * 8 + d]) / (n + 1);
       ++mode_seeds[hit];
+      auto range = by_x.equal_range(old_x);
+      for (auto it = range.first; it != range.second; ++it)
+        if (it->second == uint64_t(hit)) {
+          by_x.erase(it);
+          break;
+        }
+      by_x.emplace(mode_pos[hit * 6], uint64_t(hit));
     }
   }
   uint64_t nm = mode_seeds.size();
@@ -665,12 +368,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
       for (int d = 0; d < 6; ++d) mp[m * 8 + d] = float(mode_pos[m * 6 + d]);
     float *dmodes = call.upload(mp.data(), mp.size());
     unsigned long long *dsup = call.alloc<unsigned long long>(nm);
-    SYM_CUDA(cudaMemsetAsync(dsup, 0, nm * 8, st));
-    float gap = float(o.bandwidth) + 1e-6f;
-    mode_support<<<unsigned(nchunks), kChunk, 0, st>>>(desc, cbox, nchunks, q, dmodes, nm, float(h2),
-                                                     gap * gap, dsup);
-    check_launch();
-    call.launched();
+    count_within(call, vs, dmodes, nm, h2, dsup);
     call.d2h(support.data(), dsup, nm * 8);
     call.sync();
   }
@@ -794,6 +492,105 @@ void sym_mesh_free(sym_mesh_handle *h) {
   cudaStreamSynchronize(h->ctx->stream);
   cudaFree(h->block);
   delete h;
+}
+
+namespace {
+// 6-D votes given as q x 6 doubles -> the 8-wide FP32 / FP64 layout.
+__global__ void pack_votes(const double *in, uint64_t q, float *d32, double *d64) {
+  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= q) return;
+  double n2 = 0;
+  float n2f = 0;
+  for (int d = 0; d < 6; ++d) {
+    double x = in[v * 6 + d];
+    d64[v * 8 + d] = x, d32[v * 8 + d] = float(x);
+    n2 += x * x, n2f += float(x) * float(x);
+  }
+  d64[v * 8 + 6] = n2, d64[v * 8 + 7] = 0;
+  d32[v * 8 + 6] = n2f, d32[v * 8 + 7] = 0;
+}
+}  // namespace
+
+sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q, const int64_t *seeds,
+                          uint64_t k, double bandwidth, int32_t precision, int32_t max_iterations,
+                          int32_t polish_iterations, double *means_out, uint8_t *state_out,
+                          int32_t *iterations_out) {
+  if (!ctx || (q && !votes) || (k && (!seeds || !means_out || !state_out)) || !iterations_out)
+    return SYM_INVALID_ARGUMENT;
+  try {
+    sym::Call call(ctx, "mean_shift6");
+    if (!(bandwidth > 0) || max_iterations < 1 || polish_iterations < 0)
+      sym::fail(SYM_INVALID_ARGUMENT, "Invalid parameter range; see --help");
+    if (q > uint64_t(std::numeric_limits<int32_t>::max()))
+      sym::fail(SYM_OVERFLOW, "vote ids exceed int32 range");
+    for (uint64_t i = 0; i < k; ++i)
+      if (seeds[i] < 0 || uint64_t(seeds[i]) >= q)
+        sym::fail(SYM_INVALID_ARGUMENT, "seed vote index out of range");
+    iterations_out[0] = iterations_out[1] = 0;
+    if (!k) return SYM_OK;
+    cudaStream_t st = call.stream();
+    double *raw = call.upload(votes, q * 6);
+    float *d32 = call.alloc<float>(q * 8);
+    double *d64 = call.alloc<double>(q * 8);
+    pack_votes<<<sym::blocks_for(q), sym::kThreads, 0, st>>>(raw, q, d32, d64);
+    sym::check_launch();
+    sym::VoteSet vs = sym::build_vote_set(call, d32, d64, q);
+    int64_t *dseeds = call.upload(seeds, k);
+    int64_t *rank = call.alloc<int64_t>(k);
+    sym::ranks_of<<<sym::blocks_for(k), sym::kThreads, 0, st>>>(vs.rank, dseeds, k, rank);
+    sym::check_launch();
+    uint8_t *state = call.alloc<uint8_t>(k);
+    SYM_CUDA(cudaMemsetAsync(state, 0, k, st));
+    double h2 = bandwidth * bandwidth;
+    std::vector<double> out(k * 8);
+    if (precision == SYM_MS_FP64) {
+      double *m = call.alloc<double>(k * 8);
+      sym::init_means(call, vs, rank, k, m);
+      iterations_out[0] = sym::shift(call, vs, m, state, k, h2, max_iterations, nullptr, nullptr);
+      call.d2h(out.data(), m, k * 8 * 8);
+    } else {
+      float *m = call.alloc<float>(k * 8);
+      sym::init_means(call, vs, rank, k, m);
+      int bulk = 0;
+      double ev = 0;
+      if (precision == SYM_MS_BF16_REFINED &&
+          sym::meanshift_bf16_bulk(call, vs, m, state, k, h2, max_iterations, &bulk, &ev)) {
+        SYM_CUDA(cudaMemsetAsync(state, 0, k, st));
+        iterations_out[1] = sym::shift(call, vs, m, state, k, h2, polish_iterations, nullptr, nullptr);
+      } else {
+        bulk = sym::shift(call, vs, m, state, k, h2, max_iterations, nullptr, nullptr);
+      }
+      iterations_out[0] = bulk;
+      std::vector<float> mf(k * 8);
+      call.d2h(mf.data(), m, k * 8 * 4);
+      call.sync();
+      for (uint64_t i = 0; i < k * 8; ++i) out[i] = mf[i];
+    }
+    call.d2h(state_out, state, k);
+    call.check_status("mean_shift6");
+    for (uint64_t i = 0; i < k; ++i)
+      for (int d = 0; d < 6; ++d) means_out[i * 6 + d] = out[i * 8 + d];
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
+  }
+}
+
+sym_status sym_tc_selftest(sym_context *ctx, const uint16_t *a1, const uint16_t *b1,
+                           const uint16_t *a2, const uint16_t *b2, float *d_out, float *acc_out) {
+  if (!ctx || !a1 || !b1 || !a2 || !b2 || !d_out || !acc_out) return SYM_INVALID_ARGUMENT;
+  try {
+    sym::Call call(ctx, "tc_selftest");
+    sym::tc_selftest_host(call, a1, b1, a2, b2, d_out, acc_out);
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  }
 }
 
 sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh, const int32_t *sample,

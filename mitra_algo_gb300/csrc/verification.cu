@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <numeric>
 #include <vector>
 
@@ -164,8 +165,14 @@ constexpr int kStack = 96;
 // Near-first search identical to the reference's recursion: a node is
 // skipped when its box is farther than the best so far, the nearer child
 // is searched first, faces win only with a strictly smaller distance.
-__device__ double nearest_face(const Surface &s, D3 p, int32_t &face, int *status) {
-  double best = INFINITY;
+// The search starts from `limit` (the next double above tau^2) instead of
+// infinity: the caller rejects every distance above tau^2, nodes farther
+// than the limit can hold no face the reference would accept, and the
+// visiting order of the nodes that remain is unchanged, so an accepted
+// query finds the reference's face and distance.  Rejected queries report
+// no face.
+__device__ double nearest_face(const Surface &s, D3 p, double limit, int32_t &face, int *status) {
+  double best = limit;
   face = -1;
   int stack[kStack], top = 0;
   stack[top++] = 0;
@@ -203,7 +210,8 @@ struct ClusterMotion {
 
 // flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).
 __global__ void verify_vertices(Surface s, const double *vn, const ClusterMotion *clusters,
-                                uint64_t nc, double tau, uint8_t *flags, double *err, int *status) {
+                                uint64_t nc, double tau, double limit, uint8_t *flags, double *err,
+                                int *status) {
   uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   uint64_t nv = s.nv;
   if (row >= nc * 2 * nv) return;
@@ -225,7 +233,7 @@ __global__ void verify_vertices(Surface s, const double *vn, const ClusterMotion
     if (inverse ? side <= tau : side >= -tau) return;
   }
   int32_t face;
-  double d = nearest_face(s, q, face, status);
+  double d = nearest_face(s, q, limit, face, status);
   if (d > tau * tau || face < 0) return;
   D3 a = corner(s, face, 0), b = corner(s, face, 1), cc = corner(s, face, 2);
   D3 fnorm = unit(cross(b - a, cc - a));
@@ -390,7 +398,8 @@ void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, co
   uint64_t rows = nc * 2 * nv;
   uint8_t *flags = call.alloc<uint8_t>(rows);
   double *err = call.alloc<double>(nc * nv);
-  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, flags, err,
+  double limit = std::nextafter(tau * tau, std::numeric_limits<double>::infinity());
+  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, limit, flags, err,
                                                          call.status());
   check_launch();
   double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
