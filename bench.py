@@ -6,7 +6,9 @@ subdivided 6 times, radially displaced by a seeded 12-bump motif repeated in
 5-fold rotation about z, plus a partial copy translated 0.4 along x, Gaussian
 vertex noise 1e-3 of the bbox diagonal (54,756 vertices, 109,102 faces);
 20,000 area-weighted samples, pair threshold 0.25 (~1e7 pairs), 6-D rigid
-votes, 2,048 mean-shift seeds, bandwidth 0.05.  Synthetic data, seeded.
+votes, 2,048 mean-shift seeds, bandwidth 0.1, up to 300 mean-shift iterations
+(and up to 50 FP32 polish iterations after the BF16 bulk).  Synthetic data,
+seeded.
 
 One step = the whole hot path on one mesh: curvature, prune, exact pairing,
 6-D votes, vote sort, mean-shift, modes, verification of the top 20 modes.
@@ -41,8 +43,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "meshes/s and pair votes/s, BF16-refined vs plain FP32 on GPU at ≤1e-4 mode error"
 SAMPLES = 20000
 PAIR_THRESHOLD = 0.25
-BANDWIDTH = 0.05
+BANDWIDTH = 0.1
 SEEDS = 2048
+ITERATIONS = 300  # bulk mean-shift iterations (FP32, or BF16 before the polish)
+POLISH = 50       # FP32 polish iterations after the BF16 bulk
 
 
 def workload(small=False):
@@ -216,6 +220,7 @@ def run_gpu(args):
 
     def step(precision, reference_seeds=0):
         return gpu.detect_fast(resident, sample, opts, precision=precision, seeds=SEEDS,
+                               max_iterations=ITERATIONS, polish_iterations=POLISH,
                                reference_seeds=reference_seeds)
 
     def timed(precision, steps, warmup):
@@ -271,7 +276,8 @@ def run_gpu(args):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         mesh_i = gpu.load_mesh(pp)
-        r = gpu.detect_fast(mesh_i, sample, opts, precision="bf16", seeds=SEEDS)
+        r = gpu.detect_fast(mesh_i, sample, opts, precision="bf16", seeds=SEEDS,
+                            max_iterations=ITERATIONS, polish_iterations=POLISH)
         b.record(stream)
         b.synchronize()
         mesh_i.close()
@@ -305,7 +311,12 @@ def run_gpu(args):
         "mode_error": {pr: {"max": e["mode_error_max"], "mean": e["mode_error_mean"],
                             "seeds": 256} for pr, e in err.items()},
         "mean_shift": {"bulk_iterations": r["iterations"], "polish_iterations": r["polish_iterations"],
-                       "modes": r["modes"], "evaluations": evals},
+                       "modes": r["modes"], "evaluations": evals,
+                       "bulk_ms": round(r["bulk_ms"], 3), "polish_ms": round(r["polish_ms"], 3),
+                       "fp32_ms": round(res_fp32[-1]["bulk_ms"], 3),
+                       "fp32_iterations": res_fp32[-1]["iterations"],
+                       "bulk_trace": r["bulk_trace"][:24], "polish_trace": r["polish_trace"][:24],
+                       "fp32_trace": res_fp32[-1]["bulk_trace"][:24]},
         "stage_ms": {k: round(statistics.mean(x["stage_ms"][k] for x in res_bf16), 3)
                      for k in r["stage_ms"]},
         "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",

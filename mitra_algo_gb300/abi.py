@@ -155,6 +155,8 @@ class FastResult(C.Structure):
                 ("polish_iterations", C.c_int32), ("mode_error_max", C.c_double),
                 ("mode_error_mean", C.c_double), ("stage_ms", C.c_double * 8),
                 ("mean_shift_pairs", C.c_double), ("seed_iterations", C.c_double),
+                ("bulk_ms", C.c_double), ("polish_ms", C.c_double),
+                ("bulk_trace", C.c_uint32 * 64), ("polish_trace", C.c_uint32 * 64),
                 ("launches", C.c_uint64), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("records", ClusterRecord * FAST_MAX_CLUSTERS),
                 ("support", C.c_uint64 * FAST_MAX_CLUSTERS),

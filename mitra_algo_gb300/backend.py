@@ -174,7 +174,9 @@ class Gb300Backend:
                                             "iterations", "polish_iterations", "mode_error_max",
                                             "mode_error_mean", "mean_shift_pairs",
                                             "seed_iterations", "launches", "h2d_bytes",
-                                            "d2h_bytes")}
+                                            "d2h_bytes", "bulk_ms", "polish_ms")}
+        out["bulk_trace"] = [int(x) for x in res.bulk_trace][:max(0, res.iterations)]
+        out["polish_trace"] = [int(x) for x in res.polish_trace][:max(0, res.polish_iterations)]
         out["stage_ms"] = dict(zip(abi.STAGES, list(res.stage_ms)))
         out["support"] = list(res.support)[:n]
         out["coverage"] = list(res.coverage)[:n]

@@ -55,6 +55,21 @@ public:
   size_t peak() const { return peak_; }
   size_t capacity() const;
   void release();
+  // Scoped reuse inside one call: allocations made after mark() are given
+  // back by rewind() (loops that allocate per iteration).
+  struct Mark {
+    std::vector<size_t> tops;
+    size_t used;
+  };
+  Mark mark() const {
+    Mark m{{}, used_};
+    for (auto &b : blocks_) m.tops.push_back(b.top);
+    return m;
+  }
+  void rewind(const Mark &m) {
+    for (size_t i = 0; i < blocks_.size(); ++i) blocks_[i].top = i < m.tops.size() ? m.tops[i] : 0;
+    used_ = m.used;
+  }
 
 private:
   struct Block {

@@ -309,7 +309,8 @@ Grid grid_for(uint64_t nactive, uint64_t nchunks) {
 
 template <typename T>
 int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *state, uint64_t k,
-               double h2, int max_iter, double *seed_iterations, unsigned long long *evals) {
+               double h2, int max_iter, double *seed_iterations, unsigned long long *evals,
+               uint32_t *trace = nullptr, int trace_len = 0) {
   cudaStream_t st = call.stream();
   int32_t *ids = call.alloc<int32_t>(k);
   unsigned *nact = call.alloc<unsigned>(1);
@@ -327,6 +328,7 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
     call.launched();
     if (!n) break;
     if (seed_iterations) *seed_iterations += n;
+    if (trace && it < trace_len) trace[it] = n;
     Grid g = grid_for(n, v.nchunks);
     if (g.splits * g.slots > cap) fail(SYM_RUNTIME_ERROR, "mean-shift partial buffer too small");
     ms_tile<T, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
@@ -391,8 +393,10 @@ void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t
 }
 
 int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k, double h2,
-          int max_iter, double *seed_iterations, unsigned long long *evals) {
-  return shift_impl<float>(call, v, v.desc, means, state, k, h2, max_iter, seed_iterations, evals);
+          int max_iter, double *seed_iterations, unsigned long long *evals, uint32_t *trace,
+          int trace_len) {
+  return shift_impl<float>(call, v, v.desc, means, state, k, h2, max_iter, seed_iterations, evals,
+                           trace, trace_len);
 }
 
 int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,

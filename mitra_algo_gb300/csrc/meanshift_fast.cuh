@@ -37,7 +37,8 @@ void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t
 // (0 moving, 1 converged, 2 exhausted).  Adds the seed-iterations to
 // *seed_iterations and seed-vote evaluations to *evals (device counter).
 int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k, double h2,
-          int max_iter, double *seed_iterations, unsigned long long *evals);
+          int max_iter, double *seed_iterations, unsigned long long *evals,
+          uint32_t *trace = nullptr, int trace_len = 0);
 int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,
           int max_iter, double *seed_iterations, unsigned long long *evals);
 

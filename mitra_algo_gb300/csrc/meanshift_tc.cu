@@ -16,6 +16,7 @@
 // mbarrier wait is bounded; on timeout the CTA records a status, drains and
 // frees its TMEM.
 #include "meanshift_fast.cuh"
+#include "primitives.cuh"
 
 #include <cuda_bf16.h>
 
@@ -191,29 +192,10 @@ __global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, co
   xx[t] = v < q ? n2 : 1e30f;  // padding votes sit infinitely far away
 }
 
-struct TcArgs {
-  const uint8_t *images;
-  const float *centers;  // nchunks x 8
-  const float *cbox;     // nchunks x 12
-  uint64_t nchunks;
-  const float *means;    // k x 8
-  const int32_t *ids;
-  uint64_t nactive;
-  float inv_h2, skip_gap2;
-  uint64_t chunks_per_split;
-  float *partial;        // splits x slots x 8
-  unsigned long long *evals;
-  int *status;
-};
-
-// Dynamic shared memory layout (bytes).
+// Shared-memory plan of the self-test (one tile, one stage).
 constexpr uint32_t kOffA1 = 0, kOffA2 = 4096, kOffStage = 4096 + 32768;
-constexpr uint32_t kOffBars = kOffStage + 2 * kImage;  // 54272
+constexpr uint32_t kOffBars = kOffStage + 2 * kImage;
 constexpr uint32_t kOffMisc = kOffBars + 64;
-constexpr uint32_t kOffRed = kOffMisc + 64;            // 128 rows x 8 floats
-constexpr uint32_t kSmemUsed = kOffRed + 128 * 8 * 4;
-static_assert(kSmemUsed <= 100 * 1024, "shared memory plan exceeds the request");
-// Two CTAs per SM: their 2 x 256 TMEM columns fill the SM's 512 exactly.
 constexpr uint32_t kSmemRequest = 100 * 1024;
 constexpr uint32_t kTmemCols = 256, kColD = 0, kColAcc = 128;
 
@@ -226,197 +208,300 @@ __device__ __forceinline__ float box_gap2_tc(const float *lo, const float *hi, c
   return g;
 }
 
-__global__ void __launch_bounds__(256, 2) ms_tile_tc(TcArgs a) {
+// ------------------------------------------------- work lists per tile
+// Box of each tile's active seeds (one block of kChunk threads per tile).
+__global__ void tile_boxes(const float *means, const int32_t *ids, uint64_t nactive, float *boxes) {
+  __shared__ float part[4][12];
+  uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
+  bool live = slot < nactive;
+  float lo[6], hi[6];
+  for (int d = 0; d < 6; ++d) {
+    float m = live ? means[uint64_t(ids[slot]) * 8 + d] : 0.f;
+    lo[d] = live ? m : INFINITY, hi[d] = live ? m : -INFINITY;
+  }
+  for (int o = 16; o; o >>= 1)
+    for (int d = 0; d < 6; ++d) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+  int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int d = 0; d < 6; ++d) part[warp][d] = lo[d], part[warp][6 + d] = hi[d];
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    float v = part[0][threadIdx.x];
+    for (int w = 1; w < 4; ++w)
+      v = threadIdx.x < 6 ? fminf(v, part[w][threadIdx.x]) : fmaxf(v, part[w][threadIdx.x]);
+    boxes[blockIdx.x * 12 + threadIdx.x] = v;
+  }
+}
+
+// need[t * nchunks + c]: chunk c lies within the bandwidth of tile t's box.
+__global__ void tile_needs(const float *boxes, const float *cbox, uint64_t nchunks, float skip_gap2,
+                           uint8_t *need) {
+  uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint64_t t = blockIdx.y;
+  if (c >= nchunks) return;
+  const float *tb = boxes + t * 12;
+  need[t * nchunks + c] = box_gap2_tc(tb, tb + 6, cbox + c * 12) <= skip_gap2;
+}
+
+// offsets[t] = first list entry of tile t (entries are t * nchunks + c,
+// ascending); offsets[tiles] = list length.
+__global__ void tile_offsets(const int32_t *list, const uint64_t *count, uint64_t tiles,
+                             uint64_t nchunks, uint64_t *offsets) {
+  uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t > tiles) return;
+  uint64_t n = *count;
+  if (t == tiles) {
+    offsets[t] = n;
+    return;
+  }
+  uint64_t key = t * nchunks, lo = 0, hi = n;
+  while (lo < hi) {
+    uint64_t mid = (lo + hi) / 2;
+    if (uint64_t(list[mid]) < key) lo = mid + 1;
+    else hi = mid;
+  }
+  offsets[t] = lo;
+}
+
+// --------------------------------------------- pipelined tensor kernel
+// Warp roles: warps 0..15 form four epilogue warpgroups (warpgroup g owns
+// D columns 32g..32g+31 of every row; warp w reads TMEM lanes 32(w%4)..),
+// warp 16 is the producer (TMA, A1 staging, MMA issue).
+//   stages   3 TMA buffers of one chunk image each
+//   D[2]     two TMEM accumulators for MMA1 (columns 0..127, 128..255)
+//   ACC      TMEM columns 256..271
+//   A1[2]    seeds centred on the chunk, A2[2] BF16 weights
+// Handshakes (mbarriers): load_full[s] (TMA bytes), d_full[b] (MMA1 done),
+// d_free[b] (epilogue read D[b]), a2_full[b] (epilogue wrote A2[b]),
+// a2_free[b] and stage_free[s] (MMA2 done), acc_done.
+constexpr int kStages = 3;
+constexpr int kEpiWarps = 16, kThreads2 = (kEpiWarps + 1) * 32;
+constexpr uint32_t kT2A1 = 0;                                 // 2 x 4096
+constexpr uint32_t kT2A2 = 8192;                              // 2 x 32768
+constexpr uint32_t kT2Stage = kT2A2 + 2 * 32768;              // 3 x kImage
+constexpr uint32_t kT2Bars = kT2Stage + kStages * kImage;     // 14 barriers
+constexpr uint32_t kT2Misc = kT2Bars + 16 * 8;
+constexpr uint32_t kT2Seeds = kT2Misc + 64;                   // 128 x 8 floats
+constexpr uint32_t kT2Red = kT2Seeds + 128 * 8 * 4;           // 4 x 128 x 8 floats
+constexpr uint32_t kT2Smem = kT2Red + 4 * 128 * 8 * 4;
+static_assert(kT2Stage % 128 == 0 && kImage % 16 == 0, "TMA alignment");
+constexpr uint32_t kT2Cols = 512, kT2ColAcc = 256;
+
+struct Tc2Args {
+  const uint8_t *images;
+  const float *centers;  // nchunks x 8
+  uint64_t nchunks;
+  const int32_t *list;   // needed (tile, chunk) entries, t * nchunks + c
+  const uint64_t *offsets;  // tiles + 1
+  uint64_t splits;
+  const float *means;
+  const int32_t *ids;
+  uint64_t nactive;
+  float inv_h2;
+  float *partial;
+  unsigned long long *evals;
+  int *status;
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *A1 = smem + kOffA1, *A2 = smem + kOffA2;
-  uint8_t *stage[2] = {smem + kOffStage, smem + kOffStage + kImage};
-  uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + kOffBars);  // [2]
-  uint64_t *bar_mma1 = bar_load + 2, *bar_mma2 = bar_load + 3;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kOffMisc);
-  float *tile_box = reinterpret_cast<float *>(smem + kOffMisc + 16);  // written by warp 0: 12
-  float *red = reinterpret_cast<float *>(smem + kOffRed);
+  uint8_t *A1 = smem + kT2A1, *A2 = smem + kT2A2, *stage = smem + kT2Stage;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kT2Bars);
+  uint64_t *load_full = bars, *stage_free = bars + 3, *d_full = bars + 6, *d_free = bars + 8;
+  uint64_t *a2_full = bars + 10, *a2_free = bars + 12, *acc_done = bars + 14;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kT2Misc);
+  float *seeds = reinterpret_cast<float *>(smem + kT2Seeds);
+  float *red = reinterpret_cast<float *>(smem + kT2Red);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int wg = warp >> 2, quad = warp & 3, row = quad * 32 + lane;
-  const uint64_t slot = uint64_t(blockIdx.x) * kChunk + row, split = blockIdx.y;
+  const uint64_t tile = blockIdx.x, split = blockIdx.y;
   const uint64_t slots = uint64_t(gridDim.x) * kChunk;
-  const bool live = slot < a.nactive;
-  float m[6];
-  {
-    int32_t seed = live ? a.ids[slot] : 0;
-    for (int d = 0; d < 6; ++d) m[d] = live ? a.means[uint64_t(seed) * 8 + d] : 0.f;
-  }
-  // tile box over live seeds (warpgroup 0 covers every row once)
-  if (wg == 0) {
-    float lo[6], hi[6];
-    for (int d = 0; d < 6; ++d) lo[d] = live ? m[d] : INFINITY, hi[d] = live ? m[d] : -INFINITY;
-    for (int o = 16; o; o >>= 1)
-      for (int d = 0; d < 6; ++d) {
-        lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-        hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
-      }
-    if (lane == 0)
-      for (int d = 0; d < 6; ++d) red[quad * 12 + d] = lo[d], red[quad * 12 + 6 + d] = hi[d];
+  const uint64_t lt0 = a.offsets[tile], lt1 = a.offsets[tile + 1], len = lt1 - lt0;
+  const uint64_t e0 = lt0 + len * split / a.splits, e1 = lt0 + len * (split + 1) / a.splits;
+  const uint32_t n = uint32_t(e1 - e0);
+  const uint64_t tbase = tile * a.nchunks;
+  auto chunk_of = [&](uint32_t i) { return uint64_t(a.list[e0 + i]) - tbase; };
+
+  if (tid < kChunk) {  // seed means of the tile -> shared memory
+    uint64_t slot = tile * kChunk + tid;
+    bool live = slot < a.nactive;
+    int32_t sd = live ? a.ids[slot] : 0;
+    for (int d = 0; d < 8; ++d) seeds[tid * 8 + d] = live && d < 6 ? a.means[uint64_t(sd) * 8 + d] : 0.f;
   }
   if (tid == 0) {
-    mbar_init(&bar_load[0], 1);
-    mbar_init(&bar_load[1], 1);
-    mbar_init(bar_mma1, 1);
-    mbar_init(bar_mma2, 1);
+    for (int s = 0; s < kStages; ++s) mbar_init(&load_full[s], 1), mbar_init(&stage_free[s], 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&d_full[b], 1);
+      mbar_init(&d_free[b], kEpiWarps);
+      mbar_init(&a2_full[b], kEpiWarps);
+      mbar_init(&a2_free[b], 1);
+    }
+    mbar_init(acc_done, 1);
     fence_mbar_init();
   }
-  if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+  if (warp == 0 && n) tmem_alloc(tmem_slot, kT2Cols);
+  tc_fence_before();
   __syncthreads();
-  if (tid < 12) {
-    float v = red[tid];
-    for (int qd = 1; qd < 4; ++qd) v = tid < 6 ? fminf(v, red[qd * 12 + tid]) : fmaxf(v, red[qd * 12 + tid]);
-    tile_box[tid] = v;
-  }
   tc_fence_after();
-  __syncthreads();
-  const uint32_t tmem = *tmem_slot;
-  float tlo[6], thi[6];
-  for (int d = 0; d < 6; ++d) tlo[d] = tile_box[d], thi[d] = tile_box[6 + d];
-
-  const uint64_t c0 = split * a.chunks_per_split;
-  const uint64_t c1 = c0 + a.chunks_per_split < a.nchunks ? c0 + a.chunks_per_split : a.nchunks;
-  auto next_needed = [&](uint64_t c) {
-    while (c < c1 && box_gap2_tc(tlo, thi, a.cbox + c * 12) > a.skip_gap2) ++c;
-    return c;
-  };
-  const float inv_h2 = a.inv_h2, two_inv_h2 = 2.f * a.inv_h2;
-  float sumw = 0, corr[6] = {0, 0, 0, 0, 0, 0};
+  const uint32_t tmem = n ? *tmem_slot : 0;
   bool ok = true;
-  uint64_t processed = 0;
-  uint64_t c = next_needed(c0);
-  // issued[b] / consumed[b]: loads issued into / waited on buffer b
-  uint32_t issued[2] = {0, 0}, consumed[2] = {0, 0}, mma_issued = 0, mma_done = 0;
-  if (tid == 0 && c < c1) {
-    mbar_expect_tx(&bar_load[0], kImage);
-    tma_bulk_load(stage[0], a.images + c * kImage, kImage, &bar_load[0]);
-  }
-  if (c < c1) issued[0] = 1;
-  uint32_t i = 0;
-  for (; c < c1 && ok; ++i) {
-    const uint32_t buf = i & 1;
-    const uint64_t cn = next_needed(c + 1);
-    if (tid == 0 && cn < c1) {  // prefetch the next needed chunk
-      mbar_expect_tx(&bar_load[buf ^ 1], kImage);
-      tma_bulk_load(stage[buf ^ 1], a.images + cn * kImage, kImage, &bar_load[buf ^ 1]);
+
+  if (warp == kEpiWarps) {
+    // ------------------------------------------------------- producer
+    for (uint32_t i = 0; i < n && i < uint32_t(kStages); ++i)
+      if (lane == 0) {
+        mbar_expect_tx(&load_full[i], kImage);
+        tma_bulk_load(stage + i * kImage, a.images + chunk_of(i) * kImage, kImage, &load_full[i]);
+      }
+    for (uint32_t i = 0; i < n && ok; ++i) {
+      const uint32_t b = i & 1, s = i % kStages;
+      const float *cen = a.centers + chunk_of(i) * 8;
+      if (i >= 2) ok = mbar_wait(&d_full[b], ((i - 2) / 2) & 1);  // MMA1(i-2) done with A1[b]
+      // A1[b]: 4 rows per lane, seeds centred on the chunk, BF16
+      for (int r = lane; r < kChunk && ok; r += 32) {
+        __align__(16) __nv_bfloat16 h[16];
+        for (int k = 0; k < 16; ++k)
+          h[k] = __float2bfloat16_rn(k < 6 ? seeds[r * 8 + k] - cen[k] : 0.f);
+        uint8_t *dst = A1 + b * 4096;
+        *reinterpret_cast<uint4 *>(dst + kmajor_offset(r, 0, 128, 256)) = *reinterpret_cast<uint4 *>(&h[0]);
+        *reinterpret_cast<uint4 *>(dst + kmajor_offset(r, 8, 128, 256)) = *reinterpret_cast<uint4 *>(&h[8]);
+      }
+      fence_async_smem();
+      __syncwarp();
+      ok = ok && mbar_wait(&load_full[s], (i / kStages) & 1);
+      if (ok && i >= 2) ok = mbar_wait(&d_free[b], ((i - 2) / 2) & 1);  // D[b] read
+      if (!ok) break;
+      tc_fence_after();
+      if (lane == 0) {
+        mma_bf16(tmem + 128 * b, smem_desc(A1 + b * 4096, 128, 256),
+                 smem_desc(stage + s * kImage, 128, 256), idesc_bf16(128, 128), 0);
+        mma_commit(&d_full[b]);
+      }
+      if (i >= 1) {  // MMA2 of the previous chunk, then refill its stage
+        const uint32_t j = i - 1, bj = j & 1, sj = j % kStages;
+        ok = mbar_wait(&a2_full[bj], (j / 2) & 1);
+        if (!ok) break;
+        tc_fence_after();
+        if (lane == 0) {
+          for (uint32_t q = 0; q < 8; ++q)
+            mma_bf16(tmem + kT2ColAcc, smem_desc(A2 + bj * 32768 + q * 256, 128, 2048),
+                     smem_desc(stage + sj * kImage + kB1Bytes + q * 256, 128, 2048),
+                     idesc_bf16(128, 16), (j > 0 || q > 0) ? 1u : 0u);
+          mma_commit(&a2_free[bj]);
+          mma_commit(&stage_free[sj]);
+        }
+        if (j + kStages < n) {
+          ok = mbar_wait(&stage_free[sj], (j / kStages) & 1);
+          if (!ok) break;
+          if (lane == 0) {
+            mbar_expect_tx(&load_full[sj], kImage);
+            tma_bulk_load(stage + sj * kImage, a.images + chunk_of(j + kStages) * kImage, kImage,
+                          &load_full[sj]);
+          }
+        }
+      }
     }
-    if (cn < c1) ++issued[buf ^ 1];
-    // A1: this tile's seeds centred on the chunk, BF16, 16 features
-    const float *cen = a.centers + c * 8;
-    float sp[6], ss = 0;
-    for (int d = 0; d < 6; ++d) {
-      float r = __bfloat162float(__float2bfloat16_rn(m[d] - cen[d]));
-      sp[d] = r;
-      ss += r * r;
+    if (ok && n) {  // last MMA2
+      const uint32_t j = n - 1, bj = j & 1, sj = j % kStages;
+      ok = mbar_wait(&a2_full[bj], (j / 2) & 1);
+      tc_fence_after();
+      if (ok && lane == 0) {
+        for (uint32_t q = 0; q < 8; ++q)
+          mma_bf16(tmem + kT2ColAcc, smem_desc(A2 + bj * 32768 + q * 256, 128, 2048),
+                   smem_desc(stage + sj * kImage + kB1Bytes + q * 256, 128, 2048),
+                   idesc_bf16(128, 16), (j > 0 || q > 0) ? 1u : 0u);
+        mma_commit(acc_done);
+      }
     }
-    if (wg == 0) {
-      __align__(16) __nv_bfloat16 h[16];
-      for (int k = 0; k < 16; ++k) h[k] = __float2bfloat16_rn(k < 6 ? sp[k] : 0.f);
-      *reinterpret_cast<uint4 *>(A1 + kmajor_offset(row, 0, 128, 256)) = *reinterpret_cast<uint4 *>(&h[0]);
-      *reinterpret_cast<uint4 *>(A1 + kmajor_offset(row, 8, 128, 256)) = *reinterpret_cast<uint4 *>(&h[8]);
+    if (!ok && lane == 0) {
+      atomicExch(a.status, DS_SPIN_LIMIT);
+      mbar_arrive(acc_done);  // release the epilogue
     }
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (!__syncthreads_and(mbar_wait(&bar_load[buf], (i >> 1) & 1))) {
-      ok = false;
-      break;
-    }
-    ++consumed[buf];
-    if (tid == 0) {
-      mma_bf16(tmem + kColD, smem_desc(A1, 128, 256), smem_desc(stage[buf], 128, 256),
-               idesc_bf16(128, 128), 0);
-      mma_commit(bar_mma1);
-    }
-    ++mma_issued;
-    if (!__syncthreads_and(mbar_wait(bar_mma1, i & 1))) {
-      ok = false;
-      break;
-    }
-    tc_fence_after();
-    // epilogue: 64 columns of this thread's row
-    const float *xx = reinterpret_cast<const float *>(stage[buf] + kB1Bytes + kB2Bytes);
-    const float rowc = 1.f - ss * inv_h2;
-    float sw = 0;
-    for (int half = 0; half < 2; ++half) {
-      const uint32_t col = 64 * wg + 32 * half;
+  } else {
+    // ------------------------------------------------------- epilogue
+    const int quad = warp & 3, g = warp >> 2, row = quad * 32 + lane;
+    float m[6];
+    for (int d = 0; d < 6; ++d) m[d] = seeds[row * 8 + d];
+    const float two_inv_h2 = 2.f * a.inv_h2;
+    float sumw = 0, corr[6] = {0, 0, 0, 0, 0, 0};
+    for (uint32_t i = 0; i < n; ++i) {
+      const uint32_t b = i & 1, s = i % kStages;
+      const float *cen = a.centers + chunk_of(i) * 8;
+      float ss = 0;
+      for (int d = 0; d < 6; ++d) {
+        float r = __bfloat162float(__float2bfloat16_rn(m[d] - cen[d]));
+        ss += r * r;
+      }
+      const float rowc = 1.f - ss * a.inv_h2;
+      if (!mbar_wait(&load_full[s], (i / kStages) & 1) || !mbar_wait(&d_full[b], (i / 2) & 1)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
       float dot[32];
-      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kColD + col, dot);
+      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + 128 * b + 32 * g, dot);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&d_free[b]);
+      const float *xx = reinterpret_cast<const float *>(stage + s * kImage + kB1Bytes + kB2Bytes) + 32 * g;
       __align__(16) __nv_bfloat16 w[32];
+      float sw = 0;
       for (int j = 0; j < 32; ++j) {
-        float t = fmaf(dot[j], two_inv_h2, fmaf(xx[col + j], -inv_h2, rowc));
+        float t = fmaf(dot[j], two_inv_h2, fmaf(xx[j], -a.inv_h2, rowc));
         float wj = fmaxf(t, 0.f);
         sw += wj;
         w[j] = __float2bfloat16_rn(wj);
       }
+      if (i >= 2 && !mbar_wait(&a2_free[b], ((i - 2) / 2) & 1)) {
+        ok = false;
+        break;
+      }
+      uint8_t *dst = A2 + b * 32768;
       for (int kb = 0; kb < 4; ++kb)
-        *reinterpret_cast<uint4 *>(A2 + kmajor_offset(row, col + 8 * kb, 128, 2048)) =
+        *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, 32 * g + 8 * kb, 128, 2048)) =
             *reinterpret_cast<uint4 *>(&w[8 * kb]);
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&a2_full[b]);
+      sumw += sw;
+      for (int d = 0; d < 6; ++d) corr[d] = fmaf(cen[d], sw, corr[d]);
     }
-    sumw += sw;
-    for (int d = 0; d < 6; ++d) corr[d] = fmaf(cen[d], sw, corr[d]);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    if (tid == 0) {
-      for (uint32_t s = 0; s < 8; ++s)
-        mma_bf16(tmem + kColAcc, smem_desc(A2 + s * 256, 128, 2048),
-                 smem_desc(stage[buf] + kB1Bytes + s * 256, 128, 2048), idesc_bf16(128, 16),
-                 (processed > 0 || s > 0) ? 1u : 0u);
-      mma_commit(bar_mma2);
-    }
-    ++mma_issued;
-    if (!__syncthreads_and(mbar_wait(bar_mma2, i & 1))) {
-      ok = false;
-      break;
-    }
-    mma_done = mma_issued;
-    tc_fence_after();
-    ++processed;
-    c = cn;
-  }
-  if (!ok && tid == 0) {
-    // Drain: wait (bounded) for every copy and MMA still in flight before
-    // the shared memory and TMEM of this CTA are released.
-    for (uint32_t b = 0; b < 2; ++b)
-      for (uint32_t n = consumed[b]; n < issued[b]; ++n) mbar_wait(&bar_load[b], n & 1);
-    if (mma_issued > mma_done) {
-      mbar_wait(bar_mma1, (mma_done / 2) & 1);
-      mbar_wait(bar_mma2, (mma_done / 2) & 1);
-    }
-  }
-  // combine: warpgroup 1 hands its FP32 parts to warpgroup 0
-  __syncthreads();
-  if (wg == 1) {
-    red[row * 8 + 6] = sumw;
-    for (int d = 0; d < 6; ++d) red[row * 8 + d] = corr[d];
+    float *mine = red + (g * 128 + row) * 8;
+    for (int d = 0; d < 6; ++d) mine[d] = corr[d];
+    mine[6] = sumw;
+    if (!ok && lane == 0) atomicExch(a.status, DS_SPIN_LIMIT);
   }
   __syncthreads();
-  if (wg == 0) {
+  if (warp < 4) {  // warpgroup 0 writes the tile's partial sums
+    const int quad = warp & 3, row = quad * 32 + lane;
     float acc[32];
-    if (processed && ok) {
-      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kColAcc, acc);
-    } else {
-      for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+    for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+    if (n && mbar_wait(acc_done, 0)) {
+      tc_fence_after();
+      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kT2ColAcc, acc);
     }
-    float *out = a.partial + (split * slots + slot) * 8;
-    for (int d = 0; d < 6; ++d) out[d] = acc[d] + corr[d] + red[row * 8 + d];
-    out[6] = sumw + red[row * 8 + 6];
+    float tot[7];
+    for (int d = 0; d < 7; ++d) {
+      float v = 0;
+      for (int gg = 0; gg < 4; ++gg) v += red[(gg * 128 + row) * 8 + d];
+      tot[d] = v;
+    }
+    float *out = a.partial + (split * slots + tile * kChunk + row) * 8;
+    for (int d = 0; d < 6; ++d) out[d] = acc[d] + tot[d];
+    out[6] = tot[6];
     out[7] = 0.f;
   }
-  if (tid == 0) {
-    if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
-    if (processed && a.evals) atomicAdd(a.evals, processed * (unsigned long long)(kChunk * kChunk));
-  }
+  if (tid == 0 && n && a.evals) atomicAdd(a.evals, uint64_t(n) * uint64_t(kChunk * kChunk));
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+  if (warp == 0 && n) tmem_dealloc(tmem, kT2Cols);
 }
 
 // ------------------------------------------------------ tensor self-test
@@ -524,15 +609,17 @@ unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const ui
                       uint64_t k, int32_t *ids);
 
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
-                         double h2, int max_iter, int *iterations, double *evaluations) {
+                         double h2, int max_iter, int *iterations, double *evaluations,
+                         uint32_t *trace, int trace_len) {
   *iterations = 0;
   *evaluations = 0;
   if (!k || !v.q) return false;
+  const uint64_t max_tiles = (k + kChunk - 1) / kChunk;
+  if (max_tiles * v.nchunks >= (uint64_t(1) << 31)) return false;  // list entries are int32
   cudaStream_t st = call.stream();
   static bool configured = false;
   if (!configured) {
-    SYM_CUDA(cudaFuncSetAttribute(ms_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemRequest));
+    SYM_CUDA(cudaFuncSetAttribute(ms_tile_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kT2Smem));
     configured = true;
   }
   uint8_t *images = call.alloc<uint8_t>(v.nchunks * kImage);
@@ -541,8 +628,12 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
                                                        centers);
   check_launch();
   int32_t *ids = call.alloc<int32_t>(k);
-  uint64_t cap = (64 * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
-  float *partial = call.alloc<float>(cap * 8);
+  float *boxes = call.alloc<float>(max_tiles * 12);
+  uint8_t *need = call.alloc<uint8_t>(max_tiles * v.nchunks);
+  int32_t *list = call.alloc<int32_t>(max_tiles * v.nchunks);
+  uint64_t *count = call.alloc<uint64_t>(1), *offsets = call.alloc<uint64_t>(max_tiles + 1);
+  const uint64_t max_splits = 152;
+  float *partial = call.alloc<float>(max_splits * max_tiles * kChunk * 8);
   unsigned long long *evals = call.alloc<unsigned long long>(1);
   SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
   float gap = float(std::sqrt(h2)) + 1e-6f;
@@ -551,21 +642,27 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   for (; it < max_iter; ++it) {
     unsigned n = active_seeds(call, v, means, state, k, ids);
     if (!n) break;
-    uint64_t tiles = (n + kChunk - 1) / kChunk;
-    uint64_t want = (2 * 152 + tiles - 1) / tiles;
-    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(v.nchunks, want));
-    uint64_t cps = (v.nchunks + splits - 1) / splits;
-    splits = (v.nchunks + cps - 1) / cps;
-    uint64_t slots = tiles * kChunk;
-    if (splits * slots > cap) fail(SYM_RUNTIME_ERROR, "tensor mean-shift partial buffer too small");
-    TcArgs args{images, centers, v.cbox, v.nchunks, means, ids, n, float(1.0 / h2), gap * gap,
-                cps, partial, evals, call.status()};
-    ms_tile_tc<<<dim3(unsigned(tiles), unsigned(splits)), 256, kSmemRequest, st>>>(args);
+    if (trace && it < trace_len) trace[it] = n;
+    const uint64_t tiles = (n + kChunk - 1) / kChunk;
+    const uint64_t splits = std::max<uint64_t>(1, max_splits / tiles);
+    auto mark = call.ctx->arena.mark();
+    tile_boxes<<<unsigned(tiles), kChunk, 0, st>>>(means, ids, n, boxes);
     check_launch();
-    ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, splits, slots, ids, n,
-                                                       float(h2), 1e-4f, state);
+    tile_needs<<<dim3(blocks_for(v.nchunks), unsigned(tiles)), kThreads, 0, st>>>(
+        boxes, v.cbox, v.nchunks, gap * gap, need);
     check_launch();
-    call.launched(2);
+    compact_indices(call, need, tiles * v.nchunks, list, count);
+    tile_offsets<<<blocks_for(tiles + 1), kThreads, 0, st>>>(list, count, tiles, v.nchunks, offsets);
+    check_launch();
+    Tc2Args args{images, centers, v.nchunks, list, offsets, splits, means, ids, n,
+                 float(1.0 / h2), partial, evals, call.status()};
+    ms_tile_tc2<<<dim3(unsigned(tiles), unsigned(splits)), kThreads2, kT2Smem, st>>>(args);
+    check_launch();
+    ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, splits, tiles * kChunk, ids,
+                                                       n, float(h2), 1e-6f, state);
+    check_launch();
+    call.launched(5);
+    call.ctx->arena.rewind(mark);
   }
   call.check_status("mean_shift (tensor)");
   unsigned long long ev = 0;

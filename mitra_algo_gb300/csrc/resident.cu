@@ -41,7 +41,8 @@ void verification_core(Call &, const sym_mesh_view &, const double *, const int3
 // BF16 tensor-core bulk iterations (meanshift_tc.cu); returns false when the
 // tensor path cannot run this problem (the caller then stays in FP32).
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
-                         double h2, int max_iter, int *iterations, double *evaluations);
+                         double h2, int max_iter, int *iterations, double *evaluations,
+                         uint32_t *trace = nullptr, int trace_len = 0);
 void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,
                       const uint16_t *b2, float *d_out, float *acc_out);
 }  // namespace sym
@@ -273,13 +274,31 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   init_means(call, vs, seed_rank, k, m32);
   int bulk = 0, polish = 0;
   double tc_evals = 0;
-  if (fo.precision == SYM_MS_BF16_REFINED &&
-      meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals)) {
+  cudaEvent_t ph[3];
+  for (auto &e : ph) cudaEventCreate(&e);
+  cudaEventRecord(ph[0], st);
+  bool tensor = fo.precision == SYM_MS_BF16_REFINED &&
+                meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals,
+                                    r.bulk_trace, 64);
+  cudaEventRecord(ph[1], st);
+  if (tensor) {
     SYM_CUDA(cudaMemsetAsync(st32, 0, k, st));  // polish every seed in FP32
-    polish = shift(call, vs, m32, st32, k, h2, fo.polish_iterations, &r.seed_iterations, evals);
+    polish = shift(call, vs, m32, st32, k, h2, fo.polish_iterations, &r.seed_iterations, evals,
+                   r.polish_trace, 64);
   } else {
-    bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, &r.seed_iterations, evals);
+    bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, &r.seed_iterations, evals,
+                 r.bulk_trace, 64);
   }
+  cudaEventRecord(ph[2], st);
+  cudaEventSynchronize(ph[2]);
+  {
+    float a = 0, b = 0;
+    cudaEventElapsedTime(&a, ph[0], ph[1]);
+    cudaEventElapsedTime(&b, ph[1], ph[2]);
+    r.bulk_ms = tensor ? a : b;
+    r.polish_ms = tensor ? b : 0;
+  }
+  for (auto &e : ph) cudaEventDestroy(e);
   r.iterations = bulk;
   r.polish_iterations = polish;
   unsigned long long ev = 0;
