@@ -223,6 +223,16 @@ def run_gpu(args):
                                max_iterations=ITERATIONS, polish_iterations=POLISH,
                                reference_seeds=reference_seeds)
 
+    if args.once:  # one warm-up and one measured pipeline run (profiler captures)
+        step(args.once)
+        r = step(args.once)
+        print(json.dumps({"precision": args.once, "stage_ms": r["stage_ms"], "pairs": r["pairs"],
+                          "votes": r["votes"], "iterations": r["iterations"],
+                          "polish_iterations": r["polish_iterations"], "bulk_ms": r["bulk_ms"],
+                          "polish_ms": r["polish_ms"], "evaluations": r["mean_shift_pairs"],
+                          "seed_iterations": r["seed_iterations"], "launches": r["launches"]}))
+        return
+
     def timed(precision, steps, warmup):
         for _ in range(warmup):
             step(precision)
@@ -309,7 +319,8 @@ def run_gpu(args):
         "fp32": {"meshes_per_s": round(world * 1000.0 / ms_fp32, 4), "ms_per_step": round(ms_fp32, 3)},
         "bf16_over_fp32": round(ms_fp32 / ms_bf16, 3),
         "mode_error": {pr: {"max": e["mode_error_max"], "mean": e["mode_error_mean"],
-                            "seeds": 256} for pr, e in err.items()},
+                            "reference_seeds": 256, "compared": e["modes_compared"],
+                            "within_1e-4": e["modes_within"]} for pr, e in err.items()},
         "mean_shift": {"bulk_iterations": r["iterations"], "polish_iterations": r["polish_iterations"],
                        "modes": r["modes"], "evaluations": evals,
                        "bulk_ms": round(r["bulk_ms"], 3), "polish_ms": round(r["polish_ms"], 3),
@@ -374,6 +385,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline estimate")
     ap.add_argument("--bandwidth", type=float, default=None, help="override the bandwidth")
+    ap.add_argument("--once", choices=["bf16", "fp32"], default=None,
+                    help="run the pipeline once after one warm-up run and print its stages")
     ap.add_argument("--small", action="store_true",
                     help="level-5 mesh, 5,000 samples, 256 seeds (profiler captures)")
     args = ap.parse_args()

@@ -308,7 +308,11 @@ typedef struct sym_fast_options {
 typedef struct sym_fast_result {
   uint64_t pruned, pairs, votes, modes, clusters;
   int32_t iterations, polish_iterations;
-  double mode_error_max, mode_error_mean; /* relative to FP64, reference seeds */
+  /* relative error of each mode against FP64, over the reference seeds that
+   * converged in both runs (modes_compared of them); modes_within counts
+   * those within 1e-4 */
+  double mode_error_max, mode_error_mean;
+  uint64_t modes_compared, modes_within;
   /* device time per stage: curvature, prune, pairing, votes, vote sort,
    * mean shift, modes, verification */
   double stage_ms[8];

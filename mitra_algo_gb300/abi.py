@@ -153,7 +153,8 @@ class FastResult(C.Structure):
     _fields_ = [("pruned", C.c_uint64), ("pairs", C.c_uint64), ("votes", C.c_uint64),
                 ("modes", C.c_uint64), ("clusters", C.c_uint64), ("iterations", C.c_int32),
                 ("polish_iterations", C.c_int32), ("mode_error_max", C.c_double),
-                ("mode_error_mean", C.c_double), ("stage_ms", C.c_double * 8),
+                ("mode_error_mean", C.c_double), ("modes_compared", C.c_uint64),
+                ("modes_within", C.c_uint64), ("stage_ms", C.c_double * 8),
                 ("mean_shift_pairs", C.c_double), ("seed_iterations", C.c_double),
                 ("bulk_ms", C.c_double), ("polish_ms", C.c_double),
                 ("bulk_trace", C.c_uint32 * 64), ("polish_trace", C.c_uint32 * 64),

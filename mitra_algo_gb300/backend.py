@@ -172,7 +172,8 @@ class Gb300Backend:
         n = int(res.clusters)
         out = {k: getattr(res, k) for k in ("pruned", "pairs", "votes", "modes", "clusters",
                                             "iterations", "polish_iterations", "mode_error_max",
-                                            "mode_error_mean", "mean_shift_pairs",
+                                            "mode_error_mean", "modes_compared", "modes_within",
+                                            "mean_shift_pairs",
                                             "seed_iterations", "launches", "h2d_bytes",
                                             "d2h_bytes", "bulk_ms", "polish_ms")}
         out["bulk_trace"] = [int(x) for x in res.bulk_trace][:max(0, res.iterations)]

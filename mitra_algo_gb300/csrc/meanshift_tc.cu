@@ -4,11 +4,13 @@
 // Flash-style: per (tile of 128 seeds, chunk of 128 votes)
 //   MMA1  D[128x128] = S'[128x16] . X'[128x16]^T      (seed-vote dot products)
 //   epilogue: tcgen05.ld D, w = max(0, 1 - (|s'|^2 + |x'|^2 - 2 s'.x') / h^2)
-//             (Epanechnikov), written as BF16 into shared memory
-//   MMA2  ACC[128x16] += W[128x128] . X'[128x16]        (weighted sums)
+//             (Epanechnikov, packed FP32 FMAs), written as BF16 into shared
+//             memory
+//   MMA2  ACC[128x32] += W[128x128] . [x_hi, 1, x_lo][128x32]
 // S' and X' are centred on the chunk's centre c (X' once per vote set, S' per
 // chunk), which keeps |s'|, |x'| small so the expanded distance does not lose
-// its digits in BF16; sum w x = ACC + c sum w, with sum w kept in FP32.
+// its digits in BF16; MMA2 uses the uncentred x split into a BF16 value and
+// its BF16 residue, plus a ones column, so sum w x and sum w come out of TMEM.
 // Votes are pre-arranged per chunk in the canonical no-swizzle K-major
 // core-matrix layout (8 rows x 16 bytes per core matrix), so one TMA bulk copy
 // (cp.async.bulk + mbarrier complete_tx) stages a chunk.  Accumulators live
@@ -159,42 +161,60 @@ __host__ __device__ constexpr uint32_t kmajor_offset(uint32_t row, uint32_t k, u
   return (row / 8) * sbo + (k / 8) * lbo + (row % 8) * 16 + (k % 8) * 2;
 }
 
-// Chunk image: B1 (X' as 128 votes x 16 features, LBO 128, SBO 256), B2 (X'^T
-// as 16 features x 128 votes, LBO 128, SBO 2048), |x'|^2 (128 floats).
-constexpr uint32_t kB1Bytes = 4096, kB2Bytes = 4096, kXXBytes = 512;
-constexpr uint32_t kImage = kB1Bytes + kB2Bytes + kXXBytes;  // 8704, 16-byte multiple
+// Chunk image (one TMA bulk copy):
+//   B1   X' = x - c as 128 votes x 16 features, K-major (LBO 128, SBO 256)
+//   B2   32 "features" x 128 votes, K-major (LBO 128, SBO 2048): rows 0..5
+//        BF16(x), row 6 ones, rows 16..21 the BF16 rounding residue of x;
+//        MMA2 then yields sum w x (hi + lo) and sum w directly in TMEM
+//   XX   |x'|^2 of the rounded X' (128 floats; far away for padding votes)
+//   CEN  the chunk centre c (8 floats)
+constexpr uint32_t kB1Bytes = 4096, kB2Bytes = 8192, kXXBytes = 512, kCenBytes = 32;
+constexpr uint32_t kImage = kB1Bytes + kB2Bytes + kXXBytes + kCenBytes;  // 12832
+static_assert(kImage % 16 == 0, "TMA bulk copies move multiples of 16 bytes");
 
 __global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, const float *cbox,
-                             uint8_t *images, float *centers) {
+                             uint8_t *images) {
   uint64_t c = blockIdx.x;
   int t = threadIdx.x;  // vote in chunk
   if (c >= nchunks) return;
   const float *b = cbox + c * 12;
   float cen[6];
   for (int d = 0; d < 6; ++d) cen[d] = 0.5f * (b[d] + b[6 + d]);
-  if (t < 6) centers[c * 8 + t] = cen[t];
-  if (t >= 6 && t < 8) centers[c * 8 + t] = 0.f;
   uint64_t v = c * kChunk + t;
+  bool live = v < q;
   uint8_t *img = images + c * kImage;
   __nv_bfloat16 *b1 = reinterpret_cast<__nv_bfloat16 *>(img);
   __nv_bfloat16 *b2 = reinterpret_cast<__nv_bfloat16 *>(img + kB1Bytes);
   float *xx = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes);
+  float *ce = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes + kXXBytes);
+  if (t < 8) ce[t] = t < 6 ? cen[t] : 0.f;
   float n2 = 0;
   for (int k = 0; k < 16; ++k) {
-    float x = 0;
-    if (k < 6 && v < q) x = desc[v * 8 + k] - cen[k];
+    float x = live && k < 6 ? desc[v * 8 + k] - cen[k] : 0.f;
     __nv_bfloat16 h = __float2bfloat16_rn(x);
     float r = __bfloat162float(h);
     n2 += r * r;
     b1[kmajor_offset(t, k, 128, 256) / 2] = h;
-    b2[kmajor_offset(k, t, 128, 2048) / 2] = h;
   }
-  xx[t] = v < q ? n2 : 1e30f;  // padding votes sit infinitely far away
+  for (int k = 0; k < 32; ++k) {
+    float val = 0.f;
+    if (live && k < 6) {
+      val = desc[v * 8 + k];
+    } else if (live && k == 6) {
+      val = 1.f;
+    } else if (live && k >= 16 && k < 22) {
+      float x = desc[v * 8 + (k - 16)];
+      val = x - __bfloat162float(__float2bfloat16_rn(x));
+    }
+    b2[kmajor_offset(k, t, 128, 2048) / 2] = __float2bfloat16_rn(val);
+  }
+  xx[t] = live ? n2 : 1e30f;  // padding votes sit infinitely far away
 }
 
-// Shared-memory plan of the self-test (one tile, one stage).
+// Shared-memory plan of the self-test (one tile, one stage, N = 16 MMA2).
+constexpr uint32_t kSelfB2 = 4096;
 constexpr uint32_t kOffA1 = 0, kOffA2 = 4096, kOffStage = 4096 + 32768;
-constexpr uint32_t kOffBars = kOffStage + 2 * kImage;
+constexpr uint32_t kOffBars = kOffStage + 2 * 8704;
 constexpr uint32_t kOffMisc = kOffBars + 64;
 constexpr uint32_t kSmemRequest = 100 * 1024;
 constexpr uint32_t kTmemCols = 256, kColD = 0, kColAcc = 128;
@@ -282,19 +302,17 @@ constexpr int kEpiWarps = 16, kThreads2 = (kEpiWarps + 1) * 32;
 constexpr uint32_t kT2A1 = 0;                                 // 2 x 4096
 constexpr uint32_t kT2A2 = 8192;                              // 2 x 32768
 constexpr uint32_t kT2Stage = kT2A2 + 2 * 32768;              // 3 x kImage
-constexpr uint32_t kT2Bars = kT2Stage + kStages * kImage;     // 14 barriers
+constexpr uint32_t kT2Bars = kT2Stage + kStages * kImage;     // 15 barriers
 constexpr uint32_t kT2Misc = kT2Bars + 16 * 8;
 constexpr uint32_t kT2Seeds = kT2Misc + 64;                   // 128 x 8 floats
-constexpr uint32_t kT2Red = kT2Seeds + 128 * 8 * 4;           // 4 x 128 x 8 floats
-constexpr uint32_t kT2Smem = kT2Red + 4 * 128 * 8 * 4;
-static_assert(kT2Stage % 128 == 0 && kImage % 16 == 0, "TMA alignment");
+constexpr uint32_t kT2Smem = kT2Seeds + 128 * 8 * 4;
+static_assert(kT2Stage % 128 == 0 && (kT2Stage + kImage) % 16 == 0, "TMA alignment");
 constexpr uint32_t kT2Cols = 512, kT2ColAcc = 256;
 
 struct Tc2Args {
   const uint8_t *images;
-  const float *centers;  // nchunks x 8
   uint64_t nchunks;
-  const int32_t *list;   // needed (tile, chunk) entries, t * nchunks + c
+  const int32_t *list;      // needed (tile, chunk) entries, t * nchunks + c
   const uint64_t *offsets;  // tiles + 1
   uint64_t splits;
   const float *means;
@@ -310,6 +328,16 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+// d = a * b + c on two FP32 lanes at once.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long ra, rb, rc, rd;
+  memcpy(&ra, &a, 8), memcpy(&rb, &b, 8), memcpy(&rc, &c, 8);
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+  float2 d;
+  memcpy(&d, &rd, 8);
+  return d;
+}
+
 __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t *A1 = smem + kT2A1, *A2 = smem + kT2A2, *stage = smem + kT2Stage;
@@ -318,7 +346,6 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
   uint64_t *a2_full = bars + 10, *a2_free = bars + 12, *acc_done = bars + 14;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kT2Misc);
   float *seeds = reinterpret_cast<float *>(smem + kT2Seeds);
-  float *red = reinterpret_cast<float *>(smem + kT2Red);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint64_t tile = blockIdx.x, split = blockIdx.y;
@@ -327,7 +354,6 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
   const uint64_t e0 = lt0 + len * split / a.splits, e1 = lt0 + len * (split + 1) / a.splits;
   const uint32_t n = uint32_t(e1 - e0);
   const uint64_t tbase = tile * a.nchunks;
-  auto chunk_of = [&](uint32_t i) { return uint64_t(a.list[e0 + i]) - tbase; };
 
   if (tid < kChunk) {  // seed means of the tile -> shared memory
     uint64_t slot = tile * kChunk + tid;
@@ -355,6 +381,7 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
 
   if (warp == kEpiWarps) {
     // ------------------------------------------------------- producer
+    auto chunk_of = [&](uint32_t i) { return uint64_t(a.list[e0 + i]) - tbase; };
     for (uint32_t i = 0; i < n && i < uint32_t(kStages); ++i)
       if (lane == 0) {
         mbar_expect_tx(&load_full[i], kImage);
@@ -362,10 +389,11 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
       }
     for (uint32_t i = 0; i < n && ok; ++i) {
       const uint32_t b = i & 1, s = i % kStages;
-      const float *cen = a.centers + chunk_of(i) * 8;
-      if (i >= 2) ok = mbar_wait(&d_full[b], ((i - 2) / 2) & 1);  // MMA1(i-2) done with A1[b]
-      // A1[b]: 4 rows per lane, seeds centred on the chunk, BF16
-      for (int r = lane; r < kChunk && ok; r += 32) {
+      ok = mbar_wait(&load_full[s], (i / kStages) & 1);
+      if (ok && i >= 2) ok = mbar_wait(&d_full[b], ((i - 2) / 2) & 1);  // MMA1(i-2) released A1[b]
+      if (!ok) break;
+      const float *cen = reinterpret_cast<const float *>(stage + s * kImage + kB1Bytes + kB2Bytes + kXXBytes);
+      for (int r = lane; r < kChunk; r += 32) {  // A1[b]: seeds centred on the chunk, BF16
         __align__(16) __nv_bfloat16 h[16];
         for (int k = 0; k < 16; ++k)
           h[k] = __float2bfloat16_rn(k < 6 ? seeds[r * 8 + k] - cen[k] : 0.f);
@@ -375,8 +403,7 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
       }
       fence_async_smem();
       __syncwarp();
-      ok = ok && mbar_wait(&load_full[s], (i / kStages) & 1);
-      if (ok && i >= 2) ok = mbar_wait(&d_free[b], ((i - 2) / 2) & 1);  // D[b] read
+      if (i >= 2) ok = mbar_wait(&d_free[b], ((i - 2) / 2) & 1);  // epilogue read D[b]
       if (!ok) break;
       tc_fence_after();
       if (lane == 0) {
@@ -393,7 +420,7 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
           for (uint32_t q = 0; q < 8; ++q)
             mma_bf16(tmem + kT2ColAcc, smem_desc(A2 + bj * 32768 + q * 256, 128, 2048),
                      smem_desc(stage + sj * kImage + kB1Bytes + q * 256, 128, 2048),
-                     idesc_bf16(128, 16), (j > 0 || q > 0) ? 1u : 0u);
+                     idesc_bf16(128, 32), (j > 0 || q > 0) ? 1u : 0u);
           mma_commit(&a2_free[bj]);
           mma_commit(&stage_free[sj]);
         }
@@ -416,7 +443,7 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
         for (uint32_t q = 0; q < 8; ++q)
           mma_bf16(tmem + kT2ColAcc, smem_desc(A2 + bj * 32768 + q * 256, 128, 2048),
                    smem_desc(stage + sj * kImage + kB1Bytes + q * 256, 128, 2048),
-                   idesc_bf16(128, 16), (j > 0 || q > 0) ? 1u : 0u);
+                   idesc_bf16(128, 32), (j > 0 || q > 0) ? 1u : 0u);
         mma_commit(acc_done);
       }
     }
@@ -426,20 +453,15 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
     }
   } else {
     // ------------------------------------------------------- epilogue
+    // warpgroup g owns D columns 32g..32g+31; the weights are
+    // w = max(0, 1 - (|s'|^2 + |x'|^2 - 2 s'.x') / h^2)
     const int quad = warp & 3, g = warp >> 2, row = quad * 32 + lane;
     float m[6];
     for (int d = 0; d < 6; ++d) m[d] = seeds[row * 8 + d];
-    const float two_inv_h2 = 2.f * a.inv_h2;
-    float sumw = 0, corr[6] = {0, 0, 0, 0, 0, 0};
+    const float2 two_inv_h2 = make_float2(2.f * a.inv_h2, 2.f * a.inv_h2);
+    const float2 neg_inv_h2 = make_float2(-a.inv_h2, -a.inv_h2);
     for (uint32_t i = 0; i < n; ++i) {
       const uint32_t b = i & 1, s = i % kStages;
-      const float *cen = a.centers + chunk_of(i) * 8;
-      float ss = 0;
-      for (int d = 0; d < 6; ++d) {
-        float r = __bfloat162float(__float2bfloat16_rn(m[d] - cen[d]));
-        ss += r * r;
-      }
-      const float rowc = 1.f - ss * a.inv_h2;
       if (!mbar_wait(&load_full[s], (i / kStages) & 1) || !mbar_wait(&d_full[b], (i / 2) & 1)) {
         ok = false;
         break;
@@ -450,14 +472,25 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&d_free[b]);
-      const float *xx = reinterpret_cast<const float *>(stage + s * kImage + kB1Bytes + kB2Bytes) + 32 * g;
-      __align__(16) __nv_bfloat16 w[32];
-      float sw = 0;
-      for (int j = 0; j < 32; ++j) {
-        float t = fmaf(dot[j], two_inv_h2, fmaf(xx[j], -a.inv_h2, rowc));
-        float wj = fmaxf(t, 0.f);
-        sw += wj;
-        w[j] = __float2bfloat16_rn(wj);
+      const uint8_t *st_s = stage + s * kImage;
+      const float *cen = reinterpret_cast<const float *>(st_s + kB1Bytes + kB2Bytes + kXXBytes);
+      float ss = 0;
+      for (int d = 0; d < 6; ++d) {
+        float r = __bfloat162float(__float2bfloat16_rn(m[d] - cen[d]));
+        ss = fmaf(r, r, ss);
+      }
+      const float rowc = 1.f - ss * a.inv_h2;
+      const float2 rowc2 = make_float2(rowc, rowc);
+      const float4 *xx4 = reinterpret_cast<const float4 *>(st_s + kB1Bytes + kB2Bytes) + 8 * g;
+      __align__(16) __nv_bfloat162 w[16];
+      for (int j4 = 0; j4 < 8; ++j4) {
+        float4 x = xx4[j4];
+        float2 t0 = fma2(make_float2(dot[4 * j4], dot[4 * j4 + 1]), two_inv_h2,
+                         fma2(make_float2(x.x, x.y), neg_inv_h2, rowc2));
+        float2 t1 = fma2(make_float2(dot[4 * j4 + 2], dot[4 * j4 + 3]), two_inv_h2,
+                         fma2(make_float2(x.z, x.w), neg_inv_h2, rowc2));
+        w[2 * j4] = __floats2bfloat162_rn(fmaxf(t0.x, 0.f), fmaxf(t0.y, 0.f));
+        w[2 * j4 + 1] = __floats2bfloat162_rn(fmaxf(t1.x, 0.f), fmaxf(t1.y, 0.f));
       }
       if (i >= 2 && !mbar_wait(&a2_free[b], ((i - 2) / 2) & 1)) {
         ok = false;
@@ -466,16 +499,11 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
       uint8_t *dst = A2 + b * 32768;
       for (int kb = 0; kb < 4; ++kb)
         *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, 32 * g + 8 * kb, 128, 2048)) =
-            *reinterpret_cast<uint4 *>(&w[8 * kb]);
+            *reinterpret_cast<uint4 *>(&w[4 * kb]);
       fence_async_smem();
       __syncwarp();
       if (lane == 0) mbar_arrive(&a2_full[b]);
-      sumw += sw;
-      for (int d = 0; d < 6; ++d) corr[d] = fmaf(cen[d], sw, corr[d]);
     }
-    float *mine = red + (g * 128 + row) * 8;
-    for (int d = 0; d < 6; ++d) mine[d] = corr[d];
-    mine[6] = sumw;
     if (!ok && lane == 0) atomicExch(a.status, DS_SPIN_LIMIT);
   }
   __syncthreads();
@@ -487,15 +515,9 @@ __global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
       tc_fence_after();
       tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kT2ColAcc, acc);
     }
-    float tot[7];
-    for (int d = 0; d < 7; ++d) {
-      float v = 0;
-      for (int gg = 0; gg < 4; ++gg) v += red[(gg * 128 + row) * 8 + d];
-      tot[d] = v;
-    }
     float *out = a.partial + (split * slots + tile * kChunk + row) * 8;
-    for (int d = 0; d < 6; ++d) out[d] = acc[d] + tot[d];
-    out[6] = tot[6];
+    for (int d = 0; d < 6; ++d) out[d] = acc[d] + acc[16 + d];  // BF16 x + its residue
+    out[6] = acc[6];
     out[7] = 0.f;
   }
   if (tid == 0 && n && a.evals) atomicAdd(a.evals, uint64_t(n) * uint64_t(kChunk * kChunk));
@@ -547,8 +569,8 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
   bool ok = true;
   if (tid == 0) {
     asm volatile("fence.proxy.async.global;" ::: "memory");
-    mbar_expect_tx(&bar[0], kB1Bytes + kB2Bytes);
-    tma_bulk_load(S, scratch, kB1Bytes + kB2Bytes, &bar[0]);
+    mbar_expect_tx(&bar[0], kB1Bytes + kSelfB2);
+    tma_bulk_load(S, scratch, kB1Bytes + kSelfB2, &bar[0]);
   }
   ok = __syncthreads_and(mbar_wait(&bar[0], 0));
   if (ok && tid == 0) {
@@ -623,9 +645,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     configured = true;
   }
   uint8_t *images = call.alloc<uint8_t>(v.nchunks * kImage);
-  float *centers = call.alloc<float>(v.nchunks * 8);
-  build_images<<<unsigned(v.nchunks), kChunk, 0, st>>>(v.desc, v.q, v.nchunks, v.cbox, images,
-                                                       centers);
+  build_images<<<unsigned(v.nchunks), kChunk, 0, st>>>(v.desc, v.q, v.nchunks, v.cbox, images);
   check_launch();
   int32_t *ids = call.alloc<int32_t>(k);
   float *boxes = call.alloc<float>(max_tiles * 12);
@@ -654,12 +674,12 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     compact_indices(call, need, tiles * v.nchunks, list, count);
     tile_offsets<<<blocks_for(tiles + 1), kThreads, 0, st>>>(list, count, tiles, v.nchunks, offsets);
     check_launch();
-    Tc2Args args{images, centers, v.nchunks, list, offsets, splits, means, ids, n,
+    Tc2Args args{images, v.nchunks, list, offsets, splits, means, ids, n,
                  float(1.0 / h2), partial, evals, call.status()};
     ms_tile_tc2<<<dim3(unsigned(tiles), unsigned(splits)), kThreads2, kT2Smem, st>>>(args);
     check_launch();
     ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, splits, tiles * kChunk, ids,
-                                                       n, float(h2), 1e-6f, state);
+                                                       n, float(h2), 1e-5f, state);
     check_launch();
     call.launched(5);
     call.ctx->arena.rewind(mark);
@@ -686,7 +706,7 @@ void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const 
   };
   const __nv_bfloat16 *da1 = up(a1, 128 * 16), *db1 = up(b1, 128 * 16), *da2 = up(a2, 128 * 128),
                       *db2 = up(b2, 16 * 128);
-  uint8_t *scratch = call.alloc<uint8_t>(kB1Bytes + kB2Bytes);
+  uint8_t *scratch = call.alloc<uint8_t>(kB1Bytes + kSelfB2);
   float *dd = call.alloc<float>(128 * 128), *dacc = call.alloc<float>(128 * 16);
   tc_selftest<<<1, 256, kSmemRequest, call.stream()>>>(da1, db1, da2, db2, scratch, dd, dacc,
                                                        call.status());

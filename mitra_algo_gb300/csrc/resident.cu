@@ -321,20 +321,27 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     init_means(call, vs, seed_rank, k64, m64);
     shift(call, vs, m64, st64, k64, h2, 1000, nullptr, nullptr);
     std::vector<double> hm(k64 * 8);
+    std::vector<uint8_t> hs64(k64);
     call.d2h(hm.data(), m64, k64 * 8 * 8);
+    call.d2h(hs64.data(), st64, k64);
     call.sync();
     double emax = 0, esum = 0;
+    uint64_t compared = 0, within = 0;
     for (uint64_t i = 0; i < k64; ++i) {
+      if (hs64[i] != 1 || state[i] != 1) continue;  // a mode exists in both runs
       double num = 0, den = 0;
       for (int d = 0; d < 6; ++d) {
         double e = double(means[i * 8 + d]) - hm[i * 8 + d];
         num += e * e, den += hm[i * 8 + d] * hm[i * 8 + d];
       }
       double rel = std::sqrt(num) / std::max(std::sqrt(den), 1e-300);
-      emax = std::max(emax, rel), esum += rel;
+      emax = std::max(emax, rel), esum += rel, ++compared;
+      within += rel <= 1e-4;
     }
     r.mode_error_max = emax;
-    r.mode_error_mean = k64 ? esum / k64 : 0;
+    r.mode_error_mean = compared ? esum / compared : 0;
+    r.modes_compared = compared;
+    r.modes_within = within;
   }
   clock.mark(7);
   // ---- modes: greedy merge (h^2/4, first mode wins) + support
