@@ -230,7 +230,9 @@ def run_gpu(args):
                           "votes": r["votes"], "iterations": r["iterations"],
                           "polish_iterations": r["polish_iterations"], "bulk_ms": r["bulk_ms"],
                           "polish_ms": r["polish_ms"], "evaluations": r["mean_shift_pairs"],
-                          "seed_iterations": r["seed_iterations"], "launches": r["launches"]}))
+                          "seed_iterations": r["seed_iterations"], "launches": r["launches"],
+                          "bulk_trace": list(r["bulk_trace"]),
+                          "polish_trace": list(r["polish_trace"])}))
         return
 
     def timed(precision, steps, warmup):
@@ -326,8 +328,8 @@ def run_gpu(args):
                        "bulk_ms": round(r["bulk_ms"], 3), "polish_ms": round(r["polish_ms"], 3),
                        "fp32_ms": round(res_fp32[-1]["bulk_ms"], 3),
                        "fp32_iterations": res_fp32[-1]["iterations"],
-                       "bulk_trace": r["bulk_trace"][:24], "polish_trace": r["polish_trace"][:24],
-                       "fp32_trace": res_fp32[-1]["bulk_trace"][:24]},
+                       "bulk_trace": r["bulk_trace"][::10], "polish_trace": r["polish_trace"][::5],
+                       "fp32_trace": res_fp32[-1]["bulk_trace"][::10]},
         "stage_ms": {k: round(statistics.mean(x["stage_ms"][k] for x in res_bf16), 3)
                      for k in r["stage_ms"]},
         "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",

@@ -319,8 +319,8 @@ typedef struct sym_fast_result {
   double mean_shift_pairs; /* seed-vote evaluations actually made */
   double seed_iterations;  /* sum over seeds of the iterations each ran */
   double bulk_ms, polish_ms; /* device time of the two mean-shift phases */
-  /* active seeds at the start of the first 64 bulk / polish iterations */
-  uint32_t bulk_trace[64], polish_trace[64];
+  /* active seeds at the start of the first 320 bulk / polish iterations */
+  uint32_t bulk_trace[320], polish_trace[320];
   uint64_t launches, h2d_bytes, d2h_bytes;
   sym_cluster_record records[SYM_FAST_MAX_CLUSTERS];
   uint64_t support[SYM_FAST_MAX_CLUSTERS];

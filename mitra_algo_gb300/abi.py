@@ -157,7 +157,7 @@ class FastResult(C.Structure):
                 ("modes_within", C.c_uint64), ("stage_ms", C.c_double * 8),
                 ("mean_shift_pairs", C.c_double), ("seed_iterations", C.c_double),
                 ("bulk_ms", C.c_double), ("polish_ms", C.c_double),
-                ("bulk_trace", C.c_uint32 * 64), ("polish_trace", C.c_uint32 * 64),
+                ("bulk_trace", C.c_uint32 * 320), ("polish_trace", C.c_uint32 * 320),
                 ("launches", C.c_uint64), ("h2d_bytes", C.c_uint64), ("d2h_bytes", C.c_uint64),
                 ("records", ClusterRecord * FAST_MAX_CLUSTERS),
                 ("support", C.c_uint64 * FAST_MAX_CLUSTERS),

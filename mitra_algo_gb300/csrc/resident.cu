@@ -279,15 +279,15 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   cudaEventRecord(ph[0], st);
   bool tensor = fo.precision == SYM_MS_BF16_REFINED &&
                 meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals,
-                                    r.bulk_trace, 64);
+                                    r.bulk_trace, 320);
   cudaEventRecord(ph[1], st);
   if (tensor) {
     SYM_CUDA(cudaMemsetAsync(st32, 0, k, st));  // polish every seed in FP32
     polish = shift(call, vs, m32, st32, k, h2, fo.polish_iterations, &r.seed_iterations, evals,
-                   r.polish_trace, 64);
+                   r.polish_trace, 320);
   } else {
     bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, &r.seed_iterations, evals,
-                 r.bulk_trace, 64);
+                 r.bulk_trace, 320);
   }
   cudaEventRecord(ph[2], st);
   cudaEventSynchronize(ph[2]);
