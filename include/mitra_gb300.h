@@ -355,6 +355,32 @@ sym_status sym_tc_selftest(sym_context *ctx, const uint16_t *a1, const uint16_t 
                            const uint16_t *a2, const uint16_t *b2, float *d_out,
                            float *acc_out);
 
+/* ------------------------------------------------ allocation-free prune */
+/* No counterpart in the reference: an allocation-free form of the prune half
+ * of select() (src/cpu/selection.cpp:20-27, src/cuda/backend.cu:21-30).
+ * For callers that must not allocate device memory during a call -- services
+ * that size every buffer at start-up, code between allocator checkpoints.
+ * Every pointer is a device pointer owned by the caller: `pruned` has room
+ * for `count` entries, `*pruned_count` receives the number kept (UINT64_MAX
+ * when an entry of `sample` lies outside [0, vertex_count)).  Kept samples
+ * come out in sample order, identical to sym_select's `pruned`.  `stream` is
+ * a cudaStream_t (NULL: the legacy default stream); the call only enqueues
+ * work and returns.
+ * Scratch is a fixed 64 KiB array in the library's static device memory, so
+ * `count` is limited to sym_prune_static_max_samples() (16,777,216); larger
+ * counts are rejected with SYM_INVALID_ARGUMENT.  That array is shared by all
+ * calls on a device: calls that may overlap (two streams, two host threads)
+ * race and must be ordered by the caller.  sym_prune_static_setup() resolves
+ * the array's address for the current device; call it once per device, with
+ * that device current, before any stream capture (the first
+ * sym_prune_static on a device otherwise does it). */
+uint64_t sym_prune_static_max_samples(void);
+sym_status sym_prune_static_setup(void);
+sym_status sym_prune_static(const int32_t *sample, uint64_t count, const double *kmin,
+                            const double *kmax, const uint8_t *valid, uint64_t vertex_count,
+                            double prune, int32_t *pruned, uint64_t *pruned_count,
+                            void *stream);
+
 /* --------------------------------------------------------------- metrics */
 /* Per-stage accounting, the fields of the reference CudaMetric
  * (include/symmetry/cuda.h:7-13, src/cuda/profile.cpp). */

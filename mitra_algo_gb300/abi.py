@@ -207,6 +207,11 @@ PROTOTYPES = [
                                  C.c_int32, C.c_int32, C.c_int32, _d, _u8, P(C.c_int32)]),
     ("sym_tc_selftest", C.c_int, [C.c_void_p, P(C.c_uint16), P(C.c_uint16), P(C.c_uint16),
                                   P(C.c_uint16), _f, _f]),
+    # allocation-free prune: device pointers + a cudaStream_t
+    ("sym_prune_static_max_samples", C.c_uint64, []),
+    ("sym_prune_static_setup", C.c_int, []),
+    ("sym_prune_static", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_uint64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
     ("sym_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("sym_take_metrics", C.c_uint64, [C.c_void_p, P(Metric), C.c_uint64]),
 ]
