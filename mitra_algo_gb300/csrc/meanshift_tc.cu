@@ -1,22 +1,27 @@
 // SPDX-License-Identifier: MPL-2.0
 // BF16 tensor-core mean-shift bulk iterations on sm_103a (tcgen05 + TMEM).
 //
-// Flash-style: per (tile of 128 seeds, chunk of 128 votes)
-//   MMA1  D[128x128] = S'[128x16] . X'[128x16]^T      (seed-vote dot products)
-//   epilogue: tcgen05.ld D, w = max(0, 1 - (|s'|^2 + |x'|^2 - 2 s'.x') / h^2)
-//             (Epanechnikov, packed FP32 FMAs), written as BF16 into shared
-//             memory
-//   MMA2  ACC[128x32] += W[128x128] . [x_hi, 1, x_lo][128x32]
-// S' and X' are centred on the chunk's centre c (X' once per vote set, S' per
-// chunk), which keeps |s'|, |x'| small so the expanded distance does not lose
-// its digits in BF16; MMA2 uses the uncentred x split into a BF16 value and
-// its BF16 residue, plus a ones column, so sum w x and sum w come out of TMEM.
-// Votes are pre-arranged per chunk in the canonical no-swizzle K-major
-// core-matrix layout (8 rows x 16 bytes per core matrix), so one TMA bulk copy
-// (cp.async.bulk + mbarrier complete_tx) stages a chunk.  Accumulators live
-// in TMEM (256 columns per CTA: D at 0..127, ACC at 128..143).  Every
-// mbarrier wait is bounded; on timeout the CTA records a status, drains and
-// frees its TMEM.
+// Flash-style, per (tile of 128 seeds, chunk of 128 votes), in units of the
+// bandwidth h with the vote set's centre c_g and the chunk centre c_c:
+//   u = (s - c_g)/h per seed, as a BF16 value + residue (once per tile)
+//   E = (c_c - c_g)/h per chunk, v = (x - c_c)/h per vote, and the per-vote
+//       constant f = -2 E.v as a BF16 value + residue (the chunk image)
+//   MMA1  D[128x128] = [2u_hi, 1, 1 | 2u_lo, 1, 1] . [v, -|v|^2 | v, f]^T
+//                    = 2 (u - E).v - |v|^2                 (tcgen05.mma K=16)
+//   epilogue: w = relu(D + 1 - |u - E|^2) = max(0, 1 - |s - x|^2/h^2),
+//           one packed FP32 add and one cvt.rn.relu.bf16x2 per two weights,
+//           written as BF16 into shared memory
+//   MMA2  ACC[128x16] += W[128x128] . [x_hi, 1, 0, x_lo]  (sum w x, sum w)
+// The seed offsets are represented to ~2^-17 by their BF16 pairs and the
+// epilogue uses the same represented values, so the large offsets cancel
+// exactly; v is chunk-relative (small) and rounds once.  MMA2 uses the
+// uncentred x split into BF16 value and residue plus a ones column, so sum
+// w x and sum w come out of TMEM directly.
+// The chunk image is laid out in the canonical no-swizzle K-major
+// core-matrix order (8 rows x 16 bytes per core matrix), so one TMA bulk copy
+// (cp.async.bulk + mbarrier complete_tx) stages a chunk.  Every mbarrier wait
+// is bounded; on timeout the CTA records a status, drains its copies and
+// MMAs, and frees its TMEM.
 #include "meanshift_fast.cuh"
 #include "primitives.cuh"
 
@@ -67,6 +72,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   for (uint32_t i = 0; i < kSpinLimit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
+}
+
+// Bounded wait whose outcome is the same in every lane of the warp (each
+// lane polls, so each performs the acquire; all agree on success).
+__device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity) {
+  return __all_sync(0xffffffffu, mbar_wait(bar, parity));
 }
 
 __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, uint32_t bytes,
@@ -128,6 +139,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b
       : "memory");
 }
 
+// Same, with the A operand (M x 16 BF16) read from TMEM at column a_tmem:
+// row m in lane m, two K-consecutive elements per 32-bit column (the lower
+// K index in the low half).
+__device__ __forceinline__ void mma_bf16_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b,
+                                            uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -152,6 +176,57 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// This thread's TMEM lane, 32 (or 8) consecutive 32-bit columns from
+// registers; tmem_wait_st makes them visible before the next handshake.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
+      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
+      "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15])
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(
+                   taddr),
+               "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]),
+               "r"(r[7])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() {
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// tcgen05.ld of 32 columns without the wait (pair with tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 // ------------------------------------------------------------- layouts
 // Canonical no-swizzle K-major tile of 16-bit elements: core matrices of 8
 // rows x 8 elements (16 bytes per row), `lbo` bytes between K-adjacent core
@@ -161,63 +236,71 @@ __host__ __device__ constexpr uint32_t kmajor_offset(uint32_t row, uint32_t k, u
   return (row / 8) * sbo + (k / 8) * lbo + (row % 8) * 16 + (k % 8) * 2;
 }
 
-// Chunk image (one TMA bulk copy):
-//   B1   X' = x - c as 128 votes x 16 features, K-major (LBO 128, SBO 256)
-//   B2   32 "features" x 128 votes, K-major (LBO 128, SBO 2048): rows 0..5
-//        BF16(x), row 6 ones, rows 16..21 the BF16 rounding residue of x;
-//        MMA2 then yields sum w x (hi + lo) and sum w directly in TMEM
-//   XX   |x'|^2 of the rounded X' (128 floats; far away for padding votes)
-//   CEN  the chunk centre c (8 floats)
-constexpr uint32_t kB1Bytes = 4096, kB2Bytes = 8192, kXXBytes = 512, kCenBytes = 32;
-constexpr uint32_t kImage = kB1Bytes + kB2Bytes + kXXBytes + kCenBytes;  // 12832
+// Chunk image (one TMA bulk copy), built per mean-shift call for 1/h:
+//   B1   128 votes x 16, K-major (LBO 128, SBO 256): v = (x - c_c)/h in k
+//        0..5 and again in k 8..13; -|v|^2 of the rounded v as a BF16 value
+//        and residue in k 6, 7 (-1e30 for padding votes, which then get
+//        w = 0); f = -2 E.v as a BF16 value and residue in k 14, 15
+//   B2   16 features x 128 votes, K-major (LBO 128, SBO 2048): BF16(x) in
+//        features 0..5, ones in 6, the BF16 residue x - BF16(x) in 8..13
+//   CEN  E = (c_c - c_g)/h (8 floats)
+constexpr uint32_t kB1Bytes = 4096, kB2Bytes = 4096, kCenBytes = 32;
+constexpr uint32_t kImage = kB1Bytes + kB2Bytes + kCenBytes;  // 8224
 static_assert(kImage % 16 == 0, "TMA bulk copies move multiples of 16 bytes");
 
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+  hi = __float2bfloat16_rn(x);
+  lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+// Two consecutive BF16 values as one 32-bit TMEM column (first in the low half).
+__device__ __forceinline__ uint32_t bf16_pair(const __nv_bfloat16 *p) {
+  return uint32_t(__bfloat16_as_ushort(p[0])) | (uint32_t(__bfloat16_as_ushort(p[1])) << 16);
+}
+
 __global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, const float *cbox,
-                             uint8_t *images) {
+                             const float *gbox, float inv_h, uint8_t *images) {
   uint64_t c = blockIdx.x;
   int t = threadIdx.x;  // vote in chunk
   if (c >= nchunks) return;
   const float *b = cbox + c * 12;
-  float cen[6];
-  for (int d = 0; d < 6; ++d) cen[d] = 0.5f * (b[d] + b[6 + d]);
+  float cen[6], e[6];
+  for (int d = 0; d < 6; ++d) {
+    cen[d] = 0.5f * (b[d] + b[6 + d]);
+    e[d] = (cen[d] - 0.5f * (gbox[d] + gbox[6 + d])) * inv_h;
+  }
   uint64_t v = c * kChunk + t;
   bool live = v < q;
   uint8_t *img = images + c * kImage;
   __nv_bfloat16 *b1 = reinterpret_cast<__nv_bfloat16 *>(img);
   __nv_bfloat16 *b2 = reinterpret_cast<__nv_bfloat16 *>(img + kB1Bytes);
-  float *xx = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes);
-  float *ce = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes + kXXBytes);
-  if (t < 8) ce[t] = t < 6 ? cen[t] : 0.f;
-  float n2 = 0;
-  for (int k = 0; k < 16; ++k) {
-    float x = live && k < 6 ? desc[v * 8 + k] - cen[k] : 0.f;
-    __nv_bfloat16 h = __float2bfloat16_rn(x);
+  float *ce = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes);
+  if (t < 8) ce[t] = t < 6 ? e[t] : 0.f;
+  const __nv_bfloat16 zero = __float2bfloat16_rn(0.f);
+  float n2 = 0, f = 0;
+  for (int d = 0; d < 6; ++d) {
+    float x = live ? desc[v * 8 + d] : 0.f;
+    __nv_bfloat16 h = __float2bfloat16_rn(live ? (x - cen[d]) * inv_h : 0.f);
     float r = __bfloat162float(h);
-    n2 += r * r;
-    b1[kmajor_offset(t, k, 128, 256) / 2] = h;
+    n2 = fmaf(r, r, n2);
+    f = fmaf(-2.f * e[d], r, f);
+    b1[kmajor_offset(t, d, 128, 256) / 2] = h;
+    b1[kmajor_offset(t, 8 + d, 128, 256) / 2] = h;
+    __nv_bfloat16 xh, xl;
+    split_bf16(x, xh, xl);
+    b2[kmajor_offset(d, t, 128, 2048) / 2] = xh;
+    b2[kmajor_offset(8 + d, t, 128, 2048) / 2] = xl;
   }
-  for (int k = 0; k < 32; ++k) {
-    float val = 0.f;
-    if (live && k < 6) {
-      val = desc[v * 8 + k];
-    } else if (live && k == 6) {
-      val = 1.f;
-    } else if (live && k >= 16 && k < 22) {
-      float x = desc[v * 8 + (k - 16)];
-      val = x - __bfloat162float(__float2bfloat16_rn(x));
-    }
-    b2[kmajor_offset(k, t, 128, 2048) / 2] = __float2bfloat16_rn(val);
-  }
-  xx[t] = live ? n2 : 1e30f;  // padding votes sit infinitely far away
+  __nv_bfloat16 nh, nl, fh, fl;
+  split_bf16(live ? -n2 : -1e30f, nh, nl);
+  split_bf16(f, fh, fl);
+  b1[kmajor_offset(t, 6, 128, 256) / 2] = nh;
+  b1[kmajor_offset(t, 7, 128, 256) / 2] = nl;
+  b1[kmajor_offset(t, 14, 128, 256) / 2] = fh;
+  b1[kmajor_offset(t, 15, 128, 256) / 2] = fl;
+  b2[kmajor_offset(6, t, 128, 2048) / 2] = __float2bfloat16_rn(live ? 1.f : 0.f);
+  for (int k : {7, 14, 15}) b2[kmajor_offset(k, t, 128, 2048) / 2] = zero;
 }
-
-// Shared-memory plan of the self-test (one tile, one stage, N = 16 MMA2).
-constexpr uint32_t kSelfB2 = 4096;
-constexpr uint32_t kOffA1 = 0, kOffA2 = 4096, kOffStage = 4096 + 32768;
-constexpr uint32_t kOffBars = kOffStage + 2 * 8704;
-constexpr uint32_t kOffMisc = kOffBars + 64;
-constexpr uint32_t kSmemRequest = 100 * 1024;
-constexpr uint32_t kTmemCols = 256, kColD = 0, kColAcc = 128;
 
 __device__ __forceinline__ float box_gap2_tc(const float *lo, const float *hi, const float *b) {
   float g = 0;
@@ -287,38 +370,52 @@ __global__ void tile_offsets(const int32_t *list, const uint64_t *count, uint64_
 }
 
 // --------------------------------------------- pipelined tensor kernel
-// Warp roles: warps 0..15 form four epilogue warpgroups (warpgroup g owns
-// D columns 32g..32g+31 of every row; warp w reads TMEM lanes 32(w%4)..),
-// warp 16 is the producer (TMA, A1 staging, MMA issue).
-//   stages   3 TMA buffers of one chunk image each
-//   D[2]     two TMEM accumulators for MMA1 (columns 0..127, 128..255)
-//   ACC      TMEM columns 256..271
-//   A1[2]    seeds centred on the chunk, A2[2] BF16 weights
-// Handshakes (mbarriers): load_full[s] (TMA bytes), d_full[b] (MMA1 done),
-// d_free[b] (epilogue read D[b]), a2_full[b] (epilogue wrote A2[b]),
-// a2_free[b] and stage_free[s] (MMA2 done), acc_done.
-constexpr int kStages = 3;
-constexpr int kEpiWarps = 16, kThreads2 = (kEpiWarps + 1) * 32;
-constexpr uint32_t kT2A1 = 0;                                 // 2 x 4096
-constexpr uint32_t kT2A2 = 8192;                              // 2 x 32768
-constexpr uint32_t kT2Stage = kT2A2 + 2 * 32768;              // 3 x kImage
-constexpr uint32_t kT2Bars = kT2Stage + kStages * kImage;     // 15 barriers
-constexpr uint32_t kT2Misc = kT2Bars + 16 * 8;
-constexpr uint32_t kT2Seeds = kT2Misc + 64;                   // 128 x 8 floats
-constexpr uint32_t kT2Smem = kT2Seeds + 128 * 8 * 4;
-static_assert(kT2Stage % 128 == 0 && (kT2Stage + kImage) % 16 == 0, "TMA alignment");
-constexpr uint32_t kT2Cols = 512, kT2ColAcc = 256;
+// Warp roles: warp 16 streams the chunk images with TMA (and does nothing
+// else); warps 0..15 form two pairs of warpgroups that take alternate
+// chunks (pair p = warp / 8 owns the chunks i with i % 2 == p).  A pair
+// issues its own MMAs from one elected thread, so the hand-offs of a chunk
+// (D read -> next MMA1, weights written -> MMA2) are pair-local named
+// barriers instead of round trips through another warp.  In a pair, warp w
+// reads TMEM lanes 32(w%4).. and D columns 64((w/4)%2)..+63.
+//   shared memory  kStagesTc TMA buffers of one chunk image each, ATILE
+//                  (A operand of MMA1, once per tile), U
+//   TMEM columns   D[p] = 128p (MMA1 accumulators), W[p] = 256 + 64p (the
+//                  BF16 weights, A operand of MMA2), ACC[p] = 384 + 64p
+//                  (four 16-column accumulators per pair, one per K-step
+//                  q % 4 of MMA2; all eight summed once at the end)
+// mbarriers: load_full[s] (TMA bytes), stage_free[s] (MMA2 of the chunk in
+// stage s done), d_full[p] (MMA1 done), w_free[p] (MMA2 done), acc_done.
+// Pair p, chunk i: wait D[p] -> tcgen05.ld -> pair barrier -> MMA1(i+2)
+// into D[p] -> weights -> wait W[p] free -> tcgen05.st -> pair barrier ->
+// MMA2(i).  Every wait is bounded and every pair barrier also ANDs the
+// warps' wait results, so a timeout ends the whole pair at the same
+// barrier (no warp is left waiting at a barrier the others skipped).
+constexpr int kStagesTc = 12;
+constexpr int kEpiWarps = 16, kPairWarps = 8, kThreadsTc = (kEpiWarps + 1) * 32;
+constexpr uint32_t kTcStage = 0;                                     // kStagesTc x kImage
+constexpr uint32_t kTcU = (kStagesTc * kImage + 1023) / 1024 * 1024; // 128 x 8 floats
+constexpr uint32_t kTcATile = kTcU + 128 * 8 * 4;                    // 4096, K-major
+constexpr uint32_t kTcBars = kTcATile + 4096;                        // 2 kStagesTc + 5
+constexpr uint32_t kTcMisc = kTcBars + 48 * 8;
+constexpr uint32_t kTcSmem = kTcMisc + 64;
+static_assert(kImage % 16 == 0, "TMA alignment");
+static_assert(kTcATile % 1024 == 0, "descriptor alignment");
+static_assert(2 * kStagesTc + 5 <= 48, "barrier slots");
+static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
+constexpr uint32_t kTcCols = 512, kTcColW = 256, kTcColAcc = 384;
 
-struct Tc2Args {
+struct TcArgs {
   const uint8_t *images;
   uint64_t nchunks;
   const int32_t *list;      // needed (tile, chunk) entries, t * nchunks + c
-  const uint64_t *offsets;  // tiles + 1
-  uint64_t splits;
+  const uint64_t *offsets;  // tiles + 1: first list entry of each tile
+  const uint32_t *pieces;   // tiles + 1: first piece (CTA) of each tile
+  uint64_t tiles;
   const float *means;
   const int32_t *ids;
   uint64_t nactive;
-  float inv_h2;
+  const float *gbox;        // box of all votes; its centre is c_g
+  float inv_h;
   float *partial;
   unsigned long long *evals;
   int *status;
@@ -326,6 +423,21 @@ struct Tc2Args {
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Named barrier over the 256 threads of pair p (ids 1, 2); returns the AND
+// of every thread's `ok`.
+__device__ __forceinline__ bool pair_and(int p, bool ok) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred a, b;\n\t"
+      "setp.ne.b32 a, %1, 0;\n\t"
+      "bar.red.and.pred b, %2, 256, a;\n\t"
+      "selp.u32 %0, 1, 0, b;\n\t}"
+      : "=r"(r)
+      : "r"(uint32_t(ok)), "r"(p + 1)
+      : "memory");
+  return r != 0;
 }
 
 // d = a * b + c on two FP32 lanes at once.
@@ -338,204 +450,254 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
   return d;
 }
 
-__global__ void __launch_bounds__(kThreads2, 1) ms_tile_tc2(Tc2Args a) {
+// {relu(lo), relu(hi)} rounded to BF16 and packed, lo in the low half.
+__device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
+  uint32_t r;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// ACC[q % 4] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for q = 0..7 (the
+// chunk's 128 votes in K-steps of 16), W in TMEM.
+__device__ __forceinline__ void mma2_chunk(uint32_t acc, uint32_t w_tmem, const uint8_t *b2,
+                                           bool first) {
+  for (uint32_t q = 0; q < 8; ++q)
+    mma_bf16_ts(acc + 16 * (q % 4), w_tmem + 8 * q, smem_desc(b2 + q * 256, 128, 2048),
+                idesc_bf16(128, 16), (first && q < 4) ? 0u : 1u);
+}
+
+__global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *A1 = smem + kT2A1, *A2 = smem + kT2A2, *stage = smem + kT2Stage;
-  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kT2Bars);
-  uint64_t *load_full = bars, *stage_free = bars + 3, *d_full = bars + 6, *d_free = bars + 8;
-  uint64_t *a2_full = bars + 10, *a2_free = bars + 12, *acc_done = bars + 14;
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kT2Misc);
-  float *seeds = reinterpret_cast<float *>(smem + kT2Seeds);
+  uint8_t *stage = smem + kTcStage;
+  float *U = reinterpret_cast<float *>(smem + kTcU);
+  uint8_t *ATILE = smem + kTcATile;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcBars);
+  uint64_t *load_full = bars, *stage_free = bars + kStagesTc;
+  uint64_t *d_full = bars + 2 * kStagesTc, *w_free = d_full + 2, *acc_done = d_full + 4;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcMisc);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const uint64_t tile = blockIdx.x, split = blockIdx.y;
-  const uint64_t slots = uint64_t(gridDim.x) * kChunk;
-  const uint64_t lt0 = a.offsets[tile], lt1 = a.offsets[tile + 1], len = lt1 - lt0;
-  const uint64_t e0 = lt0 + len * split / a.splits, e1 = lt0 + len * (split + 1) / a.splits;
+  // piece -> (tile, share of the tile's list)
+  const uint32_t piece = blockIdx.x;
+  if (piece >= a.pieces[a.tiles]) return;
+  uint64_t lo_t = 0, hi_t = a.tiles;  // last tile whose first piece is <= piece
+  while (hi_t - lo_t > 1) {
+    uint64_t mid = (lo_t + hi_t) / 2;
+    if (a.pieces[mid] <= piece) lo_t = mid;
+    else hi_t = mid;
+  }
+  const uint64_t tile = lo_t;
+  const uint64_t k = piece - a.pieces[tile], np = a.pieces[tile + 1] - a.pieces[tile];
+  const uint64_t lt0 = a.offsets[tile], len = a.offsets[tile + 1] - lt0;
+  const uint64_t e0 = lt0 + len * k / np, e1 = lt0 + len * (k + 1) / np;
   const uint32_t n = uint32_t(e1 - e0);
   const uint64_t tbase = tile * a.nchunks;
 
-  if (tid < kChunk) {  // seed means of the tile -> shared memory
+  // u = (s - c_g)/h of this tile's seeds: U (FP32 sums of the BF16 pairs)
+  // and ATILE rows [2u_hi, 1, 1 | 2u_lo, 1, 1] in shared memory
+  if (tid < kChunk) {
     uint64_t slot = tile * kChunk + tid;
     bool live = slot < a.nactive;
     int32_t sd = live ? a.ids[slot] : 0;
-    for (int d = 0; d < 8; ++d) seeds[tid * 8 + d] = live && d < 6 ? a.means[uint64_t(sd) * 8 + d] : 0.f;
+    __align__(16) __nv_bfloat16 k0[8], k1[8];
+    const __nv_bfloat16 one = __float2bfloat16_rn(1.f);
+    for (int d = 0; d < 6; ++d) {
+      float cg = 0.5f * (a.gbox[d] + a.gbox[6 + d]);
+      float u = live ? (a.means[uint64_t(sd) * 8 + d] - cg) * a.inv_h : 0.f;
+      __nv_bfloat16 hi, lo;
+      split_bf16(u, hi, lo);
+      U[tid * 8 + d] = __bfloat162float(hi) + __bfloat162float(lo);
+      k0[d] = __float2bfloat16_rn(2.f * __bfloat162float(hi));  // exact
+      k1[d] = __float2bfloat16_rn(2.f * __bfloat162float(lo));
+    }
+    k0[6] = k0[7] = k1[6] = k1[7] = one;
+    *reinterpret_cast<uint4 *>(ATILE + kmajor_offset(tid, 0, 128, 256)) = *reinterpret_cast<uint4 *>(k0);
+    *reinterpret_cast<uint4 *>(ATILE + kmajor_offset(tid, 8, 128, 256)) = *reinterpret_cast<uint4 *>(k1);
   }
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&load_full[s], 1), mbar_init(&stage_free[s], 1);
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&d_full[b], 1);
-      mbar_init(&d_free[b], kEpiWarps);
-      mbar_init(&a2_full[b], kEpiWarps);
-      mbar_init(&a2_free[b], 1);
-    }
-    mbar_init(acc_done, 1);
+    for (int s = 0; s < kStagesTc; ++s) mbar_init(&load_full[s], 1), mbar_init(&stage_free[s], 1);
+    for (int p = 0; p < 2; ++p) mbar_init(&d_full[p], 1), mbar_init(&w_free[p], 1);
+    mbar_init(acc_done, 2);  // one commit (or arrival) per pair
     fence_mbar_init();
   }
-  if (warp == 0 && n) tmem_alloc(tmem_slot, kT2Cols);
+  if (warp == 0 && n) tmem_alloc(tmem_slot, kTcCols);
+  fence_async_smem();  // ATILE written by the generic proxy, read by the MMA
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = n ? *tmem_slot : 0;
-  bool ok = true;
+  auto stage_of = [&](uint32_t i) { return stage + (i % kStagesTc) * kImage; };
 
   if (warp == kEpiWarps) {
-    // ------------------------------------------------------- producer
-    auto chunk_of = [&](uint32_t i) { return uint64_t(a.list[e0 + i]) - tbase; };
-    for (uint32_t i = 0; i < n && i < uint32_t(kStages); ++i)
+    // ------------------------------------------------ TMA producer
+    // chunk ids of the work list, 32 per batch, lane l holding entry
+    // 32 * batch + l; the next batch is loaded one batch ahead, so no
+    // global-load latency sits on the issue path.  chunk_of is called by the
+    // whole warp with non-decreasing i.
+    auto load_batch = [&](uint32_t batch) -> uint32_t {
+      uint32_t idx = batch * 32 + lane;
+      return idx < n ? uint32_t(uint64_t(a.list[e0 + idx]) - tbase) : 0u;
+    };
+    uint32_t cur = load_batch(0), nxt = load_batch(1), cur_batch = 0;
+    auto chunk_of = [&](uint32_t i) -> uint64_t {
+      while (i / 32 != cur_batch) {
+        cur = nxt;
+        nxt = load_batch(++cur_batch + 1);
+      }
+      return __shfl_sync(0xffffffffu, cur, i % 32);
+    };
+    bool ok = true;
+    uint32_t issued = 0;
+    for (; issued < n && issued < uint32_t(kStagesTc); ++issued) {
+      const uint64_t c = chunk_of(issued);
       if (lane == 0) {
-        mbar_expect_tx(&load_full[i], kImage);
-        tma_bulk_load(stage + i * kImage, a.images + chunk_of(i) * kImage, kImage, &load_full[i]);
-      }
-    for (uint32_t i = 0; i < n && ok; ++i) {
-      const uint32_t b = i & 1, s = i % kStages;
-      ok = mbar_wait(&load_full[s], (i / kStages) & 1);
-      if (ok && i >= 2) ok = mbar_wait(&d_full[b], ((i - 2) / 2) & 1);  // MMA1(i-2) released A1[b]
-      if (!ok) break;
-      const float *cen = reinterpret_cast<const float *>(stage + s * kImage + kB1Bytes + kB2Bytes + kXXBytes);
-      for (int r = lane; r < kChunk; r += 32) {  // A1[b]: seeds centred on the chunk, BF16
-        __align__(16) __nv_bfloat16 h[16];
-        for (int k = 0; k < 16; ++k)
-          h[k] = __float2bfloat16_rn(k < 6 ? seeds[r * 8 + k] - cen[k] : 0.f);
-        uint8_t *dst = A1 + b * 4096;
-        *reinterpret_cast<uint4 *>(dst + kmajor_offset(r, 0, 128, 256)) = *reinterpret_cast<uint4 *>(&h[0]);
-        *reinterpret_cast<uint4 *>(dst + kmajor_offset(r, 8, 128, 256)) = *reinterpret_cast<uint4 *>(&h[8]);
-      }
-      fence_async_smem();
-      __syncwarp();
-      if (i >= 2) ok = mbar_wait(&d_free[b], ((i - 2) / 2) & 1);  // epilogue read D[b]
-      if (!ok) break;
-      tc_fence_after();
-      if (lane == 0) {
-        mma_bf16(tmem + 128 * b, smem_desc(A1 + b * 4096, 128, 256),
-                 smem_desc(stage + s * kImage, 128, 256), idesc_bf16(128, 128), 0);
-        mma_commit(&d_full[b]);
-      }
-      if (i >= 1) {  // MMA2 of the previous chunk, then refill its stage
-        const uint32_t j = i - 1, bj = j & 1, sj = j % kStages;
-        ok = mbar_wait(&a2_full[bj], (j / 2) & 1);
-        if (!ok) break;
-        tc_fence_after();
-        if (lane == 0) {
-          for (uint32_t q = 0; q < 8; ++q)
-            mma_bf16(tmem + kT2ColAcc, smem_desc(A2 + bj * 32768 + q * 256, 128, 2048),
-                     smem_desc(stage + sj * kImage + kB1Bytes + q * 256, 128, 2048),
-                     idesc_bf16(128, 32), (j > 0 || q > 0) ? 1u : 0u);
-          mma_commit(&a2_free[bj]);
-          mma_commit(&stage_free[sj]);
-        }
-        if (j + kStages < n) {
-          ok = mbar_wait(&stage_free[sj], (j / kStages) & 1);
-          if (!ok) break;
-          if (lane == 0) {
-            mbar_expect_tx(&load_full[sj], kImage);
-            tma_bulk_load(stage + sj * kImage, a.images + chunk_of(j + kStages) * kImage, kImage,
-                          &load_full[sj]);
-          }
-        }
+        mbar_expect_tx(&load_full[issued], kImage);
+        tma_bulk_load(stage + issued * kImage, a.images + c * kImage, kImage, &load_full[issued]);
       }
     }
-    if (ok && n) {  // last MMA2
-      const uint32_t j = n - 1, bj = j & 1, sj = j % kStages;
-      ok = mbar_wait(&a2_full[bj], (j / 2) & 1);
-      tc_fence_after();
-      if (ok && lane == 0) {
-        for (uint32_t q = 0; q < 8; ++q)
-          mma_bf16(tmem + kT2ColAcc, smem_desc(A2 + bj * 32768 + q * 256, 128, 2048),
-                   smem_desc(stage + sj * kImage + kB1Bytes + q * 256, 128, 2048),
-                   idesc_bf16(128, 32), (j > 0 || q > 0) ? 1u : 0u);
-        mma_commit(acc_done);
+    // chunk j + kStagesTc reuses the stage of chunk j once MMA2(j) is done
+    for (uint32_t j = 0; j + kStagesTc < n; ++j) {
+      const uint64_t c = chunk_of(j + kStagesTc);
+      ok = warp_wait(&stage_free[j % kStagesTc], (j / kStagesTc) & 1);
+      if (!ok) break;
+      if (lane == 0) {
+        mbar_expect_tx(&load_full[j % kStagesTc], kImage);
+        tma_bulk_load(stage_of(j), a.images + c * kImage, kImage, &load_full[j % kStagesTc]);
       }
+      ++issued;
     }
     if (!ok && lane == 0) {
       atomicExch(a.status, DS_SPIN_LIMIT);
-      mbar_arrive(acc_done);  // release the epilogue
+      // drain: wait (bounded) for every copy issued, so none lands after exit
+      for (uint32_t c = 0; c < issued; ++c) mbar_wait(&load_full[c % kStagesTc], (c / kStagesTc) & 1);
     }
   } else {
-    // ------------------------------------------------------- epilogue
-    // warpgroup g owns D columns 32g..32g+31; the weights are
-    // w = max(0, 1 - (|s'|^2 + |x'|^2 - 2 s'.x') / h^2)
-    const int quad = warp & 3, g = warp >> 2, row = quad * 32 + lane;
-    float m[6];
-    for (int d = 0; d < 6; ++d) m[d] = seeds[row * 8 + d];
-    const float2 two_inv_h2 = make_float2(2.f * a.inv_h2, 2.f * a.inv_h2);
-    const float2 neg_inv_h2 = make_float2(-a.inv_h2, -a.inv_h2);
-    for (uint32_t i = 0; i < n; ++i) {
-      const uint32_t b = i & 1, s = i % kStages;
-      if (!mbar_wait(&load_full[s], (i / kStages) & 1) || !mbar_wait(&d_full[b], (i / 2) & 1)) {
-        ok = false;
-        break;
-      }
+    // ------------------------------------------------ pair p
+    // row `row`, D columns 64h..64h+63:  w = relu(D + 1 - |u - E|^2)
+    const int p = warp / kPairWarps, quad = warp & 3, h = (warp >> 2) & 1, row = quad * 32 + lane;
+    const bool leader = (warp % kPairWarps) == 0;  // issues the pair's MMAs (lane 0)
+    const float *u = U + row * 8;
+    const float2 one2 = make_float2(1.f, 1.f);
+    const uint32_t lane_base = uint32_t(quad * 32) << 16;
+    const uint32_t dcol = tmem + 128 * p + 64 * h, wcol = tmem + kTcColW + 64 * p + 32 * h;
+    // MMA1(i) into D[p], once chunk i has landed (leader warp only)
+    auto mma1 = [&](uint32_t i) {
+      bool good = warp_wait(&load_full[i % kStagesTc], (i / kStagesTc) & 1);
       tc_fence_after();
-      float dot[32];
-      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + 128 * b + 32 * g, dot);
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&d_free[b]);
-      const uint8_t *st_s = stage + s * kImage;
-      const float *cen = reinterpret_cast<const float *>(st_s + kB1Bytes + kB2Bytes + kXXBytes);
-      float ss = 0;
+      if (good && lane == 0) {
+        mma_bf16(tmem + 128 * p, smem_desc(ATILE, 128, 256), smem_desc(stage_of(i), 128, 256),
+                 idesc_bf16(128, 128), 0);
+        mma_commit(&d_full[p]);
+      }
+      return good;
+    };
+    bool ok = true;
+    if (leader && uint32_t(p) < n) ok = mma1(p);
+    ok = pair_and(p, ok);
+    uint32_t i = p, kth = 0;  // kth: index of chunk i among the pair's chunks
+    for (; ok && i < n; i += 2, ++kth) {
+      bool good = warp_wait(&d_full[p], kth & 1) &&
+                  warp_wait(&load_full[i % kStagesTc], (i / kStagesTc) & 1);
+      tc_fence_after();
+      const float *E = reinterpret_cast<const float *>(stage_of(i) + kB1Bytes + kB2Bytes);
+      float rowc = 1.f;
       for (int d = 0; d < 6; ++d) {
-        float r = __bfloat162float(__float2bfloat16_rn(m[d] - cen[d]));
-        ss = fmaf(r, r, ss);
+        float r = u[d] - E[d];
+        rowc = fmaf(-r, r, rowc);
       }
-      const float rowc = 1.f - ss * a.inv_h2;
-      const float2 rowc2 = make_float2(rowc, rowc);
-      const float4 *xx4 = reinterpret_cast<const float4 *>(st_s + kB1Bytes + kB2Bytes) + 8 * g;
-      __align__(16) __nv_bfloat162 w[16];
-      for (int j4 = 0; j4 < 8; ++j4) {
-        float4 x = xx4[j4];
-        float2 t0 = fma2(make_float2(dot[4 * j4], dot[4 * j4 + 1]), two_inv_h2,
-                         fma2(make_float2(x.x, x.y), neg_inv_h2, rowc2));
-        float2 t1 = fma2(make_float2(dot[4 * j4 + 2], dot[4 * j4 + 3]), two_inv_h2,
-                         fma2(make_float2(x.z, x.w), neg_inv_h2, rowc2));
-        w[2 * j4] = __floats2bfloat162_rn(fmaxf(t0.x, 0.f), fmaxf(t0.y, 0.f));
-        w[2 * j4 + 1] = __floats2bfloat162_rn(fmaxf(t1.x, 0.f), fmaxf(t1.y, 0.f));
+      uint32_t w[16], w2[16];
+      {
+        uint32_t d0[32], d1[32];
+        if (good) {
+          tmem_ld32_async(lane_base + dcol, d0);
+          tmem_ld32_async(lane_base + dcol + 32, d1);
+          tmem_wait_ld();
+        } else {
+          for (int j = 0; j < 32; ++j) d0[j] = d1[j] = 0u;
+        }
+        const float2 rowc2 = make_float2(rowc, rowc);
+        for (int j = 0; j < 16; ++j) {
+          float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
+                          one2, rowc2);
+          w[j] = relu_bf16x2(t.x, t.y);
+        }
+        for (int j = 0; j < 16; ++j) {
+          float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
+                          one2, rowc2);
+          w2[j] = relu_bf16x2(t.x, t.y);
+        }
       }
-      if (i >= 2 && !mbar_wait(&a2_free[b], ((i - 2) / 2) & 1)) {
-        ok = false;
-        break;
+      tc_fence_before();
+      if (!(ok = pair_and(p, good))) break;  // the pair has read D[p]
+      if (leader && i + 2 < n) good = mma1(i + 2);
+      if (kth > 0) good = warp_wait(&w_free[p], (kth - 1) & 1) && good;  // MMA2(i-2) read W[p]
+      tc_fence_after();
+      if (good) {
+        tmem_st16(lane_base + wcol, w);
+        tmem_st16(lane_base + wcol + 16, w2);
+        tmem_wait_st();
       }
-      uint8_t *dst = A2 + b * 32768;
-      for (int kb = 0; kb < 4; ++kb)
-        *reinterpret_cast<uint4 *>(dst + kmajor_offset(row, 32 * g + 8 * kb, 128, 2048)) =
-            *reinterpret_cast<uint4 *>(&w[4 * kb]);
-      fence_async_smem();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&a2_full[b]);
+      tc_fence_before();
+      if (!(ok = pair_and(p, good))) break;  // the pair has written W[p]
+      if (leader) {
+        tc_fence_after();
+        if (lane == 0) {
+          mma2_chunk(tmem + kTcColAcc + 64 * p, tmem + kTcColW + 64 * p, stage_of(i) + kB1Bytes,
+                     kth == 0);
+          mma_commit(&w_free[p]);
+          mma_commit(&stage_free[i % kStagesTc]);
+        }
+        __syncwarp();
+      }
     }
-    if (!ok && lane == 0) atomicExch(a.status, DS_SPIN_LIMIT);
+    if (leader && lane == 0) {
+      if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
+      if (uint32_t(p) < n) mma_commit(acc_done);  // once every MMA of the pair is done
+      else mbar_arrive(acc_done);
+    }
   }
   __syncthreads();
   if (warp < 4) {  // warpgroup 0 writes the tile's partial sums
     const int quad = warp & 3, row = quad * 32 + lane;
-    float acc[32];
-    for (int j = 0; j < 32; ++j) acc[j] = 0.f;
-    if (n && mbar_wait(acc_done, 0)) {
+    float acc[16];
+    for (int j = 0; j < 16; ++j) acc[j] = 0.f;
+    if (n && warp_wait(acc_done, 0)) {
       tc_fence_after();
-      tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kT2ColAcc, acc);
+      for (int q2 = 0; q2 < (n >= 2 ? 4 : 2); ++q2) {  // eight accumulators (pair 1's only if
+        float v[32];                                    // it had a chunk), two per load
+        tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kTcColAcc + 32 * q2, v);
+        for (int j = 0; j < 16; ++j) acc[j] += v[j];
+        for (int j = 0; j < 16; ++j) acc[j] += v[16 + j];
+      }
     }
-    float *out = a.partial + (split * slots + tile * kChunk + row) * 8;
-    for (int d = 0; d < 6; ++d) out[d] = acc[d] + acc[16 + d];  // BF16 x + its residue
+    float *out = a.partial + (uint64_t(piece) * kChunk + row) * 8;
+    for (int d = 0; d < 6; ++d) out[d] = acc[d] + acc[8 + d];  // BF16 x + its residue
     out[6] = acc[6];
     out[7] = 0.f;
   }
   if (tid == 0 && n && a.evals) atomicAdd(a.evals, uint64_t(n) * uint64_t(kChunk * kChunk));
   tc_fence_before();
   __syncthreads();
-  if (warp == 0 && n) tmem_dealloc(tmem, kT2Cols);
+  if (warp == 0 && n) tmem_dealloc(tmem, kTcCols);
 }
 
 // ------------------------------------------------------ tensor self-test
 // One tile: D = A1 . B1^T (128 x 128 x 16) and ACC = A2 . B2^T (128 x 16 x
-// 128) from row-major BF16 inputs, through the same layouts, TMA, MMA and
-// TMEM path as ms_tile_tc.
+// 128) from row-major BF16 inputs, through the same paths as ms_tile_tc: B
+// operands in the canonical shared-memory layout staged by one TMA bulk
+// copy, A operands written to TMEM with tcgen05.st, tcgen05.mma with A from
+// TMEM, results read with tcgen05.ld.
+constexpr uint32_t kSelfB2 = 4096;
+constexpr uint32_t kOffStage = 0, kOffBars = 8192, kOffMisc = kOffBars + 64;
+constexpr uint32_t kSmemRequest = 16 * 1024;
+constexpr uint32_t kTmemCols = 256, kColD = 0, kColAcc = 128, kColA1 = 160, kColA2 = 192;
+
 __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, const __nv_bfloat16 *b1,
                                                       const __nv_bfloat16 *a2, const __nv_bfloat16 *b2,
                                                       uint8_t *scratch, float *d_out, float *acc_out,
                                                       int *status) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t *A1 = smem + kOffA1, *A2 = smem + kOffA2, *S = smem + kOffStage;
+  uint8_t *S = smem + kOffStage;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kOffBars);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kOffMisc);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, quad = warp & 3, wg = warp >> 2;
@@ -548,10 +710,6 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
       g1[kmajor_offset(tid, k, 128, 256) / 2] = b1[tid * 16 + k];
       g2[kmajor_offset(k, tid, 128, 2048) / 2] = b2[k * 128 + tid];
     }
-    __nv_bfloat16 *s1 = reinterpret_cast<__nv_bfloat16 *>(A1);
-    __nv_bfloat16 *s2 = reinterpret_cast<__nv_bfloat16 *>(A2);
-    for (int k = 0; k < 16; ++k) s1[kmajor_offset(tid, k, 128, 256) / 2] = a1[tid * 16 + k];
-    for (int k = 0; k < 128; ++k) s2[kmajor_offset(tid, k, 128, 2048) / 2] = a2[tid * 128 + k];
     asm volatile("fence.proxy.async.global;" ::: "memory");
   }
   if (tid == 0) {
@@ -561,11 +719,24 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
   }
   if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
   __threadfence();
-  fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
+  if (wg == 0) {  // A1 and A2 rows into TMEM, lane = row
+    const uint32_t lane_base = uint32_t(quad * 32) << 16;
+    uint32_t r8[8], r32[32];
+    for (int c = 0; c < 8; ++c) r8[c] = bf16_pair(a1 + row * 16 + 2 * c);
+    tmem_st8(tmem + lane_base + kColA1, r8);
+    for (int half = 0; half < 2; ++half) {
+      for (int c = 0; c < 32; ++c) r32[c] = bf16_pair(a2 + row * 128 + 64 * half + 2 * c);
+      tmem_st32(tmem + lane_base + kColA2 + 32 * half, r32);
+    }
+    tmem_wait_st();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
   bool ok = true;
   if (tid == 0) {
     asm volatile("fence.proxy.async.global;" ::: "memory");
@@ -574,10 +745,11 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
   }
   ok = __syncthreads_and(mbar_wait(&bar[0], 0));
   if (ok && tid == 0) {
-    mma_bf16(tmem + kColD, smem_desc(A1, 128, 256), smem_desc(S, 128, 256), idesc_bf16(128, 128), 0);
+    tc_fence_after();
+    mma_bf16_ts(tmem + kColD, tmem + kColA1, smem_desc(S, 128, 256), idesc_bf16(128, 128), 0);
     for (uint32_t s = 0; s < 8; ++s)
-      mma_bf16(tmem + kColAcc, smem_desc(A2 + s * 256, 128, 2048),
-               smem_desc(S + kB1Bytes + s * 256, 128, 2048), idesc_bf16(128, 16), s > 0);
+      mma_bf16_ts(tmem + kColAcc, tmem + kColA2 + 8 * s, smem_desc(S + kB1Bytes + s * 256, 128, 2048),
+                  idesc_bf16(128, 16), s > 0);
     mma_commit(&bar[1]);
   }
   if (ok) ok = __syncthreads_and(mbar_wait(&bar[1], 0));
@@ -601,15 +773,35 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-__global__ void ms_update_bulk(float *means, const float *partial, uint64_t splits, uint64_t slots,
+// Work plan of one bulk iteration: tile t gets pieces[t+1] - pieces[t] CTAs,
+// about len_t * budget / total of them (at least one), so every CTA streams
+// a similar number of chunks; the pieces add up to at most budget + tiles.
+__global__ void plan_pieces(const uint64_t *offsets, uint64_t tiles, uint32_t budget,
+                            uint32_t *pieces) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const uint64_t total = offsets[tiles] - offsets[0];
+  uint32_t at = 0;
+  for (uint64_t t = 0; t < tiles; ++t) {
+    pieces[t] = at;
+    const uint64_t len = offsets[t + 1] - offsets[t];
+    const uint64_t want = total ? (len * budget + total - 1) / total : 1;
+    at += uint32_t(want ? want : 1);
+  }
+  pieces[tiles] = at;
+}
+
+// Sum of a seed's pieces (fixed order), then the mean-shift step; the bulk
+// stops a seed when its squared move falls under stop * h^2.
+__global__ void ms_update_bulk(float *means, const float *partial, const uint32_t *pieces,
                                const int32_t *ids, uint64_t nactive, float h2, float stop,
                                uint8_t *state) {
   uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (slot >= nactive) return;
   int32_t s = ids[slot];
+  const uint64_t tile = slot / kChunk, row = slot % kChunk;
   float acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (uint64_t p = 0; p < splits; ++p)
-    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * slots + slot) * 8 + d];
+  for (uint32_t p = pieces[tile]; p < pieces[tile + 1]; ++p)
+    for (int d = 0; d < 7; ++d) acc[d] += partial[(uint64_t(p) * kChunk + row) * 8 + d];
   if (acc[6] <= 1e-14f) {
     state[s] = 2;
     return;
@@ -641,19 +833,22 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   cudaStream_t st = call.stream();
   static bool configured = false;
   if (!configured) {
-    SYM_CUDA(cudaFuncSetAttribute(ms_tile_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, kT2Smem));
+    SYM_CUDA(cudaFuncSetAttribute(ms_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
     configured = true;
   }
   uint8_t *images = call.alloc<uint8_t>(v.nchunks * kImage);
-  build_images<<<unsigned(v.nchunks), kChunk, 0, st>>>(v.desc, v.q, v.nchunks, v.cbox, images);
+  build_images<<<unsigned(v.nchunks), kChunk, 0, st>>>(v.desc, v.q, v.nchunks, v.cbox, v.gbox,
+                                                       float(1.0 / std::sqrt(h2)), images);
   check_launch();
   int32_t *ids = call.alloc<int32_t>(k);
   float *boxes = call.alloc<float>(max_tiles * 12);
   uint8_t *need = call.alloc<uint8_t>(max_tiles * v.nchunks);
   int32_t *list = call.alloc<int32_t>(max_tiles * v.nchunks);
   uint64_t *count = call.alloc<uint64_t>(1), *offsets = call.alloc<uint64_t>(max_tiles + 1);
-  const uint64_t max_splits = 152;
-  float *partial = call.alloc<float>(max_splits * max_tiles * kChunk * 8);
+  uint32_t *pieces = call.alloc<uint32_t>(max_tiles + 1);
+  const uint64_t sms = 152;  // one wave: budget + tiles CTAs on the 152 SMs
+  const uint64_t max_grid = std::max<uint64_t>(sms, 2 * max_tiles);
+  float *partial = call.alloc<float>(max_grid * kChunk * 8);
   unsigned long long *evals = call.alloc<unsigned long long>(1);
   SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
   float gap = float(std::sqrt(h2)) + 1e-6f;
@@ -664,7 +859,8 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     if (!n) break;
     if (trace && it < trace_len) trace[it] = n;
     const uint64_t tiles = (n + kChunk - 1) / kChunk;
-    const uint64_t splits = std::max<uint64_t>(1, max_splits / tiles);
+    const uint32_t budget = uint32_t(tiles < sms ? sms - tiles : tiles);
+    const uint64_t grid = budget + tiles;
     auto mark = call.ctx->arena.mark();
     tile_boxes<<<unsigned(tiles), kChunk, 0, st>>>(means, ids, n, boxes);
     check_launch();
@@ -674,14 +870,16 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     compact_indices(call, need, tiles * v.nchunks, list, count);
     tile_offsets<<<blocks_for(tiles + 1), kThreads, 0, st>>>(list, count, tiles, v.nchunks, offsets);
     check_launch();
-    Tc2Args args{images, v.nchunks, list, offsets, splits, means, ids, n,
-                 float(1.0 / h2), partial, evals, call.status()};
-    ms_tile_tc2<<<dim3(unsigned(tiles), unsigned(splits)), kThreads2, kT2Smem, st>>>(args);
+    plan_pieces<<<1, 32, 0, st>>>(offsets, tiles, budget, pieces);
     check_launch();
-    ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, splits, tiles * kChunk, ids,
-                                                       n, float(h2), 1e-5f, state);
+    TcArgs args{images, v.nchunks, list, offsets, pieces, tiles, means, ids, n, v.gbox,
+                float(1.0 / std::sqrt(h2)), partial, evals, call.status()};
+    ms_tile_tc<<<unsigned(grid), kThreadsTc, kTcSmem, st>>>(args);
     check_launch();
-    call.launched(5);
+    ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, pieces, ids, n, float(h2),
+                                                       1e-5f, state);
+    check_launch();
+    call.launched(6);
     call.ctx->arena.rewind(mark);
   }
   call.check_status("mean_shift (tensor)");
