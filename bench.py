@@ -6,9 +6,10 @@ subdivided 6 times, radially displaced by a seeded 12-bump motif repeated in
 5-fold rotation about z, plus a partial copy translated 0.4 along x, Gaussian
 vertex noise 1e-3 of the bbox diagonal (54,756 vertices, 109,102 faces);
 20,000 area-weighted samples, pair threshold 0.25 (~1e7 pairs), 6-D rigid
-votes, 2,048 mean-shift seeds, bandwidth 0.1, up to 300 mean-shift iterations
-(and up to 50 FP32 polish iterations after the BF16 bulk).  Synthetic data,
-seeded.
+votes, 2,048 mean-shift seeds, bandwidth 0.1; mean-shift approach phase of
+up to 300 iterations (BF16 tensor cores, or FP32 for the comparison form),
+then up to 30 FP32 polish iterations (Newton steps near the modes) for both
+forms.  Synthetic data, seeded.
 
 One step = the whole hot path on one mesh: curvature, prune, exact pairing,
 6-D votes, vote sort, mean-shift, modes, verification of the top 20 modes.
@@ -45,8 +46,8 @@ SAMPLES = 20000
 PAIR_THRESHOLD = 0.25
 BANDWIDTH = 0.1
 SEEDS = 2048
-ITERATIONS = 300  # bulk mean-shift iterations (FP32, or BF16 before the polish)
-POLISH = 50       # FP32 polish iterations after the BF16 bulk
+ITERATIONS = 300  # mean-shift approach-phase iterations (BF16, or FP32)
+POLISH = 30       # FP32 polish iterations (both forms)
 
 
 def workload(small=False):
@@ -323,13 +324,14 @@ def run_gpu(args):
         "mode_error": {pr: {"max": e["mode_error_max"], "mean": e["mode_error_mean"],
                             "reference_seeds": 256, "compared": e["modes_compared"],
                             "within_1e-4": e["modes_within"]} for pr, e in err.items()},
-        "mean_shift": {"bulk_iterations": r["iterations"], "polish_iterations": r["polish_iterations"],
-                       "modes": r["modes"], "evaluations": evals,
-                       "bulk_ms": round(r["bulk_ms"], 3), "polish_ms": round(r["polish_ms"], 3),
-                       "fp32_ms": round(res_fp32[-1]["bulk_ms"], 3),
-                       "fp32_iterations": res_fp32[-1]["iterations"],
-                       "bulk_trace": r["bulk_trace"][::10], "polish_trace": r["polish_trace"][::5],
-                       "fp32_trace": res_fp32[-1]["bulk_trace"][::10]},
+        "mean_shift": {pr: {"approach_iterations": x["iterations"],
+                            "approach_ms": round(x["bulk_ms"], 3),
+                            "polish_iterations": x["polish_iterations"],
+                            "polish_ms": round(x["polish_ms"], 3),
+                            "approach_trace": x["bulk_trace"][::10],
+                            "polish_trace": x["polish_trace"][::3]}
+                       for pr, x in (("bf16", r), ("fp32", res_fp32[-1]))},
+        "modes": r["modes"], "evaluations": evals,
         "stage_ms": {k: round(statistics.mean(x["stage_ms"][k] for x in res_bf16), 3)
                      for k in r["stage_ms"]},
         "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",

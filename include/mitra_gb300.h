@@ -282,9 +282,10 @@ sym_status sym_triangle_distances(sym_context *ctx, const double *queries,
  * 6-D rigid votes (axis-angle/2 + centred translation/box, FP32 transforms,
  * FP64 log map near pi), a spatially sorted vote set, mean-shift from K seeds
  * with Epanechnikov weights, mode merging, and verification of the top
- * modes.  The mean-shift precision is selectable: plain FP32, or BF16 tensor-
- * core bulk iterations refined by FP32 polish; a subset of seeds can be
- * re-run in FP64 to report the mode error. */
+ * modes.  The mean-shift approach phase runs in FP32 (SIMT) or BF16 (tensor
+ * cores); both forms then share the same FP32 polish phase (Newton steps near
+ * the modes, see sym_meanshift6); a subset of seeds can be re-run in FP64 to
+ * report the mode error. */
 typedef struct sym_mesh_handle sym_mesh_handle;
 /* Uploads the mesh and its topology; the host views must stay valid while
  * the handle is used (the verification BVH is built from them). */
@@ -298,8 +299,8 @@ typedef struct sym_fast_options {
   int32_t precision;         /* SYM_MS_FP32 or SYM_MS_BF16_REFINED */
   int32_t seeds;             /* mean-shift seeds K (votes drawn uniformly) */
   uint64_t seed_rng;         /* seed of the seed-drawing std::mt19937_64 */
-  int32_t max_iterations;    /* bulk iterations (BF16 or FP32) */
-  int32_t polish_iterations; /* FP32 refinement iterations after BF16 */
+  int32_t max_iterations;    /* approach-phase iterations (BF16 or FP32) */
+  int32_t polish_iterations; /* FP32 polish iterations (both forms) */
   int32_t reference_seeds;   /* seeds re-run in FP64 for the mode error */
   int32_t verify;            /* verify the top modes (max_clusters) */
 } sym_fast_options;
@@ -309,8 +310,8 @@ typedef struct sym_fast_result {
   uint64_t pruned, pairs, votes, modes, clusters;
   int32_t iterations, polish_iterations;
   /* relative error of each mode against FP64, over the reference seeds that
-   * converged in both runs (modes_compared of them); modes_within counts
-   * those within 1e-4 */
+   * converged (Newton, a well-defined mode) in both runs (modes_compared of
+   * them); modes_within counts those within 1e-4 */
   double mode_error_max, mode_error_mean;
   uint64_t modes_compared, modes_within;
   /* device time per stage: curvature, prune, pairing, votes, vote sort,
@@ -335,10 +336,19 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
 
 /* The mean-shift kernels of sym_detect_fast on their own (no reference
  * counterpart): K seeds over Q 6-D votes (host, q x 6 doubles), seeds are
- * vote indices.  Writes the K final means (k x 6), each seed's state (0 still
- * moving, 1 converged, 2 exhausted) and the bulk / polish iteration counts.
- * `precision`: SYM_MS_FP32, SYM_MS_BF16_REFINED, or SYM_MS_FP64 (the FP64
- * form used to measure mode errors). */
+ * vote indices.  Approach phase (at most max_iterations, in the requested
+ * precision: FP32, BF16 tensor cores, or FP64): plain mean-shift steps until a
+ * seed's squared step is below 1e-4 h^2.  Polish phase (at most
+ * polish_iterations, FP32; FP64 for SYM_MS_FP64): safeguarded Newton steps on
+ * m(x) = x until a Newton step is below 1e-4 h (converged).  A rejected
+ * Newton step (singular system, step longer than h/4 or against the plain
+ * step: the density is flat along some direction, the mode has no
+ * well-defined position) settles the seed after one plain step.  Writes
+ * the K final means (k x 6), each seed's state (0 still approaching,
+ * 1 converged, 2 exhausted, 3 near a mode when the iterations ran out,
+ * 4 settled) and the approach / polish iteration counts.  `precision`: SYM_MS_FP32,
+ * SYM_MS_BF16_REFINED, or SYM_MS_FP64 (the form used to measure mode
+ * errors). */
 enum { SYM_MS_FP64 = 2 };
 sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q,
                           const int64_t *seeds, uint64_t k, double bandwidth,

@@ -189,9 +189,10 @@ class Gb300Backend:
     def meanshift6(self, votes, seeds, bandwidth, precision="fp32", max_iterations=100,
                    polish_iterations=100):
         """Mean-shift of the seed votes over 6-D votes (q x 6); returns the
-        final means (k x 6), per-seed state and the (bulk, polish) iteration
-        counts.  precision: "fp32", "bf16" (BF16 bulk + FP32 polish) or
-        "fp64"."""
+        final means (k x 6), per-seed state and the (approach, polish)
+        iteration counts.  precision: "fp32" (FP32 approach), "bf16" (BF16
+        tensor-core approach), both followed by the same FP32 polish, or
+        "fp64" (both phases in FP64)."""
         v = np.ascontiguousarray(votes, np.float64).reshape(-1, 6)
         s = np.ascontiguousarray(seeds, np.int64)
         means = np.zeros((s.size, 6))

@@ -111,20 +111,26 @@ __device__ __forceinline__ float box_gap2(const float *a_lo, const float *a_hi, 
 
 // One block = one tile of up to kChunk active seeds (ids[tile*kChunk + t])
 // x one split of the chunk range.  Each thread accumulates, for its seed,
-// sum w x and sum w over the votes of the chunks its tile cannot skip.
+// sum w x and sum w over the votes of the chunks its tile cannot skip, and
+// for a kNear seed also the unweighted in-window sums of d = v - x and
+// d d^T (the Jacobian of the Newton step).
 // COUNT: count the votes within the bandwidth instead.
-template <typename T, bool COUNT>
+// NEWTON: some seed of the launch is kNear (the plain instance keeps its
+// register footprint small).
+template <typename T, bool COUNT, bool NEWTON>
 __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cbox, uint64_t nchunks,
-                                                  uint64_t q, const T *means, const int32_t *ids,
-                                                  uint64_t nactive, T h2, float skip_gap2,
-                                                  uint64_t chunks_per_split, T *partial,
-                                                  unsigned long long *evals) {
+                                                  uint64_t q, const T *means, const uint8_t *state,
+                                                  const int32_t *ids, uint64_t nactive, T h2,
+                                                  float skip_gap2, uint64_t chunks_per_split,
+                                                  T *partial, unsigned long long *evals) {
+  constexpr int stride = COUNT ? 8 : kPartial;
   __shared__ T xs[kChunk * 8];
   __shared__ float tlo[6][4], thi[6][4];
   uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x, split = blockIdx.y;
   uint64_t slots = uint64_t(gridDim.x) * kChunk;
   bool live = slot < nactive;
   int32_t seed = live ? ids[slot] : 0;
+  const bool newton = NEWTON && !COUNT && live && state[seed] == kNear;
   T m[6];
   for (int d = 0; d < 6; ++d) m[d] = live ? means[uint64_t(seed) * 8 + d] : T(0);
   float lo[6], hi[6];
@@ -146,6 +152,8 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
     hi[d] = fmaxf(fmaxf(thi[d][0], thi[d][1]), fmaxf(thi[d][2], thi[d][3]));
   }
   T acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  T sd[6] = {0, 0, 0, 0, 0, 0}, sdd[21];
+  for (int j = 0; j < 21; ++j) sdd[j] = 0;
   uint64_t c0 = split * chunks_per_split;
   uint64_t c1 = c0 + chunks_per_split < nchunks ? c0 + chunks_per_split : nchunks;
   unsigned long long done = 0;
@@ -159,11 +167,11 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
     int n = rest < uint64_t(kChunk) ? int(rest) : kChunk;
     done += n;
     for (int j = 0; j < n; ++j) {
-      T d2 = 0;
+      T e[6], d2 = 0;
 #pragma unroll
       for (int d = 0; d < 6; ++d) {
-        T e = m[d] - xs[j * 8 + d];
-        d2 += e * e;
+        e[d] = xs[j * 8 + d] - m[d];
+        d2 += e[d] * e[d];
       }
       if (d2 < h2) {
         if (COUNT) {
@@ -173,57 +181,142 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
 #pragma unroll
           for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
           acc[6] += w;
+          if (newton) {
+            int at = 0;
+#pragma unroll
+            for (int d = 0; d < 6; ++d) {
+              sd[d] += e[d];
+#pragma unroll
+              for (int l = d; l < 6; ++l) sdd[at++] += e[d] * e[l];
+            }
+          }
         }
       }
     }
   }
-  for (int d = 0; d < 7; ++d) partial[(split * slots + slot) * 8 + d] = acc[d];
+  T *out = partial + (split * slots + slot) * stride;
+  for (int d = 0; d < 7; ++d) out[d] = acc[d];
+  if (newton) {
+    for (int d = 0; d < 6; ++d) out[8 + d] = sd[d];
+    for (int j = 0; j < 21; ++j) out[14 + j] = sdd[j];
+  }
   if (threadIdx.x == 0 && done && evals) atomicAdd(evals, done * (unsigned long long)kChunk);
 }
 
-// Sum of the splits (fixed order) then the Epanechnikov mean-shift step and
-// the reference's stopping rules: exhausted when the weight is <= 1e-14,
-// converged when the squared movement is < 1e-6 h^2.
+// b <- M^-1 b by Gaussian elimination with partial pivoting; false when a
+// pivot is below `tiny` (singular system).
+template <typename T>
+__device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
+  for (int c = 0; c < 6; ++c) {
+    int piv = c;
+    T best = fabs(M[c][c]);
+    for (int r = c + 1; r < 6; ++r)
+      if (fabs(M[r][c]) > best) best = fabs(M[r][c]), piv = r;
+    if (!(best > tiny)) return false;
+    if (piv != c) {
+      for (int j = 0; j < 6; ++j) {
+        T t = M[c][j];
+        M[c][j] = M[piv][j], M[piv][j] = t;
+      }
+      T t = b[c];
+      b[c] = b[piv], b[piv] = t;
+    }
+    for (int r = c + 1; r < 6; ++r) {
+      T f = M[r][c] / M[c][c];
+      for (int j = c; j < 6; ++j) M[r][j] -= f * M[c][j];
+      b[r] -= f * b[c];
+    }
+  }
+  for (int c = 5; c >= 0; --c) {
+    T s = b[c];
+    for (int j = c + 1; j < 6; ++j) s -= M[c][j] * b[j];
+    b[c] = s / M[c][c];
+  }
+  return true;
+}
+
+// Sum of the splits (fixed order), then one step of the seed: the
+// Epanechnikov mean-shift step m - x for a kMoving seed, the safeguarded
+// Newton step (I - J)^-1 (m - x) for a kNear seed, where
+//   J = dm/dx = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T),
+// d = v - x over the votes within the bandwidth.  Stopping rules: exhausted
+// when the weight is <= 1e-14 (reference, src/cpu/clustering.cpp:169-181),
+// converged when a Newton step^2 < kNewtonStop2 h^2, settled (plain step
+// taken) when the Newton step is rejected.
 template <typename T>
 __global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t slots,
                           const int32_t *ids, uint64_t nactive, T h2, uint8_t *state) {
   uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (slot >= nactive) return;
   int32_t s = ids[slot];
+  const bool near = state[s] == kNear;
   T acc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (uint64_t p = 0; p < splits; ++p)
-    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * slots + slot) * 8 + d];
+    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * slots + slot) * kPartial + d];
   if (acc[6] <= T(1e-14)) {
-    state[s] = 2;
+    state[s] = kExhausted;
     return;
   }
-  T move = 0;
+  T x[6], delta[6], move = 0;
   for (int d = 0; d < 6; ++d) {
-    T nx = acc[d] / acc[6];
-    T e = means[uint64_t(s) * 8 + d] - nx;
-    move += e * e;
-    means[uint64_t(s) * 8 + d] = nx;
+    x[d] = means[uint64_t(s) * 8 + d];
+    delta[d] = acc[d] / acc[6] - x[d];
+    move += delta[d] * delta[d];
   }
-  if (move < T(1e-6) * h2) state[s] = 1;
+  if (!near) {
+    for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + delta[d];
+    if (move < T(kSwitch2) * h2) state[s] = kNear;
+    return;
+  }
+  T sd[6] = {0, 0, 0, 0, 0, 0}, sdd[21];
+  for (int j = 0; j < 21; ++j) sdd[j] = 0;
+  for (uint64_t p = 0; p < splits; ++p) {
+    const T *in = partial + (p * slots + slot) * kPartial;
+    for (int d = 0; d < 6; ++d) sd[d] += in[8 + d];
+    for (int j = 0; j < 21; ++j) sdd[j] += in[14 + j];
+  }
+  T M[6][6], step[6];
+  const T g = T(2) / (h2 * acc[6]);
+  for (int d = 0, at = 0; d < 6; ++d)
+    for (int l = d; l < 6; ++l, ++at) M[d][l] = M[l][d] = sdd[at];
+  for (int d = 0; d < 6; ++d) {
+    for (int l = 0; l < 6; ++l) M[d][l] = (d == l ? T(1) : T(0)) - g * (M[d][l] - delta[d] * sd[l]);
+    step[d] = delta[d];
+  }
+  bool ok = solve6(M, step, T(sizeof(T) == 4 ? 1e-6 : 1e-12));
+  T len = 0, along = 0;
+  for (int d = 0; d < 6; ++d) len += step[d] * step[d], along += step[d] * delta[d];
+  ok = ok && isfinite(len) && len <= T(kTrust * kTrust) * h2 &&
+       (along > T(0) || len < T(kNewtonStop2) * h2);
+  if (ok) {
+    for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + step[d];
+    if (len < T(kNewtonStop2) * h2) state[s] = kConverged;
+  } else {
+    for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + delta[d];
+    state[s] = kSettled;
+  }
 }
 
 constexpr int kRetile = 2048;  // seeds sorted in one block (static shared memory)
 
-// Active seeds (state 0) in seed order, then sorted by the Morton key of
-// their current mean (ties by seed id) when k <= kRetile.
+// Active seeds (kMoving, and kNear when include_near) in seed order, then
+// sorted by the Morton key of
+// their current mean (ties by seed id) when k <= kRetile.  nactive[0] = the
+// number of active seeds, nactive[1] = how many of them are kNear.
 template <typename T>
 __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *state, uint64_t k,
-                                               const float *box, int32_t *ids, unsigned *nactive) {
+                                               const float *box, bool include_near, int32_t *ids,
+                                               unsigned *nactive) {
   __shared__ unsigned long long keys[kRetile];
   __shared__ int32_t vals[kRetile];
   __shared__ unsigned warp_tot[32];
-  __shared__ unsigned base_s;
-  if (threadIdx.x == 0) base_s = 0;
+  __shared__ unsigned base_s, near_s;
+  if (threadIdx.x == 0) base_s = 0, near_s = 0;
   __syncthreads();
   bool sort = k <= kRetile;
   for (uint64_t at = 0; at < k; at += blockDim.x) {
     uint64_t s = at + threadIdx.x;
-    bool act = s < k && state[s] == 0;
+    bool act = s < k && (state[s] == kMoving || (include_near && state[s] == kNear));
     unsigned bal = __ballot_sync(0xffffffffu, act);
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) warp_tot[warp] = __popc(bal);
@@ -234,6 +327,7 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
       total += warp_tot[w];
     }
     unsigned pos = base_s + before + __popc(bal & ((1u << lane) - 1));
+    if (act && state[s] == kNear) atomicAdd(&near_s, 1u);
     if (act) {
       if (sort) {
         float x[6];
@@ -273,7 +367,8 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
       }
     for (unsigned i = threadIdx.x; i < n; i += blockDim.x) ids[i] = vals[i];
   }
-  if (threadIdx.x == 0) *nactive = n;
+  __syncthreads();
+  if (threadIdx.x == 0) nactive[0] = n, nactive[1] = near_s;
 }
 
 template <typename T>
@@ -309,30 +404,36 @@ Grid grid_for(uint64_t nactive, uint64_t nchunks) {
 
 template <typename T>
 int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *state, uint64_t k,
-               double h2, int max_iter, double *seed_iterations, unsigned long long *evals,
-               uint32_t *trace = nullptr, int trace_len = 0) {
+               double h2, int max_iter, bool polish, double *seed_iterations,
+               unsigned long long *evals, uint32_t *trace = nullptr, int trace_len = 0) {
   cudaStream_t st = call.stream();
   int32_t *ids = call.alloc<int32_t>(k);
-  unsigned *nact = call.alloc<unsigned>(1);
+  unsigned *nact = call.alloc<unsigned>(2);
   // partial capacity: splits x slots is at most ~64*152*kChunk (+ one tile)
   uint64_t cap = (64 * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
-  T *partial = call.alloc<T>(cap * 8);
+  T *partial = call.alloc<T>(cap * kPartial);
   float gap = float(std::sqrt(h2)) + 1e-6f;
   int it = 0;
   for (; it < max_iter; ++it) {
-    retile<T><<<1, 1024, 0, st>>>(means, state, k, v.gbox, ids, nact);
+    retile<T><<<1, 1024, 0, st>>>(means, state, k, v.gbox, polish, ids, nact);
     check_launch();
-    unsigned n = 0;
-    SYM_CUDA(cudaMemcpyAsync(&n, nact, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    unsigned counts[2] = {0, 0};
+    SYM_CUDA(cudaMemcpyAsync(counts, nact, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
     call.sync();
     call.launched();
+    const unsigned n = counts[0];
     if (!n) break;
     if (seed_iterations) *seed_iterations += n;
     if (trace && it < trace_len) trace[it] = n;
     Grid g = grid_for(n, v.nchunks);
     if (g.splits * g.slots > cap) fail(SYM_RUNTIME_ERROR, "mean-shift partial buffer too small");
-    ms_tile<T, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
-        desc, v.cbox, v.nchunks, v.q, means, ids, n, T(h2), gap * gap, g.cps, partial, evals);
+    const dim3 grid(unsigned(g.tiles), unsigned(g.splits));
+    if (counts[1])
+      ms_tile<T, false, true><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state, ids,
+                                                      n, T(h2), gap * gap, g.cps, partial, evals);
+    else
+      ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state,
+                                                       ids, n, T(h2), gap * gap, g.cps, partial, evals);
     check_launch();
     ms_update<T><<<blocks_for(n), kThreads, 0, st>>>(means, partial, g.splits, g.slots, ids, n,
                                                      T(h2), state);
@@ -393,21 +494,22 @@ void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t
 }
 
 int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k, double h2,
-          int max_iter, double *seed_iterations, unsigned long long *evals, uint32_t *trace,
-          int trace_len) {
-  return shift_impl<float>(call, v, v.desc, means, state, k, h2, max_iter, seed_iterations, evals,
-                           trace, trace_len);
+          int max_iter, bool polish, double *seed_iterations, unsigned long long *evals,
+          uint32_t *trace, int trace_len) {
+  return shift_impl<float>(call, v, v.desc, means, state, k, h2, max_iter, polish, seed_iterations,
+                           evals, trace, trace_len);
 }
 
 int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,
-          int max_iter, double *seed_iterations, unsigned long long *evals) {
-  return shift_impl<double>(call, v, v.desc64, means, state, k, h2, max_iter, seed_iterations, evals);
+          int max_iter, bool polish, double *seed_iterations, unsigned long long *evals) {
+  return shift_impl<double>(call, v, v.desc64, means, state, k, h2, max_iter, polish,
+                            seed_iterations, evals);
 }
 
 unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
                       uint64_t k, int32_t *ids) {
-  unsigned *nact = call.alloc<unsigned>(1);
-  retile<float><<<1, 1024, 0, call.stream()>>>(means, state, k, v.gbox, ids, nact);
+  unsigned *nact = call.alloc<unsigned>(2);
+  retile<float><<<1, 1024, 0, call.stream()>>>(means, state, k, v.gbox, false, ids, nact);
   check_launch();
   call.launched();
   unsigned n = 0;
@@ -423,14 +525,15 @@ void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm
   uint8_t *state = call.alloc<uint8_t>(nm);
   SYM_CUDA(cudaMemsetAsync(state, 0, nm, st));
   int32_t *ids = call.alloc<int32_t>(nm);
-  unsigned *nact = call.alloc<unsigned>(1);
-  retile<float><<<1, 1024, 0, st>>>(points, state, nm, v.gbox, ids, nact);
+  unsigned *nact = call.alloc<unsigned>(2);
+  retile<float><<<1, 1024, 0, st>>>(points, state, nm, v.gbox, false, ids, nact);
   check_launch();
   Grid g = grid_for(nm, v.nchunks);
   float *partial = call.alloc<float>(g.splits * g.slots * 8);
   float gap = float(std::sqrt(h2)) + 1e-6f;
-  ms_tile<float, true><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
-      v.desc, v.cbox, v.nchunks, v.q, points, ids, nm, float(h2), gap * gap, g.cps, partial, nullptr);
+  ms_tile<float, true, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
+      v.desc, v.cbox, v.nchunks, v.q, points, nullptr, ids, nm, float(h2), gap * gap, g.cps, partial,
+      nullptr);
   check_launch();
   sum_counts<<<blocks_for(nm), kThreads, 0, st>>>(partial, g.splits, g.slots, ids, nm, counts);
   check_launch();

@@ -16,6 +16,22 @@ namespace sym {
 
 constexpr int kChunk = 128;  // votes per chunk = seeds per tile
 
+// Seed states.  A seed approaches its mode with plain mean-shift steps
+// (kMoving) until its squared step falls under kSwitch2 h^2, then takes
+// safeguarded Newton steps on m(x) - x = 0 (kNear) until a Newton step's
+// square falls under kNewtonStop2 h^2 (kConverged: a mode whose position is
+// well defined).  A Newton step is rejected when the 6x6 system is
+// singular, the step is longer than kTrust h or points against the plain
+// step (unless it already meets the convergence test) - the density is flat along some direction there (a ridge), so the
+// mode has no well-defined position: the seed takes the plain step and
+// stops (kSettled).  kExhausted: total weight <= 1e-14.
+constexpr uint8_t kMoving = 0, kConverged = 1, kExhausted = 2, kNear = 3, kSettled = 4;
+constexpr double kSwitch2 = 1e-4, kNewtonStop2 = 1e-8, kTrust = 0.25;
+// Floats (or doubles) per partial sum of one seed: sum w x (6), sum w, pad,
+// then for kNear seeds the unweighted in-window sums of d = v - x: sum d
+// (6) and sum d d^T (21, upper triangle row by row), pad.
+constexpr int kPartial = 40;
+
 struct VoteSet {
   uint64_t q = 0, nchunks = 0;
   float *desc = nullptr;      // q x 8, Morton order
@@ -33,17 +49,21 @@ VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_r
 void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, float *means);
 void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, double *means);
 
-// Iterates until every seed converged/exhausted or max_iter; state[k] in/out
-// (0 moving, 1 converged, 2 exhausted).  Adds the seed-iterations to
-// *seed_iterations and seed-vote evaluations to *evals (device counter).
+// At most max_iter iterations over the active seeds; state[k] in/out
+// (kMoving, kNear, kConverged, kExhausted, kSettled).  Approach phase (polish = false):
+// only kMoving seeds step, and a seed leaves once it is kNear.  Polish phase
+// (polish = true): kMoving and kNear seeds step until converged, settled or
+// exhausted.
+// Adds the seed-iterations to *seed_iterations and seed-vote evaluations to
+// *evals (device counter).
 int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k, double h2,
-          int max_iter, double *seed_iterations, unsigned long long *evals,
+          int max_iter, bool polish, double *seed_iterations, unsigned long long *evals,
           uint32_t *trace = nullptr, int trace_len = 0);
 int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,
-          int max_iter, double *seed_iterations, unsigned long long *evals);
+          int max_iter, bool polish, double *seed_iterations, unsigned long long *evals);
 
-// Active seeds (state 0), Morton-sorted by position when k <= 2048; returns
-// their number (synchronises).
+// kMoving seeds, Morton-sorted by position when k <= 2048; returns their
+// number (synchronises).
 unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
                       uint64_t k, int32_t *ids);
 

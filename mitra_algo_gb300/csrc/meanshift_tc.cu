@@ -790,11 +790,11 @@ __global__ void plan_pieces(const uint64_t *offsets, uint64_t tiles, uint32_t bu
   pieces[tiles] = at;
 }
 
-// Sum of a seed's pieces (fixed order), then the mean-shift step; the bulk
-// stops a seed when its squared move falls under stop * h^2.
+// Sum of a seed's pieces (fixed order), then the mean-shift step; a seed
+// leaves the bulk (kNear: the FP32 polish takes it on with Newton steps)
+// when its squared move falls under kSwitch2 h^2.
 __global__ void ms_update_bulk(float *means, const float *partial, const uint32_t *pieces,
-                               const int32_t *ids, uint64_t nactive, float h2, float stop,
-                               uint8_t *state) {
+                               const int32_t *ids, uint64_t nactive, float h2, uint8_t *state) {
   uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (slot >= nactive) return;
   int32_t s = ids[slot];
@@ -803,7 +803,7 @@ __global__ void ms_update_bulk(float *means, const float *partial, const uint32_
   for (uint32_t p = pieces[tile]; p < pieces[tile + 1]; ++p)
     for (int d = 0; d < 7; ++d) acc[d] += partial[(uint64_t(p) * kChunk + row) * 8 + d];
   if (acc[6] <= 1e-14f) {
-    state[s] = 2;
+    state[s] = kExhausted;
     return;
   }
   float move = 0;
@@ -813,7 +813,7 @@ __global__ void ms_update_bulk(float *means, const float *partial, const uint32_
     move += e * e;
     means[uint64_t(s) * 8 + d] = nx;
   }
-  if (move < stop * h2) state[s] = 1;
+  if (move < float(kSwitch2) * h2) state[s] = kNear;
 }
 
 }  // namespace
@@ -877,7 +877,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     ms_tile_tc<<<unsigned(grid), kThreadsTc, kTcSmem, st>>>(args);
     check_launch();
     ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, pieces, ids, n, float(h2),
-                                                       1e-5f, state);
+                                                       state);
     check_launch();
     call.launched(6);
     call.ctx->arena.rewind(mark);

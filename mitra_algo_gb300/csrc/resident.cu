@@ -12,7 +12,9 @@
 //   merge (h^2/4 as the reference) and support counts -> verification of
 //   the top modes (verification.cu).
 // Precision: FP32 SIMT or BF16 tensor-core bulk (meanshift_tc.cu) polished
-// in FP32; a subset of seeds re-runs in FP64 to measure the mode error.
+// in FP32 (the seeds near a mode finish with Newton steps, see
+// meanshift_fast.cuh); a subset of seeds re-runs in FP64 to measure the mode
+// error.
 #include "common.cuh"
 #include "primitives.cuh"
 #include "meanshift_fast.cuh"
@@ -277,26 +279,26 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   cudaEvent_t ph[3];
   for (auto &e : ph) cudaEventCreate(&e);
   cudaEventRecord(ph[0], st);
+  // approach phase (BF16 tensor cores or FP32 SIMT), then the same FP32
+  // polish for both forms: kNear seeds take Newton steps, kMoving ones keep
+  // approaching
   bool tensor = fo.precision == SYM_MS_BF16_REFINED &&
                 meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals,
                                     r.bulk_trace, 320);
-  cudaEventRecord(ph[1], st);
-  if (tensor) {
-    SYM_CUDA(cudaMemsetAsync(st32, 0, k, st));  // polish every seed in FP32
-    polish = shift(call, vs, m32, st32, k, h2, fo.polish_iterations, &r.seed_iterations, evals,
-                   r.polish_trace, 320);
-  } else {
-    bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, &r.seed_iterations, evals,
+  if (!tensor)
+    bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, false, &r.seed_iterations, evals,
                  r.bulk_trace, 320);
-  }
+  cudaEventRecord(ph[1], st);
+  polish = shift(call, vs, m32, st32, k, h2, fo.polish_iterations, true, &r.seed_iterations, evals,
+                 r.polish_trace, 320);
   cudaEventRecord(ph[2], st);
   cudaEventSynchronize(ph[2]);
   {
     float a = 0, b = 0;
     cudaEventElapsedTime(&a, ph[0], ph[1]);
     cudaEventElapsedTime(&b, ph[1], ph[2]);
-    r.bulk_ms = tensor ? a : b;
-    r.polish_ms = tensor ? b : 0;
+    r.bulk_ms = a;
+    r.polish_ms = b;
   }
   for (auto &e : ph) cudaEventDestroy(e);
   r.iterations = bulk;
@@ -319,7 +321,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     uint8_t *st64 = call.alloc<uint8_t>(k64);
     SYM_CUDA(cudaMemsetAsync(st64, 0, k64, st));
     init_means(call, vs, seed_rank, k64, m64);
-    shift(call, vs, m64, st64, k64, h2, 1000, nullptr, nullptr);
+    shift(call, vs, m64, st64, k64, h2, fo.max_iterations, false, nullptr, nullptr);
+    shift(call, vs, m64, st64, k64, h2, fo.polish_iterations, true, nullptr, nullptr);
     std::vector<double> hm(k64 * 8);
     std::vector<uint8_t> hs64(k64);
     call.d2h(hm.data(), m64, k64 * 8 * 8);
@@ -328,7 +331,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     double emax = 0, esum = 0;
     uint64_t compared = 0, within = 0;
     for (uint64_t i = 0; i < k64; ++i) {
-      if (hs64[i] != 1 || state[i] != 1) continue;  // a mode exists in both runs
+      if (hs64[i] != kConverged || state[i] != kConverged) continue;  // a well-defined mode in both
       double num = 0, den = 0;
       for (int d = 0; d < 6; ++d) {
         double e = double(means[i * 8 + d]) - hm[i * 8 + d];
@@ -353,7 +356,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   std::multimap<double, uint64_t> by_x;
   const double half = 0.5 * std::sqrt(h2) * (1 + 1e-12);
   for (uint64_t i = 0; i < k; ++i) {
-    if (state[i] == 2) continue;  // exhausted
+    if (state[i] == kExhausted) continue;
     double x0 = means[i * 8];
     int64_t hit = -1;
     for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
@@ -572,21 +575,22 @@ sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q, con
     if (precision == SYM_MS_FP64) {
       double *m = call.alloc<double>(k * 8);
       sym::init_means(call, vs, rank, k, m);
-      iterations_out[0] = sym::shift(call, vs, m, state, k, h2, max_iterations, nullptr, nullptr);
+      iterations_out[0] =
+          sym::shift(call, vs, m, state, k, h2, max_iterations, false, nullptr, nullptr);
+      iterations_out[1] =
+          sym::shift(call, vs, m, state, k, h2, polish_iterations, true, nullptr, nullptr);
       call.d2h(out.data(), m, k * 8 * 8);
     } else {
       float *m = call.alloc<float>(k * 8);
       sym::init_means(call, vs, rank, k, m);
       int bulk = 0;
       double ev = 0;
-      if (precision == SYM_MS_BF16_REFINED &&
-          sym::meanshift_bf16_bulk(call, vs, m, state, k, h2, max_iterations, &bulk, &ev)) {
-        SYM_CUDA(cudaMemsetAsync(state, 0, k, st));
-        iterations_out[1] = sym::shift(call, vs, m, state, k, h2, polish_iterations, nullptr, nullptr);
-      } else {
-        bulk = sym::shift(call, vs, m, state, k, h2, max_iterations, nullptr, nullptr);
-      }
+      if (!(precision == SYM_MS_BF16_REFINED &&
+            sym::meanshift_bf16_bulk(call, vs, m, state, k, h2, max_iterations, &bulk, &ev)))
+        bulk = sym::shift(call, vs, m, state, k, h2, max_iterations, false, nullptr, nullptr);
       iterations_out[0] = bulk;
+      iterations_out[1] =
+          sym::shift(call, vs, m, state, k, h2, polish_iterations, true, nullptr, nullptr);
       std::vector<float> mf(k * 8);
       call.d2h(mf.data(), m, k * 8 * 4);
       call.sync();

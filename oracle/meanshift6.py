@@ -1,20 +1,80 @@
 """ORACLE - test infrastructure only.  FP64 restatement of the K-seed
 mean-shift of the throughput extension (no reference counterpart; parity
-unpinned): Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2, and the
-reference's stopping rules (src/cpu/clustering.cpp:169-181): a seed is
-exhausted when its total weight is <= 1e-14 and converged when its squared
-movement is below 1e-6 h^2."""
+unpinned).
+
+Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2.  A seed takes plain
+mean-shift steps m(x) - x until its squared step is below 1e-4 h^2, then
+safeguarded Newton steps on m(x) = x:
+    (I - J) s = m(x) - x,   J = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T)
+with d = v - x over the votes within the bandwidth.  A Newton step is taken
+when the 6x6 system is regular (pivots above 1e-12), |s| <= h/4 and
+s.(m - x) > 0 (or the step already meets the convergence test); otherwise the density is flat along some direction (a ridge,
+no well-defined mode position): the plain step is taken and the seed stops
+(settled).  Stopping rules: exhausted when the total weight is <= 1e-14 (the
+reference's rule, src/cpu/clustering.cpp:169-181), converged when a Newton
+step's square is below 1e-8 h^2.  States: 0 approaching, 1 converged,
+2 exhausted, 3 near a mode, 4 settled.
+"""
 import numpy as np
 
+MOVING, CONVERGED, EXHAUSTED, NEAR, SETTLED = 0, 1, 2, 3, 4
+SWITCH2, NEWTON_STOP2, TRUST = 1e-4, 1e-8, 0.25
 
-def meanshift6(votes, seeds, bandwidth, max_iterations=100, block=64):
+
+def solve6(M, b, tiny=1e-12):
+    """b <- M^-1 b by Gaussian elimination with partial pivoting (the order
+    of the device solver); None when a pivot is below `tiny`."""
+    M = np.array(M, np.float64)
+    b = np.array(b, np.float64)
+    for c in range(6):
+        piv = c + int(np.argmax(np.abs(M[c:, c])))
+        if not abs(M[piv, c]) > tiny:
+            return None
+        if piv != c:
+            M[[c, piv]] = M[[piv, c]]
+            b[[c, piv]] = b[[piv, c]]
+        for r in range(c + 1, 6):
+            f = M[r, c] / M[c, c]
+            M[r, c:] -= f * M[c, c:]
+            b[r] -= f * b[c]
+    for c in range(5, -1, -1):
+        b[c] = (b[c] - M[c, c + 1:] @ b[c + 1:]) / M[c, c]
+    return b
+
+
+def newton_seed(x, m, w, tot, delta, move, h2):
+    """The kNear step of one seed from its weights w over all votes x."""
+    inside = w > 0
+    di = x[inside] - m
+    sd = di.sum(0)
+    g = 2.0 / (h2 * tot)
+    M = np.eye(6) - g * (di.T @ di - np.outer(delta, sd))
+    s = solve6(M, delta)
+    if (s is not None and np.all(np.isfinite(s)) and s @ s <= TRUST * TRUST * h2
+            and (s @ delta > 0 or s @ s < NEWTON_STOP2 * h2)):
+        return m + s, CONVERGED if s @ s < NEWTON_STOP2 * h2 else NEAR
+    return m + delta, SETTLED
+
+
+def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=100, block=64):
+    """Approach phase (at most max_iterations; kMoving seeds only, a seed
+    leaves once it is near a mode), then the polish phase (at most
+    polish_iterations; kMoving and kNear seeds).  Returns the means, the
+    states and the (approach, polish) iteration counts."""
     x = np.ascontiguousarray(votes, np.float64).reshape(-1, 6)
     means = x[np.asarray(seeds, np.int64)].copy()
     state = np.zeros(len(means), np.uint8)
     h2 = bandwidth * bandwidth
+    counts = []
+    for phase, budget in ((False, max_iterations), (True, polish_iterations)):
+        counts.append(_phase(x, means, state, h2, budget, phase, block))
+    return means, state, tuple(counts)
+
+
+def _phase(x, means, state, h2, budget, polish, block):
     iterations = 0
-    for _ in range(max_iterations):
-        act = np.flatnonzero(state == 0)
+    for _ in range(budget):
+        act = np.flatnonzero((state == MOVING) | ((state == NEAR) & polish))
         if act.size == 0:
             break
         iterations += 1
@@ -24,14 +84,19 @@ def meanshift6(votes, seeds, bandwidth, max_iterations=100, block=64):
             d2 = ((x[None, :, :] - m[:, None, :]) ** 2).sum(-1)
             w = np.where(d2 < h2, 1 - d2 / h2, 0.0)
             tot = w.sum(1)
-            exhausted = tot <= 1e-14
-            nxt = (w @ x) / np.where(exhausted, 1, tot)[:, None]
-            move = ((m - nxt) ** 2).sum(1)
-            upd = ~exhausted
-            means[ids[upd]] = nxt[upd]
-            state[ids[exhausted]] = 2
-            state[ids[upd & (move < 1e-6 * h2)]] = 1
-    return means, state, iterations
+            safe = np.where(tot <= 1e-14, 1.0, tot)
+            delta = (w @ x) / safe[:, None] - m
+            move = (delta * delta).sum(1)
+            for j, i in enumerate(ids):
+                if tot[j] <= 1e-14:
+                    state[i] = EXHAUSTED
+                elif state[i] == MOVING:
+                    means[i] = m[j] + delta[j]
+                    if move[j] < SWITCH2 * h2:
+                        state[i] = NEAR
+                else:
+                    means[i], state[i] = newton_seed(x, m[j], w[j], tot[j], delta[j], move[j], h2)
+    return iterations
 
 
 def clustered_votes(clusters=6, per_cluster=3000, noise=30000, sigma=0.01, seed=0):
