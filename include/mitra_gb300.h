@@ -326,6 +326,16 @@ typedef struct sym_fast_result {
   sym_cluster_record records[SYM_FAST_MAX_CLUSTERS];
   uint64_t support[SYM_FAST_MAX_CLUSTERS];
   double coverage[SYM_FAST_MAX_CLUSTERS], rms[SYM_FAST_MAX_CLUSTERS];
+  /* connected patches supporting each verified mode (forward, inverse) */
+  uint32_t patches[2 * SYM_FAST_MAX_CLUSTERS];
+  /* 1 when the mode was formed by Newton-converged seeds (a well-defined
+   * position), 0 when only by seeds that settled on a ridge or ran out of
+   * iterations */
+  uint8_t precise[SYM_FAST_MAX_CLUSTERS];
+  /* the BF16 tensor-core kernel alone: launches, summed device time (CUDA
+   * events around each launch) and the seed-vote evaluations it made */
+  uint64_t tc_launches;
+  double tc_kernel_ms, tc_evaluations;
 } sym_fast_result;
 void sym_fast_options_default(sym_fast_options *out);
 /* `sample` is a host array of vertex ids (the area-weighted sample). */

@@ -162,7 +162,11 @@ class FastResult(C.Structure):
                 ("records", ClusterRecord * FAST_MAX_CLUSTERS),
                 ("support", C.c_uint64 * FAST_MAX_CLUSTERS),
                 ("coverage", C.c_double * FAST_MAX_CLUSTERS),
-                ("rms", C.c_double * FAST_MAX_CLUSTERS)]
+                ("rms", C.c_double * FAST_MAX_CLUSTERS),
+                ("patches", C.c_uint32 * (2 * FAST_MAX_CLUSTERS)),
+                ("precise", C.c_uint8 * FAST_MAX_CLUSTERS),
+                ("tc_launches", C.c_uint64), ("tc_kernel_ms", C.c_double),
+                ("tc_evaluations", C.c_double)]
 
 
 MS_FP32, MS_BF16_REFINED, MS_FP64 = 0, 1, 2

@@ -182,6 +182,11 @@ class Gb300Backend:
         out["support"] = list(res.support)[:n]
         out["coverage"] = list(res.coverage)[:n]
         out["rms"] = list(res.rms)[:n]
+        out["patches"] = [(res.patches[2 * i], res.patches[2 * i + 1]) for i in range(n)]
+        out["precise"] = [bool(res.precise[i]) for i in range(n)]
+        out["tc_launches"] = int(res.tc_launches)
+        out["tc_kernel_ms"] = float(res.tc_kernel_ms)
+        out["tc_evaluations"] = float(res.tc_evaluations)
         out["rotation"] = [list(res.records[i].rotation) for i in range(n)]
         out["translation"] = [list(res.records[i].translation) for i in range(n)]
         return out

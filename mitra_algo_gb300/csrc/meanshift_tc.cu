@@ -824,9 +824,12 @@ unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const ui
 
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
                          double h2, int max_iter, int *iterations, double *evaluations,
-                         uint32_t *trace, int trace_len) {
+                         uint32_t *trace, int trace_len, double *kernel_ms,
+                         uint64_t *kernel_launches) {
   *iterations = 0;
   *evaluations = 0;
+  if (kernel_ms) *kernel_ms = 0;
+  if (kernel_launches) *kernel_launches = 0;
   if (!k || !v.q) return false;
   const uint64_t max_tiles = (k + kChunk - 1) / kChunk;
   if (max_tiles * v.nchunks >= (uint64_t(1) << 31)) return false;  // list entries are int32
@@ -853,6 +856,14 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
   float gap = float(std::sqrt(h2)) + 1e-6f;
   call.launched();
+  // CUDA events around every launch of the tensor kernel (its own time)
+  std::vector<cudaEvent_t> marks;
+  auto mark_event = [&]() {
+    cudaEvent_t e;
+    SYM_CUDA(cudaEventCreate(&e));
+    SYM_CUDA(cudaEventRecord(e, st));
+    marks.push_back(e);
+  };
   int it = 0;
   for (; it < max_iter; ++it) {
     unsigned n = active_seeds(call, v, means, state, k, ids);
@@ -874,8 +885,10 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     check_launch();
     TcArgs args{images, v.nchunks, list, offsets, pieces, tiles, means, ids, n, v.gbox,
                 float(1.0 / std::sqrt(h2)), partial, evals, call.status()};
+    if (kernel_ms) mark_event();
     ms_tile_tc<<<unsigned(grid), kThreadsTc, kTcSmem, st>>>(args);
     check_launch();
+    if (kernel_ms) mark_event();
     ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, pieces, ids, n, float(h2),
                                                        state);
     check_launch();
@@ -888,6 +901,13 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   call.sync();
   *iterations = it;
   *evaluations = double(ev);
+  for (size_t i = 0; i + 1 < marks.size(); i += 2) {
+    float ms = 0;
+    SYM_CUDA(cudaEventElapsedTime(&ms, marks[i], marks[i + 1]));
+    *kernel_ms += ms;
+  }
+  if (kernel_launches) *kernel_launches = marks.size() / 2;
+  for (auto e : marks) cudaEventDestroy(e);
   return true;
 }
 

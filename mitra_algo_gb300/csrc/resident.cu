@@ -19,6 +19,7 @@
 #include "primitives.cuh"
 #include "meanshift_fast.cuh"
 #include "rng.hpp"
+#include "verification.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -34,17 +35,15 @@ void prune_device(Call &, const int32_t *, uint64_t, const double *, const doubl
                   const uint8_t *, double, int32_t *, uint64_t *);
 uint64_t pairing_device(Call &, const int32_t *, uint64_t, const double *, uint64_t, const double *,
                         const double *, double, double, uint64_t, int32_t **, int32_t **);
-void verification_core(Call &, const sym_mesh_view &, const double *, const int32_t *,
-                       const double *, const double *, const uint64_t *, const int32_t *,
-                       const sym_cluster_record *, uint64_t, double,
-                       std::vector<std::vector<int32_t>> &,
-                       std::vector<std::vector<std::vector<int32_t>>> &, std::vector<double> &,
-                       std::vector<double> &);
+void verification_fast(Call &, const Lbvh &, const double *, const double *, const double *,
+                       const uint64_t *, const int32_t *, const sym_cluster_record *, uint64_t,
+                       double, double *, double *, uint32_t *);
 // BF16 tensor-core bulk iterations (meanshift_tc.cu); returns false when the
 // tensor path cannot run this problem (the caller then stays in FP32).
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
                          double h2, int max_iter, int *iterations, double *evaluations,
-                         uint32_t *trace = nullptr, int trace_len = 0);
+                         uint32_t *trace = nullptr, int trace_len = 0, double *kernel_ms = nullptr,
+                         uint64_t *kernel_launches = nullptr);
 void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,
                       const uint16_t *b2, float *d_out, float *acc_out);
 }  // namespace sym
@@ -60,6 +59,7 @@ struct sym_mesh_handle {
   int32_t *faces = nullptr, *nbr = nullptr;
   uint64_t *nbr_off = nullptr;
   sym_edge *edges = nullptr;
+  sym::Lbvh lbvh;  // FP32 linear BVH of the faces (verification of the fast path)
 };
 
 namespace sym {
@@ -284,7 +284,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   // approaching
   bool tensor = fo.precision == SYM_MS_BF16_REFINED &&
                 meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals,
-                                    r.bulk_trace, 320);
+                                    r.bulk_trace, 320, &r.tc_kernel_ms, &r.tc_launches);
+  r.tc_evaluations = tc_evals;
   if (!tensor)
     bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, false, &r.seed_iterations, evals,
                  r.bulk_trace, 320);
@@ -350,44 +351,52 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   // ---- modes: greedy merge (h^2/4, first mode wins) + support
   // Greedy merge in seed order: a seed joins the earliest-created mode within
   // h/2 (squared distance < h^2/4).  Candidates come from a window of the
-  // modes sorted by their first coordinate.
+  // modes sorted by their first coordinate.  Newton-converged seeds (a mode
+  // with a well-defined position) go first and average into their mode;
+  // the other seeds then join a mode within h/2 without moving it, or start
+  // a mode of their own (averaged only with seeds of the same kind).
   std::vector<double> mode_pos;
   std::vector<uint64_t> mode_seeds;
+  std::vector<uint8_t> mode_precise;
   std::multimap<double, uint64_t> by_x;
   const double half = 0.5 * std::sqrt(h2) * (1 + 1e-12);
-  for (uint64_t i = 0; i < k; ++i) {
-    if (state[i] == kExhausted) continue;
-    double x0 = means[i * 8];
-    int64_t hit = -1;
-    for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
-      uint64_t m = it->second;
-      if (hit >= 0 && int64_t(m) > hit) continue;
-      double d2 = 0;
-      for (int d = 0; d < 6; ++d) {
-        double e = double(means[i * 8 + d]) - mode_pos[m * 6 + d];
-        d2 += e * e;
-      }
-      if (d2 < h2 / 4) hit = int64_t(m);
-    }
-    if (hit < 0) {
-      for (int d = 0; d < 6; ++d) mode_pos.push_back(means[i * 8 + d]);
-      mode_seeds.push_back(1);
-      by_x.emplace(mode_pos[(mode_seeds.size() - 1) * 6], mode_seeds.size() - 1);
-    } else {
-      double n = double(mode_seeds[hit]);
-      double old_x = mode_pos[hit * 6];
-      for (int d = 0; d < 6; ++d)
-        mode_pos[hit * 6 + d] = (n * mode_pos[hit * 6 + d] + means[i * 8 + d]) / (n + 1);
-      ++mode_seeds[hit];
-      auto range = by_x.equal_range(old_x);
-      for (auto it = range.first; it != range.second; ++it)
-        if (it->second == uint64_t(hit)) {
-          by_x.erase(it);
-          break;
+  for (int pass = 0; pass < 2; ++pass)
+    for (uint64_t i = 0; i < k; ++i) {
+      if (state[i] == kExhausted || (state[i] == kConverged) != (pass == 0)) continue;
+      double x0 = means[i * 8];
+      int64_t hit = -1;
+      for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
+        uint64_t m = it->second;
+        if (hit >= 0 && int64_t(m) > hit) continue;
+        double d2 = 0;
+        for (int d = 0; d < 6; ++d) {
+          double e = double(means[i * 8 + d]) - mode_pos[m * 6 + d];
+          d2 += e * e;
         }
-      by_x.emplace(mode_pos[hit * 6], uint64_t(hit));
+        if (d2 < h2 / 4) hit = int64_t(m);
+      }
+      if (hit < 0) {
+        for (int d = 0; d < 6; ++d) mode_pos.push_back(means[i * 8 + d]);
+        mode_seeds.push_back(1);
+        mode_precise.push_back(pass == 0);
+        by_x.emplace(mode_pos[(mode_seeds.size() - 1) * 6], mode_seeds.size() - 1);
+      } else if (bool(mode_precise[hit]) != (pass == 0)) {
+        ++mode_seeds[hit];  // a settled seed in a precise mode: counted, not averaged
+      } else {
+        double n = double(mode_seeds[hit]);
+        double old_x = mode_pos[hit * 6];
+        for (int d = 0; d < 6; ++d)
+          mode_pos[hit * 6 + d] = (n * mode_pos[hit * 6 + d] + means[i * 8 + d]) / (n + 1);
+        ++mode_seeds[hit];
+        auto range = by_x.equal_range(old_x);
+        for (auto it = range.first; it != range.second; ++it)
+          if (it->second == uint64_t(hit)) {
+            by_x.erase(it);
+            break;
+          }
+        by_x.emplace(mode_pos[hit * 6], uint64_t(hit));
+      }
     }
-  }
   uint64_t nm = mode_seeds.size();
   r.modes = nm;
   std::vector<uint64_t> support(nm, 0);
@@ -418,16 +427,13 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
       rec.translation[x] = d[3 + x] * h.model.box_size + c[x] - rc;
     }
     r.support[i] = support[rank[i]];
+    r.precise[i] = mode_precise[rank[i]];
   }
   clock.mark(8);
   // ---- (d) verification of the top modes
   if (fo.verify && nc) {
-    std::vector<std::vector<int32_t>> side;
-    std::vector<std::vector<std::vector<int32_t>>> patches;
-    std::vector<double> coverage, rms;
-    verification_core(call, h.host, h.xyz, h.faces, h.vn, h.w, h.nbr_off, h.nbr, r.records, nc,
-                      o.verify_threshold * h.model.box_size, side, patches, coverage, rms);
-    for (uint64_t i = 0; i < nc; ++i) r.coverage[i] = coverage[i], r.rms[i] = rms[i];
+    verification_fast(call, h.lbvh, h.xyz, h.vn, h.w, h.nbr_off, h.nbr, r.records, nc,
+                      o.verify_threshold * h.model.box_size, r.coverage, r.rms, r.patches);
   }
   clock.mark(9);
   call.sync();
@@ -507,6 +513,17 @@ sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_
     put(h->nbr, g->neighbors.indices, 4 * h->nbr_count);
     put(h->edges, g->edges, 24 * ne);
     SYM_CUDA(cudaStreamSynchronize(st));
+    try {
+      if (nf >= (uint64_t(1) << 30)) sym::fail(SYM_INVALID_ARGUMENT, "too many faces for the LBVH");
+      sym::Call call(ctx, "mesh_load");
+      h->lbvh = sym::lbvh_build(call, h->xyz, nv, h->faces, nf);
+      call.check_status("mesh_load");
+    } catch (...) {
+      sym::lbvh_free(h->lbvh);
+      cudaFree(h->block);
+      delete h;
+      throw;
+    }
     *out = h;
     return SYM_OK;
   } catch (const sym::Error &e) {
@@ -519,6 +536,7 @@ void sym_mesh_free(sym_mesh_handle *h) {
   if (!h) return;
   cudaSetDevice(h->ctx->device);
   cudaStreamSynchronize(h->ctx->stream);
+  sym::lbvh_free(h->lbvh);
   cudaFree(h->block);
   delete h;
 }

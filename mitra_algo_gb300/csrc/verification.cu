@@ -21,6 +21,7 @@
 //    (patches by smallest vertex, members ascending).
 #include "common.cuh"
 #include "primitives.cuh"
+#include "verification.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -268,17 +269,9 @@ __global__ void ordered_sums(const uint8_t *flags, const double *err, const doub
   side_a_size[c] = na;
 }
 
-__device__ int32_t find_root(int32_t *parent, int32_t x) {
-  for (int guard = 0; guard < (1 << 26); ++guard) {
-    int32_t p = parent[x];
-    if (p == x) return x;
-    int32_t g = parent[p];
-    if (g != p) parent[x] = g;  // path halving; parents only decrease
-    x = p;
-  }
-  return -1;
-}
+}  // namespace
 
+// Union-find over (set, vertex) rows (find_root: verification.cuh).
 // parent index space: (c * 2 + dir) * nv + i ; -1 marks excluded vertices.
 __global__ void init_parents(const uint8_t *flags, uint64_t n, int32_t *parent, uint64_t nv) {
   uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -316,6 +309,8 @@ __global__ void unite_edges(const uint64_t *nbr_off, const int32_t *nbr, uint64_
     }
   }
 }
+
+namespace {
 
 // keys for the grouping sort: (set << 32) | root, values: vertex.
 __global__ void root_keys(int32_t *parent_all, uint64_t nv, uint64_t sets, uint64_t *keys,

@@ -1,0 +1,482 @@
+// SPDX-License-Identifier: MPL-2.0
+// Stage (d) on the throughput path: verification of sym_detect_fast's top
+// modes with a linear BVH built on the GPU and FP32 closest-point queries.
+//
+// The tests are the reference's (src/cpu/verification.cpp:22-110): a vertex
+// supports a mode in one direction when its image under the mode's motion
+// lies at least 2 tau from itself, on the correct side of a reflection
+// plane, within tau of the surface, and its transformed normal is within
+// 60 degrees of the nearest face's normal; coverage is the supporting
+// vertices' weight over the total, rms the root mean square of the forward
+// distances; patches are the connected components of the supporting
+// vertices (region growing), counted here.  What differs from the exact
+// path (verification.cu): the BVH is an LBVH (Karras 2012: 30-bit Morton
+// codes of the face centroids, radix sort, longest-common-prefix splits,
+// boxes merged bottom-up), built on the device once per resident mesh; the
+// closest-point search runs in FP32 (the nearest face can differ from the
+// reference's on ties closer than FP32 resolves); the sums are fixed-order
+// block reductions instead of the reference's serial loop.
+#include "primitives.cuh"
+#include "verification.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace sym {
+namespace {
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float dotf(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 crossf(F3 a, F3 b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+__device__ float segment_d2f(F3 p, F3 a, F3 b) {
+  F3 d = b - a;
+  float l = dotf(d, d), t = 0;
+  if (l > 1e-14f) t = fminf(fmaxf(dotf(p - a, d) / l, 0.f), 1.f);
+  F3 e = p - (a + d * t);
+  return dotf(e, e);
+}
+
+// The region test of triangle_d2 (verification.cu) in FP32.
+__device__ float triangle_d2f(F3 p, F3 a, F3 b, F3 c) {
+  F3 ab = b - a, ac = c - a, ap = p - a;
+  F3 n = crossf(ab, ac);
+  if (dotf(n, n) < 1e-28f)
+    return fminf(fminf(segment_d2f(p, a, b), segment_d2f(p, a, c)), segment_d2f(p, b, c));
+  float d1 = dotf(ab, ap), d2 = dotf(ac, ap);
+  if (d1 <= 0 && d2 <= 0) return dotf(ap, ap);
+  F3 bp = p - b;
+  float d3 = dotf(ab, bp), d4 = dotf(ac, bp);
+  if (d3 >= 0 && d4 <= d3) return dotf(bp, bp);
+  float vc = d1 * d4 - d3 * d2;
+  if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+    F3 e = p - (a + ab * (d1 / (d1 - d3)));
+    return dotf(e, e);
+  }
+  F3 cp = p - c;
+  float d5 = dotf(ab, cp), d6 = dotf(ac, cp);
+  if (d6 >= 0 && d5 <= d6) return dotf(cp, cp);
+  float vb = d5 * d2 - d1 * d6;
+  if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+    F3 e = p - (a + ac * (d2 / (d2 - d6)));
+    return dotf(e, e);
+  }
+  float va = d3 * d6 - d5 * d4;
+  if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
+    F3 e = p - (b + (c - b) * ((d4 - d3) / ((d4 - d3) + (d5 - d6))));
+    return dotf(e, e);
+  }
+  float den = va + vb + vc;
+  F3 e = p - (a + ab * (vb / den) + ac * (vc / den));
+  return fmaxf(dotf(e, e), 0.f);
+}
+
+// --------------------------------------------------------------- LBVH build
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {  // 10 bits -> every third of 30
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void lbvh_vertices(const double *xyz, uint64_t nv, float *xyz32) {
+  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < 3 * nv) xyz32[i] = float(xyz[i]);
+}
+
+// key = Morton code of the face centroid (30 bits) << 32 | face: unique.
+__global__ void lbvh_keys(const float *xyz, uint64_t nv, const int32_t *faces, uint64_t nf,
+                          float3 lo, float3 inv, uint64_t *keys, int32_t *ids) {
+  uint64_t f = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  float c[3] = {0, 0, 0};
+  for (int k = 0; k < 3; ++k) {
+    int32_t v = faces[uint64_t(k) * nf + f];
+    for (int a = 0; a < 3; ++a) c[a] += xyz[uint64_t(a) * nv + v];
+  }
+  float l[3] = {lo.x, lo.y, lo.z}, s[3] = {inv.x, inv.y, inv.z};
+  uint32_t q[3];
+  for (int a = 0; a < 3; ++a) {
+    float u = (c[a] / 3.f - l[a]) * s[a];
+    q[a] = uint32_t(fminf(fmaxf(u * 1024.f, 0.f), 1023.f));
+  }
+  uint32_t code = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
+  keys[f] = (uint64_t(code) << 32) | uint64_t(uint32_t(f));
+  ids[f] = int32_t(f);
+}
+
+__device__ __forceinline__ int lcp(const uint64_t *keys, int64_t n, int64_t i, int64_t j) {
+  if (j < 0 || j >= n) return -1;
+  return __clzll(keys[i] ^ keys[j]);
+}
+
+// Internal node i of n - 1 (Karras 2012): its range, split and children;
+// child < 0 encodes the leaf ~sorted position; parent_* = 2 * parent + slot.
+__global__ void lbvh_internal(const uint64_t *keys, int64_t n, int32_t *child, int32_t *parent_in,
+                              int32_t *parent_leaf) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  const int d = lcp(keys, n, i, i + 1) > lcp(keys, n, i, i - 1) ? 1 : -1;
+  const int dmin = lcp(keys, n, i, i - d);
+  int64_t lmax = 2;
+  while (lcp(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+  int64_t l = 0;
+  for (int64_t t = lmax / 2; t >= 1; t /= 2)
+    if (lcp(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  const int64_t j = i + l * d;
+  const int dnode = lcp(keys, n, i, j);
+  int64_t s = 0, t = l;
+  do {
+    t = (t + 1) / 2;
+    if (lcp(keys, n, i, i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const int64_t gamma = i + s * d + (d < 0 ? d : 0);
+  const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+  int32_t left = lo == gamma ? ~int32_t(gamma) : int32_t(gamma);
+  int32_t right = hi == gamma + 1 ? ~int32_t(gamma + 1) : int32_t(gamma + 1);
+  child[2 * i] = left, child[2 * i + 1] = right;
+  if (left < 0) parent_leaf[gamma] = int32_t(2 * i);
+  else parent_in[gamma] = int32_t(2 * i);
+  if (right < 0) parent_leaf[gamma + 1] = int32_t(2 * i + 1);
+  else parent_in[gamma + 1] = int32_t(2 * i + 1);
+}
+
+// Boxes bottom-up: every leaf writes its box into its parent's slot; the
+// second child to arrive at a node merges both slots into the node's box
+// and carries it one level up.  Leaves are renamed from sorted positions to
+// face ids on the way.
+__global__ void lbvh_boxes(const float *xyz, uint64_t nv, const int32_t *faces, int64_t n,
+                           const int32_t *sorted_ids, int32_t *child, const int32_t *parent_in,
+                           const int32_t *parent_leaf, float *box, unsigned *arrivals) {
+  int64_t leaf = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (leaf >= n) return;
+  const int32_t f = sorted_ids[leaf];
+  float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+  for (int k = 0; k < 3; ++k) {
+    int32_t v = faces[uint64_t(k) * uint64_t(n) + f];
+    for (int a = 0; a < 3; ++a) {
+      float x = xyz[uint64_t(a) * nv + v];
+      b[a] = fminf(b[a], x), b[3 + a] = fmaxf(b[3 + a], x);
+    }
+  }
+  int32_t node = parent_leaf[leaf] >> 1;
+  int slot = parent_leaf[leaf] & 1;
+  child[2 * node + slot] = ~f;  // leaves now name faces
+  for (int guard = 0; guard < 128; ++guard) {
+    volatile float *dst = box + int64_t(node) * 12 + slot * 6;
+    for (int k = 0; k < 6; ++k) dst[k] = b[k];
+    __threadfence();
+    if (atomicAdd(&arrivals[node], 1u) == 0) return;  // the sibling finishes the node
+    __threadfence();
+    volatile const float *src = box + int64_t(node) * 12;
+    for (int a = 0; a < 3; ++a) {
+      b[a] = fminf(src[a], src[6 + a]);
+      b[3 + a] = fmaxf(src[3 + a], src[9 + a]);
+    }
+    if (node == 0) return;
+    slot = parent_in[node] & 1;
+    node = parent_in[node] >> 1;
+  }
+}
+
+// ------------------------------------------------------------ verification
+struct Motion32 {
+  double r[9], t[3], n[3], offset;
+  int32_t reflection;
+};
+
+constexpr int kStackFast = 96;
+
+__device__ __forceinline__ float box_d2f(F3 p, const float *b) {
+  float dx = fmaxf(fmaxf(b[0] - p.x, p.x - b[3]), 0.f);
+  float dy = fmaxf(fmaxf(b[1] - p.y, p.y - b[4]), 0.f);
+  float dz = fmaxf(fmaxf(b[2] - p.z, p.z - b[5]), 0.f);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+struct BvhView {
+  uint64_t nv, nf;
+  const int32_t *faces;
+  const float *xyz;
+  const int32_t *child;
+  const float *box;
+};
+
+__device__ __forceinline__ F3 vtx(const BvhView &b, int32_t v) {
+  return {b.xyz[v], b.xyz[b.nv + v], b.xyz[2 * b.nv + v]};
+}
+__device__ __forceinline__ float face_d2(const BvhView &b, F3 p, int32_t f) {
+  return triangle_d2f(p, vtx(b, b.faces[f]), vtx(b, b.faces[b.nf + f]), vtx(b, b.faces[2 * b.nf + f]));
+}
+
+// Nearest face within `best` (FP32), near-first; -1 when none.
+__device__ int32_t nearest_face_fast(const BvhView &b, F3 p, float &best, int *status) {
+  int32_t face = -1;
+  if (b.nf == 1) {
+    float d = face_d2(b, p, 0);
+    if (d < best) best = d, face = 0;
+    return face;
+  }
+  int32_t stack[kStackFast];
+  float dist[kStackFast];
+  int top = 0;
+  stack[top] = 0, dist[top++] = 0.f;
+  while (top) {
+    --top;
+    if (dist[top] >= best) continue;
+    const int32_t node = stack[top];
+    const float *bx = b.box + int64_t(node) * 12;
+    const int32_t c0 = b.child[2 * node], c1 = b.child[2 * node + 1];
+    float d0 = box_d2f(p, bx), d1 = box_d2f(p, bx + 6);
+    if (c0 < 0 && d0 < best) {
+      float d = face_d2(b, p, ~c0);
+      if (d < best) best = d, face = ~c0;
+    }
+    if (c1 < 0 && d1 < best) {
+      float d = face_d2(b, p, ~c1);
+      if (d < best) best = d, face = ~c1;
+    }
+    const bool p0 = c0 >= 0 && d0 < best, p1 = c1 >= 0 && d1 < best;
+    if (top + 2 > kStackFast) {
+      atomicExch(status, DS_CAPACITY);
+      return face;
+    }
+    if (p0 && p1) {  // the nearer child is popped first
+      bool first0 = d0 <= d1;
+      stack[top] = first0 ? c1 : c0, dist[top++] = first0 ? d1 : d0;
+      stack[top] = first0 ? c0 : c1, dist[top++] = first0 ? d0 : d1;
+    } else if (p0) {
+      stack[top] = c0, dist[top++] = d0;
+    } else if (p1) {
+      stack[top] = c1, dist[top++] = d1;
+    }
+  }
+  return face;
+}
+
+// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction); the
+// motion is applied in FP64, the search runs in FP32.
+__global__ void verify_vertices_fast(BvhView b, const double *xyz, const double *vn,
+                                     const Motion32 *motions, uint64_t nc, double tau, float tau2,
+                                     uint8_t *flags, double *err, int *status) {
+  uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t nv = b.nv;
+  if (row >= nc * 2 * nv) return;
+  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  const bool inverse = rem >= nv;
+  const uint64_t i = rem % nv;
+  flags[row] = 0;
+  if (!inverse) err[c * nv + i] = 0;
+  const Motion32 &m = motions[c];
+  double r[9];
+  for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
+  const double p[3] = {xyz[i], xyz[nv + i], xyz[2 * nv + i]};
+  double q[3], move2 = 0;
+  for (int a = 0; a < 3; ++a) {
+    double s = 0;
+    for (int k = 0; k < 3; ++k) s += r[a * 3 + k] * (inverse ? p[k] - m.t[k] : p[k]);
+    q[a] = inverse ? s : s + m.t[a];
+    move2 += (q[a] - p[a]) * (q[a] - p[a]);
+  }
+  if (move2 < 4 * tau * tau) return;
+  if (m.reflection) {
+    double side = m.n[0] * p[0] + m.n[1] * p[1] + m.n[2] * p[2] + m.offset;
+    if (inverse ? side <= tau : side >= -tau) return;
+  }
+  float best = tau2;
+  const F3 qf{float(q[0]), float(q[1]), float(q[2])};
+  const int32_t face = nearest_face_fast(b, qf, best, status);
+  if (face < 0) return;
+  const F3 a = vtx(b, b.faces[face]), bb = vtx(b, b.faces[b.nf + face]),
+           cc = vtx(b, b.faces[2 * b.nf + face]);
+  F3 fn = crossf(bb - a, cc - a);
+  float len = sqrtf(dotf(fn, fn));
+  if (!(len > 0.f)) return;
+  const double ni[3] = {vn[i], vn[nv + i], vn[2 * nv + i]};
+  float rn[3];
+  for (int k = 0; k < 3; ++k)
+    rn[k] = float(r[k * 3] * ni[0] + r[k * 3 + 1] * ni[1] + r[k * 3 + 2] * ni[2]);
+  if ((rn[0] * fn.x + rn[1] * fn.y + rn[2] * fn.z) / len < 0.5f) return;
+  flags[row] = 1;
+  if (!inverse) err[c * nv + i] = double(best);
+}
+
+// Block c < nc: sum of the forward errors, supporting weight (both
+// directions) and forward count of cluster c; block nc: the total weight.
+// Fixed-order strided partials and a fixed tree, so the result is
+// reproducible.
+__global__ void __launch_bounds__(256) block_sums(const uint8_t *flags, const double *err,
+                                                  const double *w, uint64_t nv, uint64_t nc,
+                                                  double *error, double *area, uint64_t *count,
+                                                  double *total) {
+  __shared__ double se[256], sa[256];
+  __shared__ unsigned long long sn[256];
+  const uint64_t c = blockIdx.x;
+  double e = 0, a = 0;
+  unsigned long long n = 0;
+  if (c == nc) {
+    for (uint64_t i = threadIdx.x; i < nv; i += 256) a += w[i];
+  } else {
+    const uint8_t *fa = flags + c * 2 * nv, *fb = fa + nv;
+    for (uint64_t i = threadIdx.x; i < nv; i += 256) {
+      if (fa[i]) e += err[c * nv + i], a += w[i], ++n;
+      if (fb[i]) a += w[i];
+    }
+  }
+  se[threadIdx.x] = e, sa[threadIdx.x] = a, sn[threadIdx.x] = n;
+  __syncthreads();
+  for (int s = 128; s; s >>= 1) {
+    if (int(threadIdx.x) < s) {
+      se[threadIdx.x] += se[threadIdx.x + s];
+      sa[threadIdx.x] += sa[threadIdx.x + s];
+      sn[threadIdx.x] += sn[threadIdx.x + s];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (c == nc) {
+      *total = sa[0];
+    } else {
+      error[c] = se[0], area[c] = sa[0], count[c] = sn[0];
+    }
+  }
+}
+
+// patches[set] += 1 for every component root of the set.
+__global__ void count_roots(int32_t *parent_all, uint64_t nv, uint64_t sets, unsigned *patches) {
+  uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= sets * nv) return;
+  const uint64_t set = k / nv;
+  int32_t *parent = parent_all + set * nv;
+  const int32_t i = int32_t(k % nv);
+  if (parent[i] >= 0 && find_root(parent, i) == i) atomicAdd(&patches[set], 1u);
+}
+
+}  // namespace
+
+Lbvh lbvh_build(Call &call, const double *xyz, uint64_t nv, const int32_t *faces, uint64_t nf) {
+  Lbvh b;
+  b.nv = nv, b.nf = nf, b.faces = faces;
+  if (!nf) return b;
+  cudaStream_t st = call.stream();
+  const uint64_t ni = nf - 1;
+  auto pad = [](uint64_t x) { return (x + 255) & ~uint64_t(255); };
+  const uint64_t s_xyz = pad(12 * nv), s_child = pad(8 * ni + 8), s_box = pad(48 * ni + 48);
+  SYM_CUDA(cudaMalloc(&b.block, s_xyz + s_child + s_box));
+  b.xyz = reinterpret_cast<float *>(b.block);
+  b.child = reinterpret_cast<int32_t *>(b.block + s_xyz);
+  b.box = reinterpret_cast<float *>(b.block + s_xyz + s_child);
+  lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(xyz, nv, b.xyz);
+  check_launch();
+  // the mesh box, for the Morton quantisation
+  std::vector<float> h(3 * nv);
+  SYM_CUDA(cudaMemcpyAsync(h.data(), b.xyz, 12 * nv, cudaMemcpyDeviceToHost, st));
+  call.sync();
+  float lo[3], hi[3];
+  for (int a = 0; a < 3; ++a) {
+    auto mm = std::minmax_element(h.begin() + a * nv, h.begin() + (a + 1) * nv);
+    lo[a] = *mm.first, hi[a] = *mm.second;
+  }
+  float ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-30f});
+  uint64_t *keys = call.alloc<uint64_t>(nf), *skeys = call.alloc<uint64_t>(nf);
+  int32_t *ids = call.alloc<int32_t>(nf), *sids = call.alloc<int32_t>(nf);
+  lbvh_keys<<<blocks_for(nf), kThreads, 0, st>>>(b.xyz, nv, faces, nf, make_float3(lo[0], lo[1], lo[2]),
+                                                 make_float3(1 / ext, 1 / ext, 1 / ext), keys, ids);
+  check_launch();
+  radix_sort_pairs(call, keys, ids, skeys, sids, nf, 64);
+  if (ni) {
+    int32_t *parent_in = call.alloc<int32_t>(ni), *parent_leaf = call.alloc<int32_t>(nf);
+    unsigned *arrivals = call.alloc<unsigned>(ni);
+    SYM_CUDA(cudaMemsetAsync(arrivals, 0, 4 * ni, st));
+    lbvh_internal<<<blocks_for(ni), kThreads, 0, st>>>(skeys, int64_t(nf), b.child, parent_in,
+                                                        parent_leaf);
+    check_launch();
+    lbvh_boxes<<<blocks_for(nf), kThreads, 0, st>>>(b.xyz, nv, faces, int64_t(nf), sids, b.child,
+                                                     parent_in, parent_leaf, b.box, arrivals);
+    check_launch();
+  }
+  call.launched(ni ? 6 : 4);
+  call.sync();
+  return b;
+}
+
+void lbvh_free(Lbvh &b) {
+  if (b.block) cudaFree(b.block);
+  b = Lbvh{};
+}
+
+// Coverage, rms and patch counts of the nc modes (the throughput path).
+void verification_fast(Call &call, const Lbvh &bvh, const double *xyz, const double *vn,
+                       const double *w, const uint64_t *nbr_off, const int32_t *nbr,
+                       const sym_cluster_record *records, uint64_t nc, double tau,
+                       double *coverage, double *rms, uint32_t *patches) {
+  const uint64_t nv = bvh.nv;
+  if (!nc || !nv) {
+    for (uint64_t c = 0; c < nc; ++c) coverage[c] = rms[c] = 0, patches[2 * c] = patches[2 * c + 1] = 0;
+    return;
+  }
+  cudaStream_t st = call.stream();
+  std::vector<Motion32> motions(nc);
+  for (uint64_t c = 0; c < nc; ++c) {
+    const sym_cluster_record &r = records[c];
+    for (int k = 0; k < 9; ++k) motions[c].r[k] = r.rotation[k];
+    for (int k = 0; k < 3; ++k) motions[c].t[k] = r.translation[k], motions[c].n[k] = r.plane_normal[k];
+    motions[c].offset = r.plane_offset;
+    motions[c].reflection = r.reflection != 0;
+  }
+  Motion32 *dm = call.upload(motions.data(), nc);
+  const uint64_t rows = nc * 2 * nv;
+  uint8_t *flags = call.alloc<uint8_t>(rows);
+  double *err = call.alloc<double>(nc * nv);
+  BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
+  if (bvh.nf) {
+    verify_vertices_fast<<<blocks_for(rows), kThreads, 0, st>>>(view, xyz, vn, dm, nc, tau,
+                                                                float(tau * tau), flags, err,
+                                                                call.status());
+  } else {
+    SYM_CUDA(cudaMemsetAsync(flags, 0, rows, st));
+    SYM_CUDA(cudaMemsetAsync(err, 0, nc * nv * 8, st));
+  }
+  check_launch();
+  double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
+  uint64_t *na = call.alloc<uint64_t>(nc);
+  block_sums<<<unsigned(nc + 1), 256, 0, st>>>(flags, err, w, nv, nc, error, area, na, total);
+  check_launch();
+  int32_t *parent = call.alloc<int32_t>(rows);
+  unsigned *dpatch = call.alloc<unsigned>(2 * nc);
+  SYM_CUDA(cudaMemsetAsync(dpatch, 0, 8 * nc, st));
+  init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
+  check_launch();
+  unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(nbr_off, nbr, nv, 2 * nc, parent, call.status());
+  check_launch();
+  count_roots<<<blocks_for(rows), kThreads, 0, st>>>(parent, nv, 2 * nc, dpatch);
+  check_launch();
+  call.launched(6);
+  std::vector<double> herr(nc), harea(nc);
+  std::vector<uint64_t> hna(nc);
+  std::vector<unsigned> hp(2 * nc);
+  double htotal = 0;
+  call.d2h(herr.data(), error, nc * 8);
+  call.d2h(harea.data(), area, nc * 8);
+  call.d2h(hna.data(), na, nc * 8);
+  call.d2h(&htotal, total, 8);
+  call.d2h(hp.data(), dpatch, 8 * nc);
+  call.check_status("verification");
+  for (uint64_t c = 0; c < nc; ++c) {
+    rms[c] = hna[c] ? std::sqrt(herr[c] / double(hna[c])) : 0;
+    coverage[c] = htotal > 0 ? std::min(1.0, harea[c] / htotal) : 0;
+    patches[2 * c] = hp[2 * c], patches[2 * c + 1] = hp[2 * c + 1];
+  }
+}
+
+}  // namespace sym
