@@ -126,6 +126,9 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
   constexpr int stride = COUNT ? 8 : kPartial;
   __shared__ T xs[kChunk * 8];
   __shared__ float tlo[6][4], thi[6][4];
+  // NEWTON: the 27 unweighted in-window sums of each thread's seed, in
+  // shared memory (in-window votes are rare; registers stay free)
+  __shared__ T nsum[NEWTON ? 27 * kChunk : 1];
   uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x, split = blockIdx.y;
   uint64_t slots = uint64_t(gridDim.x) * kChunk;
   bool live = slot < nactive;
@@ -152,14 +155,23 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
     hi[d] = fmaxf(fmaxf(thi[d][0], thi[d][1]), fmaxf(thi[d][2], thi[d][3]));
   }
   T acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  T sd[6] = {0, 0, 0, 0, 0, 0}, sdd[21];
-  for (int j = 0; j < 21; ++j) sdd[j] = 0;
+  if (NEWTON)
+    for (int j = 0; j < 27; ++j) nsum[j * kChunk + threadIdx.x] = T(0);
   uint64_t c0 = split * chunks_per_split;
   uint64_t c1 = c0 + chunks_per_split < nchunks ? c0 + chunks_per_split : nchunks;
   unsigned long long done = 0;
   for (uint64_t c = c0; c < c1; ++c) {
     if (box_gap2(lo, hi, cbox + c * 12) > skip_gap2) continue;
-    __syncthreads();
+    // skip the chunk unless some seed of the block lies within the bandwidth
+    // of its box (exact for Epanechnikov weights)
+    const float *cb = cbox + c * 12;
+    float g = 0;
+    for (int d = 0; d < 6; ++d) {
+      const float x = float(m[d]);
+      const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
+      g += e * e;
+    }
+    if (!__syncthreads_or(live && g <= skip_gap2)) continue;
     uint64_t v = c * kChunk + threadIdx.x;
     for (int d = 0; d < 8; ++d) xs[threadIdx.x * 8 + d] = v < q ? desc[v * 8 + d] : T(1e30);
     __syncthreads();
@@ -182,12 +194,13 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
           for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
           acc[6] += w;
           if (newton) {
-            int at = 0;
+            T *ns = nsum + threadIdx.x;
+            int at = 6;
 #pragma unroll
             for (int d = 0; d < 6; ++d) {
-              sd[d] += e[d];
+              ns[d * kChunk] += e[d];
 #pragma unroll
-              for (int l = d; l < 6; ++l) sdd[at++] += e[d] * e[l];
+              for (int l = d; l < 6; ++l, ++at) ns[at * kChunk] += e[d] * e[l];
             }
           }
         }
@@ -196,10 +209,8 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
   }
   T *out = partial + (split * slots + slot) * stride;
   for (int d = 0; d < 7; ++d) out[d] = acc[d];
-  if (newton) {
-    for (int d = 0; d < 6; ++d) out[8 + d] = sd[d];
-    for (int j = 0; j < 21; ++j) out[14 + j] = sdd[j];
-  }
+  if (newton)
+    for (int j = 0; j < 27; ++j) out[8 + j] = nsum[j * kChunk + threadIdx.x];
   if (threadIdx.x == 0 && done && evals) atomicAdd(evals, done * (unsigned long long)kChunk);
 }
 
@@ -242,10 +253,13 @@ __device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
 // d = v - x over the votes within the bandwidth.  Stopping rules: exhausted
 // when the weight is <= 1e-14 (reference, src/cpu/clustering.cpp:169-181),
 // converged when a Newton step^2 < kNewtonStop2 h^2, settled (plain step
-// taken) when the Newton step is rejected.
+// taken) when the Newton step is rejected, or when an accepted Newton step
+// is still too long at polish iteration kNewtonCap (polish_it, -1 in the
+// approach phase).
 template <typename T>
 __global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t slots,
-                          const int32_t *ids, uint64_t nactive, T h2, uint8_t *state) {
+                          const int32_t *ids, uint64_t nactive, T h2, int polish_it,
+                          uint8_t *state) {
   uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (slot >= nactive) return;
   int32_t s = ids[slot];
@@ -291,6 +305,7 @@ __global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t 
   if (ok) {
     for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + step[d];
     if (len < T(kNewtonStop2) * h2) state[s] = kConverged;
+    else if (polish_it >= kNewtonCap) state[s] = kSettled;
   } else {
     for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + delta[d];
     state[s] = kSettled;
@@ -436,7 +451,7 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
                                                        ids, n, T(h2), gap * gap, g.cps, partial, evals);
     check_launch();
     ms_update<T><<<blocks_for(n), kThreads, 0, st>>>(means, partial, g.splits, g.slots, ids, n,
-                                                     T(h2), state);
+                                                     T(h2), polish ? it : -1, state);
     check_launch();
     call.launched(2);
   }

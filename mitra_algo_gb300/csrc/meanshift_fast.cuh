@@ -25,8 +25,11 @@ constexpr int kChunk = 128;  // votes per chunk = seeds per tile
 // step (unless it already meets the convergence test) - the density is flat along some direction there (a ridge), so the
 // mode has no well-defined position: the seed takes the plain step and
 // stops (kSettled).  kExhausted: total weight <= 1e-14.
+// A kNear seed still unconverged after kNewtonCap polish iterations (Newton
+// steps that keep being accepted without shrinking) settles too.
 constexpr uint8_t kMoving = 0, kConverged = 1, kExhausted = 2, kNear = 3, kSettled = 4;
 constexpr double kSwitch2 = 1e-4, kNewtonStop2 = 1e-8, kTrust = 0.25;
+constexpr int kNewtonCap = 10;
 // Floats (or doubles) per partial sum of one seed: sum w x (6), sum w, pad,
 // then for kNear seeds the unweighted in-window sums of d = v - x: sum d
 // (6) and sum d d^T (21, upper triangle row by row), pad.

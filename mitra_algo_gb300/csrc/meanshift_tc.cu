@@ -339,14 +339,39 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, uint64_t nact
   }
 }
 
-// need[t * nchunks + c]: chunk c lies within the bandwidth of tile t's box.
-__global__ void tile_needs(const float *boxes, const float *cbox, uint64_t nchunks, float skip_gap2,
-                           uint8_t *need) {
-  uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  uint64_t t = blockIdx.y;
+// need[t * nchunks + c]: some seed of tile t lies within the bandwidth of
+// chunk c's box (the tile's box is tested first).  Exact for Epanechnikov
+// weights: every vote of a skipped chunk is farther than the bandwidth from
+// every seed of the tile.
+__global__ void __launch_bounds__(kThreads) tile_needs(const float *boxes, const float *means,
+                                                       const int32_t *ids, uint64_t nactive,
+                                                       const float *cbox, uint64_t nchunks,
+                                                       float skip_gap2, uint8_t *need) {
+  __shared__ float seed[kChunk * 6];
+  const uint64_t t = blockIdx.y;
+  for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
+    const uint64_t slot = t * kChunk + i;
+    const bool live = slot < nactive;
+    for (int d = 0; d < 6; ++d) seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
+  }
+  __syncthreads();
+  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
-  const float *tb = boxes + t * 12;
-  need[t * nchunks + c] = box_gap2_tc(tb, tb + 6, cbox + c * 12) <= skip_gap2;
+  const float *tb = boxes + t * 12, *cb = cbox + c * 12;
+  bool keep = box_gap2_tc(tb, tb + 6, cb) <= skip_gap2;
+  if (keep) {
+    keep = false;
+    for (int i = 0; i < kChunk && !keep; ++i) {
+      float g = 0;
+      for (int d = 0; d < 6; ++d) {
+        const float x = seed[i * 6 + d];
+        const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
+        g += e * e;
+      }
+      keep = g <= skip_gap2;
+    }
+  }
+  need[t * nchunks + c] = keep;
 }
 
 // offsets[t] = first list entry of tile t (entries are t * nchunks + c,
@@ -370,37 +395,41 @@ __global__ void tile_offsets(const int32_t *list, const uint64_t *count, uint64_
 }
 
 // --------------------------------------------- pipelined tensor kernel
-// Warp roles: warp 16 streams the chunk images with TMA (and does nothing
-// else); warps 0..15 form two pairs of warpgroups that take alternate
-// chunks (pair p = warp / 8 owns the chunks i with i % 2 == p).  A pair
-// issues its own MMAs from one elected thread, so the hand-offs of a chunk
-// (D read -> next MMA1, weights written -> MMA2) are pair-local named
-// barriers instead of round trips through another warp.  In a pair, warp w
-// reads TMEM lanes 32(w%4).. and D columns 64((w/4)%2)..+63.
+// Warp roles (18 warps):
+//   warps 0..15  the epilogue, two pairs of warpgroups taking alternate
+//                chunks (pair p = warp / 8 owns the chunks i with
+//                i % 2 == p); in a pair, warp w reads TMEM lanes 32(w%4)..
+//                and D columns 64((w/4)%2)..+63
+//   warp 16      TMA: streams the chunk images through the stage ring
+//   warp 17      MMA issue (one elected lane), event-driven: it polls the
+//                hand-off barriers without blocking and issues whichever
+//                MMA is ready - MMA1(j) once chunk j landed and D[j%2] was
+//                read, MMA2(i) (in chunk order) once W[i%2] was written -
+//                so neither the epilogue nor the other pair waits on MMA
+//                issue, and the tensor pipe sees one in-order stream
 //   shared memory  kStagesTc TMA buffers of one chunk image each, ATILE
 //                  (A operand of MMA1, once per tile), U
 //   TMEM columns   D[p] = 128p (MMA1 accumulators), W[p] = 256 + 64p (the
-//                  BF16 weights, A operand of MMA2), ACC[p] = 384 + 64p
-//                  (four 16-column accumulators per pair, one per K-step
-//                  q % 4 of MMA2; all eight summed once at the end)
+//                  BF16 weights, A operand of MMA2), ACC[q] = 384 + 16q for
+//                  q = 0..7 (one accumulator per K-step of MMA2, zeroed at
+//                  the start, summed once at the end)
 // mbarriers: load_full[s] (TMA bytes), stage_free[s] (MMA2 of the chunk in
-// stage s done), d_full[p] (MMA1 done), w_free[p] (MMA2 done), acc_done.
-// Pair p, chunk i: wait D[p] -> tcgen05.ld -> pair barrier -> MMA1(i+2)
-// into D[p] -> weights -> wait W[p] free -> tcgen05.st -> pair barrier ->
-// MMA2(i).  Every wait is bounded and every pair barrier also ANDs the
-// warps' wait results, so a timeout ends the whole pair at the same
-// barrier (no warp is left waiting at a barrier the others skipped).
+// stage s done), d_full[p] (MMA1 done), d_free[p] (pair p read D[p]),
+// w_full[p] (pair p wrote W[p]), w_free[p] (MMA2 done), acc_done.  Every
+// wait is bounded; on timeout a warp records the status and stops, the MMA
+// warp drains its MMAs into acc_done, the TMA warp its copies.
 constexpr int kStagesTc = 12;
-constexpr int kEpiWarps = 16, kPairWarps = 8, kThreadsTc = (kEpiWarps + 1) * 32;
+constexpr int kPairWarps = 8, kTmaWarp = 16, kMmaWarp = 17;  // warps 0..15: the two pairs
+constexpr int kThreadsTc = 18 * 32;
 constexpr uint32_t kTcStage = 0;                                     // kStagesTc x kImage
 constexpr uint32_t kTcU = (kStagesTc * kImage + 1023) / 1024 * 1024; // 128 x 8 floats
 constexpr uint32_t kTcATile = kTcU + 128 * 8 * 4;                    // 4096, K-major
-constexpr uint32_t kTcBars = kTcATile + 4096;                        // 2 kStagesTc + 5
-constexpr uint32_t kTcMisc = kTcBars + 48 * 8;
+constexpr uint32_t kTcBars = kTcATile + 4096;                        // 2 kStagesTc + 9
+constexpr uint32_t kTcMisc = kTcBars + 48 * 8;                      // TMEM address, K-step masks
 constexpr uint32_t kTcSmem = kTcMisc + 64;
 static_assert(kImage % 16 == 0, "TMA alignment");
 static_assert(kTcATile % 1024 == 0, "descriptor alignment");
-static_assert(2 * kStagesTc + 5 <= 48, "barrier slots");
+static_assert(2 * kStagesTc + 9 <= 48, "barrier slots");
 static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
 constexpr uint32_t kTcCols = 512, kTcColW = 256, kTcColAcc = 384;
 
@@ -425,19 +454,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Named barrier over the 256 threads of pair p (ids 1, 2); returns the AND
-// of every thread's `ok`.
-__device__ __forceinline__ bool pair_and(int p, bool ok) {
-  uint32_t r;
+// Non-blocking test of a barrier phase.
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
   asm volatile(
-      "{\n\t.reg .pred a, b;\n\t"
-      "setp.ne.b32 a, %1, 0;\n\t"
-      "bar.red.and.pred b, %2, 256, a;\n\t"
-      "selp.u32 %0, 1, 0, b;\n\t}"
-      : "=r"(r)
-      : "r"(uint32_t(ok)), "r"(p + 1)
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
       : "memory");
-  return r != 0;
+  return ok != 0;
 }
 
 // d = a * b + c on two FP32 lanes at once.
@@ -457,13 +484,16 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
   return r;
 }
 
-// ACC[q % 4] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for q = 0..7 (the
-// chunk's 128 votes in K-steps of 16), W in TMEM.
+// ACC[q] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for the K-steps q of
+// the chunk (16 votes each) whose bit is set in `steps`; W in TMEM.  A K-step
+// whose 16 x 128 weights are all zero adds nothing and is skipped (the
+// accumulators start at zero).
 __device__ __forceinline__ void mma2_chunk(uint32_t acc, uint32_t w_tmem, const uint8_t *b2,
-                                           bool first) {
+                                           uint32_t steps) {
   for (uint32_t q = 0; q < 8; ++q)
-    mma_bf16_ts(acc + 16 * (q % 4), w_tmem + 8 * q, smem_desc(b2 + q * 256, 128, 2048),
-                idesc_bf16(128, 16), (first && q < 4) ? 0u : 1u);
+    if (steps >> q & 1u)
+      mma_bf16_ts(acc + 16 * q, w_tmem + 8 * q, smem_desc(b2 + q * 256, 128, 2048),
+                  idesc_bf16(128, 16), 1u);
 }
 
 __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
@@ -473,8 +503,12 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   uint8_t *ATILE = smem + kTcATile;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcBars);
   uint64_t *load_full = bars, *stage_free = bars + kStagesTc;
-  uint64_t *d_full = bars + 2 * kStagesTc, *w_free = d_full + 2, *acc_done = d_full + 4;
+  uint64_t *d_full = bars + 2 * kStagesTc, *d_free = d_full + 2, *w_full = d_full + 4;
+  uint64_t *w_free = d_full + 6, *acc_done = d_full + 8;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcMisc);
+  // kmask[p * 8 + w]: bit j set when warp w of pair p wrote a nonzero weight
+  // in K-step 4 * (w / 4) + j of its rows (written before w_full[p])
+  volatile uint8_t *kmask = smem + kTcMisc + 16;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // piece -> (tile, share of the tile's list)
@@ -516,8 +550,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   }
   if (tid == 0) {
     for (int s = 0; s < kStagesTc; ++s) mbar_init(&load_full[s], 1), mbar_init(&stage_free[s], 1);
-    for (int p = 0; p < 2; ++p) mbar_init(&d_full[p], 1), mbar_init(&w_free[p], 1);
-    mbar_init(acc_done, 2);  // one commit (or arrival) per pair
+    for (int p = 0; p < 2; ++p) {
+      mbar_init(&d_full[p], 1), mbar_init(&w_free[p], 1);
+      mbar_init(&d_free[p], kPairWarps), mbar_init(&w_full[p], kPairWarps);
+    }
+    mbar_init(acc_done, 1);
     fence_mbar_init();
   }
   if (warp == 0 && n) tmem_alloc(tmem_slot, kTcCols);
@@ -527,8 +564,17 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem = n ? *tmem_slot : 0;
   auto stage_of = [&](uint32_t i) { return stage + (i % kStagesTc) * kImage; };
+  if (n && warp < 4) {  // ACC starts at zero (MMA2 always accumulates)
+    uint32_t z[32];
+    for (int j = 0; j < 32; ++j) z[j] = 0u;
+    for (int q2 = 0; q2 < 4; ++q2) tmem_st32(tmem + (uint32_t(warp * 32) << 16) + kTcColAcc + 32 * q2, z);
+    tmem_wait_st();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
 
-  if (warp == kEpiWarps) {
+  if (warp == kTmaWarp) {
     // ------------------------------------------------ TMA producer
     // chunk ids of the work list, 32 per batch, lane l holding entry
     // 32 * batch + l; the next batch is loaded one batch ahead, so no
@@ -571,33 +617,61 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
       // drain: wait (bounded) for every copy issued, so none lands after exit
       for (uint32_t c = 0; c < issued; ++c) mbar_wait(&load_full[c % kStagesTc], (c / kStagesTc) & 1);
     }
+  } else if (warp == kMmaWarp) {
+    // ------------------------------------------------ MMA issue
+    if (lane == 0 && n) {
+      uint32_t next1 = 0, next2 = 0;  // next MMA1 / MMA2 chunk
+      uint32_t idle = 0;
+      bool ok = true;
+      while (next2 < n) {
+        bool progressed = false;
+        // MMA1(j): chunk j landed and the pair read D[j % 2] for chunk j - 2
+        if (next1 < n && mbar_test(&load_full[next1 % kStagesTc], (next1 / kStagesTc) & 1) &&
+            (next1 < 2 || mbar_test(&d_free[next1 & 1], ((next1 - 2) / 2) & 1))) {
+          tc_fence_after();
+          mma_bf16(tmem + 128 * (next1 & 1), smem_desc(ATILE, 128, 256),
+                   smem_desc(stage_of(next1), 128, 256), idesc_bf16(128, 128), 0);
+          mma_commit(&d_full[next1 & 1]);
+          ++next1, progressed = true;
+        }
+        // MMA2(i): the pair wrote W[i % 2] for chunk i
+        if (next2 < next1 && mbar_test(&w_full[next2 & 1], (next2 / 2) & 1)) {
+          tc_fence_after();
+          const volatile uint8_t *km = kmask + 8 * (next2 & 1);
+          const uint32_t lo = km[0] | km[1] | km[2] | km[3], hi = km[4] | km[5] | km[6] | km[7];
+          mma2_chunk(tmem + kTcColAcc, tmem + kTcColW + 64 * (next2 & 1), stage_of(next2) + kB1Bytes,
+                     (lo & 15u) | ((hi & 15u) << 4));
+          mma_commit(&w_free[next2 & 1]);
+          mma_commit(&stage_free[next2 % kStagesTc]);
+          ++next2, progressed = true;
+        }
+        if (progressed) {
+          idle = 0;
+        } else if (++idle > (1u << 26)) {  // nothing became ready: give up
+          ok = false;
+          break;
+        }
+      }
+      if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
+      mma_commit(acc_done);  // once every MMA issued has completed
+    }
+    __syncwarp();
   } else {
     // ------------------------------------------------ pair p
     // row `row`, D columns 64h..64h+63:  w = relu(D + 1 - |u - E|^2)
     const int p = warp / kPairWarps, quad = warp & 3, h = (warp >> 2) & 1, row = quad * 32 + lane;
-    const bool leader = (warp % kPairWarps) == 0;  // issues the pair's MMAs (lane 0)
     const float *u = U + row * 8;
     const float2 one2 = make_float2(1.f, 1.f);
     const uint32_t lane_base = uint32_t(quad * 32) << 16;
     const uint32_t dcol = tmem + 128 * p + 64 * h, wcol = tmem + kTcColW + 64 * p + 32 * h;
-    // MMA1(i) into D[p], once chunk i has landed (leader warp only)
-    auto mma1 = [&](uint32_t i) {
-      bool good = warp_wait(&load_full[i % kStagesTc], (i / kStagesTc) & 1);
-      tc_fence_after();
-      if (good && lane == 0) {
-        mma_bf16(tmem + 128 * p, smem_desc(ATILE, 128, 256), smem_desc(stage_of(i), 128, 256),
-                 idesc_bf16(128, 128), 0);
-        mma_commit(&d_full[p]);
-      }
-      return good;
-    };
     bool ok = true;
-    if (leader && uint32_t(p) < n) ok = mma1(p);
-    ok = pair_and(p, ok);
-    uint32_t i = p, kth = 0;  // kth: index of chunk i among the pair's chunks
-    for (; ok && i < n; i += 2, ++kth) {
-      bool good = warp_wait(&d_full[p], kth & 1) &&
-                  warp_wait(&load_full[i % kStagesTc], (i / kStagesTc) & 1);
+    uint32_t kth = 0;  // index of chunk i among the pair's chunks
+    for (uint32_t i = p; i < n; i += 2, ++kth) {
+      if (!warp_wait(&d_full[p], kth & 1) ||
+          !warp_wait(&load_full[i % kStagesTc], (i / kStagesTc) & 1)) {
+        ok = false;
+        break;
+      }
       tc_fence_after();
       const float *E = reinterpret_cast<const float *>(stage_of(i) + kB1Bytes + kB2Bytes);
       float rowc = 1.f;
@@ -606,55 +680,50 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         rowc = fmaf(-r, r, rowc);
       }
       uint32_t w[16], w2[16];
+      uint32_t any0 = 0, any1 = 0, any2 = 0, any3 = 0;  // per K-step (16 votes)
       {
         uint32_t d0[32], d1[32];
-        if (good) {
-          tmem_ld32_async(lane_base + dcol, d0);
-          tmem_ld32_async(lane_base + dcol + 32, d1);
-          tmem_wait_ld();
-        } else {
-          for (int j = 0; j < 32; ++j) d0[j] = d1[j] = 0u;
-        }
+        tmem_ld32_async(lane_base + dcol, d0);
+        tmem_ld32_async(lane_base + dcol + 32, d1);
+        tmem_wait_ld();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&d_free[p]);  // D[p] may be overwritten
         const float2 rowc2 = make_float2(rowc, rowc);
         for (int j = 0; j < 16; ++j) {
           float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
                           one2, rowc2);
           w[j] = relu_bf16x2(t.x, t.y);
+          if (j < 8) any0 |= w[j];
+          else any1 |= w[j];
         }
         for (int j = 0; j < 16; ++j) {
           float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
                           one2, rowc2);
           w2[j] = relu_bf16x2(t.x, t.y);
+          if (j < 8) any2 |= w2[j];
+          else any3 |= w2[j];
         }
       }
-      tc_fence_before();
-      if (!(ok = pair_and(p, good))) break;  // the pair has read D[p]
-      if (leader && i + 2 < n) good = mma1(i + 2);
-      if (kth > 0) good = warp_wait(&w_free[p], (kth - 1) & 1) && good;  // MMA2(i-2) read W[p]
+      // nonzero K-steps of this warp's 32 rows x 64 votes
+      const uint32_t steps = (__any_sync(0xffffffffu, any0 != 0) ? 1u : 0u) |
+                             (__any_sync(0xffffffffu, any1 != 0) ? 2u : 0u) |
+                             (__any_sync(0xffffffffu, any2 != 0) ? 4u : 0u) |
+                             (__any_sync(0xffffffffu, any3 != 0) ? 8u : 0u);
+      if (kth > 0 && !warp_wait(&w_free[p], (kth - 1) & 1)) {  // MMA2(i-2) read W[p]
+        ok = false;
+        break;
+      }
       tc_fence_after();
-      if (good) {
-        tmem_st16(lane_base + wcol, w);
-        tmem_st16(lane_base + wcol + 16, w2);
-        tmem_wait_st();
-      }
+      tmem_st16(lane_base + wcol, w);
+      tmem_st16(lane_base + wcol + 16, w2);
+      tmem_wait_st();
       tc_fence_before();
-      if (!(ok = pair_and(p, good))) break;  // the pair has written W[p]
-      if (leader) {
-        tc_fence_after();
-        if (lane == 0) {
-          mma2_chunk(tmem + kTcColAcc + 64 * p, tmem + kTcColW + 64 * p, stage_of(i) + kB1Bytes,
-                     kth == 0);
-          mma_commit(&w_free[p]);
-          mma_commit(&stage_free[i % kStagesTc]);
-        }
-        __syncwarp();
-      }
+      if (lane == 0) kmask[8 * p + quad + 4 * h] = uint8_t(steps);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&w_full[p]);
     }
-    if (leader && lane == 0) {
-      if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
-      if (uint32_t(p) < n) mma_commit(acc_done);  // once every MMA of the pair is done
-      else mbar_arrive(acc_done);
-    }
+    if (!ok && lane == 0) atomicExch(a.status, DS_SPIN_LIMIT);
   }
   __syncthreads();
   if (warp < 4) {  // warpgroup 0 writes the tile's partial sums
@@ -663,8 +732,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
     for (int j = 0; j < 16; ++j) acc[j] = 0.f;
     if (n && warp_wait(acc_done, 0)) {
       tc_fence_after();
-      for (int q2 = 0; q2 < (n >= 2 ? 4 : 2); ++q2) {  // eight accumulators (pair 1's only if
-        float v[32];                                    // it had a chunk), two per load
+      for (int q2 = 0; q2 < 4; ++q2) {  // the eight accumulators, two per load
+        float v[32];
         tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kTcColAcc + 32 * q2, v);
         for (int j = 0; j < 16; ++j) acc[j] += v[j];
         for (int j = 0; j < 16; ++j) acc[j] += v[16 + j];
@@ -876,7 +945,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     tile_boxes<<<unsigned(tiles), kChunk, 0, st>>>(means, ids, n, boxes);
     check_launch();
     tile_needs<<<dim3(blocks_for(v.nchunks), unsigned(tiles)), kThreads, 0, st>>>(
-        boxes, v.cbox, v.nchunks, gap * gap, need);
+        boxes, means, ids, n, v.cbox, v.nchunks, gap * gap, need);
     check_launch();
     compact_indices(call, need, tiles * v.nchunks, list, count);
     tile_offsets<<<blocks_for(tiles + 1), kThreads, 0, st>>>(list, count, tiles, v.nchunks, offsets);

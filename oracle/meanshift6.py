@@ -8,17 +8,19 @@ safeguarded Newton steps on m(x) = x:
     (I - J) s = m(x) - x,   J = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T)
 with d = v - x over the votes within the bandwidth.  A Newton step is taken
 when the 6x6 system is regular (pivots above 1e-12), |s| <= h/4 and
-s.(m - x) > 0 (or the step already meets the convergence test); otherwise the density is flat along some direction (a ridge,
-no well-defined mode position): the plain step is taken and the seed stops
-(settled).  Stopping rules: exhausted when the total weight is <= 1e-14 (the
-reference's rule, src/cpu/clustering.cpp:169-181), converged when a Newton
-step's square is below 1e-8 h^2.  States: 0 approaching, 1 converged,
-2 exhausted, 3 near a mode, 4 settled.
+s.(m - x) > 0 (or the step already meets the convergence test); otherwise the
+density is flat along some direction (a ridge, no well-defined mode
+position): the plain step is taken and the seed stops (settled).  A seed
+whose accepted Newton steps have not converged after 10 polish iterations
+settles too.  Stopping rules: exhausted when the total weight is <= 1e-14
+(the reference's rule, src/cpu/clustering.cpp:169-181), converged when a
+Newton step's square is below 1e-8 h^2.  States: 0 approaching,
+1 converged, 2 exhausted, 3 near a mode, 4 settled.
 """
 import numpy as np
 
 MOVING, CONVERGED, EXHAUSTED, NEAR, SETTLED = 0, 1, 2, 3, 4
-SWITCH2, NEWTON_STOP2, TRUST = 1e-4, 1e-8, 0.25
+SWITCH2, NEWTON_STOP2, TRUST, NEWTON_CAP = 1e-4, 1e-8, 0.25, 10
 
 
 def solve6(M, b, tiny=1e-12):
@@ -42,8 +44,9 @@ def solve6(M, b, tiny=1e-12):
     return b
 
 
-def newton_seed(x, m, w, tot, delta, move, h2):
-    """The kNear step of one seed from its weights w over all votes x."""
+def newton_seed(x, m, w, tot, delta, move, h2, polish_it):
+    """The kNear step of one seed from its weights w over all votes x
+    (polish_it: the polish iteration, -1 in the approach phase)."""
     inside = w > 0
     di = x[inside] - m
     sd = di.sum(0)
@@ -52,7 +55,9 @@ def newton_seed(x, m, w, tot, delta, move, h2):
     s = solve6(M, delta)
     if (s is not None and np.all(np.isfinite(s)) and s @ s <= TRUST * TRUST * h2
             and (s @ delta > 0 or s @ s < NEWTON_STOP2 * h2)):
-        return m + s, CONVERGED if s @ s < NEWTON_STOP2 * h2 else NEAR
+        if s @ s < NEWTON_STOP2 * h2:
+            return m + s, CONVERGED
+        return m + s, SETTLED if polish_it >= NEWTON_CAP else NEAR
     return m + delta, SETTLED
 
 
@@ -73,7 +78,7 @@ def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=10
 
 def _phase(x, means, state, h2, budget, polish, block):
     iterations = 0
-    for _ in range(budget):
+    for it in range(budget):
         act = np.flatnonzero((state == MOVING) | ((state == NEAR) & polish))
         if act.size == 0:
             break
@@ -95,7 +100,8 @@ def _phase(x, means, state, h2, budget, polish, block):
                     if move[j] < SWITCH2 * h2:
                         state[i] = NEAR
                 else:
-                    means[i], state[i] = newton_seed(x, m[j], w[j], tot[j], delta[j], move[j], h2)
+                    means[i], state[i] = newton_seed(x, m[j], w[j], tot[j], delta[j], move[j], h2,
+                                                     it if polish else -1)
     return iterations
 
 
