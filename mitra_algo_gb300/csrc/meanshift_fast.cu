@@ -207,10 +207,12 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
       }
     }
   }
-  T *out = partial + (split * slots + slot) * stride;
-  for (int d = 0; d < 7; ++d) out[d] = acc[d];
+  // split-major layout: value d of slot s of split p at (p * stride + d) *
+  // slots + s, so the reduction reads consecutive seeds contiguously
+  T *out = partial + split * stride * slots + slot;
+  for (int d = 0; d < 7; ++d) out[d * slots] = acc[d];
   if (newton)
-    for (int j = 0; j < 27; ++j) out[8 + j] = nsum[j * kChunk + threadIdx.x];
+    for (int j = 0; j < 27; ++j) out[(8 + j) * slots] = nsum[j * kChunk + threadIdx.x];
   if (threadIdx.x == 0 && done && evals) atomicAdd(evals, done * (unsigned long long)kChunk);
 }
 
@@ -257,16 +259,35 @@ __device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
 // is still too long at polish iteration kNewtonCap (polish_it, -1 in the
 // approach phase).
 template <typename T>
-__global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t slots,
-                          const int32_t *ids, uint64_t nactive, T h2, int polish_it,
-                          uint8_t *state) {
-  uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (slot >= nactive) return;
-  int32_t s = ids[slot];
+__device__ __forceinline__ T warp_sum(T v) {  // fixed butterfly order: deterministic
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One warp per seed: the lanes stride over the splits, a butterfly sums
+// them, lane 0 takes the step.
+template <typename T>
+__global__ void __launch_bounds__(256) ms_update(T *means, const T *partial, uint64_t splits,
+                                                 uint64_t slots, const int32_t *ids,
+                                                 uint64_t nactive, T h2, int polish_it,
+                                                 uint8_t *state) {
+  const uint64_t slot = uint64_t(blockIdx.x) * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (slot >= nactive) return;  // whole warp
+  const int32_t s = ids[slot];
   const bool near = state[s] == kNear;
-  T acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (uint64_t p = 0; p < splits; ++p)
-    for (int d = 0; d < 7; ++d) acc[d] += partial[(p * slots + slot) * kPartial + d];
+  T acc[7] = {0, 0, 0, 0, 0, 0, 0}, ns[27];
+  for (int j = 0; j < 27; ++j) ns[j] = 0;
+  for (uint64_t p = lane; p < splits; p += 32) {
+    const T *in = partial + p * kPartial * slots + slot;
+    for (int d = 0; d < 7; ++d) acc[d] += in[d * slots];
+    if (near)
+      for (int j = 0; j < 27; ++j) ns[j] += in[(8 + j) * slots];
+  }
+  for (int d = 0; d < 7; ++d) acc[d] = warp_sum(acc[d]);
+  if (near)
+    for (int j = 0; j < 27; ++j) ns[j] = warp_sum(ns[j]);
+  if (lane != 0) return;
   if (acc[6] <= T(1e-14)) {
     state[s] = kExhausted;
     return;
@@ -282,13 +303,7 @@ __global__ void ms_update(T *means, const T *partial, uint64_t splits, uint64_t 
     if (move < T(kSwitch2) * h2) state[s] = kNear;
     return;
   }
-  T sd[6] = {0, 0, 0, 0, 0, 0}, sdd[21];
-  for (int j = 0; j < 21; ++j) sdd[j] = 0;
-  for (uint64_t p = 0; p < splits; ++p) {
-    const T *in = partial + (p * slots + slot) * kPartial;
-    for (int d = 0; d < 6; ++d) sd[d] += in[8 + d];
-    for (int j = 0; j < 21; ++j) sdd[j] += in[14 + j];
-  }
+  const T *sd = ns, *sdd = ns + 6;
   T M[6][6], step[6];
   const T g = T(2) / (h2 * acc[6]);
   for (int d = 0, at = 0; d < 6; ++d)
@@ -398,7 +413,7 @@ __global__ void sum_counts(const float *partial, uint64_t splits, uint64_t slots
   uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (slot >= n) return;
   unsigned long long c = 0;
-  for (uint64_t p = 0; p < splits; ++p) c += (unsigned long long)partial[(p * slots + slot) * 8 + 6];
+  for (uint64_t p = 0; p < splits; ++p) c += (unsigned long long)partial[(p * 8 + 6) * slots + slot];
   counts[ids[slot]] = c;
 }
 
@@ -450,8 +465,8 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
       ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state,
                                                        ids, n, T(h2), gap * gap, g.cps, partial, evals);
     check_launch();
-    ms_update<T><<<blocks_for(n), kThreads, 0, st>>>(means, partial, g.splits, g.slots, ids, n,
-                                                     T(h2), polish ? it : -1, state);
+    ms_update<T><<<unsigned((n + 7) / 8), 256, 0, st>>>(means, partial, g.splits, g.slots, ids, n,
+                                                        T(h2), polish ? it : -1, state);
     check_launch();
     call.launched(2);
   }

@@ -739,10 +739,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         for (int j = 0; j < 16; ++j) acc[j] += v[16 + j];
       }
     }
-    float *out = a.partial + (uint64_t(piece) * kChunk + row) * 8;
-    for (int d = 0; d < 6; ++d) out[d] = acc[d] + acc[8 + d];  // BF16 x + its residue
-    out[6] = acc[6];
-    out[7] = 0.f;
+    // piece-major: value d of row r of piece p at (p * 8 + d) * 128 + r
+    float *out = a.partial + uint64_t(piece) * 8 * kChunk + row;
+    for (int d = 0; d < 6; ++d) out[d * kChunk] = acc[d] + acc[8 + d];  // BF16 x + its residue
+    out[6 * kChunk] = acc[6];
   }
   if (tid == 0 && n && a.evals) atomicAdd(a.evals, uint64_t(n) * uint64_t(kChunk * kChunk));
   tc_fence_before();
@@ -862,15 +862,22 @@ __global__ void plan_pieces(const uint64_t *offsets, uint64_t tiles, uint32_t bu
 // Sum of a seed's pieces (fixed order), then the mean-shift step; a seed
 // leaves the bulk (kNear: the FP32 polish takes it on with Newton steps)
 // when its squared move falls under kSwitch2 h^2.
-__global__ void ms_update_bulk(float *means, const float *partial, const uint32_t *pieces,
-                               const int32_t *ids, uint64_t nactive, float h2, uint8_t *state) {
-  uint64_t slot = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (slot >= nactive) return;
-  int32_t s = ids[slot];
+__global__ void __launch_bounds__(256) ms_update_bulk(float *means, const float *partial,
+                                                       const uint32_t *pieces, const int32_t *ids,
+                                                       uint64_t nactive, float h2, uint8_t *state) {
+  // one warp per seed: the lanes stride over the tile's pieces, a fixed
+  // butterfly sums them, lane 0 takes the step
+  const uint64_t slot = uint64_t(blockIdx.x) * 8 + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (slot >= nactive) return;  // whole warp
+  const int32_t s = ids[slot];
   const uint64_t tile = slot / kChunk, row = slot % kChunk;
   float acc[7] = {0, 0, 0, 0, 0, 0, 0};
-  for (uint32_t p = pieces[tile]; p < pieces[tile + 1]; ++p)
-    for (int d = 0; d < 7; ++d) acc[d] += partial[(uint64_t(p) * kChunk + row) * 8 + d];
+  for (uint32_t p = pieces[tile] + lane; p < pieces[tile + 1]; p += 32)
+    for (int d = 0; d < 7; ++d) acc[d] += partial[(uint64_t(p) * 8 + d) * kChunk + row];
+  for (int d = 0; d < 7; ++d)
+    for (int o = 16; o; o >>= 1) acc[d] += __shfl_xor_sync(0xffffffffu, acc[d], o);
+  if (lane != 0) return;
   if (acc[6] <= 1e-14f) {
     state[s] = kExhausted;
     return;
@@ -958,8 +965,8 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     ms_tile_tc<<<unsigned(grid), kThreadsTc, kTcSmem, st>>>(args);
     check_launch();
     if (kernel_ms) mark_event();
-    ms_update_bulk<<<blocks_for(n), kThreads, 0, st>>>(means, partial, pieces, ids, n, float(h2),
-                                                       state);
+    ms_update_bulk<<<unsigned((n + 7) / 8), 256, 0, st>>>(means, partial, pieces, ids, n,
+                                                          float(h2), state);
     check_launch();
     call.launched(6);
     call.ctx->arena.rewind(mark);
