@@ -395,41 +395,45 @@ __global__ void tile_offsets(const int32_t *list, const uint64_t *count, uint64_
 }
 
 // --------------------------------------------- pipelined tensor kernel
-// Warp roles (18 warps):
+// Warp roles (19 warps):
 //   warps 0..15  the epilogue, two pairs of warpgroups taking alternate
 //                chunks (pair p = warp / 8 owns the chunks i with
 //                i % 2 == p); in a pair, warp w reads TMEM lanes 32(w%4)..
 //                and D columns 64((w/4)%2)..+63
 //   warp 16      TMA: streams the chunk images through the stage ring
-//   warp 17      MMA issue (one elected lane), event-driven: it polls the
-//                hand-off barriers without blocking and issues whichever
-//                MMA is ready - MMA1(j) once chunk j landed and D[j%2] was
-//                read, MMA2(i) (in chunk order) once W[i%2] was written -
-//                so neither the epilogue nor the other pair waits on MMA
-//                issue, and the tensor pipe sees one in-order stream
+//   warps 17, 18 MMA issue for pair 0 / pair 1 (one lane each),
+//                event-driven: the issuer polls its pair's hand-off
+//                barriers without blocking and issues whichever MMA is
+//                ready - MMA1(j) once chunk j landed and D[p] was read,
+//                MMA2(i) (in the pair's chunk order) once W[p] was written.
+//                A single thread issues one tcgen05.mma per ~85 cycles
+//                whatever its N, while the tensor pipe takes an N = 16 MMA
+//                every ~40 cycles from two issuers (measured on GB300), so
+//                each pair drives its own stream of MMAs
 //   shared memory  kStagesTc TMA buffers of one chunk image each, ATILE
 //                  (A operand of MMA1, once per tile), U
 //   TMEM columns   D[p] = 128p (MMA1 accumulators), W[p] = 256 + 64p (the
-//                  BF16 weights, A operand of MMA2), ACC[q] = 384 + 16q for
-//                  q = 0..7 (one accumulator per K-step of MMA2, zeroed at
-//                  the start, summed once at the end)
+//                  BF16 weights, A operand of MMA2), ACC[p][q] = 384 + 64p
+//                  + 16q for q = 0..3 (pair p's accumulators, K-step q of
+//                  MMA2 into ACC[p][q % 4]; zeroed at the start, summed in
+//                  a fixed order at the end)
 // mbarriers: load_full[s] (TMA bytes), stage_free[s] (MMA2 of the chunk in
 // stage s done), d_full[p] (MMA1 done), d_free[p] (pair p read D[p]),
-// w_full[p] (pair p wrote W[p]), w_free[p] (MMA2 done), acc_done.  Every
-// wait is bounded; on timeout a warp records the status and stops, the MMA
-// warp drains its MMAs into acc_done, the TMA warp its copies.
+// w_full[p] (pair p wrote W[p]), w_free[p] (MMA2 done), acc_done[p].  Every
+// wait is bounded; on timeout a warp records the status and stops, an MMA
+// warp drains its MMAs into acc_done[p], the TMA warp its copies.
 constexpr int kStagesTc = 12;
 constexpr int kPairWarps = 8, kTmaWarp = 16, kMmaWarp = 17;  // warps 0..15: the two pairs
-constexpr int kThreadsTc = 18 * 32;
+constexpr int kThreadsTc = 19 * 32;
 constexpr uint32_t kTcStage = 0;                                     // kStagesTc x kImage
 constexpr uint32_t kTcU = (kStagesTc * kImage + 1023) / 1024 * 1024; // 128 x 8 floats
 constexpr uint32_t kTcATile = kTcU + 128 * 8 * 4;                    // 4096, K-major
-constexpr uint32_t kTcBars = kTcATile + 4096;                        // 2 kStagesTc + 9
+constexpr uint32_t kTcBars = kTcATile + 4096;                        // 2 kStagesTc + 10
 constexpr uint32_t kTcMisc = kTcBars + 48 * 8;                      // TMEM address, K-step masks
 constexpr uint32_t kTcSmem = kTcMisc + 64;
 static_assert(kImage % 16 == 0, "TMA alignment");
 static_assert(kTcATile % 1024 == 0, "descriptor alignment");
-static_assert(2 * kStagesTc + 9 <= 48, "barrier slots");
+static_assert(2 * kStagesTc + 10 <= 48, "barrier slots");
 static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
 constexpr uint32_t kTcCols = 512, kTcColW = 256, kTcColAcc = 384;
 
@@ -484,15 +488,15 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
   return r;
 }
 
-// ACC[q] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for the K-steps q of
-// the chunk (16 votes each) whose bit is set in `steps`; W in TMEM.  A K-step
-// whose 16 x 128 weights are all zero adds nothing and is skipped (the
-// accumulators start at zero).
+// ACC[q % 4] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for the K-steps q
+// of the chunk (16 votes each) whose bit is set in `steps`; W in TMEM.  A
+// K-step whose 16 x 128 weights are all zero adds nothing and is skipped
+// (the accumulators start at zero).
 __device__ __forceinline__ void mma2_chunk(uint32_t acc, uint32_t w_tmem, const uint8_t *b2,
                                            uint32_t steps) {
   for (uint32_t q = 0; q < 8; ++q)
     if (steps >> q & 1u)
-      mma_bf16_ts(acc + 16 * q, w_tmem + 8 * q, smem_desc(b2 + q * 256, 128, 2048),
+      mma_bf16_ts(acc + 16 * (q & 3u), w_tmem + 8 * q, smem_desc(b2 + q * 256, 128, 2048),
                   idesc_bf16(128, 16), 1u);
 }
 
@@ -504,7 +508,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcBars);
   uint64_t *load_full = bars, *stage_free = bars + kStagesTc;
   uint64_t *d_full = bars + 2 * kStagesTc, *d_free = d_full + 2, *w_full = d_full + 4;
-  uint64_t *w_free = d_full + 6, *acc_done = d_full + 8;
+  uint64_t *w_free = d_full + 6, *acc_done = d_full + 8;  // acc_done[2]
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcMisc);
   // kmask[p * 8 + w]: bit j set when warp w of pair p wrote a nonzero weight
   // in K-step 4 * (w / 4) + j of its rows (written before w_full[p])
@@ -554,7 +558,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
       mbar_init(&d_full[p], 1), mbar_init(&w_free[p], 1);
       mbar_init(&d_free[p], kPairWarps), mbar_init(&w_full[p], kPairWarps);
     }
-    mbar_init(acc_done, 1);
+    mbar_init(&acc_done[0], 1), mbar_init(&acc_done[1], 1);
     fence_mbar_init();
   }
   if (warp == 0 && n) tmem_alloc(tmem_slot, kTcCols);
@@ -617,32 +621,37 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
       // drain: wait (bounded) for every copy issued, so none lands after exit
       for (uint32_t c = 0; c < issued; ++c) mbar_wait(&load_full[c % kStagesTc], (c / kStagesTc) & 1);
     }
-  } else if (warp == kMmaWarp) {
-    // ------------------------------------------------ MMA issue
+  } else if (warp >= kMmaWarp) {
+    // ------------------------------------------------ MMA issue, pair p
+    const uint32_t p = uint32_t(warp - kMmaWarp);
+    const uint32_t np = n > p ? (n - p + 1) / 2 : 0;  // chunks 2k + p of the pair
     if (lane == 0 && n) {
-      uint32_t next1 = 0, next2 = 0;  // next MMA1 / MMA2 chunk
+      uint32_t next1 = 0, next2 = 0;  // the pair's next MMA1 / MMA2 chunk (k)
       uint32_t idle = 0;
       bool ok = true;
-      while (next2 < n) {
+      const uint32_t dcol = tmem + 128 * p, wcol = tmem + kTcColW + 64 * p;
+      const uint32_t acc = tmem + kTcColAcc + 64 * p;
+      while (next2 < np) {
         bool progressed = false;
-        // MMA1(j): chunk j landed and the pair read D[j % 2] for chunk j - 2
-        if (next1 < n && mbar_test(&load_full[next1 % kStagesTc], (next1 / kStagesTc) & 1) &&
-            (next1 < 2 || mbar_test(&d_free[next1 & 1], ((next1 - 2) / 2) & 1))) {
+        // MMA1(k): chunk 2k + p landed and the pair read D[p] for chunk k - 1
+        const uint32_t i1 = 2 * next1 + p;
+        if (next1 < np && mbar_test(&load_full[i1 % kStagesTc], (i1 / kStagesTc) & 1) &&
+            (next1 < 1 || mbar_test(&d_free[p], (next1 - 1) & 1))) {
           tc_fence_after();
-          mma_bf16(tmem + 128 * (next1 & 1), smem_desc(ATILE, 128, 256),
-                   smem_desc(stage_of(next1), 128, 256), idesc_bf16(128, 128), 0);
-          mma_commit(&d_full[next1 & 1]);
+          mma_bf16(dcol, smem_desc(ATILE, 128, 256), smem_desc(stage_of(i1), 128, 256),
+                   idesc_bf16(128, 128), 0);
+          mma_commit(&d_full[p]);
           ++next1, progressed = true;
         }
-        // MMA2(i): the pair wrote W[i % 2] for chunk i
-        if (next2 < next1 && mbar_test(&w_full[next2 & 1], (next2 / 2) & 1)) {
+        // MMA2(k): the pair wrote W[p] for chunk 2k + p
+        const uint32_t i2 = 2 * next2 + p;
+        if (next2 < next1 && mbar_test(&w_full[p], next2 & 1)) {
           tc_fence_after();
-          const volatile uint8_t *km = kmask + 8 * (next2 & 1);
+          const volatile uint8_t *km = kmask + 8 * p;
           const uint32_t lo = km[0] | km[1] | km[2] | km[3], hi = km[4] | km[5] | km[6] | km[7];
-          mma2_chunk(tmem + kTcColAcc, tmem + kTcColW + 64 * (next2 & 1), stage_of(next2) + kB1Bytes,
-                     (lo & 15u) | ((hi & 15u) << 4));
-          mma_commit(&w_free[next2 & 1]);
-          mma_commit(&stage_free[next2 % kStagesTc]);
+          mma2_chunk(acc, wcol, stage_of(i2) + kB1Bytes, (lo & 15u) | ((hi & 15u) << 4));
+          mma_commit(&w_free[p]);
+          mma_commit(&stage_free[i2 % kStagesTc]);
           ++next2, progressed = true;
         }
         if (progressed) {
@@ -653,7 +662,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         }
       }
       if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
-      mma_commit(acc_done);  // once every MMA issued has completed
+      mma_commit(&acc_done[p]);  // once every MMA issued has completed
     }
     __syncwarp();
   } else {
@@ -730,9 +739,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
     const int quad = warp & 3, row = quad * 32 + lane;
     float acc[16];
     for (int j = 0; j < 16; ++j) acc[j] = 0.f;
-    if (n && warp_wait(acc_done, 0)) {
+    if (n && warp_wait(&acc_done[0], 0) && warp_wait(&acc_done[1], 0)) {
       tc_fence_after();
-      for (int q2 = 0; q2 < 4; ++q2) {  // the eight accumulators, two per load
+      for (int q2 = 0; q2 < 4; ++q2) {  // ACC[0][0..3], ACC[1][0..3], two per load
         float v[32];
         tmem_ld32(tmem + (uint32_t(quad * 32) << 16) + kTcColAcc + 32 * q2, v);
         for (int j = 0; j < 16; ++j) acc[j] += v[j];
