@@ -418,7 +418,7 @@ __global__ void tile_offsets(const int32_t *list, const uint64_t *count, uint64_
 //                  MMA2 into ACC[p][q % 4]; zeroed at the start, summed in
 //                  a fixed order at the end)
 // mbarriers: load_full[s] (TMA bytes), stage_free[s] (MMA2 of the chunk in
-// stage s done), d_full[p] (MMA1 done), d_free[p] (pair p read D[p]),
+// stage s done; arrived at by the pair once its wait for that MMA2 passed), d_full[p] (MMA1 done), d_free[p] (pair p read D[p]),
 // w_full[p] (pair p wrote W[p]), w_free[p] (MMA2 done), acc_done[p].  Every
 // wait is bounded; on timeout a warp records the status and stops, an MMA
 // warp drains its MMAs into acc_done[p], the TMA warp its copies.
@@ -488,16 +488,18 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
   return r;
 }
 
-// ACC[q % 4] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for the K-steps q
-// of the chunk (16 votes each) whose bit is set in `steps`; W in TMEM.  A
-// K-step whose 16 x 128 weights are all zero adds nothing and is skipped
-// (the accumulators start at zero).
-__device__ __forceinline__ void mma2_chunk(uint32_t acc, uint32_t w_tmem, const uint8_t *b2,
-                                           uint32_t steps) {
+// ACC[q % 4] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for the eight
+// K-steps q of the chunk (16 votes each); W in TMEM, the accumulators start
+// at zero.  Unrolled with constant descriptor offsets: the issuing thread
+// waits ~50 cycles per tcgen05.mma, and every instruction between two MMAs
+// adds to that (a branch per K-step nearly doubled the cost on GB300).
+// Skipping all-zero K-steps saves nothing once the tile's chunk list is
+// culled per seed: under 1% of the 16-vote x 128-seed blocks are zero.
+__device__ __forceinline__ void mma2_chunk(uint32_t acc, uint32_t w_tmem, const uint8_t *b2) {
+  const uint64_t b = smem_desc(b2, 128, 2048);
+#pragma unroll
   for (uint32_t q = 0; q < 8; ++q)
-    if (steps >> q & 1u)
-      mma_bf16_ts(acc + 16 * (q & 3u), w_tmem + 8 * q, smem_desc(b2 + q * 256, 128, 2048),
-                  idesc_bf16(128, 16), 1u);
+    mma_bf16_ts(acc + 16 * (q & 3u), w_tmem + 8 * q, b + 16 * q, idesc_bf16(128, 16), 1u);
 }
 
 __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
@@ -510,9 +512,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   uint64_t *d_full = bars + 2 * kStagesTc, *d_free = d_full + 2, *w_full = d_full + 4;
   uint64_t *w_free = d_full + 6, *acc_done = d_full + 8;  // acc_done[2]
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(smem + kTcMisc);
-  // kmask[p * 8 + w]: bit j set when warp w of pair p wrote a nonzero weight
-  // in K-step 4 * (w / 4) + j of its rows (written before w_full[p])
-  volatile uint8_t *kmask = smem + kTcMisc + 16;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // piece -> (tile, share of the tile's list)
@@ -647,11 +646,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         const uint32_t i2 = 2 * next2 + p;
         if (next2 < next1 && mbar_test(&w_full[p], next2 & 1)) {
           tc_fence_after();
-          const volatile uint8_t *km = kmask + 8 * p;
-          const uint32_t lo = km[0] | km[1] | km[2] | km[3], hi = km[4] | km[5] | km[6] | km[7];
-          mma2_chunk(acc, wcol, stage_of(i2) + kB1Bytes, (lo & 15u) | ((hi & 15u) << 4));
-          mma_commit(&w_free[p]);
-          mma_commit(&stage_free[i2 % kStagesTc]);
+          mma2_chunk(acc, wcol, stage_of(i2) + kB1Bytes);
+          mma_commit(&w_free[p]);  // W[p] and the chunk's stage are free again
           ++next2, progressed = true;
         }
         if (progressed) {
@@ -689,7 +685,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         rowc = fmaf(-r, r, rowc);
       }
       uint32_t w[16], w2[16];
-      uint32_t any0 = 0, any1 = 0, any2 = 0, any3 = 0;  // per K-step (16 votes)
       {
         uint32_t d0[32], d1[32];
         tmem_ld32_async(lane_base + dcol, d0);
@@ -703,32 +698,28 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
           float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
                           one2, rowc2);
           w[j] = relu_bf16x2(t.x, t.y);
-          if (j < 8) any0 |= w[j];
-          else any1 |= w[j];
         }
         for (int j = 0; j < 16; ++j) {
           float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
                           one2, rowc2);
           w2[j] = relu_bf16x2(t.x, t.y);
-          if (j < 8) any2 |= w2[j];
-          else any3 |= w2[j];
         }
       }
-      // nonzero K-steps of this warp's 32 rows x 64 votes
-      const uint32_t steps = (__any_sync(0xffffffffu, any0 != 0) ? 1u : 0u) |
-                             (__any_sync(0xffffffffu, any1 != 0) ? 2u : 0u) |
-                             (__any_sync(0xffffffffu, any2 != 0) ? 4u : 0u) |
-                             (__any_sync(0xffffffffu, any3 != 0) ? 8u : 0u);
-      if (kth > 0 && !warp_wait(&w_free[p], (kth - 1) & 1)) {  // MMA2(i-2) read W[p]
-        ok = false;
-        break;
+      if (kth > 0) {
+        if (!warp_wait(&w_free[p], (kth - 1) & 1)) {  // MMA2(i-2) read W[p]
+          ok = false;
+          break;
+        }
+        // MMA2(i-2) also finished reading chunk i-2's stage, and the pair
+        // read its centre before w_full: the TMA warp may refill it (the
+        // last two chunks of a pair are never refilled)
+        if (quad == 0 && h == 0 && lane == 0) mbar_arrive(&stage_free[(i - 2) % kStagesTc]);
       }
       tc_fence_after();
       tmem_st16(lane_base + wcol, w);
       tmem_st16(lane_base + wcol + 16, w2);
       tmem_wait_st();
       tc_fence_before();
-      if (lane == 0) kmask[8 * p + quad + 4 * h] = uint8_t(steps);
       __syncwarp();
       if (lane == 0) mbar_arrive(&w_full[p]);
     }
