@@ -332,11 +332,14 @@ constexpr int kRetile = 2048;  // seeds sorted in one block (static shared memor
 // Active seeds (kMoving, and kNear when include_near) in seed order, then
 // sorted by the Morton key of
 // their current mean (ties by seed id) when k <= kRetile.  nactive[0] = the
-// number of active seeds, nactive[1] = how many of them are kNear.
+// number of active seeds, nactive[1] = how many of them are kNear.  With
+// `iter`, an iteration that finds active seeds records their number in
+// trace[*iter] (while *iter < trace_cap) and counts itself in *iter.
 template <typename T>
 __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *state, uint64_t k,
                                                const float *box, bool include_near, int32_t *ids,
-                                               unsigned *nactive) {
+                                               unsigned *nactive, unsigned *iter = nullptr,
+                                               uint32_t *trace = nullptr, unsigned trace_cap = 0) {
   __shared__ unsigned long long keys[kRetile];
   __shared__ int32_t vals[kRetile];
   __shared__ unsigned warp_tot[32];
@@ -398,7 +401,13 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
     for (unsigned i = threadIdx.x; i < n; i += blockDim.x) ids[i] = vals[i];
   }
   __syncthreads();
-  if (threadIdx.x == 0) nactive[0] = n, nactive[1] = near_s;
+  if (threadIdx.x == 0) {
+    nactive[0] = n, nactive[1] = near_s;
+    if (iter && n) {
+      if (*iter < trace_cap) trace[*iter] = n;
+      ++*iter;
+    }
+  }
 }
 
 template <typename T>
@@ -546,6 +555,15 @@ unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const ui
   SYM_CUDA(cudaMemcpyAsync(&n, nact, sizeof(unsigned), cudaMemcpyDeviceToHost, call.stream()));
   call.sync();
   return n;
+}
+
+void active_seeds_async(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
+                        uint64_t k, int32_t *ids, unsigned *nact, unsigned *iter, uint32_t *trace,
+                        unsigned trace_cap) {
+  retile<float><<<1, 1024, 0, call.stream()>>>(means, state, k, v.gbox, false, ids, nact, iter,
+                                               trace, trace_cap);
+  check_launch();
+  call.launched();
 }
 
 void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm, double h2,

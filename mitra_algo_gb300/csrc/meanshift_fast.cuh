@@ -69,6 +69,12 @@ int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t 
 // number (synchronises).
 unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
                       uint64_t k, int32_t *ids);
+// The same list with its size left on the device (nact[0]); an iteration
+// that finds active seeds records their number in trace[*iter] (while
+// *iter < trace_cap) and increments *iter.  No synchronisation.
+void active_seeds_async(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
+                        uint64_t k, int32_t *ids, unsigned *nact, unsigned *iter, uint32_t *trace,
+                        unsigned trace_cap);
 
 // Number of votes within the bandwidth of each of `nm` points (nm x 8).
 void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm, double h2,

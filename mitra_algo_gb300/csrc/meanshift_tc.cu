@@ -312,11 +312,21 @@ __device__ __forceinline__ float box_gap2_tc(const float *lo, const float *hi, c
 }
 
 // ------------------------------------------------- work lists per tile
-// Box of each tile's active seeds (one block of kChunk threads per tile).
-__global__ void tile_boxes(const float *means, const int32_t *ids, uint64_t nactive, float *boxes) {
+// The number of active seeds n = nact[0] is read on the device by every
+// kernel of an iteration, so the host never waits for it: grids are sized
+// for all k seeds and blocks past the active tiles return at once.
+__device__ __forceinline__ uint32_t active_tiles(const unsigned *nact) {
+  return (nact[0] + kChunk - 1) / kChunk;
+}
+
+// boxes[t * 60 ..]: the box of tile t's active seeds (12 floats: lo, hi),
+// then the boxes of its four groups of 32 seeds (one block per tile).
+__global__ void tile_boxes(const float *means, const int32_t *ids, const unsigned *nact,
+                           float *boxes) {
   __shared__ float part[4][12];
-  uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
-  bool live = slot < nactive;
+  if (blockIdx.x >= active_tiles(nact)) return;
+  const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
+  const bool live = slot < nact[0];
   float lo[6], hi[6];
   for (int d = 0; d < 6; ++d) {
     float m = live ? means[uint64_t(ids[slot]) * 8 + d] : 0.f;
@@ -327,71 +337,146 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, uint64_t nact
       lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
       hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
     }
-  int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0)
     for (int d = 0; d < 6; ++d) part[warp][d] = lo[d], part[warp][6 + d] = hi[d];
   __syncthreads();
+  float *out = boxes + uint64_t(blockIdx.x) * 60;
   if (threadIdx.x < 12) {
     float v = part[0][threadIdx.x];
     for (int w = 1; w < 4; ++w)
       v = threadIdx.x < 6 ? fminf(v, part[w][threadIdx.x]) : fmaxf(v, part[w][threadIdx.x]);
-    boxes[blockIdx.x * 12 + threadIdx.x] = v;
+    out[threadIdx.x] = v;
+  } else if (threadIdx.x < 60) {
+    out[threadIdx.x] = part[(threadIdx.x - 12) / 12][(threadIdx.x - 12) % 12];
   }
 }
 
+constexpr int kListThreads = 256;  // chunks per block of the list kernels
+
 // need[t * nchunks + c]: some seed of tile t lies within the bandwidth of
-// chunk c's box (the tile's box is tested first).  Exact for Epanechnikov
-// weights: every vote of a skipped chunk is farther than the bandwidth from
-// every seed of the tile.
-__global__ void __launch_bounds__(kThreads) tile_needs(const float *boxes, const float *means,
-                                                       const int32_t *ids, uint64_t nactive,
-                                                       const float *cbox, uint64_t nchunks,
-                                                       float skip_gap2, uint8_t *need) {
+// chunk c's box (tested against the tile's box, then each group's box, then
+// the group's seeds).  Exact for Epanechnikov weights: every vote of a
+// skipped chunk is farther than the bandwidth from every seed of the tile.
+// bcount[t * gridDim.x + blockIdx.x] = the block's kept chunks.
+__global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, const float *means,
+                                                           const int32_t *ids, const unsigned *nact,
+                                                           const float *cbox, uint64_t nchunks,
+                                                           float skip_gap2, uint8_t *need,
+                                                           uint32_t *bcount) {
   __shared__ float seed[kChunk * 6];
+  __shared__ float gb[60];
   const uint64_t t = blockIdx.y;
+  if (t >= active_tiles(nact)) return;
+  const unsigned nactive = nact[0];
   for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
     const uint64_t slot = t * kChunk + i;
     const bool live = slot < nactive;
     for (int d = 0; d < 6; ++d) seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
   }
+  if (threadIdx.x < 60) gb[threadIdx.x] = boxes[t * 60 + threadIdx.x];
   __syncthreads();
   const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (c >= nchunks) return;
-  const float *tb = boxes + t * 12, *cb = cbox + c * 12;
-  bool keep = box_gap2_tc(tb, tb + 6, cb) <= skip_gap2;
-  if (keep) {
-    keep = false;
-    for (int i = 0; i < kChunk && !keep; ++i) {
-      float g = 0;
-      for (int d = 0; d < 6; ++d) {
-        const float x = seed[i * 6 + d];
-        const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
-        g += e * e;
+  bool keep = false;
+  if (c < nchunks) {
+    float cb[12];
+    for (int d = 0; d < 12; ++d) cb[d] = cbox[c * 12 + d];
+    if (box_gap2_tc(gb, gb + 6, cb) <= skip_gap2)
+      for (int g = 0; g < 4 && !keep; ++g) {
+        const float *b = gb + 12 + 12 * g;
+        if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
+        for (int i = 32 * g; i < 32 * g + 32 && !keep; ++i) {
+          float q = 0;
+          for (int d = 0; d < 6; ++d) {
+            const float x = seed[i * 6 + d];
+            const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
+            q += e * e;
+          }
+          keep = q <= skip_gap2;
+        }
       }
-      keep = g <= skip_gap2;
-    }
+    need[t * nchunks + c] = keep;
   }
-  need[t * nchunks + c] = keep;
+  const int kept = __syncthreads_count(keep);
+  if (threadIdx.x == 0) bcount[t * gridDim.x + blockIdx.x] = uint32_t(kept);
 }
 
-// offsets[t] = first list entry of tile t (entries are t * nchunks + c,
-// ascending); offsets[tiles] = list length.
-__global__ void tile_offsets(const int32_t *list, const uint64_t *count, uint64_t tiles,
-                             uint64_t nchunks, uint64_t *offsets) {
-  uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t > tiles) return;
-  uint64_t n = *count;
-  if (t == tiles) {
-    offsets[t] = n;
-    return;
+// One block: boff = exclusive scan of the active tiles' block counts,
+// offsets[t] = first list entry of tile t (offsets[tiles] = list length),
+// and the work plan: tile t gets pieces[t+1] - pieces[t] CTAs, about
+// len_t * budget / total of them (at least one), so every CTA streams a
+// similar number of chunks; budget = sms - tiles (at least tiles), so the
+// pieces fill one wave of the GPU.
+__global__ void __launch_bounds__(1024) scan_lists(const uint32_t *bcount, const unsigned *nact,
+                                                   uint32_t nblk, uint32_t sms, uint32_t *boff,
+                                                   uint64_t *offsets, uint32_t *pieces) {
+  __shared__ uint32_t warp_sum[32];
+  __shared__ uint32_t carry_s;
+  const uint32_t tiles = active_tiles(nact), total = tiles * nblk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < total; base += blockDim.x) {
+    const uint32_t j = base + threadIdx.x;
+    const uint32_t v = j < total ? bcount[j] : 0u;
+    uint32_t x = v;  // inclusive warp scan
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < int(blockDim.x >> 5) ? warp_sum[lane] : 0u;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_sum[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const uint32_t before = carry_s + (warp ? warp_sum[warp - 1] : 0u) + x - v;
+    if (j < total) boff[j] = before;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s += warp_sum[(blockDim.x >> 5) - 1];
+    __syncthreads();
   }
-  uint64_t key = t * nchunks, lo = 0, hi = n;
-  while (lo < hi) {
-    uint64_t mid = (lo + hi) / 2;
-    if (uint64_t(list[mid]) < key) lo = mid + 1;
-    else hi = mid;
+  const uint32_t list_len = carry_s;
+  for (uint32_t t = threadIdx.x; t <= tiles; t += blockDim.x)
+    offsets[t] = t < tiles ? boff[t * nblk] : list_len;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const uint32_t budget = tiles < sms ? sms - tiles : tiles;
+    uint32_t at = 0;
+    for (uint32_t t = 0; t < tiles; ++t) {
+      pieces[t] = at;
+      const uint64_t len = offsets[t + 1] - offsets[t];
+      const uint64_t want = list_len ? (len * budget + list_len - 1) / list_len : 1;
+      at += uint32_t(want ? want : 1);
+    }
+    pieces[tiles] = at;
   }
-  offsets[t] = lo;
+}
+
+// list[boff[..] + r] = t * nchunks + c for the r-th kept chunk c of the block
+// (ascending c), same grid as tile_count.
+__global__ void __launch_bounds__(kListThreads) scatter_lists(const uint8_t *need,
+                                                              const uint32_t *boff,
+                                                              const unsigned *nact,
+                                                              uint64_t nchunks, int32_t *list) {
+  __shared__ uint32_t warp_cnt[kListThreads / 32];
+  const uint64_t t = blockIdx.y;
+  if (t >= active_tiles(nact)) return;
+  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const bool keep = c < nchunks && need[t * nchunks + c];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+  if (lane == 0) warp_cnt[warp] = __popc(bal);
+  __syncthreads();
+  uint32_t before = boff[t * gridDim.x + blockIdx.x];
+  for (int w = 0; w < warp; ++w) before += warp_cnt[w];
+  before += __popc(bal & ((1u << lane) - 1u));
+  if (keep) list[before] = int32_t(t * nchunks + c);
 }
 
 // --------------------------------------------- pipelined tensor kernel
@@ -443,10 +528,9 @@ struct TcArgs {
   const int32_t *list;      // needed (tile, chunk) entries, t * nchunks + c
   const uint64_t *offsets;  // tiles + 1: first list entry of each tile
   const uint32_t *pieces;   // tiles + 1: first piece (CTA) of each tile
-  uint64_t tiles;
+  const unsigned *nact;     // nact[0] = active seeds (tiles of kChunk)
   const float *means;
   const int32_t *ids;
-  uint64_t nactive;
   const float *gbox;        // box of all votes; its centre is c_g
   float inv_h;
   float *partial;
@@ -516,8 +600,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // piece -> (tile, share of the tile's list)
   const uint32_t piece = blockIdx.x;
-  if (piece >= a.pieces[a.tiles]) return;
-  uint64_t lo_t = 0, hi_t = a.tiles;  // last tile whose first piece is <= piece
+  const uint32_t ntiles = active_tiles(a.nact);
+  if (piece >= a.pieces[ntiles]) return;
+  const uint64_t nactive = a.nact[0];
+  uint64_t lo_t = 0, hi_t = ntiles;  // last tile whose first piece is <= piece
   while (hi_t - lo_t > 1) {
     uint64_t mid = (lo_t + hi_t) / 2;
     if (a.pieces[mid] <= piece) lo_t = mid;
@@ -534,7 +620,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
   // and ATILE rows [2u_hi, 1, 1 | 2u_lo, 1, 1] in shared memory
   if (tid < kChunk) {
     uint64_t slot = tile * kChunk + tid;
-    bool live = slot < a.nactive;
+    bool live = slot < nactive;
     int32_t sd = live ? a.ids[slot] : 0;
     __align__(16) __nv_bfloat16 k0[8], k1[8];
     const __nv_bfloat16 one = __float2bfloat16_rn(1.f);
@@ -842,34 +928,18 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-// Work plan of one bulk iteration: tile t gets pieces[t+1] - pieces[t] CTAs,
-// about len_t * budget / total of them (at least one), so every CTA streams
-// a similar number of chunks; the pieces add up to at most budget + tiles.
-__global__ void plan_pieces(const uint64_t *offsets, uint64_t tiles, uint32_t budget,
-                            uint32_t *pieces) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const uint64_t total = offsets[tiles] - offsets[0];
-  uint32_t at = 0;
-  for (uint64_t t = 0; t < tiles; ++t) {
-    pieces[t] = at;
-    const uint64_t len = offsets[t + 1] - offsets[t];
-    const uint64_t want = total ? (len * budget + total - 1) / total : 1;
-    at += uint32_t(want ? want : 1);
-  }
-  pieces[tiles] = at;
-}
-
 // Sum of a seed's pieces (fixed order), then the mean-shift step; a seed
 // leaves the bulk (kNear: the FP32 polish takes it on with Newton steps)
 // when its squared move falls under kSwitch2 h^2.
 __global__ void __launch_bounds__(256) ms_update_bulk(float *means, const float *partial,
                                                        const uint32_t *pieces, const int32_t *ids,
-                                                       uint64_t nactive, float h2, uint8_t *state) {
+                                                       const unsigned *nact, float h2,
+                                                       uint8_t *state) {
   // one warp per seed: the lanes stride over the tile's pieces, a fixed
   // butterfly sums them, lane 0 takes the step
   const uint64_t slot = uint64_t(blockIdx.x) * 8 + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (slot >= nactive) return;  // whole warp
+  if (slot >= nact[0]) return;  // whole warp
   const int32_t s = ids[slot];
   const uint64_t tile = slot / kChunk, row = slot % kChunk;
   float acc[7] = {0, 0, 0, 0, 0, 0, 0};
@@ -894,10 +964,6 @@ __global__ void __launch_bounds__(256) ms_update_bulk(float *means, const float 
 
 }  // namespace
 
-// Active-seed list as in the SIMT path (meanshift_fast.cu).
-unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
-                      uint64_t k, int32_t *ids);
-
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
                          double h2, int max_iter, int *iterations, double *evaluations,
                          uint32_t *trace, int trace_len, double *kernel_ms,
@@ -920,18 +986,26 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
                                                        float(1.0 / std::sqrt(h2)), images);
   check_launch();
   int32_t *ids = call.alloc<int32_t>(k);
-  float *boxes = call.alloc<float>(max_tiles * 12);
+  float *boxes = call.alloc<float>(max_tiles * 60);
+  const uint32_t nblk = uint32_t((v.nchunks + kListThreads - 1) / kListThreads);
   uint8_t *need = call.alloc<uint8_t>(max_tiles * v.nchunks);
+  uint32_t *bcount = call.alloc<uint32_t>(max_tiles * nblk), *boff = call.alloc<uint32_t>(max_tiles * nblk);
   int32_t *list = call.alloc<int32_t>(max_tiles * v.nchunks);
-  uint64_t *count = call.alloc<uint64_t>(1), *offsets = call.alloc<uint64_t>(max_tiles + 1);
+  uint64_t *offsets = call.alloc<uint64_t>(max_tiles + 1);
   uint32_t *pieces = call.alloc<uint32_t>(max_tiles + 1);
-  const uint64_t sms = 152;  // one wave: budget + tiles CTAs on the 152 SMs
+  const uint32_t sms = 152;  // one wave: budget + tiles CTAs on the 152 SMs
   const uint64_t max_grid = std::max<uint64_t>(sms, 2 * max_tiles);
   float *partial = call.alloc<float>(max_grid * kChunk * 8);
+  unsigned *nact = call.alloc<unsigned>(2), *iter = call.alloc<unsigned>(1);
+  const unsigned trace_cap = unsigned(std::max(max_iter, 1));
+  uint32_t *trace_dev = call.alloc<uint32_t>(trace_cap);
   unsigned long long *evals = call.alloc<unsigned long long>(1);
   SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
-  float gap = float(std::sqrt(h2)) + 1e-6f;
+  SYM_CUDA(cudaMemsetAsync(iter, 0, 4, st));
+  const float gap = float(std::sqrt(h2)) + 1e-6f;
   call.launched();
+  TcArgs args{images, v.nchunks, list, offsets, pieces, nact, means, ids, v.gbox,
+              float(1.0 / std::sqrt(h2)), partial, evals, call.status()};
   // CUDA events around every launch of the tensor kernel (its own time)
   std::vector<cudaEvent_t> marks;
   auto mark_event = [&]() {
@@ -940,49 +1014,64 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     SYM_CUDA(cudaEventRecord(e, st));
     marks.push_back(e);
   };
+  // Iterations are launched back to back: each reads the active-seed count
+  // that the previous one left on the device, and one whose count is zero
+  // returns at once.  The host looks at the count every kCheck iterations.
+  constexpr int kCheck = 8;
   int it = 0;
   for (; it < max_iter; ++it) {
-    unsigned n = active_seeds(call, v, means, state, k, ids);
-    if (!n) break;
-    if (trace && it < trace_len) trace[it] = n;
-    const uint64_t tiles = (n + kChunk - 1) / kChunk;
-    const uint32_t budget = uint32_t(tiles < sms ? sms - tiles : tiles);
-    const uint64_t grid = budget + tiles;
-    auto mark = call.ctx->arena.mark();
-    tile_boxes<<<unsigned(tiles), kChunk, 0, st>>>(means, ids, n, boxes);
+    active_seeds_async(call, v, means, state, k, ids, nact, iter, trace_dev, trace_cap);
+    tile_boxes<<<unsigned(max_tiles), kChunk, 0, st>>>(means, ids, nact, boxes);
     check_launch();
-    tile_needs<<<dim3(blocks_for(v.nchunks), unsigned(tiles)), kThreads, 0, st>>>(
-        boxes, means, ids, n, v.cbox, v.nchunks, gap * gap, need);
+    tile_count<<<dim3(nblk, unsigned(max_tiles)), kListThreads, 0, st>>>(
+        boxes, means, ids, nact, v.cbox, v.nchunks, gap * gap, need, bcount);
     check_launch();
-    compact_indices(call, need, tiles * v.nchunks, list, count);
-    tile_offsets<<<blocks_for(tiles + 1), kThreads, 0, st>>>(list, count, tiles, v.nchunks, offsets);
+    scan_lists<<<1, 1024, 0, st>>>(bcount, nact, nblk, sms, boff, offsets, pieces);
     check_launch();
-    plan_pieces<<<1, 32, 0, st>>>(offsets, tiles, budget, pieces);
-    check_launch();
-    TcArgs args{images, v.nchunks, list, offsets, pieces, tiles, means, ids, n, v.gbox,
-                float(1.0 / std::sqrt(h2)), partial, evals, call.status()};
-    if (kernel_ms) mark_event();
-    ms_tile_tc<<<unsigned(grid), kThreadsTc, kTcSmem, st>>>(args);
+    scatter_lists<<<dim3(nblk, unsigned(max_tiles)), kListThreads, 0, st>>>(need, boff, nact,
+                                                                              v.nchunks, list);
     check_launch();
     if (kernel_ms) mark_event();
-    ms_update_bulk<<<unsigned((n + 7) / 8), 256, 0, st>>>(means, partial, pieces, ids, n,
+    ms_tile_tc<<<unsigned(max_grid), kThreadsTc, kTcSmem, st>>>(args);
+    check_launch();
+    if (kernel_ms) mark_event();
+    ms_update_bulk<<<unsigned((k + 7) / 8), 256, 0, st>>>(means, partial, pieces, ids, nact,
                                                           float(h2), state);
     check_launch();
     call.launched(6);
-    call.ctx->arena.rewind(mark);
+    if (it % kCheck == kCheck - 1) {
+      unsigned n = 0;
+      call.d2h(&n, nact, sizeof(unsigned));
+      call.sync();
+      if (!n) {
+        ++it;
+        break;
+      }
+    }
   }
   call.check_status("mean_shift (tensor)");
   unsigned long long ev = 0;
+  unsigned active_iterations = 0;
   call.d2h(&ev, evals, 8);
+  call.d2h(&active_iterations, iter, sizeof(unsigned));
   call.sync();
-  *iterations = it;
+  *iterations = int(active_iterations);
   *evaluations = double(ev);
-  for (size_t i = 0; i + 1 < marks.size(); i += 2) {
+  if (trace && trace_len > 0) {
+    std::vector<uint32_t> tr(trace_cap);
+    call.d2h(tr.data(), trace_dev, trace_cap * sizeof(uint32_t));
+    call.sync();
+    for (int i = 0; i < trace_len && i < int(active_iterations) && i < int(trace_cap); ++i)
+      trace[i] = tr[i];
+  }
+  // launches after the last iteration with active seeds found none and
+  // returned at once: only the active ones are timed
+  for (size_t i = 0; i + 1 < marks.size() && i / 2 < active_iterations; i += 2) {
     float ms = 0;
     SYM_CUDA(cudaEventElapsedTime(&ms, marks[i], marks[i + 1]));
     *kernel_ms += ms;
   }
-  if (kernel_launches) *kernel_launches = marks.size() / 2;
+  if (kernel_launches) *kernel_launches = std::min<uint64_t>(marks.size() / 2, active_iterations);
   for (auto e : marks) cudaEventDestroy(e);
   return true;
 }
