@@ -53,24 +53,37 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                : "memory");
 }
 
+// A waiting thread is suspended by the hardware until the phase completes
+// (or kSuspendNs pass), so waiting warps take no issue slots from the
+// working ones.
+constexpr uint32_t kSuspendNs = 20000;
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // a wait gives up after 2 s
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
       : "memory");
   return ok != 0;
 }
 
-constexpr uint32_t kSpinLimit = 1u << 24;
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
-// Bounded wait: false when the barrier phase never completed.
+// Bounded wait: false when the barrier phase did not complete in time.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  do {
     if (mbar_try_wait(bar, parity)) return true;
+  } while (global_ns() - t0 < kWaitLimitNs);
   return false;
 }
 
@@ -486,11 +499,9 @@ __global__ void __launch_bounds__(kListThreads) scatter_lists(const uint8_t *nee
 //                i % 2 == p); in a pair, warp w reads TMEM lanes 32(w%4)..
 //                and D columns 64((w/4)%2)..+63
 //   warp 16      TMA: streams the chunk images through the stage ring
-//   warps 17, 18 MMA issue for pair 0 / pair 1 (one lane each),
-//                event-driven: the issuer polls its pair's hand-off
-//                barriers without blocking and issues whichever MMA is
-//                ready - MMA1(j) once chunk j landed and D[p] was read,
-//                MMA2(i) (in the pair's chunk order) once W[p] was written.
+//   warps 17, 18 MMA issue for pair 0 / pair 1 (one lane each): MMA1 of
+//                the pair's chunk k + 1 once it landed and D[p] was read,
+//                then MMA2 of chunk k once W[p] was written.
 //                A single thread issues one tcgen05.mma per ~85 cycles
 //                whatever its N, while the tensor pipe takes an N = 16 MMA
 //                every ~40 cycles from two issuers (measured on GB300), so
@@ -542,18 +553,6 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Non-blocking test of a barrier phase.
-__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
 
 // d = a * b + c on two FP32 lanes at once.
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
@@ -711,37 +710,31 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
     const uint32_t p = uint32_t(warp - kMmaWarp);
     const uint32_t np = n > p ? (n - p + 1) / 2 : 0;  // chunks 2k + p of the pair
     if (lane == 0 && n) {
-      uint32_t next1 = 0, next2 = 0;  // the pair's next MMA1 / MMA2 chunk (k)
-      uint32_t idle = 0;
       bool ok = true;
       const uint32_t dcol = tmem + 128 * p, wcol = tmem + kTcColW + 64 * p;
       const uint32_t acc = tmem + kTcColAcc + 64 * p;
-      while (next2 < np) {
-        bool progressed = false;
-        // MMA1(k): chunk 2k + p landed and the pair read D[p] for chunk k - 1
-        const uint32_t i1 = 2 * next1 + p;
-        if (next1 < np && mbar_test(&load_full[i1 % kStagesTc], (i1 / kStagesTc) & 1) &&
-            (next1 < 1 || mbar_test(&d_free[p], (next1 - 1) & 1))) {
-          tc_fence_after();
-          mma_bf16(dcol, smem_desc(ATILE, 128, 256), smem_desc(stage_of(i1), 128, 256),
-                   idesc_bf16(128, 128), 0);
-          mma_commit(&d_full[p]);
-          ++next1, progressed = true;
-        }
-        // MMA2(k): the pair wrote W[p] for chunk 2k + p
-        const uint32_t i2 = 2 * next2 + p;
-        if (next2 < next1 && mbar_test(&w_full[p], next2 & 1)) {
-          tc_fence_after();
-          mma2_chunk(acc, wcol, stage_of(i2) + kB1Bytes);
-          mma_commit(&w_free[p]);  // W[p] and the chunk's stage are free again
-          ++next2, progressed = true;
-        }
-        if (progressed) {
-          idle = 0;
-        } else if (++idle > (1u << 26)) {  // nothing became ready: give up
-          ok = false;
-          break;
-        }
+      // MMA1 of the pair's chunk k (chunk 2k + p) once it landed and the
+      // pair read D[p] for chunk k - 1
+      auto mma1 = [&](uint32_t k) -> bool {
+        const uint32_t i = 2 * k + p;
+        if (!mbar_wait(&load_full[i % kStagesTc], (i / kStagesTc) & 1)) return false;
+        if (k > 0 && !mbar_wait(&d_free[p], (k - 1) & 1)) return false;
+        tc_fence_after();
+        mma_bf16(dcol, smem_desc(ATILE, 128, 256), smem_desc(stage_of(i), 128, 256),
+                 idesc_bf16(128, 128), 0);
+        mma_commit(&d_full[p]);
+        return true;
+      };
+      // the pair reads D for chunk k before it writes W for chunk k, so
+      // MMA1(k + 1) is always ready before MMA2(k): the issuer takes them in
+      // that order, sleeping in each wait
+      if (np) ok = mma1(0);
+      for (uint32_t k = 0; ok && k < np; ++k) {
+        if (k + 1 < np && !(ok = mma1(k + 1))) break;
+        if (!(ok = mbar_wait(&w_full[p], k & 1))) break;  // the pair wrote W[p]
+        tc_fence_after();
+        mma2_chunk(acc, wcol, stage_of(2 * k + p) + kB1Bytes);
+        mma_commit(&w_free[p]);  // W[p] and the chunk's stage are free again
       }
       if (!ok) atomicExch(a.status, DS_SPIN_LIMIT);
       mma_commit(&acc_done[p]);  // once every MMA issued has completed
