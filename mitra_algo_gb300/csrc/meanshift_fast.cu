@@ -248,7 +248,7 @@ __device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
   return true;
 }
 
-// Sum of the splits (fixed order), then one step of the seed: the
+// One step of a seed from its summed values (ms_reduce): the
 // Epanechnikov mean-shift step m - x for a kMoving seed, the safeguarded
 // Newton step (I - J)^-1 (m - x) for a kNear seed, where
 //   J = dm/dx = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T),
@@ -258,36 +258,46 @@ __device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
 // taken) when the Newton step is rejected, or when an accepted Newton step
 // is still too long at polish iteration kNewtonCap (polish_it, -1 in the
 // approach phase).
+
+// Sum of the splits of one value of a tile's seeds: block (tile, j, g) adds
+// value d = j (j < 7) or j + 1 (the Newton sums) over split group g (splits
+// g, g + kGroups, ...), one thread per seed slot, so each split's row of 128
+// values is read contiguously.  red[(g * kPartial + d) * slots + slot] = the
+// group's sum; ms_update adds the groups in order.
+constexpr int kGroups = 8;
 template <typename T>
-__device__ __forceinline__ T warp_sum(T v) {  // fixed butterfly order: deterministic
-  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+__global__ void __launch_bounds__(kChunk) ms_reduce(const T *partial, uint64_t splits, uint64_t slots,
+                                                    uint64_t nactive, T *red) {
+  const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
+  if (slot >= nactive) return;
+  const int d = blockIdx.y < 7 ? int(blockIdx.y) : int(blockIdx.y) + 1;
+  const uint64_t g = blockIdx.z;
+  const T *in = partial + uint64_t(d) * slots + slot;
+  const uint64_t step = uint64_t(kPartial) * slots;
+  T s0 = 0, s1 = 0;  // two interleaved sums, added in a fixed order
+  uint64_t p = g;
+  for (; p + kGroups < splits; p += 2 * kGroups) s0 += in[p * step], s1 += in[(p + kGroups) * step];
+  if (p < splits) s0 += in[p * step];
+  red[(g * kPartial + d) * slots + slot] = s0 + s1;
 }
 
-// One warp per seed: the lanes stride over the splits, a butterfly sums
-// them, lane 0 takes the step.
+// One thread per seed: the step from the summed values (ms_reduce).
 template <typename T>
-__global__ void __launch_bounds__(256) ms_update(T *means, const T *partial, uint64_t splits,
-                                                 uint64_t slots, const int32_t *ids,
-                                                 uint64_t nactive, T h2, int polish_it,
-                                                 uint8_t *state) {
-  const uint64_t slot = uint64_t(blockIdx.x) * 8 + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (slot >= nactive) return;  // whole warp
+__global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint64_t slots,
+                                                    const int32_t *ids, uint64_t nactive, T h2,
+                                                    int polish_it, uint8_t *state) {
+  const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
+  if (slot >= nactive) return;
   const int32_t s = ids[slot];
   const bool near = state[s] == kNear;
   T acc[7] = {0, 0, 0, 0, 0, 0, 0}, ns[27];
-  for (int j = 0; j < 27; ++j) ns[j] = 0;
-  for (uint64_t p = lane; p < splits; p += 32) {
-    const T *in = partial + p * kPartial * slots + slot;
-    for (int d = 0; d < 7; ++d) acc[d] += in[d * slots];
-    if (near)
-      for (int j = 0; j < 27; ++j) ns[j] += in[(8 + j) * slots];
-  }
-  for (int d = 0; d < 7; ++d) acc[d] = warp_sum(acc[d]);
+  for (int g = 0; g < kGroups; ++g)
+    for (int d = 0; d < 7; ++d) acc[d] += red[(uint64_t(g) * kPartial + d) * slots + slot];
   if (near)
-    for (int j = 0; j < 27; ++j) ns[j] = warp_sum(ns[j]);
-  if (lane != 0) return;
+    for (int j = 0; j < 27; ++j) {
+      ns[j] = 0;
+      for (int g = 0; g < kGroups; ++g) ns[j] += red[(uint64_t(g) * kPartial + 8 + j) * slots + slot];
+    }
   if (acc[6] <= T(1e-14)) {
     state[s] = kExhausted;
     return;
@@ -451,6 +461,7 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
   // partial capacity: splits x slots is at most ~64*152*kChunk (+ one tile)
   uint64_t cap = (64 * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
   T *partial = call.alloc<T>(cap * kPartial);
+  T *red = call.alloc<T>(uint64_t(kGroups) * kPartial * std::max<uint64_t>(k, kChunk) * 2);
   float gap = float(std::sqrt(h2)) + 1e-6f;
   int it = 0;
   for (; it < max_iter; ++it) {
@@ -474,10 +485,13 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
       ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state,
                                                        ids, n, T(h2), gap * gap, g.cps, partial, evals);
     check_launch();
-    ms_update<T><<<unsigned((n + 7) / 8), 256, 0, st>>>(means, partial, g.splits, g.slots, ids, n,
-                                                        T(h2), polish ? it : -1, state);
+    ms_reduce<T><<<dim3(unsigned(g.tiles), counts[1] ? 34u : 7u, kGroups), kChunk, 0, st>>>(
+        partial, g.splits, g.slots, n, red);
     check_launch();
-    call.launched(2);
+    ms_update<T><<<unsigned(g.tiles), kChunk, 0, st>>>(means, red, g.slots, ids, n, T(h2),
+                                                       polish ? it : -1, state);
+    check_launch();
+    call.launched(3);
   }
   return it;
 }
