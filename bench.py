@@ -51,6 +51,7 @@ POLISH = 30       # FP32 polish iterations (both forms)
 # DRAM bytes (read + write) per (seed tile, vote chunk) pair of ms_tile_tc,
 # from the ncu capture summarised in profiles/ms_tile_tc.md
 TRAFFIC_PER_CHUNK_PAIR = 8322.0
+IMAGE_BYTES = 8224.0  # one chunk image: the algorithmic bytes of a (tile, chunk) pair
 
 
 def workload(small=False):
@@ -322,6 +323,7 @@ def run_gpu(args):
     flops_per_launch = tc_evals * 64 / max(tc_launches, 1)
     achieved = flops_per_launch / (per_launch_ms * 1e-3) / 1e12 if tc_ms else 0.0
     chunk_pairs_per_launch = tc_evals / (128 * 128) / max(tc_launches, 1)
+    gbs = IMAGE_BYTES * chunk_pairs_per_launch / (per_launch_ms * 1e-3) / 1e9 if tc_ms else 0.0
     line = {
         "metric": METRIC, "value": round(meshes, 4), "unit": "meshes/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_bf16, 3),
@@ -346,17 +348,24 @@ def run_gpu(args):
                      for k in r["stage_ms"]},
         "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"kernel": "ms_tile_tc (BF16 tcgen05 mean-shift tile)", "bound": "tensor",
-                     "achieved": round(achieved, 3), "peak": pk["bf16_tflops_sustained"],
-                     "unit": "TFLOP/s", "frac": round(achieved / pk["bf16_tflops_sustained"], 5),
+        "roofline": {"kernel": "ms_tile_tc (BF16 tcgen05 mean-shift tile)", "bound": "hbm",
+                     "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(gbs / pk["hbm_gbs"], 4),
                      "traffic": round(TRAFFIC_PER_CHUNK_PAIR * chunk_pairs_per_launch),
-                     "peak_source": pk_kind + " (sustained: the kernel runs inside a long step)",
+                     "peak_source": pk_kind,
                      "launches": tc_launches, "ms_per_launch": round(per_launch_ms, 4),
                      "chunk_pairs_per_launch": round(chunk_pairs_per_launch, 1),
-                     "note": "achieved = 64 MMA FLOPs per evaluated (seed, vote) pair (MMA1 K=16 "
-                             "plus MMA2 with D padded to 16) x evaluations per launch / CUDA-event "
-                             "time per launch; traffic = DRAM bytes per (tile, chunk) pair from the "
-                             "ncu capture in profiles/ms_tile_tc.md x pairs per launch"},
+                     "tensor": {"achieved": round(achieved, 3), "unit": "TFLOP/s",
+                                "peak": pk["bf16_tflops_sustained"],
+                                "frac": round(achieved / pk["bf16_tflops_sustained"], 5)},
+                     "note": "the kernel streams one 8,224-byte chunk image per (tile of 128 "
+                             "seeds, chunk of 128 votes) pair and makes 64 MMA FLOPs per seed-vote "
+                             "evaluation: 127 FLOP/B, below the GB300 ridge (sustained BF16 / HBM "
+                             "= 255 FLOP/B), so HBM bounds it. achieved = 8,224 B x pairs per "
+                             "launch / CUDA-event time per launch; tensor.achieved = 64 x "
+                             "evaluations per launch / the same time; traffic = DRAM bytes per "
+                             "pair from the ncu capture in profiles/ms_tile_tc.md x pairs per "
+                             "launch"},
         "clocks": clocks,
         "gpu_launches": int(sum(x["launches"] for x in res_bf16)),
     }

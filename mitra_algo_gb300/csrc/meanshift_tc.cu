@@ -332,11 +332,13 @@ __device__ __forceinline__ uint32_t active_tiles(const unsigned *nact) {
   return (nact[0] + kChunk - 1) / kChunk;
 }
 
-// boxes[t * 60 ..]: the box of tile t's active seeds (12 floats: lo, hi),
-// then the boxes of its four groups of 32 seeds (one block per tile).
+// boxes[t * kBoxFloats ..]: the box of tile t's active seeds (12 floats:
+// lo, hi), then the boxes of its eight groups of 16 seeds (one block per
+// tile).
+constexpr int kGroupSeeds = 16, kBoxFloats = 12 * (1 + kChunk / kGroupSeeds);
 __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigned *nact,
                            float *boxes) {
-  __shared__ float part[4][12];
+  __shared__ float part[kChunk / kGroupSeeds][12];
   if (blockIdx.x >= active_tiles(nact)) return;
   const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
   const bool live = slot < nact[0];
@@ -345,22 +347,23 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigne
     float m = live ? means[uint64_t(ids[slot]) * 8 + d] : 0.f;
     lo[d] = live ? m : INFINITY, hi[d] = live ? m : -INFINITY;
   }
-  for (int o = 16; o; o >>= 1)
+  for (int o = kGroupSeeds / 2; o; o >>= 1)  // within each group of 16 lanes
     for (int d = 0; d < 6; ++d) {
       lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
       hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
     }
-  const int warp = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-    for (int d = 0; d < 6; ++d) part[warp][d] = lo[d], part[warp][6 + d] = hi[d];
+  const int group = threadIdx.x / kGroupSeeds;
+  if (threadIdx.x % kGroupSeeds == 0)
+    for (int d = 0; d < 6; ++d) part[group][d] = lo[d], part[group][6 + d] = hi[d];
   __syncthreads();
-  float *out = boxes + uint64_t(blockIdx.x) * 60;
+  float *out = boxes + uint64_t(blockIdx.x) * kBoxFloats;
+  constexpr int kGroups = kChunk / kGroupSeeds;
   if (threadIdx.x < 12) {
     float v = part[0][threadIdx.x];
-    for (int w = 1; w < 4; ++w)
+    for (int w = 1; w < kGroups; ++w)
       v = threadIdx.x < 6 ? fminf(v, part[w][threadIdx.x]) : fmaxf(v, part[w][threadIdx.x]);
     out[threadIdx.x] = v;
-  } else if (threadIdx.x < 60) {
+  } else if (threadIdx.x < kBoxFloats) {
     out[threadIdx.x] = part[(threadIdx.x - 12) / 12][(threadIdx.x - 12) % 12];
   }
 }
@@ -369,7 +372,7 @@ constexpr int kListThreads = 256;  // chunks per block of the list kernels
 
 // need[t * nchunks + c]: some seed of tile t lies within the bandwidth of
 // chunk c's box (tested against the tile's box, then each group's box, then
-// the group's seeds).  Exact for Epanechnikov weights: every vote of a
+// the group's 16 seeds).  Exact for Epanechnikov weights: every vote of a
 // skipped chunk is farther than the bandwidth from every seed of the tile.
 // bcount[t * gridDim.x + blockIdx.x] = the block's kept chunks.
 __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, const float *means,
@@ -378,7 +381,7 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
                                                            float skip_gap2, uint8_t *need,
                                                            uint32_t *bcount) {
   __shared__ float seed[kChunk * 6];
-  __shared__ float gb[60];
+  __shared__ float gb[kBoxFloats];
   const uint64_t t = blockIdx.y;
   if (t >= active_tiles(nact)) return;
   const unsigned nactive = nact[0];
@@ -387,7 +390,7 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
     const bool live = slot < nactive;
     for (int d = 0; d < 6; ++d) seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
   }
-  if (threadIdx.x < 60) gb[threadIdx.x] = boxes[t * 60 + threadIdx.x];
+  if (threadIdx.x < kBoxFloats) gb[threadIdx.x] = boxes[t * kBoxFloats + threadIdx.x];
   __syncthreads();
   const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   bool keep = false;
@@ -395,10 +398,10 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
     float cb[12];
     for (int d = 0; d < 12; ++d) cb[d] = cbox[c * 12 + d];
     if (box_gap2_tc(gb, gb + 6, cb) <= skip_gap2)
-      for (int g = 0; g < 4 && !keep; ++g) {
+      for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
         const float *b = gb + 12 + 12 * g;
         if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
-        for (int i = 32 * g; i < 32 * g + 32 && !keep; ++i) {
+        for (int i = kGroupSeeds * g; i < kGroupSeeds * (g + 1) && !keep; ++i) {
           float q = 0;
           for (int d = 0; d < 6; ++d) {
             const float x = seed[i * 6 + d];
@@ -979,7 +982,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
                                                        float(1.0 / std::sqrt(h2)), images);
   check_launch();
   int32_t *ids = call.alloc<int32_t>(k);
-  float *boxes = call.alloc<float>(max_tiles * 60);
+  float *boxes = call.alloc<float>(max_tiles * kBoxFloats);
   const uint32_t nblk = uint32_t((v.nchunks + kListThreads - 1) / kListThreads);
   uint8_t *need = call.alloc<uint8_t>(max_tiles * v.nchunks);
   uint32_t *bcount = call.alloc<uint32_t>(max_tiles * nblk), *boff = call.alloc<uint32_t>(max_tiles * nblk);
