@@ -228,6 +228,88 @@ __global__ void fill_pairs(const int32_t *selected, uint64_t s, const double *xy
   }
 }
 
+// Single-evaluation form, used while the accept bitmaps of all sources fit
+// the kBitmapBudget: mark_pairs evaluates the acceptance test once per
+// candidate, counts the accepted partners b > a of source a and stores the
+// bitmap over b in [(a + 1) & ~31, s) at bitmap[a * stride ..]; fill_from_bits
+// then writes the pairs in ascending b from those words, so the (FP64) test
+// is not evaluated a second time.  Same pairs, same order as fill_pairs.
+constexpr uint64_t kBitmapBudget = 256ull << 20;  // bytes
+
+__global__ void mark_pairs(const int32_t *selected, uint64_t s, const double *xyz, uint64_t nv,
+                           const double *kmin, const double *kmax, SortedSamples srt,
+                           const uint64_t *lo, const uint64_t *hi, double t, double min_dist,
+                           uint64_t stride, uint64_t *counts, unsigned *bitmap) {
+  __shared__ unsigned bits[kChunkWords];
+  const uint64_t a = blockIdx.x;
+  const int32_t v = selected[a];
+  const double a0 = kmin[v], a1 = kmax[v];
+  const D3 ap = {xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  const uint64_t base = (a + 1) & ~uint64_t(31);
+  const unsigned words = unsigned((s - base + 31) / 32);  // <= stride <= kChunkWords
+  for (unsigned w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
+  __syncthreads();
+  for (uint64_t k = lo[a] + threadIdx.x; k < hi[a]; k += blockDim.x) {
+    const int32_t b = srt.ordinal[k];
+    if (uint64_t(b) <= a) continue;
+    if (accept(a0, a1, ap, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t, min_dist)) {
+      const uint64_t bit = uint64_t(b) - base;
+      atomicOr(&bits[bit >> 5], 1u << (bit & 31));
+    }
+  }
+  __syncthreads();
+  unsigned c = 0;
+  for (unsigned w = threadIdx.x; w < words; w += blockDim.x) {
+    const unsigned m = bits[w];
+    c += __popc(m);
+    bitmap[a * stride + w] = m;
+  }
+  const unsigned total = block_sum(c);
+  if (threadIdx.x == 0) counts[a] = total;
+}
+
+__global__ void fill_from_bits(const int32_t *selected, uint64_t s, const unsigned *bitmap,
+                               uint64_t stride, const uint64_t *offsets, int32_t *out_a,
+                               int32_t *out_b) {
+  __shared__ unsigned warp_tot[kFillThreads / 32];
+  const uint64_t a = blockIdx.x;
+  const uint64_t out = offsets[a], end_out = offsets[a + 1];
+  if (out == end_out) return;
+  const int32_t v = selected[a];
+  const uint64_t base = (a + 1) & ~uint64_t(31);
+  const unsigned words = unsigned((s - base + 31) / 32);
+  const unsigned *bits = bitmap + a * stride;
+  // Each thread owns a contiguous run of words; prefix of popcounts.
+  const unsigned per = (words + blockDim.x - 1) / blockDim.x;
+  const unsigned w0 = min(words, threadIdx.x * per), w1 = min(words, w0 + per);
+  unsigned mine = 0;
+  for (unsigned w = w0; w < w1; ++w) mine += __popc(bits[w]);
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned incl = mine;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= unsigned(o)) incl += y;
+  }
+  if (lane == 31) warp_tot[warp] = incl;
+  __syncthreads();
+  unsigned before = 0;
+  for (unsigned w = 0; w < warp; ++w) before += warp_tot[w];
+  uint64_t pos = out + before + incl - mine;
+  for (unsigned w = w0; w < w1; ++w) {
+    unsigned m = bits[w];
+    while (m) {
+      const unsigned bit = __ffs(m) - 1;
+      m &= m - 1;
+      const uint64_t b = base + uint64_t(w) * 32 + bit;
+      if (pos < end_out) {
+        out_a[pos] = v;
+        out_b[pos] = selected[b];
+      }
+      ++pos;
+    }
+  }
+}
+
 }  // namespace
 
 void prune_device(Call &call, const int32_t *sample, uint64_t count, const double *kmin,
@@ -294,8 +376,15 @@ uint64_t pairing_device(Call &call, const int32_t *selected, uint64_t s, const d
   check_launch();
   uint64_t *counts = call.alloc<uint64_t>(s), *offsets = call.alloc<uint64_t>(s + 1);
   double min_dist = 0.03 * box;
-  count_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo, hi,
-                                                    t, min_dist, counts);
+  const uint64_t stride = (s + 31) / 32 + 1;  // words of one source's bitmap, at most
+  const bool single = stride <= uint64_t(kChunkWords) && s * stride * 4 <= kBitmapBudget;
+  unsigned *bitmap = single ? call.alloc<unsigned>(s * stride) : nullptr;
+  if (single)
+    mark_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo, hi,
+                                                     t, min_dist, stride, counts, bitmap);
+  else
+    count_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo,
+                                                      hi, t, min_dist, counts);
   check_launch();
   exclusive_scan(call, counts, offsets, s);
   call.launched(4);
@@ -307,8 +396,12 @@ uint64_t pairing_device(Call &call, const int32_t *selected, uint64_t s, const d
   if (!total) return 0;
   *out_a = call.alloc<int32_t>(total);
   *out_b = call.alloc<int32_t>(total);
-  fill_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo, hi,
-                                                   offsets, t, min_dist, *out_a, *out_b);
+  if (single)
+    fill_from_bits<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, bitmap, stride, offsets,
+                                                         *out_a, *out_b);
+  else
+    fill_pairs<<<unsigned(s), kFillThreads, 0, st>>>(selected, s, xyz, nv, kmin, kmax, srt, lo, hi,
+                                                     offsets, t, min_dist, *out_a, *out_b);
   check_launch();
   call.launched();
   return total;

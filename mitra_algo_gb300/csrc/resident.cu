@@ -141,6 +141,110 @@ __global__ void votes6(const double *pos, const double *nrm, const double *dmn, 
   }
 }
 
+// The FP32 form of votes6 in two passes.  frames_f32 converts each
+// vertex's position, normal and principal directions once into a 48-byte
+// record (three float4), so a pair gathers two records instead of 24
+// scattered doubles.  votes6_f32 writes every vote whose rotation is not
+// near pi (the FP32 log map) and lists the others; votes6_near_pi then
+// takes the listed votes through the FP64 branch of log_map in full warps
+// (near pi the FP64 branch would otherwise run in almost every warp).  Each
+// vote follows the formulas of votes6<float>; the compiler may contract
+// them into FMAs differently, so votes can differ from votes6<float> in the
+// last bit.
+__global__ void frames_f32(const double *pos, const double *nrm, const double *dmn,
+                           const double *dmx, uint64_t nv, float4 *frames) {
+  const uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  auto f = [&](const double *l, int d) { return float(l[uint64_t(d) * nv + v]); };
+  frames[3 * v] = make_float4(f(pos, 0), f(pos, 1), f(pos, 2), f(nrm, 0));
+  frames[3 * v + 1] = make_float4(f(nrm, 1), f(nrm, 2), f(dmn, 0), f(dmn, 1));
+  frames[3 * v + 2] = make_float4(f(dmn, 2), f(dmx, 0), f(dmx, 1), f(dmx, 2));
+}
+
+struct Frame32 {
+  float p[3], n[3], dn[3], dx[3];
+};
+__device__ __forceinline__ Frame32 load_frame(const float4 *frames, int32_t v) {
+  const float4 a = frames[3 * uint64_t(v)], b = frames[3 * uint64_t(v) + 1],
+               c = frames[3 * uint64_t(v) + 2];
+  return {{a.x, a.y, a.z}, {a.w, b.x, b.y}, {b.z, b.w, c.x}, {c.y, c.z, c.w}};
+}
+
+// Rotation of vote sgn of the pair (a's frame to b's), as votes6.
+__device__ __forceinline__ void pair_rotation(const Frame32 &fa, const Frame32 &fb, int sgn,
+                                              float r[9]) {
+  const float s = sgn ? -1.f : 1.f;
+  for (int x = 0; x < 3; ++x)
+    for (int y = 0; y < 3; ++y)
+      r[x * 3 + y] = s * fb.dn[x] * fa.dn[y] + s * fb.dx[x] * fa.dx[y] + fb.n[x] * fa.n[y];
+}
+
+__device__ __forceinline__ void finish_vote(const float r[9], float d[8], const Frame32 &fa,
+                                            const Frame32 &fb, const float c[3], float inv_box) {
+  for (int k = 0; k < 3; ++k) d[k] *= 0.5f;
+  for (int x = 0; x < 3; ++x) {
+    float rp = r[x * 3] * fa.p[0] + r[x * 3 + 1] * fa.p[1] + r[x * 3 + 2] * fa.p[2];
+    float rc = r[x * 3] * c[0] + r[x * 3 + 1] * c[1] + r[x * 3 + 2] * c[2];
+    float t = fb.p[x] - rp;
+    d[3 + x] = (rc + t - c[x]) * inv_box;
+  }
+  float n2 = 0;
+  for (int k = 0; k < 6; ++k) n2 += d[k] * d[k];
+  d[6] = n2;
+  d[7] = 0;
+}
+
+__device__ __forceinline__ bool near_pi(const float r[9]) {
+  float c = (r[0] + r[4] + r[8] - 1.f) * 0.5f;
+  c = c > 1.f ? 1.f : (c < -1.f ? -1.f : c);
+  return !(c > 0.9999f) && !(c > -0.99f);  // log_map's FP64 branch
+}
+
+__global__ void votes6_f32(const float4 *frames, const int32_t *pa, const int32_t *pb, uint64_t np,
+                           double box, double cx, double cy, double cz, float *desc,
+                           unsigned long long *near_list, unsigned long long *near_count) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const Frame32 fa = load_frame(frames, pa[i]), fb = load_frame(frames, pb[i]);
+  const float c[3] = {float(cx), float(cy), float(cz)};
+  const float inv_box = 1.f / float(box);
+  for (int sgn = 0; sgn < 2; ++sgn) {
+    float r[9], d[8];
+    pair_rotation(fa, fb, sgn, r);
+    const uint64_t v = 2 * i + sgn;
+    if (near_pi(r)) {
+      near_list[atomicAdd(near_count, 1ull)] = v;
+      continue;
+    }
+    log_map<float>(r, d);
+    finish_vote(r, d, fa, fb, c, inv_box);
+    float4 *o = reinterpret_cast<float4 *>(desc + v * 8);
+    o[0] = make_float4(d[0], d[1], d[2], d[3]);
+    o[1] = make_float4(d[4], d[5], d[6], d[7]);
+  }
+}
+
+__global__ void votes6_near_pi(const float4 *frames, const int32_t *pa, const int32_t *pb,
+                               double box, double cx, double cy, double cz, float *desc,
+                               const unsigned long long *near_list,
+                               const unsigned long long *near_count) {
+  const float c[3] = {float(cx), float(cy), float(cz)};
+  const float inv_box = 1.f / float(box);
+  const unsigned long long n = *near_count;
+  for (unsigned long long j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n;
+       j += uint64_t(gridDim.x) * blockDim.x) {
+    const uint64_t v = near_list[j], i = v / 2;
+    const Frame32 fa = load_frame(frames, pa[i]), fb = load_frame(frames, pb[i]);
+    float r[9], d[8];
+    pair_rotation(fa, fb, int(v & 1), r);
+    log_map<float>(r, d);
+    finish_vote(r, d, fa, fb, c, inv_box);
+    float4 *o = reinterpret_cast<float4 *>(desc + v * 8);
+    o[0] = make_float4(d[0], d[1], d[2], d[3]);
+    o[1] = make_float4(d[4], d[5], d[6], d[7]);
+  }
+}
+
 // K distinct vote indices drawn uniformly (Floyd's algorithm), ascending.
 std::vector<int64_t> draw_seeds(uint64_t q, uint64_t k, uint64_t seed) {
   std::mt19937_64 rng(seed);
@@ -245,17 +349,29 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   float *desc_raw = call.alloc<float>(q * 8);
   double *desc64_raw = want64 ? call.alloc<double>(q * 8) : nullptr;
   const double *c = h.model.center;
-  votes6<float><<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x, nv, pa,
-                                                     pb, np, h.model.box_size, c[0], c[1], c[2],
-                                                     desc_raw);
-  check_launch();
+  {
+    float4 *frames = call.alloc<float4>(3 * nv);
+    unsigned long long *near_list = call.alloc<unsigned long long>(q);
+    unsigned long long *near_count = call.alloc<unsigned long long>(1);
+    SYM_CUDA(cudaMemsetAsync(near_count, 0, 8, st));
+    frames_f32<<<blocks_for(nv), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x, nv,
+                                                     frames);
+    check_launch();
+    votes6_f32<<<blocks_for(np), kThreads, 0, st>>>(frames, pa, pb, np, h.model.box_size, c[0],
+                                                     c[1], c[2], desc_raw, near_list, near_count);
+    check_launch();
+    votes6_near_pi<<<152 * 8, kThreads, 0, st>>>(frames, pa, pb, h.model.box_size, c[0], c[1], c[2],
+                                                 desc_raw, near_list, near_count);
+    check_launch();
+    call.launched(3);
+  }
   if (want64) {
     votes6<double><<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x, nv,
                                                         pa, pb, np, h.model.box_size, c[0], c[1],
                                                         c[2], desc64_raw);
     check_launch();
   }
-  call.launched(want64 ? 2 : 1);
+  if (want64) call.launched();
   clock.mark(4);
   // ---- Morton sort into chunks
   VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q);
