@@ -43,22 +43,30 @@ __global__ void box_final(const float *partial, int n, float *box) {
   box[k] = v;
 }
 
-__device__ __forceinline__ uint64_t morton6(const float *x, const float *box) {
+// Morton key of a 6-D point over `bits` bits per coordinate (cells of
+// 1/2^bits of the box; at most 10).
+__device__ __forceinline__ uint64_t morton6(const float *x, const float *box, int bits = 10) {
   uint64_t key = 0;
+  const int cells = 1 << bits;
   for (int k = 0; k < 6; ++k) {
     float lo = box[k], span = box[6 + k] - lo;
     float t = span > 0 ? (x[k] - lo) / span : 0.f;
-    uint64_t cell = uint64_t(min(1023, max(0, int(t * 1024.f))));
-    for (int b = 0; b < 10; ++b) key |= ((cell >> b) & 1ull) << (6 * b + k);
+    uint64_t cell = uint64_t(min(cells - 1, max(0, int(t * float(cells)))));
+    for (int b = 0; b < bits; ++b) key |= ((cell >> b) & 1ull) << (6 * b + k);
   }
   return key;
 }
+
+// Votes are ordered by 8 bits per coordinate: a cell of the vote space is
+// then ~1/256 of its extent (well under the bandwidth on the benchmark
+// workloads), and the 48-bit key sorts in six 8-bit radix passes.
+constexpr int kVoteMortonBits = 8;
 
 __global__ void morton_keys(const float *desc, uint64_t q, const float *box, uint64_t *keys,
                             int32_t *idx) {
   uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (v >= q) return;
-  keys[v] = morton6(desc + v * 8, box);
+  keys[v] = morton6(desc + v * 8, box, kVoteMortonBits);
   idx[v] = int32_t(v);
 }
 
@@ -516,7 +524,7 @@ VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_r
   v.rank = call.alloc<int32_t>(q);
   morton_keys<<<blocks_for(q), kThreads, 0, st>>>(desc_raw, q, v.gbox, keys, idx);
   check_launch();
-  radix_sort_pairs(call, keys, idx, skeys, v.order, q, 60);
+  radix_sort_pairs(call, keys, idx, skeys, v.order, q, 6 * kVoteMortonBits);
   invert<<<blocks_for(q), kThreads, 0, st>>>(v.order, q, v.rank);
   check_launch();
   v.desc = call.alloc<float>(q * 8);

@@ -17,7 +17,10 @@
 //     turns the key-ordered window back into the reference's nested-loop
 //     order (source ordinal, then target ordinal) with no segmented sort.
 // The acceptance test is the reference's FP64 expression, evaluated in the
-// same order without FMA contraction, so the pair set is bit-exact.
+// same order without FMA contraction, so the pair set is bit-exact.  An FP32
+// form of the test runs first and decides every candidate whose values clear
+// the thresholds by more than the FP32 rounding of its inputs can move them;
+// the others take the FP64 test.
 #include "common.cuh"
 #include "primitives.cuh"
 #include "rng.hpp"
@@ -59,9 +62,10 @@ __global__ void gather_samples(const int32_t *selected, uint64_t s, const double
   keys[a] = orderable_key(k0);
 }
 
-struct SortedSamples {  // SoA in kmin-key order
+struct SortedSamples {  // SoA in kmin-key order (FP64, and its FP32 rounding)
   int32_t *ordinal;
   double *kmin, *kmax, *x, *y, *z;
+  float *kmin32, *kmax32, *x32, *y32, *z32;
 };
 
 __global__ void build_sorted(const int32_t *sorted_ord, const int32_t *selected, uint64_t s,
@@ -77,6 +81,11 @@ __global__ void build_sorted(const int32_t *sorted_ord, const int32_t *selected,
   out.x[k] = xyz[v];
   out.y[k] = xyz[nv + v];
   out.z[k] = xyz[2 * nv + v];
+  out.kmin32[k] = float(kmin[v]);
+  out.kmax32[k] = float(kmax[v]);
+  out.x32[k] = float(xyz[v]);
+  out.y32[k] = float(xyz[nv + v]);
+  out.z32[k] = float(xyz[2 * nv + v]);
 }
 
 __device__ uint64_t lower_bound_key(const uint64_t *keys, uint64_t n, uint64_t key, bool upper) {
@@ -127,6 +136,50 @@ __device__ __forceinline__ bool accept(double pa0, double pa1, D3 pp, double qb0
   return !(norm(pp - qp) < min_dist);
 }
 
+// A source's values for the test, in FP64 and rounded to FP32.
+struct Source {
+  int32_t v;
+  double k0, k1;
+  D3 p;
+  float k0f, k1f, xf, yf, zf;
+};
+__device__ __forceinline__ Source load_source(const int32_t *selected, uint64_t a, const double *xyz,
+                                              uint64_t nv, const double *kmin, const double *kmax) {
+  Source o;
+  o.v = selected[a];
+  o.k0 = kmin[o.v], o.k1 = kmax[o.v];
+  o.p = {xyz[o.v], xyz[nv + o.v], xyz[2 * nv + o.v]};
+  o.k0f = float(o.k0), o.k1f = float(o.k1);
+  o.xf = float(o.p.x), o.yf = float(o.p.y), o.zf = float(o.p.z);
+  return o;
+}
+
+// accept() for source src and the k-th sorted sample.  Rounding the inputs
+// to FP32 moves each curvature by at most 2^-24 of itself, so |dk| and t M
+// move by less than 5e-7 M with M >= max |k|; each coordinate moves by at
+// most 2^-24 of the largest coordinate magnitude S of the two points, so the
+// distance moves by at most 2.1e-7 S.  Outside those bands (widened further
+// for the FP32 arithmetic) the FP32 verdict is the FP64 one.
+__device__ __forceinline__ bool accept_filtered(const Source &src, const SortedSamples &srt,
+                                                uint64_t k, float tf, float min_dist_f, double t,
+                                                double min_dist) {
+  const float b0 = srt.kmin32[k], b1 = srt.kmax32[k];
+  const float bx = srt.x32[k], by = srt.y32[k], bz = srt.z32[k];
+  const float m = fmaxf(fmaxf(fmaxf(fmaxf(fabsf(src.k0f), fabsf(src.k1f)), fabsf(b0)), fabsf(b1)),
+                        1e-10f);
+  const float tol = tf * m, slack = 2e-6f * m;
+  const float e0 = fabsf(src.k0f - b0), e1 = fabsf(src.k1f - b1);
+  const float dx = src.xf - bx, dy = src.yf - by, dz = src.zf - bz;
+  const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+  const float S = fmaxf(fmaxf(fmaxf(fabsf(src.xf), fabsf(src.yf)), fmaxf(fabsf(src.zf), fabsf(bx))),
+                        fmaxf(fabsf(by), fabsf(bz)));
+  const float dslack = 1e-6f * S + 1e-5f * min_dist_f;
+  if (e0 > tol + slack || e1 > tol + slack || d < min_dist_f - dslack) return false;
+  if (e0 < tol - slack && e1 < tol - slack && d > min_dist_f + dslack) return true;
+  return accept(src.k0, src.k1, src.p, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t,
+                min_dist);
+}
+
 __device__ unsigned block_sum(unsigned v) {
   __shared__ unsigned warp_sum[32];
   for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -145,14 +198,13 @@ __global__ void count_pairs(const int32_t *selected, uint64_t s, const double *x
                             const uint64_t *lo, const uint64_t *hi, double t, double min_dist,
                             uint64_t *counts) {
   uint64_t a = blockIdx.x;
-  int32_t v = selected[a];
-  double a0 = kmin[v], a1 = kmax[v];
-  D3 ap = {xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  const Source src = load_source(selected, a, xyz, nv, kmin, kmax);
+  const float tf = float(t), mdf = float(min_dist);
   unsigned c = 0;
   for (uint64_t k = lo[a] + threadIdx.x; k < hi[a]; k += blockDim.x) {
     int32_t b = srt.ordinal[k];
     if (uint64_t(b) <= a) continue;
-    c += accept(a0, a1, ap, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t, min_dist);
+    c += accept_filtered(src, srt, k, tf, mdf, t, min_dist);
   }
   unsigned total = block_sum(c);
   if (threadIdx.x == 0) counts[a] = total;
@@ -168,9 +220,9 @@ __global__ void fill_pairs(const int32_t *selected, uint64_t s, const double *xy
   __shared__ unsigned bits[kChunkWords];
   __shared__ unsigned warp_tot[kFillThreads / 32];
   uint64_t a = blockIdx.x;
-  int32_t v = selected[a];
-  double a0 = kmin[v], a1 = kmax[v];
-  D3 ap = {xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  const Source src = load_source(selected, a, xyz, nv, kmin, kmax);
+  const int32_t v = src.v;
+  const float tf = float(t), mdf = float(min_dist);
   uint64_t out = offsets[a];
   const uint64_t end_out = offsets[a + 1];
   if (out == end_out) return;
@@ -184,8 +236,7 @@ __global__ void fill_pairs(const int32_t *selected, uint64_t s, const double *xy
     for (uint64_t k = lo[a] + threadIdx.x; k < hi[a]; k += blockDim.x) {
       int32_t b = srt.ordinal[k];
       if (uint64_t(b) <= a || uint64_t(b) < cb || uint64_t(b) >= ce) continue;
-      if (accept(a0, a1, ap, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t,
-                 min_dist)) {
+      if (accept_filtered(src, srt, k, tf, mdf, t, min_dist)) {
         uint64_t bit = uint64_t(b) - cb;
         atomicOr(&bits[bit >> 5], 1u << (bit & 31));
       }
@@ -242,9 +293,8 @@ __global__ void mark_pairs(const int32_t *selected, uint64_t s, const double *xy
                            uint64_t stride, uint64_t *counts, unsigned *bitmap) {
   __shared__ unsigned bits[kChunkWords];
   const uint64_t a = blockIdx.x;
-  const int32_t v = selected[a];
-  const double a0 = kmin[v], a1 = kmax[v];
-  const D3 ap = {xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  const Source src = load_source(selected, a, xyz, nv, kmin, kmax);
+  const float tf = float(t), mdf = float(min_dist);
   const uint64_t base = (a + 1) & ~uint64_t(31);
   const unsigned words = unsigned((s - base + 31) / 32);  // <= stride <= kChunkWords
   for (unsigned w = threadIdx.x; w < words; w += blockDim.x) bits[w] = 0;
@@ -252,7 +302,7 @@ __global__ void mark_pairs(const int32_t *selected, uint64_t s, const double *xy
   for (uint64_t k = lo[a] + threadIdx.x; k < hi[a]; k += blockDim.x) {
     const int32_t b = srt.ordinal[k];
     if (uint64_t(b) <= a) continue;
-    if (accept(a0, a1, ap, srt.kmin[k], srt.kmax[k], {srt.x[k], srt.y[k], srt.z[k]}, t, min_dist)) {
+    if (accept_filtered(src, srt, k, tf, mdf, t, min_dist)) {
       const uint64_t bit = uint64_t(b) - base;
       atomicOr(&bits[bit >> 5], 1u << (bit & 31));
     }
@@ -368,7 +418,9 @@ uint64_t pairing_device(Call &call, const int32_t *selected, uint64_t s, const d
   call.check_status("pairing");
   radix_sort_pairs(call, keys, ord, sorted_keys, sorted_ord, s, 64);
   SortedSamples srt{call.alloc<int32_t>(s), call.alloc<double>(s), call.alloc<double>(s),
-                    call.alloc<double>(s), call.alloc<double>(s), call.alloc<double>(s)};
+                    call.alloc<double>(s), call.alloc<double>(s), call.alloc<double>(s),
+                    call.alloc<float>(s),  call.alloc<float>(s),  call.alloc<float>(s),
+                    call.alloc<float>(s),  call.alloc<float>(s)};
   build_sorted<<<blocks_for(s), kThreads, 0, st>>>(sorted_ord, selected, s, xyz, nv, kmin, kmax, srt);
   check_launch();
   uint64_t *lo = call.alloc<uint64_t>(s), *hi = call.alloc<uint64_t>(s);
