@@ -50,7 +50,7 @@ ITERATIONS = 300  # mean-shift approach-phase iterations (BF16, or FP32)
 POLISH = 30       # FP32 polish iterations (both forms)
 # DRAM bytes (read + write) per (seed tile, vote chunk) pair of ms_tile_tc,
 # from the ncu capture summarised in profiles/ms_tile_tc.md
-TRAFFIC_PER_CHUNK_PAIR = 8322.0
+TRAFFIC_PER_CHUNK_PAIR = 8309.0
 IMAGE_BYTES = 8224.0  # one chunk image: the algorithmic bytes of a (tile, chunk) pair
 
 
