@@ -52,6 +52,62 @@ POLISH = 30       # FP32 polish iterations (both forms)
 # from the ncu capture summarised in profiles/ms_tile_tc.md
 TRAFFIC_PER_CHUNK_PAIR = 8309.0
 IMAGE_BYTES = 8224.0  # one chunk image: the algorithmic bytes of a (tile, chunk) pair
+BATCH_SAMPLES, BATCH_SEEDS = 4000, 512  # per mesh of the uneven batch
+
+
+def batch_bench(gpu, n, workers):
+    """Meshes/s of an uneven batch (motif icospheres of 3.5k-54k vertices,
+    drawn so that sizes spread over that range, 2-5 fold rotations, noise
+    sigma in [0, 5e-3] of the diagonal): sym_detect_fast one mesh after the
+    other on one context, against sym_detect_fast_batch with `workers`
+    contexts.  Host wall clock around each pass (both calls are
+    synchronous); mesh preparation, curvature and sampling are not timed."""
+    import torch
+    from mitra_algo_gb300.mesh import motif_sphere, prepare
+    from mitra_algo_gb300.types import Options, Rng
+    rng = np.random.default_rng(2024)
+    jobs, sizes = [], []
+    for i in range(n):
+        u = rng.random()
+        level = 4 if u < 0.37 else (5 if u < 0.77 else 6)
+        mesh = motif_sphere(level=level, bumps=int(rng.integers(6, 13)),
+                            folds=int(rng.integers(2, 6)), partial_shift=float(rng.uniform(0.2, 0.5)),
+                            noise=float(rng.uniform(0.0, 5e-3)), seed=100 + i)
+        opts = Options(sample_ratio=min(1.0, BATCH_SAMPLES / mesh.vertex_count),
+                       pair_threshold=PAIR_THRESHOLD, bandwidth=BANDWIDTH, max_pairs=2 * 10 ** 7,
+                       max_votes=5 * 10 ** 7, max_clusters=8)
+        p = prepare(mesh, opts)
+        f = gpu.curvature(p.mesh, p.topology, opts)
+        sample = gpu.select(p.mesh, f, p.topology.weights, opts, Rng(opts.seed)).sample
+        jobs.append((gpu.load_mesh(p), sample, opts))
+        sizes.append(mesh.vertex_count)
+    kw = dict(precision="bf16", seeds=BATCH_SEEDS, max_iterations=100, polish_iterations=POLISH)
+
+    def loop():
+        return [gpu.detect_fast(m, s, o, **kw) for m, s, o in jobs]
+
+    def together():
+        return gpu.detect_fast_batch(jobs, workers=workers, **kw)
+
+    out = {}
+    for name, fn in (("per_mesh_loop", loop), ("batched", together)):
+        fn()  # warm-up: workspaces reach their size
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        out[name] = (time.perf_counter() - t0, r)
+    for m, _, _ in jobs:
+        m.close()
+    (t_loop, r_loop), (t_batch, r_batch) = out["per_mesh_loop"], out["batched"]
+    same = all(a["pairs"] == b["pairs"] and a["modes"] == b["modes"] and
+               a["rotation"] == b["rotation"] for a, b in zip(r_loop, r_batch))
+    return {"meshes": n, "vertices": [int(min(sizes)), int(max(sizes))],
+            "samples_per_mesh": BATCH_SAMPLES, "seeds": BATCH_SEEDS, "workers": workers,
+            "per_mesh_loop_meshes_per_s": round(n / t_loop, 3),
+            "batched_meshes_per_s": round(n / t_batch, 3),
+            "pairs": int(sum(r["pairs"] for r in r_batch)),
+            "results_equal": bool(same), "clock": "host wall clock, synchronous calls"}
 
 
 def workload(small=False):
@@ -307,6 +363,7 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
     ms_bf16, ms_fp32, ms_e2e = ms.tolist()
+    batch = batch_bench(gpu, args.batch, args.batch_workers) if args.batch else None
     if rank != 0:
         return
     r = res_bf16[-1]
@@ -369,6 +426,8 @@ def run_gpu(args):
         "clocks": clocks,
         "gpu_launches": int(sum(x["launches"] for x in res_bf16)),
     }
+    if batch:
+        line["batch"] = batch
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_estimate(prepared, opts, sample, r)
     print(json.dumps(line))
@@ -413,6 +472,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline estimate")
+    ap.add_argument("--batch", type=int, default=48,
+                    help="meshes of the uneven batch measurement (0: skip)")
+    ap.add_argument("--batch-workers", type=int, default=4,
+                    help="worker contexts of sym_detect_fast_batch")
     ap.add_argument("--bandwidth", type=float, default=None, help="override the bandwidth")
     ap.add_argument("--once", choices=["bf16", "fp32"], default=None,
                     help="run the pipeline once after one warm-up run and print its stages")

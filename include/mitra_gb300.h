@@ -344,6 +344,30 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
                            const sym_options *options,
                            const sym_fast_options *fast, sym_fast_result *out);
 
+/* Batched detection (no reference counterpart; the reference's detect() runs
+ * one mesh per call, src/core/pipeline.cpp:27-47).  Runs sym_detect_fast on
+ * every item, one host thread per worker context: each worker (its own CUDA
+ * stream and workspace) takes the next item in order, so the launches and
+ * host round trips of different meshes overlap on the GPU.  The contexts
+ * are the caller's (created once with sym_context_create, on the device the
+ * meshes were loaded on, and reused across calls so their workspaces stay
+ * allocated); no two workers may share one.  Each item's result is the one
+ * sym_detect_fast gives for it alone.  Returns SYM_OK when every item
+ * succeeded, else the status of the first failing item (each item keeps its
+ * own status and message). */
+typedef struct sym_batch_item {
+  sym_mesh_handle *mesh;
+  const int32_t *sample;
+  uint64_t sample_count;
+  const sym_options *options;
+  const sym_fast_options *fast;
+  sym_fast_result *out; /* caller-owned */
+  sym_status status;    /* written by the call */
+  char message[256];    /* the item's error message, "" on success */
+} sym_batch_item;
+sym_status sym_detect_fast_batch(sym_context *const *workers, int32_t worker_count,
+                                 sym_batch_item *items, uint64_t count);
+
 /* The mean-shift kernels of sym_detect_fast on their own (no reference
  * counterpart): K seeds over Q 6-D votes (host, q x 6 doubles), seeds are
  * vote indices.  Approach phase (at most max_iterations, in the requested

@@ -169,6 +169,12 @@ class FastResult(C.Structure):
                 ("tc_evaluations", C.c_double)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("sample", _i), ("sample_count", C.c_uint64),
+                ("options", C.POINTER(Options)), ("fast", C.POINTER(FastOptions)),
+                ("out", C.POINTER(FastResult)), ("status", C.c_int), ("message", C.c_char * 256)]
+
+
 MS_FP32, MS_BF16_REFINED, MS_FP64 = 0, 1, 2
 STAGES = ["curvature", "prune", "pairing", "votes", "vote_sort", "mean_shift", "modes",
           "verification"]
@@ -206,6 +212,7 @@ PROTOTYPES = [
     ("sym_fast_options_default", None, [P(FastOptions)]),
     ("sym_detect_fast", C.c_int, [C.c_void_p, C.c_void_p, _i, C.c_uint64, P(Options),
                                   P(FastOptions), P(FastResult)]),
+    ("sym_detect_fast_batch", C.c_int, [P(C.c_void_p), C.c_int32, P(BatchItem), C.c_uint64]),
     ("sym_context_stream", C.c_void_p, [C.c_void_p]),
     ("sym_meanshift6", C.c_int, [C.c_void_p, _d, C.c_uint64, P(C.c_int64), C.c_uint64, C.c_double,
                                  C.c_int32, C.c_int32, C.c_int32, _d, _u8, P(C.c_int32)]),

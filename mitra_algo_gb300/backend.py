@@ -51,6 +51,8 @@ class Gb300Backend:
 
     def __init__(self, device: int = 0, profile: bool = False):
         self._lib = abi.library()
+        self._device = device
+        self._workers = []  # contexts of sym_detect_fast_batch, created on first use
         ctx = C.c_void_p()
         _check(self._lib.sym_context_create(device, C.byref(ctx)))
         self._ctx = ctx
@@ -58,6 +60,9 @@ class Gb300Backend:
             _check(self._lib.sym_set_profiling(ctx, 1))
 
     def close(self):
+        for w in getattr(self, "_workers", []):
+            self._lib.sym_context_destroy(w)
+        self._workers = []
         if getattr(self, "_ctx", None):
             self._lib.sym_context_destroy(self._ctx)
             self._ctx = None
@@ -157,18 +162,57 @@ class Gb300Backend:
     def load_mesh(self, prepared: Prepared) -> "ResidentMesh":
         return ResidentMesh(self, prepared)
 
+    @staticmethod
+    def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
+                      reference_seeds, verify):
+        return abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
+                               seed_rng, max_iterations, polish_iterations, reference_seeds,
+                               1 if verify else 0)
+
     def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
                     seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
                     reference_seeds=0, verify=True) -> dict:
         """Throughput pipeline on a resident mesh (no reference counterpart)."""
         sample = np.ascontiguousarray(sample, np.int32)
-        fo = abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
-                             seed_rng, max_iterations, polish_iterations, reference_seeds,
-                             1 if verify else 0)
+        fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
+                                reference_seeds, verify)
         res = abi.FastResult()
         _check(self._lib.sym_detect_fast(self._ctx, mesh.handle,
                                          sample.ctypes.data_as(C.POINTER(C.c_int32)), sample.size,
                                          C.byref(options.to_c()), C.byref(fo), C.byref(res)))
+        return self._fast_dict(res)
+
+    def detect_fast_batch(self, jobs, workers=4, precision="bf16", seeds=2048, seed_rng=7,
+                          max_iterations=100, polish_iterations=100, verify=True) -> list:
+        """sym_detect_fast_batch over `jobs` = [(ResidentMesh, sample, Options), ...]:
+        `workers` meshes in flight at a time, each on its own context (stream
+        and workspace), the contexts kept for later calls.  Returns one result
+        dict per job, as detect_fast gives it."""
+        while len(self._workers) < workers:
+            w = C.c_void_p()
+            _check(self._lib.sym_context_create(self._device, C.byref(w)))
+            self._workers.append(w)
+        fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations, 0,
+                                verify)
+        keep = []
+        items = (abi.BatchItem * len(jobs))()
+        results = [abi.FastResult() for _ in jobs]
+        for it, (mesh, sample, options), res in zip(items, jobs, results):
+            sample = np.ascontiguousarray(sample, np.int32)
+            opts = options.to_c()
+            keep += [sample, opts]
+            it.mesh = mesh.handle
+            it.sample = sample.ctypes.data_as(C.POINTER(C.c_int32))
+            it.sample_count = sample.size
+            it.options = C.pointer(opts)
+            it.fast = C.pointer(fo)
+            it.out = C.pointer(res)
+        pool = (C.c_void_p * workers)(*[w.value for w in self._workers[:workers]])
+        _check(self._lib.sym_detect_fast_batch(pool, workers, items, len(jobs)))
+        return [self._fast_dict(r) for r in results]
+
+    @staticmethod
+    def _fast_dict(res) -> dict:
         n = int(res.clusters)
         out = {k: getattr(res, k) for k in ("pruned", "pairs", "votes", "modes", "clusters",
                                             "iterations", "polish_iterations", "mode_error_max",

@@ -33,7 +33,6 @@ void triangle_distances_host(Call &, const double *, uint64_t, double *);
 thread_local std::string sym_error_text;
 
 namespace {
-std::string &g_error = sym_error_text;
 
 void *host_alloc(size_t bytes) { return std::malloc(bytes); }
 
@@ -43,26 +42,26 @@ sym_status guarded(F &&f) {
     f();
     return SYM_OK;
   } catch (const sym::Error &e) {
-    g_error = e.what();
+    sym_error_text = e.what();
     return e.status;
   } catch (const std::bad_alloc &) {
-    g_error = "host allocation failed";
+    sym_error_text = "host allocation failed";
     return SYM_RUNTIME_ERROR;
   } catch (const std::exception &e) {
-    g_error = e.what();
+    sym_error_text = e.what();
     return SYM_RUNTIME_ERROR;
   }
 }
 
 sym_status null_args() {
-  g_error = "null argument";
+  sym_error_text = "null argument";
   return SYM_INVALID_ARGUMENT;
 }
 }  // namespace
 
 extern "C" {
 
-const char *sym_last_error(void) { return g_error.c_str(); }
+const char *sym_last_error(void) { return sym_error_text.c_str(); }
 
 const char *sym_backend_name(void) { return "gb300"; }
 

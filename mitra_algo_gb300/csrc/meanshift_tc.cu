@@ -972,11 +972,12 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   const uint64_t max_tiles = (k + kChunk - 1) / kChunk;
   if (max_tiles * v.nchunks >= (uint64_t(1) << 31)) return false;  // list entries are int32
   cudaStream_t st = call.stream();
-  static bool configured = false;
-  if (!configured) {
+  // once per process (thread-safe: calls from several host threads may race)
+  static const bool configured = [] {
     SYM_CUDA(cudaFuncSetAttribute(ms_tile_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
-    configured = true;
-  }
+    return true;
+  }();
+  (void)configured;
   uint8_t *images = call.alloc<uint8_t>(v.nchunks * kImage);
   build_images<<<unsigned(v.nchunks), kChunk, 0, st>>>(v.desc, v.q, v.nchunks, v.cbox, v.gbox,
                                                        float(1.0 / std::sqrt(h2)), images);
@@ -1074,12 +1075,12 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
 
 void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,
                       const uint16_t *b2, float *d_out, float *acc_out) {
-  static bool configured = false;
-  if (!configured) {
+  static const bool configured = [] {
     SYM_CUDA(cudaFuncSetAttribute(tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kSmemRequest));
-    configured = true;
-  }
+    return true;
+  }();
+  (void)configured;
   auto up = [&](const uint16_t *p, size_t n) {
     return reinterpret_cast<const __nv_bfloat16 *>(call.upload(p, n));
   };

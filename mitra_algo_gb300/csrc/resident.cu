@@ -22,9 +22,12 @@
 #include "verification.cuh"
 
 #include <algorithm>
+#include <atomic>
+#include <cstdio>
 #include <cmath>
 #include <limits>
 #include <map>
+#include <thread>
 #include <vector>
 
 namespace sym {
@@ -776,6 +779,41 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh, const int32_
     sym_error_text = e.what();
     return SYM_RUNTIME_ERROR;
   }
+}
+
+sym_status sym_detect_fast_batch(sym_context *const *workers, int32_t worker_count,
+                                 sym_batch_item *items, uint64_t count) {
+  if (!workers || worker_count <= 0 || (count && !items)) return SYM_INVALID_ARGUMENT;
+  for (int32_t w = 0; w < worker_count; ++w)
+    for (int32_t x = 0; x < w; ++x)
+      if (!workers[w] || workers[w] == workers[x]) {
+        sym_error_text = "batch workers must be distinct contexts";
+        return SYM_INVALID_ARGUMENT;
+      }
+  for (uint64_t i = 0; i < count; ++i) items[i].status = SYM_OK, items[i].message[0] = 0;
+  std::atomic<uint64_t> next{0};
+  auto run = [&](sym_context *ctx) {
+    for (uint64_t i = next++; i < count; i = next++) {
+      sym_batch_item &it = items[i];
+      it.status = sym_detect_fast(ctx, it.mesh, it.sample, it.sample_count, it.options, it.fast,
+                                  it.out);
+      if (it.status != SYM_OK) {
+        std::snprintf(it.message, sizeof(it.message), "%s", sym_error_text.c_str());
+        if (!it.message[0]) std::snprintf(it.message, sizeof(it.message), "invalid argument");
+      }
+    }
+  };
+  const int32_t used = int32_t(std::min<uint64_t>(uint64_t(worker_count), count));
+  std::vector<std::thread> pool;
+  for (int32_t w = 1; w < used; ++w) pool.emplace_back(run, workers[w]);
+  if (used > 0) run(workers[0]);
+  for (auto &t : pool) t.join();
+  for (uint64_t i = 0; i < count; ++i)
+    if (items[i].status != SYM_OK) {
+      sym_error_text = items[i].message;
+      return items[i].status;
+    }
+  return SYM_OK;
 }
 
 }  // extern "C"
