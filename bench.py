@@ -55,6 +55,41 @@ IMAGE_BYTES = 8224.0  # one chunk image: the algorithmic bytes of a (tile, chunk
 BATCH_SAMPLES, BATCH_SEEDS = 4000, 512  # per mesh of the uneven batch
 
 
+def reflection_bench(gpu, steps=5):
+    """Reflection mode on the mirrored height field of the reference's
+    CPU-runnable case (128 x 128 grid, 8 bumps mirrored in x, 2,000 samples,
+    5% curvature tolerance, bandwidth 0.02): meshes/s of the BF16-refined and
+    FP32 forms (host wall clock around synchronous calls, after two warm-up
+    runs) and the plane each finds first."""
+    from mitra_algo_gb300.mesh import mirrored_heightfield, prepare
+    from mitra_algo_gb300.types import Options, Rng
+    mesh = mirrored_heightfield(size=128, bumps=8, seed=0)
+    opts = Options(sample_ratio=2000 / mesh.vertex_count, pair_threshold=0.05, bandwidth=0.02,
+                   max_pairs=10 ** 7, max_votes=2 * 10 ** 7, max_clusters=8)
+    p = prepare(mesh, opts)
+    f = gpu.curvature(p.mesh, p.topology, opts)
+    sample = gpu.select(p.mesh, f, p.topology.weights, opts, Rng(opts.seed)).sample
+    resident = gpu.load_mesh(p)
+    out = {"workload": "mirrored height field 128 x 128, reflection mode",
+           "vertices": int(mesh.vertex_count), "samples": int(len(sample))}
+    for pr in ("bf16", "fp32"):
+        kw = dict(precision=pr, seeds=512, max_iterations=100, polish_iterations=POLISH,
+                  mode="reflection")
+        for _ in range(2):
+            r = gpu.detect_fast(resident, sample, opts, **kw)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r = gpu.detect_fast(resident, sample, opts, **kw)
+        dt = (time.perf_counter() - t0) / steps
+        out[pr] = {"meshes_per_s": round(1.0 / dt, 3), "pairs": int(r["pairs"]),
+                   "votes": int(r["votes"]),
+                   "plane": [round(x, 6) for x in r["plane_normal"][0]] +
+                            [round(r["plane_offset"][0], 6)] if r["clusters"] else None,
+                   "coverage": round(r["coverage"][0], 4) if r["clusters"] else None}
+    resident.close()
+    return out
+
+
 def batch_bench(gpu, n, workers):
     """Meshes/s of an uneven batch (motif icospheres of 3.5k-54k vertices,
     drawn so that sizes spread over that range, 2-5 fold rotations, noise
@@ -364,6 +399,7 @@ def run_gpu(args):
         torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
     ms_bf16, ms_fp32, ms_e2e = ms.tolist()
     batch = batch_bench(gpu, args.batch, args.batch_workers) if args.batch else None
+    refl = reflection_bench(gpu)
     if rank != 0:
         return
     r = res_bf16[-1]
@@ -428,6 +464,7 @@ def run_gpu(args):
     }
     if batch:
         line["batch"] = batch
+    line["reflection"] = refl
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_estimate(prepared, opts, sample, r)
     print(json.dumps(line))

@@ -303,6 +303,12 @@ typedef struct sym_fast_options {
   int32_t polish_iterations; /* FP32 polish iterations (both forms) */
   int32_t reference_seeds;   /* seeds re-run in FP64 for the mode error */
   int32_t verify;            /* verify the top modes (max_clusters) */
+  /* SYM_RIGID: two rotation + translation votes per pair, 6-D
+   * [log(R)/2, (R c + t - c)/box]; SYM_REFLECTION: one plane vote per pair
+   * whose mirrored frames agree (the reference's test,
+   * transformations.cpp:17-73), [n, (d + n.c)/box] padded to 6-D with
+   * zeros, decoded as the reference does (clustering.cpp:117-124) */
+  int32_t mode;
 } sym_fast_options;
 
 #define SYM_FAST_MAX_CLUSTERS 32

@@ -164,18 +164,22 @@ class Gb300Backend:
 
     @staticmethod
     def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                      reference_seeds, verify):
+                      reference_seeds, verify, mode="rigid"):
+        if mode not in ("rigid", "reflection"):
+            raise ValueError(f"unknown detection mode {mode!r}")
         return abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
                                seed_rng, max_iterations, polish_iterations, reference_seeds,
-                               1 if verify else 0)
+                               1 if verify else 0, 1 if mode == "reflection" else 0)
 
     def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
                     seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
-                    reference_seeds=0, verify=True) -> dict:
-        """Throughput pipeline on a resident mesh (no reference counterpart)."""
+                    reference_seeds=0, verify=True, mode="rigid") -> dict:
+        """Throughput pipeline on a resident mesh (no reference counterpart);
+        mode "rigid" (rotation + translation votes) or "reflection" (plane
+        votes)."""
         sample = np.ascontiguousarray(sample, np.int32)
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                                reference_seeds, verify)
+                                reference_seeds, verify, mode)
         res = abi.FastResult()
         _check(self._lib.sym_detect_fast(self._ctx, mesh.handle,
                                          sample.ctypes.data_as(C.POINTER(C.c_int32)), sample.size,
@@ -183,7 +187,8 @@ class Gb300Backend:
         return self._fast_dict(res)
 
     def detect_fast_batch(self, jobs, workers=4, precision="bf16", seeds=2048, seed_rng=7,
-                          max_iterations=100, polish_iterations=100, verify=True) -> list:
+                          max_iterations=100, polish_iterations=100, verify=True,
+                          mode="rigid") -> list:
         """sym_detect_fast_batch over `jobs` = [(ResidentMesh, sample, Options), ...]:
         `workers` meshes in flight at a time, each on its own context (stream
         and workspace), the contexts kept for later calls.  Returns one result
@@ -193,7 +198,7 @@ class Gb300Backend:
             _check(self._lib.sym_context_create(self._device, C.byref(w)))
             self._workers.append(w)
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations, 0,
-                                verify)
+                                verify, mode)
         keep = []
         items = (abi.BatchItem * len(jobs))()
         results = [abi.FastResult() for _ in jobs]
@@ -233,6 +238,9 @@ class Gb300Backend:
         out["tc_evaluations"] = float(res.tc_evaluations)
         out["rotation"] = [list(res.records[i].rotation) for i in range(n)]
         out["translation"] = [list(res.records[i].translation) for i in range(n)]
+        out["reflection"] = [bool(res.records[i].reflection) for i in range(n)]
+        out["plane_normal"] = [list(res.records[i].plane_normal) for i in range(n)]
+        out["plane_offset"] = [float(res.records[i].plane_offset) for i in range(n)]
         return out
 
     def meanshift6(self, votes, seeds, bandwidth, precision="fp32", max_iterations=100,

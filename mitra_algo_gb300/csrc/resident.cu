@@ -248,6 +248,63 @@ __global__ void votes6_near_pi(const float4 *frames, const int32_t *pa, const in
   }
 }
 
+// Reflection mode.  The plane of a pair is the perpendicular bisector of
+// its two points, n = unit(q - p) with its dominant component made positive
+// and d = -n.(p + q)/2; the pair votes for it when the mirrored frames agree
+// (the reference's test, transformations.cpp:17-73: the mirrored normal of a
+// within 0.75 of b's, the mirrored first direction within 0.75 of +-b's).
+// The test is made in FP64 once, so the FP32 and FP64 vote sets are the
+// same pairs; the descriptors [n, (d + n.c)/box] (zero-padded to 6-D) are
+// then written in each precision.
+__device__ __forceinline__ D3 plane_of(D3 p, D3 q, double &d) {
+  D3 n = unit(q - p);
+  int dom = 0;
+  for (int k = 1; k < 3; ++k)
+    if (fabs(comp(n, k)) > fabs(comp(n, dom))) dom = k;
+  if (comp(n, dom) < 0) n = n * -1;
+  d = -dot(n, div(p + q, 2));
+  return n;
+}
+
+__global__ void plane_flags(const double *pos, const double *nrm, const double *dmn, uint64_t nv,
+                            const int32_t *pa, const int32_t *pb, uint64_t np, uint8_t *flags) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int32_t a = pa[i], b = pb[i];
+  auto ld = [&](const double *l, int32_t v) { return D3{l[v], l[nv + v], l[2 * nv + v]}; };
+  double d;
+  const D3 n = plane_of(ld(pos, a), ld(pos, b), d);
+  const M3 refl = mirror(n);
+  flags[i] = dot(mul(refl, ld(nrm, a)), ld(nrm, b)) > 0.75 &&
+             fabs(dot(mul(refl, ld(dmn, a)), ld(dmn, b))) > 0.75;
+}
+
+template <typename T>
+__global__ void plane_votes(const double *pos, uint64_t nv, const int32_t *pa, const int32_t *pb,
+                            const int32_t *list, uint64_t q, double box, double cx, double cy,
+                            double cz, T *desc) {
+  const uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= q) return;
+  const int32_t i = list[v], a = pa[i], b = pb[i];
+  T p[3] = {T(pos[a]), T(pos[nv + a]), T(pos[2 * nv + a])};
+  T r[3] = {T(pos[b]), T(pos[nv + b]), T(pos[2 * nv + b])};
+  T n[3], len = 0;
+  for (int k = 0; k < 3; ++k) n[k] = r[k] - p[k], len += n[k] * n[k];
+  len = sqrt(len);
+  int dom = 0;
+  for (int k = 0; k < 3; ++k) {
+    n[k] /= len;
+    if (fabs(n[k]) > fabs(n[dom])) dom = k;
+  }
+  if (n[dom] < T(0))
+    for (int k = 0; k < 3; ++k) n[k] = -n[k];
+  T d = 0;
+  for (int k = 0; k < 3; ++k) d -= n[k] * ((p[k] + r[k]) / T(2));
+  T out[8] = {n[0], n[1], n[2], (d + n[0] * T(cx) + n[1] * T(cy) + n[2] * T(cz)) / T(box), 0, 0, 0, 0};
+  out[6] = out[0] * out[0] + out[1] * out[1] + out[2] * out[2] + out[3] * out[3];
+  for (int k = 0; k < 8; ++k) desc[v * 8 + k] = out[k];
+}
+
 // K distinct vote indices drawn uniformly (Floyd's algorithm), ascending.
 std::vector<int64_t> draw_seeds(uint64_t q, uint64_t k, uint64_t seed) {
   std::mt19937_64 rng(seed);
@@ -340,7 +397,24 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
                                h.model.box_size, o.max_pairs, &pa, &pb);
   r.pairs = np;
   clock.mark(3);
+  const bool reflection = fo.mode == SYM_REFLECTION;
+  if (fo.mode != SYM_RIGID && !reflection) fail(SYM_INVALID_ARGUMENT, "unknown detection mode");
+  int32_t *plane_list = nullptr;
   uint64_t q = 2 * np;
+  if (reflection) {  // one vote per pair whose mirrored frames agree
+    uint8_t *flags = call.alloc<uint8_t>(std::max<uint64_t>(np, 1));
+    plane_list = call.alloc<int32_t>(std::max<uint64_t>(np, 1));
+    uint64_t *count = call.alloc<uint64_t>(1);
+    if (np) {
+      plane_flags<<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, nv, pa, pb, np,
+                                                       flags);
+      check_launch();
+      call.launched();
+    }
+    compact_indices(call, flags, np, plane_list, count);
+    call.d2h(&q, count, 8);
+    call.sync();
+  }
   if (q > o.max_votes || q > uint64_t(std::numeric_limits<int32_t>::max()))
     fail(SYM_RUNTIME_ERROR, "Vote budget exceeded; lower --sample-ratio or tighten --pair-threshold");
   r.votes = q;
@@ -352,7 +426,19 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   float *desc_raw = call.alloc<float>(q * 8);
   double *desc64_raw = want64 ? call.alloc<double>(q * 8) : nullptr;
   const double *c = h.model.center;
-  {
+  if (reflection) {
+    plane_votes<float><<<blocks_for(q), kThreads, 0, st>>>(h.xyz, nv, pa, pb, plane_list, q,
+                                                           h.model.box_size, c[0], c[1], c[2],
+                                                           desc_raw);
+    check_launch();
+    if (want64) {
+      plane_votes<double><<<blocks_for(q), kThreads, 0, st>>>(h.xyz, nv, pa, pb, plane_list, q,
+                                                              h.model.box_size, c[0], c[1], c[2],
+                                                              desc64_raw);
+      check_launch();
+    }
+    call.launched(want64 ? 2 : 1);
+  } else {
     float4 *frames = call.alloc<float4>(3 * nv);
     unsigned long long *near_list = call.alloc<unsigned long long>(q);
     unsigned long long *near_count = call.alloc<unsigned long long>(1);
@@ -367,14 +453,14 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
                                                  desc_raw, near_list, near_count);
     check_launch();
     call.launched(3);
+    if (want64) {
+      votes6<double><<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x,
+                                                          nv, pa, pb, np, h.model.box_size, c[0],
+                                                          c[1], c[2], desc64_raw);
+      check_launch();
+      call.launched();
+    }
   }
-  if (want64) {
-    votes6<double><<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x, nv,
-                                                        pa, pb, np, h.model.box_size, c[0], c[1],
-                                                        c[2], desc64_raw);
-    check_launch();
-  }
-  if (want64) call.launched();
   clock.mark(4);
   // ---- Morton sort into chunks
   VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q);
@@ -536,14 +622,28 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   r.clusters = nc;
   for (uint64_t i = 0; i < nc; ++i) {
     const double *d = &mode_pos[rank[i] * 6];
-    double w[3] = {2 * d[0], 2 * d[1], 2 * d[2]}, R[9];
-    exp_map(w, R);
     sym_cluster_record &rec = r.records[i];
     rec = sym_cluster_record{};
-    for (int j = 0; j < 9; ++j) rec.rotation[j] = R[j];
-    for (int x = 0; x < 3; ++x) {
-      double rc = R[x * 3] * c[0] + R[x * 3 + 1] * c[1] + R[x * 3 + 2] * c[2];
-      rec.translation[x] = d[3 + x] * h.model.box_size + c[x] - rc;
+    if (reflection) {  // the reference's decode, clustering.cpp:117-124
+      const D3 nr{d[0], d[1], d[2]};
+      const double len = norm(nr);
+      const D3 n = unit(nr);
+      const double off = d[3] * h.model.box_size / len - dot(n, D3{c[0], c[1], c[2]});
+      const M3 R = mirror(n);
+      rec.reflection = 1;
+      rec.plane_normal[0] = n.x, rec.plane_normal[1] = n.y, rec.plane_normal[2] = n.z;
+      rec.plane_offset = off;
+      for (int j = 0; j < 9; ++j) rec.rotation[j] = R.m[j];
+      rec.translation[0] = -2 * off * n.x, rec.translation[1] = -2 * off * n.y;
+      rec.translation[2] = -2 * off * n.z;
+    } else {
+      double w[3] = {2 * d[0], 2 * d[1], 2 * d[2]}, R[9];
+      exp_map(w, R);
+      for (int j = 0; j < 9; ++j) rec.rotation[j] = R[j];
+      for (int x = 0; x < 3; ++x) {
+        double rc = R[x * 3] * c[0] + R[x * 3 + 1] * c[1] + R[x * 3 + 2] * c[2];
+        rec.translation[x] = d[3 + x] * h.model.box_size + c[x] - rc;
+      }
     }
     r.support[i] = support[rank[i]];
     r.precise[i] = mode_precise[rank[i]];
@@ -572,7 +672,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
 extern "C" {
 
 void sym_fast_options_default(sym_fast_options *o) {
-  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1};
+  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID};
 }
 
 sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_topology_view *g,

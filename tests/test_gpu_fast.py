@@ -92,3 +92,61 @@ def test_forms_agree_on_the_top_modes(fast):
         mf = np.concatenate([np.ravel(f["rotation"][i]), f["translation"][i]])
         err = min(np.linalg.norm(m - mf) / np.linalg.norm(mf) for m in mb)
         assert err <= 1e-4, (i, err)
+
+
+# --------------------------------------------------------- reflection mode
+# The mirrored height field (128 x 128 grid, 8 bumps mirrored in x, 2,000
+# samples, 5% curvature tolerance, bandwidth 0.02) has one plane of symmetry,
+# x = 0; reflection mode votes one plane per pair whose mirrored frames agree.
+
+@pytest.fixture(scope="module")
+def refl():
+    from mitra_algo_gb300 import Gb300Backend
+    from mitra_algo_gb300.mesh import mirrored_heightfield
+    gpu = Gb300Backend(0)
+    mesh = mirrored_heightfield(size=128, bumps=8, seed=0)
+    opts = Options(sample_ratio=2000 / mesh.vertex_count, pair_threshold=0.05, bandwidth=0.02,
+                   max_pairs=10 ** 7, max_votes=2 * 10 ** 7, max_clusters=8)
+    p = prepare(mesh, opts)
+    f = gpu.curvature(p.mesh, p.topology, opts)
+    sample = gpu.select(p.mesh, f, p.topology.weights, opts, Rng(opts.seed)).sample
+    resident = gpu.load_mesh(p)
+    runs = {pr: gpu.detect_fast(resident, sample, opts, precision=pr, seeds=512,
+                                max_iterations=100, polish_iterations=30, mode="reflection")
+            for pr in ("bf16", "fp32")}
+    yield gpu, p, opts, runs
+    resident.close()
+    gpu.close()
+
+
+def test_reflection_finds_the_mirror_plane(refl):
+    _, p, _, runs = refl
+    for pr, r in runs.items():
+        assert r["clusters"] > 0 and r["votes"] > 0, pr
+        assert all(r["reflection"]), pr
+        n, off = np.array(r["plane_normal"][0]), r["plane_offset"][0]
+        assert abs(abs(n[0]) - 1) < 1e-3 and abs(off) < 1e-3 * p.context.box_size, (pr, n, off)
+        assert r["coverage"][0] > 0.5, (pr, r["coverage"])
+
+
+def test_reflection_forms_agree(refl):
+    _, _, _, runs = refl
+    b, f = runs["bf16"], runs["fp32"]
+    assert b["pairs"] == f["pairs"] and b["votes"] == f["votes"]
+    pb = np.concatenate([b["plane_normal"][0], [b["plane_offset"][0]]])
+    pf = np.concatenate([f["plane_normal"][0], [f["plane_offset"][0]]])
+    assert np.linalg.norm(pb - pf) <= 1e-4 * np.linalg.norm(pf), (pb, pf)
+
+
+def test_reflection_fast_verification_matches_exact(refl):
+    gpu, p, opts, runs = refl
+    r = runs["bf16"]
+    n = r["clusters"]
+    clusters = ClusterOutput(np.ones(n, np.uint8), np.array(r["rotation"]),
+                             np.array(r["translation"]), np.array(r["plane_normal"]),
+                             np.array(r["plane_offset"]),
+                             Csr(np.zeros(n + 1, np.uint64), np.zeros(0, np.int32)))
+    exact = gpu.verification(p.mesh, p.topology, clusters, p.context, opts)
+    assert np.all(np.abs(np.array(r["coverage"]) - exact.coverage) <= 5e-3), \
+        (r["coverage"], exact.coverage)
+    assert np.allclose(r["rms"], exact.rms, rtol=1e-2, atol=1e-9 * p.context.box_size)
