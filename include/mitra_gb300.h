@@ -350,6 +350,33 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
                            const sym_options *options,
                            const sym_fast_options *fast, sym_fast_result *out);
 
+/* GPU mesh preparation: the reference's prepare() (src/core/prepare.cpp:
+ * 102-149) without subdivision (options->subdivide must be 0) and its
+ * topology() (prepare.cpp:13-58): option and mesh validation with the
+ * reference's messages, the bounding-box diagonal, removal of degenerate
+ * faces, face and vertex normals, vertex weights, neighbour ring, incident
+ * faces, edge table and vertex centroid, bit-exact with the CPU path.  The
+ * outputs are library-owned host arrays (sym_prepared_release). */
+typedef struct sym_prepared {
+  sym_model_context context;
+  uint64_t vertex_count, face_count, edge_count, rejected_faces;
+  int32_t *faces[3]; /* the kept faces, face_count rows */
+  double *normals[3], *face_normals[3], *weights;
+  uint64_t *neighbor_offsets; /* vertex_count + 1 */
+  int32_t *neighbor_indices;
+  uint64_t *incident_offsets; /* vertex_count + 1 */
+  int32_t *incident_indices;
+  sym_edge *edges;
+  void *storage;
+} sym_prepared;
+sym_status sym_prepare(sym_context *ctx, const sym_mesh_view *mesh,
+                       const sym_options *options, sym_prepared *out);
+void sym_prepared_release(sym_prepared *p);
+/* sym_prepare straight into a resident mesh (as sym_mesh_load): only the
+ * vertices and faces cross from the host. */
+sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
+                             const sym_options *options, sym_mesh_handle **out);
+
 /* Batched detection (no reference counterpart; the reference's detect() runs
  * one mesh per call, src/core/pipeline.cpp:27-47).  Runs sym_detect_fast on
  * every item, one host thread per worker context: each worker (its own CUDA

@@ -169,6 +169,15 @@ class FastResult(C.Structure):
                 ("tc_evaluations", C.c_double)]
 
 
+class PreparedOut(C.Structure):
+    _fields_ = [("context", ModelContext), ("vertex_count", C.c_uint64),
+                ("face_count", C.c_uint64), ("edge_count", C.c_uint64),
+                ("rejected_faces", C.c_uint64), ("faces", _i * 3), ("normals", _d * 3),
+                ("face_normals", _d * 3), ("weights", _d), ("neighbor_offsets", _u64),
+                ("neighbor_indices", _i), ("incident_offsets", _u64),
+                ("incident_indices", _i), ("edges", C.POINTER(Edge)), ("storage", C.c_void_p)]
+
+
 class BatchItem(C.Structure):
     _fields_ = [("mesh", C.c_void_p), ("sample", _i), ("sample_count", C.c_uint64),
                 ("options", C.POINTER(Options)), ("fast", C.POINTER(FastOptions)),
@@ -213,6 +222,9 @@ PROTOTYPES = [
     ("sym_detect_fast", C.c_int, [C.c_void_p, C.c_void_p, _i, C.c_uint64, P(Options),
                                   P(FastOptions), P(FastResult)]),
     ("sym_detect_fast_batch", C.c_int, [P(C.c_void_p), C.c_int32, P(BatchItem), C.c_uint64]),
+    ("sym_prepare", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(PreparedOut)]),
+    ("sym_prepared_release", None, [P(PreparedOut)]),
+    ("sym_mesh_load_raw", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(C.c_void_p)]),
     ("sym_context_stream", C.c_void_p, [C.c_void_p]),
     ("sym_meanshift6", C.c_int, [C.c_void_p, _d, C.c_uint64, P(C.c_int64), C.c_uint64, C.c_double,
                                  C.c_int32, C.c_int32, C.c_int32, _d, _u8, P(C.c_int32)]),

@@ -20,8 +20,8 @@ import numpy as np
 
 from . import abi
 from .mesh import Prepared, prepare
-from .types import (ClusterOutput, Features, Mesh, ModelContext, Options, Pairs, Rng, Selection,
-                    Topology, Verification, Votes, clusters_from_c, pairs_from_c,
+from .types import (ClusterOutput, Csr, Features, Mesh, ModelContext, Options, Pairs, Rng,
+                    Selection, Topology, Verification, Votes, clusters_from_c, pairs_from_c,
                     selection_from_c, verification_from_c, votes_from_c)
 
 
@@ -161,6 +161,42 @@ class Gb300Backend:
 
     def load_mesh(self, prepared: Prepared) -> "ResidentMesh":
         return ResidentMesh(self, prepared)
+
+    def prepare(self, mesh: Mesh, options: Options) -> Prepared:
+        """The reference's prepare() (no subdivision) on the GPU, sym_prepare:
+        bit-exact with mesh.prepare."""
+        view = mesh.view()
+        out = abi.PreparedOut()
+        _check(self._lib.sym_prepare(self._ctx, C.byref(view), C.byref(options.to_c()),
+                                     C.byref(out)))
+        try:
+            nv, nf, ne = int(out.vertex_count), int(out.face_count), int(out.edge_count)
+
+            def arr(ptr, n, dtype):
+                return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True) if n else \
+                    np.zeros(0, dtype)
+            faces = np.stack([arr(out.faces[k], nf, np.int32) for k in range(3)])
+            normals = np.stack([arr(out.normals[k], nv, np.float64) for k in range(3)])
+            fnorm = np.stack([arr(out.face_normals[k], nf, np.float64) for k in range(3)])
+            weights = arr(out.weights, nv, np.float64)
+            noff = arr(out.neighbor_offsets, nv + 1, np.uint64)
+            nidx = arr(out.neighbor_indices, int(noff[-1]), np.int32)
+            ioff = arr(out.incident_offsets, nv + 1, np.uint64)
+            iidx = arr(out.incident_indices, int(ioff[-1]), np.int32)
+            edges = np.ctypeslib.as_array(C.cast(out.edges, C.POINTER(C.c_int32)),
+                                          shape=(ne * 6,)).reshape(ne, 6).copy() if ne else \
+                np.zeros((0, 6), np.int32)
+            ctx = ModelContext(float(out.context.box_size), tuple(float(c) for c in out.context.center))
+            return Prepared(Mesh(mesh.vertices.copy(), faces),
+                            Topology(normals, fnorm, weights, Csr(noff, nidx), Csr(ioff, iidx), edges),
+                            ctx, int(out.rejected_faces))
+        finally:
+            self._lib.sym_prepared_release(C.byref(out))
+
+    def load_mesh_raw(self, mesh: Mesh, options: Options) -> "ResidentMesh":
+        """A resident mesh prepared on the GPU (sym_mesh_load_raw): only the
+        vertices and faces cross from the host."""
+        return ResidentMesh(self, None, raw=(mesh, options))
 
     @staticmethod
     def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
@@ -335,18 +371,28 @@ def detect(mesh: Mesh, options: Options, backend, progress=None) -> Result:
 class ResidentMesh:
     """A prepared mesh uploaded once to the device (sym_mesh_load)."""
 
-    def __init__(self, backend: Gb300Backend, prepared: Prepared):
+    def __init__(self, backend: Gb300Backend, prepared: Prepared, raw=None):
         self._lib = backend._lib
         self.prepared = prepared
-        self._views = (prepared.mesh.view(), prepared.topology.view(), prepared.context.to_c())
         h = C.c_void_p()
-        _check(self._lib.sym_mesh_load(backend._ctx, C.byref(self._views[0]),
-                                       C.byref(self._views[1]), C.byref(self._views[2]),
-                                       C.byref(h)))
+        if raw is not None:  # prepared on the GPU from the raw mesh
+            mesh, options = raw
+            self._raw = mesh
+            view = mesh.view()
+            _check(self._lib.sym_mesh_load_raw(backend._ctx, C.byref(view),
+                                               C.byref(options.to_c()), C.byref(h)))
+        else:
+            self._views = (prepared.mesh.view(), prepared.topology.view(),
+                           prepared.context.to_c())
+            _check(self._lib.sym_mesh_load(backend._ctx, C.byref(self._views[0]),
+                                           C.byref(self._views[1]), C.byref(self._views[2]),
+                                           C.byref(h)))
         self.handle = h
 
     def bytes(self) -> int:
         """Host-to-device bytes of one load."""
+        if self.prepared is None:
+            return int(self._raw.vertices.nbytes + self._raw.faces.nbytes)
         p = self.prepared
         return int(p.mesh.vertices.nbytes + p.mesh.faces.nbytes + p.topology.normals.nbytes +
                    p.topology.face_normals.nbytes + p.topology.weights.nbytes +

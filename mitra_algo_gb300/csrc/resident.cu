@@ -20,6 +20,7 @@
 #include "meanshift_fast.cuh"
 #include "rng.hpp"
 #include "verification.cuh"
+#include "prepare.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -748,6 +749,76 @@ sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_
   } catch (const sym::Error &e) {
     sym_error_text = e.what();
     return e.status;
+  }
+}
+
+sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
+                             const sym_options *options, sym_mesh_handle **out) {
+  if (!ctx || !mesh || !options || !out) return SYM_INVALID_ARGUMENT;
+  *out = nullptr;
+  sym_mesh_handle *h = nullptr;
+  try {
+    sym::Call call(ctx, "mesh_load_raw");
+    const sym::PreparedDevice p = sym::prepare_device(call, *mesh, *options);
+    h = new sym_mesh_handle();
+    h->ctx = ctx;
+    h->host = sym_mesh_view{};  // the vertices and faces live on the device only
+    h->model = p.context;
+    h->nv = p.nv, h->nf = p.nf, h->ne = p.ne, h->nbr_count = p.nbr_count;
+    h->host_edges.resize(p.ne);
+    const uint64_t nv = p.nv, nf = p.nf, ne = p.ne;
+    auto pad = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
+    uint64_t sizes[8] = {pad(24 * nv), pad(24 * nf), pad(24 * nv), pad(8 * nv), pad(12 * nf),
+                         pad(8 * (nv + 1)), pad(4 * h->nbr_count), pad(24 * ne)};
+    uint64_t total = 0;
+    for (auto b : sizes) total += b;
+    if (cudaMalloc(&h->block, total ? total : 256) != cudaSuccess)
+      sym::fail(SYM_CUDA_ERROR, "CUDA: mesh allocation failed");
+    char *q = h->block;
+    h->xyz = reinterpret_cast<double *>(q), q += sizes[0];
+    h->fn = reinterpret_cast<double *>(q), q += sizes[1];
+    h->vn = reinterpret_cast<double *>(q), q += sizes[2];
+    h->w = reinterpret_cast<double *>(q), q += sizes[3];
+    h->faces = reinterpret_cast<int32_t *>(q), q += sizes[4];
+    h->nbr_off = reinterpret_cast<uint64_t *>(q), q += sizes[5];
+    h->nbr = reinterpret_cast<int32_t *>(q), q += sizes[6];
+    h->edges = reinterpret_cast<sym_edge *>(q);
+    cudaStream_t st = ctx->stream;
+    auto d2d = [&](void *dst, const void *src, uint64_t bytes) {
+      if (bytes) SYM_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
+    };
+    d2d(h->xyz, p.xyz, 24 * nv);
+    d2d(h->fn, p.fn, 24 * nf);
+    d2d(h->vn, p.vn, 24 * nv);
+    d2d(h->w, p.w, 8 * nv);
+    d2d(h->faces, p.faces, 12 * nf);
+    d2d(h->nbr_off, p.nbr_off, 8 * (nv + 1));
+    d2d(h->nbr, p.nbr, 4 * h->nbr_count);
+    d2d(h->edges, p.edges, 24 * ne);
+    call.d2h(h->host_edges.data(), p.edges, 24 * ne);
+    if (nf >= (uint64_t(1) << 30)) sym::fail(SYM_INVALID_ARGUMENT, "too many faces for the LBVH");
+    h->lbvh = sym::lbvh_build(call, h->xyz, nv, h->faces, nf);
+    call.check_status("mesh_load_raw");
+    *out = h;
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    if (h) {
+      cudaStreamSynchronize(ctx->stream);
+      sym::lbvh_free(h->lbvh);
+      cudaFree(h->block);
+      delete h;
+    }
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    if (h) {
+      cudaStreamSynchronize(ctx->stream);
+      sym::lbvh_free(h->lbvh);
+      cudaFree(h->block);
+      delete h;
+    }
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
   }
 }
 
