@@ -362,28 +362,21 @@ def run_gpu(args):
         ms_fp32, res_fp32 = timed("fp32", args.steps, max(1, args.warmup // 2))
         barrier()
     clocks = clk.summary(local)
-    # e2e: pinned host buffers -> public ABI -> result read back, every step
-    p = prepared
-    pinned = {}
-    for name, arr in [("v", p.mesh.vertices), ("f", p.mesh.faces), ("vn", p.topology.normals),
-                      ("fn", p.topology.face_normals), ("w", p.topology.weights),
-                      ("no", p.topology.neighbors.offsets), ("ni", p.topology.neighbors.indices),
-                      ("e", np.ascontiguousarray(p.topology.edges, np.int32))]:
-        t = torch.from_numpy(np.ascontiguousarray(arr)).pin_memory()
-        pinned[name] = t.numpy()
-    from mitra_algo_gb300.mesh import Prepared
-    from mitra_algo_gb300.types import Csr, Mesh, Topology
-    pp = Prepared(Mesh(pinned["v"], pinned["f"]),
-                  Topology(pinned["vn"], pinned["fn"], pinned["w"], Csr(pinned["no"], pinned["ni"]),
-                           p.topology.incident_faces, pinned["e"]), p.context)
-    assert pp.mesh.vertices.ctypes.data == pinned["v"].ctypes.data  # still the pinned buffer
+    # e2e: the raw mesh (vertices and faces) in pinned host buffers -> the
+    # public ABI (sym_mesh_load_raw: GPU prepare + resident load, then
+    # sym_detect_fast) -> the result read back, every step
+    from mitra_algo_gb300.types import Mesh
+    pv = torch.from_numpy(np.ascontiguousarray(prepared.mesh.vertices)).pin_memory().numpy()
+    pf = torch.from_numpy(np.ascontiguousarray(prepared.mesh.faces)).pin_memory().numpy()
+    raw = Mesh(pv, pf)
+    assert raw.vertices.ctypes.data == pv.ctypes.data  # still the pinned buffer
     e2e_ms = []
     h2d = d2h = 0
     for i in range(args.warmup + args.steps):
         barrier()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        mesh_i = gpu.load_mesh(pp)
+        mesh_i = gpu.load_mesh_raw(raw, opts)
         r = gpu.detect_fast(mesh_i, sample, opts, precision="bf16", seeds=SEEDS,
                             max_iterations=ITERATIONS, polish_iterations=POLISH)
         b.record(stream)
@@ -440,7 +433,9 @@ def run_gpu(args):
         "stage_ms": {k: round(statistics.mean(x["stage_ms"][k] for x in res_bf16), 3)
                      for k in r["stage_ms"]},
         "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "path": "raw vertices and faces in pinned host memory -> sym_mesh_load_raw "
+                        "(GPU prepare, resident mesh) -> sym_detect_fast -> result on the host"},
         "roofline": {"kernel": "ms_tile_tc (BF16 tcgen05 mean-shift tile)", "bound": "hbm",
                      "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(gbs / pk["hbm_gbs"], 4),
