@@ -32,6 +32,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 from pathlib import Path
@@ -355,8 +356,7 @@ def run_gpu(args):
     # correctness / error run (untimed): FP64 re-run of 256 seeds
     err = {p: step(p, reference_seeds=256) for p in ("bf16", "fp32")}
     barrier()
-    with Clocks(str(ROOT / "gpurun_out" / "bench_clocks.csv") if (ROOT / "gpurun_out").exists()
-                else "/tmp/bench_clocks.csv") as clk:
+    with Clocks(os.path.join(tempfile.gettempdir(), f"bench_clocks_{os.getpid()}.csv")) as clk:
         ms_bf16, res_bf16 = timed("bf16", args.steps, args.warmup)
         barrier()
         ms_fp32, res_fp32 = timed("fp32", args.steps, max(1, args.warmup // 2))
