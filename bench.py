@@ -49,6 +49,8 @@ BANDWIDTH = 0.1
 SEEDS = 2048
 ITERATIONS = 300  # mean-shift approach-phase iterations (BF16, or FP32)
 POLISH = 30       # FP32 polish iterations (both forms)
+VOTE_CAP = 0      # votes entering the mean shift (0: all)
+WORKLOAD = "motif icosphere L6, rigid mode, 6-D votes"
 # DRAM bytes (read + write) per (seed tile, vote chunk) pair of ms_tile_tc,
 # from the ncu capture summarised in profiles/ms_tile_tc.md
 TRAFFIC_PER_CHUNK_PAIR = 8309.0
@@ -146,12 +148,25 @@ def batch_bench(gpu, n, workers):
             "results_equal": bool(same), "clock": "host wall clock, synchronous calls"}
 
 
-def workload(small=False):
+def workload(small=False, name="c2"):
     """The benchmark mesh and options; `small` is a level-5, 5,000-sample,
-    256-seed variant used for profiler captures."""
-    global SAMPLES, SEEDS
-    from mitra_algo_gb300.mesh import motif_sphere, prepare
+    256-seed variant used for profiler captures.  name "c3": the large
+    single mesh - a torus (R = 1, r = 0.3) of 1e6 triangles with 12 copies of
+    a seeded bump motif placed by rotations about its axis, 2 of them
+    mirrored, 200,000 samples, 4,096 seeds and a mean shift over 1e6
+    subsampled votes."""
+    global SAMPLES, SEEDS, VOTE_CAP, PAIR_THRESHOLD, WORKLOAD
+    from mitra_algo_gb300.mesh import motif_sphere, motif_torus, prepare
     from mitra_algo_gb300.types import Options
+    if name == "c3":
+        SAMPLES, SEEDS, VOTE_CAP, PAIR_THRESHOLD = 200_000, 4096, 1_000_000, 0.05
+        WORKLOAD = "motif torus 1e6 triangles, rigid mode, 6-D votes, 1e6 subsampled votes"
+        mesh = motif_torus(R=1.0, r=0.3, nu=1000, nv=500, copies=12, mirrored=2, noise=5e-4,
+                           seed=0)
+        opts = Options(sample_ratio=SAMPLES / mesh.vertex_count, pair_threshold=PAIR_THRESHOLD,
+                       bandwidth=BANDWIDTH, max_pairs=10 ** 9, max_votes=2 * 10 ** 9 - 1,
+                       max_clusters=20)
+        return prepare(mesh, opts), opts
     if small:
         SAMPLES, SEEDS = 5000, 256
     mesh = motif_sphere(level=5 if small else 6, bumps=12, folds=5, partial_shift=0.4,
@@ -163,12 +178,14 @@ def workload(small=False):
 
 
 def config(prepared, r=None):
-    c = {"workload": "motif icosphere L6, rigid mode, 6-D votes",
+    c = {"workload": WORKLOAD,
          "vertices": prepared.mesh.vertex_count, "faces": int(prepared.mesh.faces.shape[1]),
          "samples": SAMPLES, "pair_threshold": PAIR_THRESHOLD, "bandwidth": BANDWIDTH,
          "seeds": SEEDS, "l2": "flushed (256 MiB write) before every timed step"}
     if r:
         c.update({"pruned": int(r["pruned"]), "pairs": int(r["pairs"]), "votes": int(r["votes"])})
+    if VOTE_CAP:
+        c["vote_cap"] = VOTE_CAP
     return c
 
 
@@ -305,7 +322,7 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    prepared, opts = workload(args.small)
+    prepared, opts = workload(args.small, args.config)
     gpu = Gb300Backend(local)
     stream = torch.cuda.ExternalStream(gpu.stream_handle, device=torch.device("cuda", local))
     # sample: the reference's host RNG sampling (the input of the path)
@@ -318,7 +335,7 @@ def run_gpu(args):
     def step(precision, reference_seeds=0):
         return gpu.detect_fast(resident, sample, opts, precision=precision, seeds=SEEDS,
                                max_iterations=ITERATIONS, polish_iterations=POLISH,
-                               reference_seeds=reference_seeds)
+                               reference_seeds=reference_seeds, vote_cap=VOTE_CAP)
 
     if args.once:  # one warm-up and one measured pipeline run (profiler captures)
         step(args.once)
@@ -378,7 +395,8 @@ def run_gpu(args):
         a.record(stream)
         mesh_i = gpu.load_mesh_raw(raw, opts)
         r = gpu.detect_fast(mesh_i, sample, opts, precision="bf16", seeds=SEEDS,
-                            max_iterations=ITERATIONS, polish_iterations=POLISH)
+                            max_iterations=ITERATIONS, polish_iterations=POLISH,
+                            vote_cap=VOTE_CAP)
         b.record(stream)
         b.synchronize()
         mesh_i.close()
@@ -391,8 +409,9 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
     ms_bf16, ms_fp32, ms_e2e = ms.tolist()
-    batch = batch_bench(gpu, args.batch, args.batch_workers) if args.batch else None
-    refl = reflection_bench(gpu)
+    extra = args.config == "c2"
+    batch = batch_bench(gpu, args.batch, args.batch_workers) if args.batch and extra else None
+    refl = reflection_bench(gpu) if extra else None
     if rank != 0:
         return
     r = res_bf16[-1]
@@ -459,8 +478,9 @@ def run_gpu(args):
     }
     if batch:
         line["batch"] = batch
-    line["reflection"] = refl
-    if not args.no_cpu:
+    if refl:
+        line["reflection"] = refl
+    if not args.no_cpu and extra:
         line["cpu_baseline"] = cpu_estimate(prepared, opts, sample, r)
     print(json.dumps(line))
 
@@ -504,6 +524,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline estimate")
+    ap.add_argument("--config", choices=["c2", "c3"], default="c2",
+                    help="c2: the motif icosphere (default); c3: the 1e6-triangle torus "
+                         "(no batch, reflection or CPU legs)")
     ap.add_argument("--batch", type=int, default=48,
                     help="meshes of the uneven batch measurement (0: skip)")
     ap.add_argument("--batch-workers", type=int, default=4,

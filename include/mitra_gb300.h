@@ -309,6 +309,11 @@ typedef struct sym_fast_options {
    * transformations.cpp:17-73), [n, (d + n.c)/box] padded to 6-D with
    * zeros, decoded as the reference does (clustering.cpp:117-124) */
   int32_t mode;
+  /* 0: every vote.  Otherwise at most about vote_cap votes enter the mean
+   * shift: each pair (rigid) or plane vote (reflection) is kept with
+   * probability vote_cap / votes by a hash of its index and seed_rng,
+   * order preserved (a uniform subsample, the same for every precision) */
+  uint64_t vote_cap;
 } sym_fast_options;
 
 #define SYM_FAST_MAX_CLUSTERS 32

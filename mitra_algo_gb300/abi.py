@@ -143,7 +143,8 @@ class Metric(C.Structure):
 class FastOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("seeds", C.c_int32), ("seed_rng", C.c_uint64),
                 ("max_iterations", C.c_int32), ("polish_iterations", C.c_int32),
-                ("reference_seeds", C.c_int32), ("verify", C.c_int32), ("mode", C.c_int32)]
+                ("reference_seeds", C.c_int32), ("verify", C.c_int32), ("mode", C.c_int32),
+                ("vote_cap", C.c_uint64)]
 
 
 FAST_MAX_CLUSTERS = 32

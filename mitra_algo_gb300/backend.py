@@ -200,22 +200,24 @@ class Gb300Backend:
 
     @staticmethod
     def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                      reference_seeds, verify, mode="rigid"):
+                      reference_seeds, verify, mode="rigid", vote_cap=0):
         if mode not in ("rigid", "reflection"):
             raise ValueError(f"unknown detection mode {mode!r}")
         return abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
                                seed_rng, max_iterations, polish_iterations, reference_seeds,
-                               1 if verify else 0, 1 if mode == "reflection" else 0)
+                               1 if verify else 0, 1 if mode == "reflection" else 0,
+                               int(vote_cap))
 
     def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
                     seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
-                    reference_seeds=0, verify=True, mode="rigid") -> dict:
+                    reference_seeds=0, verify=True, mode="rigid", vote_cap=0) -> dict:
         """Throughput pipeline on a resident mesh (no reference counterpart);
         mode "rigid" (rotation + translation votes) or "reflection" (plane
-        votes)."""
+        votes); vote_cap > 0 subsamples the votes that enter the mean shift
+        to about that many."""
         sample = np.ascontiguousarray(sample, np.int32)
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                                reference_seeds, verify, mode)
+                                reference_seeds, verify, mode, vote_cap)
         res = abi.FastResult()
         _check(self._lib.sym_detect_fast(self._ctx, mesh.handle,
                                          sample.ctypes.data_as(C.POINTER(C.c_int32)), sample.size,

@@ -306,6 +306,18 @@ __global__ void plane_votes(const double *pos, uint64_t nv, const int32_t *pa, c
   for (int k = 0; k < 8; ++k) desc[v * 8 + k] = out[k];
 }
 
+// keep[i]: item i of n enters the subsample (probability p, from a hash of
+// i and the seed: the same items for every precision and every run).
+__global__ void subsample_flags(uint64_t n, double p, uint64_t seed, uint8_t *keep) {
+  const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t z = i + seed * 0x9E3779B97F4A7C15ull + 0x9E3779B97F4A7C15ull;  // splitmix64
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  keep[i] = double(z >> 11) * (1.0 / 9007199254740992.0) < p;
+}
+
 // K distinct vote indices drawn uniformly (Floyd's algorithm), ascending.
 std::vector<int64_t> draw_seeds(uint64_t q, uint64_t k, uint64_t seed) {
   std::mt19937_64 rng(seed);
@@ -400,6 +412,26 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   clock.mark(3);
   const bool reflection = fo.mode == SYM_REFLECTION;
   if (fo.mode != SYM_RIGID && !reflection) fail(SYM_INVALID_ARGUMENT, "unknown detection mode");
+  // uniform subsample of n items (the parallel arrays a and, when not null,
+  // b) to about vote_cap votes, order preserved; returns the kept count
+  auto subsample = [&](uint64_t n, uint64_t votes_per_item, int32_t *&a, int32_t *&b) -> uint64_t {
+    if (!fo.vote_cap || n * votes_per_item <= fo.vote_cap) return n;
+    const double p = double(fo.vote_cap) / double(n * votes_per_item);
+    uint8_t *keep = call.alloc<uint8_t>(n);
+    subsample_flags<<<blocks_for(n), kThreads, 0, st>>>(n, p, fo.seed_rng, keep);
+    check_launch();
+    call.launched();
+    int32_t *na = call.alloc<int32_t>(n), *nb = b ? call.alloc<int32_t>(n) : nullptr;
+    uint64_t *cnt = call.alloc<uint64_t>(2);
+    compact_values(call, keep, a, n, na, cnt);
+    if (b) compact_values(call, keep, b, n, nb, cnt + 1);
+    uint64_t kept = 0;
+    call.d2h(&kept, cnt, 8);
+    call.sync();
+    a = na, b = nb;
+    return kept;
+  };
+  if (!reflection) np = subsample(np, 2, pa, pb);
   int32_t *plane_list = nullptr;
   uint64_t q = 2 * np;
   if (reflection) {  // one vote per pair whose mirrored frames agree
@@ -415,6 +447,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     compact_indices(call, flags, np, plane_list, count);
     call.d2h(&q, count, 8);
     call.sync();
+    int32_t *none = nullptr;
+    q = subsample(q, 1, plane_list, none);
   }
   if (q > o.max_votes || q > uint64_t(std::numeric_limits<int32_t>::max()))
     fail(SYM_RUNTIME_ERROR, "Vote budget exceeded; lower --sample-ratio or tighten --pair-threshold");
@@ -673,7 +707,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
 extern "C" {
 
 void sym_fast_options_default(sym_fast_options *o) {
-  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID};
+  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0};
 }
 
 sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_topology_view *g,

@@ -269,3 +269,48 @@ def motif_sphere(level=6, bumps=12, folds=5, partial_shift=0.4, noise=1e-3, seed
     diag = np.linalg.norm(verts.max(0) - verts.min(0))
     verts = verts + rng.normal(0, noise * diag, verts.shape)
     return Mesh(verts.T.copy(), faces.T.copy())
+
+
+def motif_torus(R=1.0, r=0.3, nu=1000, nv=500, copies=12, mirrored=2, bumps=6, noise=0.0,
+                seed=0):
+    """Torus (tube radius r around a circle of radius R in the xy-plane) on an
+    nu x nv grid (2 nu nv triangles; 1,000 x 500 gives 1e6), displaced along
+    the tube normal by `copies` copies of one seeded motif of `bumps` Gaussian
+    bumps (amplitude 0.01-0.03, width 0.03-0.08 in tube arc length): each
+    copy sits at a seeded angle about z (a rotation of the torus onto
+    itself), the last `mirrored` of them reflected through the xy-plane;
+    Gaussian vertex noise of `noise` x bbox diagonal."""
+    rng = np.random.default_rng(seed)
+    amp = rng.uniform(0.01, 0.03, bumps)
+    sig = rng.uniform(0.03, 0.08, bumps)
+    du = rng.uniform(-0.15, 0.15, bumps)      # motif offsets: angle about z
+    dv = rng.uniform(-0.6, 0.6, bumps)        # angle around the tube
+    base_v = rng.uniform(-1.2, 1.2, copies)  # where each copy sits around the tube
+    at_u = (np.arange(copies) + rng.uniform(0.1, 0.9, copies)) * (2 * np.pi / copies)
+    u = 2 * np.pi * np.arange(nu) / nu
+    v = 2 * np.pi * np.arange(nv) / nv
+    U, V = np.meshgrid(u, v, indexing="ij")
+    disp = np.zeros_like(U)
+    for c in range(copies):
+        sgn = -1.0 if c >= copies - mirrored else 1.0
+        for a, s, ou, ov in zip(amp, sig, du, dv):
+            cu, cv = at_u[c] + ou, sgn * (base_v[c] + ov) if sgn < 0 else base_v[c] + ov
+            eu = np.angle(np.exp(1j * (U - cu))) * R       # arc lengths, wrapped
+            ev = np.angle(np.exp(1j * (V - cv))) * r
+            disp += a * np.exp(-(eu * eu + ev * ev) / (2 * s * s))
+    rad = r + disp
+    x = (R + rad * np.cos(V)) * np.cos(U)
+    y = (R + rad * np.cos(V)) * np.sin(U)
+    z = rad * np.sin(V)
+    verts = np.stack([x.ravel(), y.ravel(), z.ravel()], axis=1)
+    i = np.arange(nu)[:, None]
+    j = np.arange(nv)[None, :]
+    a = (i * nv + j).ravel()
+    b = (((i + 1) % nu) * nv + j).ravel()
+    c2 = (((i + 1) % nu) * nv + (j + 1) % nv).ravel()
+    d = (i * nv + (j + 1) % nv).ravel()
+    faces = np.concatenate([np.stack([a, b, c2], 1), np.stack([a, c2, d], 1)]).astype(np.int32)
+    if noise:
+        diag = np.linalg.norm(verts.max(0) - verts.min(0))
+        verts = verts + rng.normal(0, noise * diag, verts.shape)
+    return Mesh(verts.T.copy(), faces.T.copy())
