@@ -150,3 +150,21 @@ def test_reflection_fast_verification_matches_exact(refl):
     assert np.all(np.abs(np.array(r["coverage"]) - exact.coverage) <= 5e-3), \
         (r["coverage"], exact.coverage)
     assert np.allclose(r["rms"], exact.rms, rtol=1e-2, atol=1e-9 * p.context.box_size)
+
+
+def test_vote_cap_subsamples_uniformly_and_deterministically(fast):
+    gpu, p, opts, runs = fast
+    full = runs["bf16"]["votes"]
+    cap = full // 4
+    sample = gpu.select(p.mesh, gpu.curvature(p.mesh, p.topology, opts), p.topology.weights, opts,
+                        Rng(opts.seed)).sample
+    resident = gpu.load_mesh(p)
+    kw = dict(seeds=128, max_iterations=60, polish_iterations=10, vote_cap=cap)
+    a = gpu.detect_fast(resident, sample, opts, precision="bf16", **kw)
+    b = gpu.detect_fast(resident, sample, opts, precision="bf16", **kw)
+    c = gpu.detect_fast(resident, sample, opts, precision="fp32", **kw)
+    resident.close()
+    assert a["pairs"] == runs["bf16"]["pairs"]          # every pair is still formed
+    assert abs(a["votes"] - cap) <= 0.02 * cap            # ~cap votes enter the mean shift
+    assert a["votes"] == b["votes"] == c["votes"]         # the same subsample every run
+    assert a["rotation"] == b["rotation"] and a["support"] == b["support"]
