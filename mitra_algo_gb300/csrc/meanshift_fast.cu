@@ -185,12 +185,13 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
     __syncthreads();
     uint64_t rest = q - c * kChunk;
     int n = rest < uint64_t(kChunk) ? int(rest) : kChunk;
-    // the polish (NEWTON) also skips per warp: a warp none of whose 32 seeds
-    // lies within the bandwidth of the chunk's box would only add zeros.
-    // The approach instances keep the tile granularity of the tensor kernel
-    // (one 128-seed tile per chunk), so the two forms of the approach make
-    // the same seed-vote evaluations.
-    const bool warp_needs = !NEWTON || __any_sync(0xffffffffu, live && g <= skip_gap2);
+    // the polish (NEWTON) and the support count (COUNT) also skip per warp:
+    // a warp none of whose 32 seeds lies within the bandwidth of the chunk's
+    // box would only add zeros.  The approach instance keeps the tile
+    // granularity of the tensor kernel (one 128-seed tile per chunk), so the
+    // two forms of the approach make the same seed-vote evaluations.
+    const bool warp_needs =
+        !(NEWTON || COUNT) || __any_sync(0xffffffffu, live && g <= skip_gap2);
     done += n;
     for (int j = 0; j < (warp_needs ? n : 0); ++j) {
       T e[6], d2 = 0;

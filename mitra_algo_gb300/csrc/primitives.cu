@@ -99,10 +99,15 @@ __global__ void radix_histogram(const uint64_t *keys, uint64_t n, int shift, uin
 
 // Stable scatter: warp w ranks its 256 keys round by round (in input order),
 // warps are then ordered by their index, blocks by the scanned histogram.
-__global__ void radix_scatter(const uint64_t *keys, const int32_t *vals, uint64_t n, int shift,
-                              const uint64_t *offsets, unsigned blocks, uint64_t *keys_out,
-                              int32_t *vals_out) {
+// The block's keys are first placed in digit order in shared memory, so the
+// global writes of each digit are one consecutive run.
+__global__ void __launch_bounds__(kSortWarps * 32) radix_scatter(
+    const uint64_t *keys, const int32_t *vals, uint64_t n, int shift, const uint64_t *offsets,
+    unsigned blocks, uint64_t *keys_out, int32_t *vals_out) {
   __shared__ unsigned warp_count[kSortWarps][256];
+  __shared__ unsigned digit_start[256];
+  __shared__ uint64_t skey[kSortTile];
+  __shared__ int32_t sval[kSortTile];
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int d = threadIdx.x; d < kSortWarps * 256; d += blockDim.x)
     (&warp_count[0][0])[d] = 0;
@@ -126,22 +131,38 @@ __global__ void radix_scatter(const uint64_t *keys, const int32_t *vals, uint64_
     __syncwarp();
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < 256; d += blockDim.x) {
-    unsigned run = 0;
+  // per digit: each warp's start among the block's keys of that digit, and
+  // the digit's count; then the digits' starts in the block
+  unsigned digit_total = 0;
+  if (threadIdx.x < 256) {
+    const int d = threadIdx.x;
     for (int w = 0; w < kSortWarps; ++w) {
       unsigned c = warp_count[w][d];
-      warp_count[w][d] = run;
-      run += c;
+      warp_count[w][d] = digit_total;
+      digit_total += c;
     }
   }
+  uint64_t all;
+  const uint64_t start = block_exclusive(digit_total, all);  // blockDim.x == 256
+  if (threadIdx.x < 256) digit_start[threadIdx.x] = unsigned(start);
   __syncthreads();
   for (int r = 0; r < kSortRounds; ++r) {
     uint64_t i = base + r * 32 + lane;
     if (i >= n) continue;
     unsigned digit = unsigned((key[r] >> shift) & 0xff);
-    uint64_t dst = offsets[uint64_t(digit) * blocks + blockIdx.x] + warp_count[warp][digit] + rank[r];
-    keys_out[dst] = key[r];
-    vals_out[dst] = val[r];
+    unsigned pos = digit_start[digit] + warp_count[warp][digit] + rank[r];
+    skey[pos] = key[r];
+    sval[pos] = val[r];
+  }
+  __syncthreads();
+  const uint64_t block_base = uint64_t(blockIdx.x) * kSortTile;
+  const unsigned count = unsigned(n - block_base < uint64_t(kSortTile) ? n - block_base : kSortTile);
+  for (unsigned j = threadIdx.x; j < count; j += blockDim.x) {
+    const uint64_t k = skey[j];
+    const unsigned digit = unsigned((k >> shift) & 0xff);
+    const uint64_t dst = offsets[uint64_t(digit) * blocks + blockIdx.x] + (j - digit_start[digit]);
+    keys_out[dst] = k;
+    vals_out[dst] = sval[j];
   }
 }
 
