@@ -18,8 +18,10 @@ One step = the whole hot path on one mesh: curvature, prune, exact pairing,
            device time from CUDA events on the library's stream, L2 flushed
            (256 MiB write) before every step;
   e2e    - meshes/s through the public C ABI from pinned host buffers: every
-           step uploads the mesh (sym_mesh_load), runs sym_detect_fast and
-           reads the result back.
+           step uploads the raw mesh (sym_mesh_load_raw: GPU prepare), runs
+           sym_detect_fast_sampled (the area-weighted sample drawn on the
+           device from the options' seed, then the whole path) and reads the
+           result back.
 
 `--impl reference` times the reference's CPU path (oracle/_ref when it was
 built on this machine, else the oracle's restatement of it) on bounded
@@ -381,7 +383,8 @@ def run_gpu(args):
     clocks = clk.summary(local)
     # e2e: the raw mesh (vertices and faces) in pinned host buffers -> the
     # public ABI (sym_mesh_load_raw: GPU prepare + resident load, then
-    # sym_detect_fast) -> the result read back, every step
+    # sym_detect_fast_sampled: GPU sampling + the path) -> the result read
+    # back, every step
     from mitra_algo_gb300.types import Mesh
     pv = torch.from_numpy(np.ascontiguousarray(prepared.mesh.vertices)).pin_memory().numpy()
     pf = torch.from_numpy(np.ascontiguousarray(prepared.mesh.faces)).pin_memory().numpy()
@@ -394,15 +397,16 @@ def run_gpu(args):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         mesh_i = gpu.load_mesh_raw(raw, opts)
-        r = gpu.detect_fast(mesh_i, sample, opts, precision="bf16", seeds=SEEDS,
+        r = gpu.detect_fast(mesh_i, None, opts, precision="bf16", seeds=SEEDS,
                             max_iterations=ITERATIONS, polish_iterations=POLISH,
                             vote_cap=VOTE_CAP)
         b.record(stream)
         b.synchronize()
         mesh_i.close()
+        assert r["sampled"] == len(sample)  # the host-drawn sample of the other legs
         if i >= args.warmup:
             e2e_ms.append(a.elapsed_time(b))
-            h2d = mesh_i.bytes() + sample.nbytes + r["h2d_bytes"]
+            h2d = mesh_i.bytes() + r["h2d_bytes"]
             d2h = r["d2h_bytes"] + ctypes_sizeof_result()
     barrier()
     ms = torch.tensor([ms_bf16, ms_fp32, statistics.mean(e2e_ms)], device=f"cuda:{local}")
@@ -454,7 +458,8 @@ def run_gpu(args):
         "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": "raw vertices and faces in pinned host memory -> sym_mesh_load_raw "
-                        "(GPU prepare, resident mesh) -> sym_detect_fast -> result on the host"},
+                        "(GPU prepare, resident mesh) -> sym_detect_fast_sampled (GPU "
+                        "sampling from the seed, then the whole path) -> result on the host"},
         "roofline": {"kernel": "ms_tile_tc (BF16 tcgen05 mean-shift tile)", "bound": "hbm",
                      "achieved": round(gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(gbs / pk["hbm_gbs"], 4),

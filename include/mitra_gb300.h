@@ -232,9 +232,21 @@ sym_status sym_curvature(sym_context *ctx, const sym_mesh_view *mesh,
                          const sym_options *options,
                          const sym_features_out *out);
 
-/* Backend::select (pipeline.h:59-60; src/cpu/selection.cpp:15-29).  Area-
- * weighted sampling runs on the host with `rng` (src/core/sampling.cpp:5-24),
- * the anisotropy prune and its stable compaction run on the GPU. */
+/* The reference's sample_vertices (src/core/sampling.cpp:5-24,
+ * include/symmetry/sampling.h:6-7) on the GPU: one draw of `rng` per
+ * positive weight in vertex order, exponential keys -log(u)/w, the
+ * ceil(count * ratio) smallest (ties by vertex id), ids ascending.  The ids
+ * and the engine state left in `rng` are bit-exact with the host function:
+ * the engine runs on the device, and keys within a relative 2^-32 of the
+ * selection boundary are re-evaluated with the host's std::log.  `weights`
+ * (count doubles) and `sample` (room for count ids) are host arrays. */
+sym_status sym_sample_vertices(sym_context *ctx, const double *weights, uint64_t count,
+                               double ratio, sym_rng *rng, int32_t *sample,
+                               uint64_t *sample_count);
+
+/* Backend::select (pipeline.h:59-60; src/cpu/selection.cpp:15-29).  The
+ * area-weighted sample (sym_sample_vertices, with `rng`), the anisotropy
+ * prune and its stable compaction all run on the GPU. */
 sym_status sym_select(sym_context *ctx, const sym_mesh_view *mesh,
                       const sym_features_view *features, const double *weights,
                       uint64_t weight_count, const sym_options *options,
@@ -318,7 +330,7 @@ typedef struct sym_fast_options {
 
 #define SYM_FAST_MAX_CLUSTERS 32
 typedef struct sym_fast_result {
-  uint64_t pruned, pairs, votes, modes, clusters;
+  uint64_t sampled, pruned, pairs, votes, modes, clusters;
   int32_t iterations, polish_iterations;
   /* relative error of each mode against FP64, over the reference seeds that
    * converged (Newton, a well-defined mode) in both runs (modes_compared of
@@ -354,6 +366,14 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
                            const int32_t *sample, uint64_t sample_count,
                            const sym_options *options,
                            const sym_fast_options *fast, sym_fast_result *out);
+/* sym_detect_fast with the sample drawn on the device from the mesh's
+ * weights, as the reference's detect() draws it (src/core/pipeline.cpp:25,
+ * src/cpu/selection.cpp:20): a std::mt19937_64 seeded with options->seed and
+ * sym_sample_vertices' keys -- the same ids, bit-exact.  out->sampled gives
+ * their number. */
+sym_status sym_detect_fast_sampled(sym_context *ctx, sym_mesh_handle *mesh,
+                                   const sym_options *options,
+                                   const sym_fast_options *fast, sym_fast_result *out);
 
 /* GPU mesh preparation: the reference's prepare() (src/core/prepare.cpp:
  * 102-149) without subdivision (options->subdivide must be 0) and its

@@ -151,8 +151,9 @@ FAST_MAX_CLUSTERS = 32
 
 
 class FastResult(C.Structure):
-    _fields_ = [("pruned", C.c_uint64), ("pairs", C.c_uint64), ("votes", C.c_uint64),
-                ("modes", C.c_uint64), ("clusters", C.c_uint64), ("iterations", C.c_int32),
+    _fields_ = [("sampled", C.c_uint64), ("pruned", C.c_uint64), ("pairs", C.c_uint64),
+                ("votes", C.c_uint64), ("modes", C.c_uint64), ("clusters", C.c_uint64),
+                ("iterations", C.c_int32),
                 ("polish_iterations", C.c_int32), ("mode_error_max", C.c_double),
                 ("mode_error_mean", C.c_double), ("modes_compared", C.c_uint64),
                 ("modes_within", C.c_uint64), ("stage_ms", C.c_double * 8),
@@ -207,6 +208,8 @@ PROTOTYPES = [
     ("sym_curvature", C.c_int, [C.c_void_p, P(MeshView), P(TopologyView), P(Options), P(FeaturesOut)]),
     ("sym_select", C.c_int, [C.c_void_p, P(MeshView), P(FeaturesView), _d, C.c_uint64,
                              P(Options), P(Rng), P(Selection)]),
+    ("sym_sample_vertices", C.c_int, [C.c_void_p, _d, C.c_uint64, C.c_double, P(Rng), _i,
+                                      P(C.c_uint64)]),
     ("sym_pairing", C.c_int, [C.c_void_p, P(MeshView), P(FeaturesView), _i, C.c_uint64,
                               P(ModelContext), P(Options), P(PairsOut)]),
     ("sym_transformations", C.c_int, [C.c_void_p, P(MeshView), P(FeaturesView), P(PairsView),
@@ -222,6 +225,8 @@ PROTOTYPES = [
     ("sym_fast_options_default", None, [P(FastOptions)]),
     ("sym_detect_fast", C.c_int, [C.c_void_p, C.c_void_p, _i, C.c_uint64, P(Options),
                                   P(FastOptions), P(FastResult)]),
+    ("sym_detect_fast_sampled", C.c_int, [C.c_void_p, C.c_void_p, P(Options), P(FastOptions),
+                                          P(FastResult)]),
     ("sym_detect_fast_batch", C.c_int, [P(C.c_void_p), C.c_int32, P(BatchItem), C.c_uint64]),
     ("sym_prepare", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(PreparedOut)]),
     ("sym_prepared_release", None, [P(PreparedOut)]),

@@ -214,15 +214,33 @@ class Gb300Backend:
         """Throughput pipeline on a resident mesh (no reference counterpart);
         mode "rigid" (rotation + translation votes) or "reflection" (plane
         votes); vote_cap > 0 subsamples the votes that enter the mean shift
-        to about that many."""
-        sample = np.ascontiguousarray(sample, np.int32)
+        to about that many.  `sample` None draws the area-weighted sample on
+        the device from options.seed, as detect() does (sym_detect_fast_sampled)."""
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
                                 reference_seeds, verify, mode, vote_cap)
         res = abi.FastResult()
+        if sample is None:
+            _check(self._lib.sym_detect_fast_sampled(self._ctx, mesh.handle,
+                                                     C.byref(options.to_c()), C.byref(fo),
+                                                     C.byref(res)))
+            return self._fast_dict(res)
+        sample = np.ascontiguousarray(sample, np.int32)
         _check(self._lib.sym_detect_fast(self._ctx, mesh.handle,
                                          sample.ctypes.data_as(C.POINTER(C.c_int32)), sample.size,
                                          C.byref(options.to_c()), C.byref(fo), C.byref(res)))
         return self._fast_dict(res)
+
+    def sample_vertices(self, weights, ratio: float, rng: Rng) -> np.ndarray:
+        """sym_sample_vertices: the reference's sample_vertices
+        (src/core/sampling.cpp:5-24) on the GPU; advances `rng` like it."""
+        w = np.ascontiguousarray(weights, np.float64)
+        out = np.empty(max(1, w.size), np.int32)
+        count = C.c_uint64()
+        _check(self._lib.sym_sample_vertices(self._ctx, w.ctypes.data_as(C.POINTER(C.c_double)),
+                                             w.size, float(ratio), C.byref(rng.state),
+                                             out.ctypes.data_as(C.POINTER(C.c_int32)),
+                                             C.byref(count)))
+        return out[:count.value].copy()
 
     def detect_fast_batch(self, jobs, workers=4, precision="bf16", seeds=2048, seed_rng=7,
                           max_iterations=100, polish_iterations=100, verify=True,
@@ -257,8 +275,9 @@ class Gb300Backend:
     @staticmethod
     def _fast_dict(res) -> dict:
         n = int(res.clusters)
-        out = {k: getattr(res, k) for k in ("pruned", "pairs", "votes", "modes", "clusters",
-                                            "iterations", "polish_iterations", "mode_error_max",
+        out = {k: getattr(res, k) for k in ("sampled", "pruned", "pairs", "votes", "modes",
+                                            "clusters", "iterations", "polish_iterations",
+                                            "mode_error_max",
                                             "mode_error_mean", "modes_compared", "modes_within",
                                             "mean_shift_pairs",
                                             "seed_iterations", "launches", "h2d_bytes",

@@ -4,6 +4,7 @@
 // exception crosses the boundary.
 #include "common.cuh"
 #include "rng.hpp"
+#include "sampling.cuh"
 
 #include <cstdlib>
 #include <new>
@@ -12,9 +13,9 @@
 namespace sym {
 void curvature_host(Call &, const sym_mesh_view &, const sym_topology_view &, const sym_options &,
                     const sym_features_out &);
-void select_host(Call &, const sym_mesh_view &, const sym_features_view &, const double *,
-                 uint64_t, const sym_options &, sym_rng *, std::vector<int32_t> &,
-                 std::vector<int32_t> &);
+void select_device(Call &, const sym_mesh_view &, const sym_features_view &, const double *,
+                   uint64_t, const sym_options &, sym_rng *, std::vector<int32_t> &,
+                   std::vector<int32_t> &);
 void pairing_host(Call &, const sym_mesh_view &, const sym_features_view &, const int32_t *,
                   uint64_t, const sym_model_context &, const sym_options &, std::vector<int32_t> &,
                   std::vector<int32_t> &);
@@ -171,7 +172,7 @@ sym_status sym_select(sym_context *ctx, const sym_mesh_view *mesh,
   return guarded([&] {
     sym::Call call(ctx, "sample_prune");
     std::vector<int32_t> sample, pruned;
-    sym::select_host(call, *mesh, *features, weights, weight_count, *options, rng, sample, pruned);
+    sym::select_device(call, *mesh, *features, weights, weight_count, *options, rng, sample, pruned);
     size_t bytes = (sample.size() + pruned.size()) * 4 + 64;
     char *block = static_cast<char *>(host_alloc(bytes));
     if (!block) throw std::bad_alloc();
@@ -182,6 +183,21 @@ sym_status sym_select(sym_context *ctx, const sym_mesh_view *mesh,
     out->pruned_count = pruned.size();
     std::copy(sample.begin(), sample.end(), out->sample);
     std::copy(pruned.begin(), pruned.end(), out->pruned);
+  });
+}
+
+sym_status sym_sample_vertices(sym_context *ctx, const double *weights, uint64_t count,
+                               double ratio, sym_rng *rng, int32_t *sample,
+                               uint64_t *sample_count) {
+  if (!ctx || !rng || !sample_count || (count && (!weights || !sample))) return null_args();
+  return guarded([&] {
+    sym::Call call(ctx, "sample");
+    double *w = call.upload(weights, count);
+    int32_t *d = call.alloc<int32_t>(count);
+    const uint64_t n = sym::sample_device(call, w, count, ratio, *rng, d);
+    call.d2h(sample, d, n * sizeof(int32_t));
+    call.sync();
+    *sample_count = n;
   });
 }
 

@@ -1,6 +1,6 @@
 // SPDX-License-Identifier: MPL-2.0
-// Stage (b), first half: anisotropy prune of the host sample and curvature
-// pair voting candidates.
+// Stage (b), first half: the area-weighted sample (on the device,
+// sampling.cu), its anisotropy prune, and curvature pair voting candidates.
 //
 // Reference: src/cpu/selection.cpp:15-29, src/cpu/pairing.cpp:14-35 (CPU);
 // src/cuda/backend.cu:21-31,128-339 (existing GPU path).
@@ -23,7 +23,7 @@
 // the others take the FP64 test.
 #include "common.cuh"
 #include "primitives.cuh"
-#include "rng.hpp"
+#include "sampling.cuh"
 
 #include <cmath>
 #include <limits>
@@ -375,25 +375,26 @@ void prune_device(Call &call, const int32_t *sample, uint64_t count, const doubl
   compact_values(call, flags, sample, count, pruned, pruned_count);
 }
 
-void select_host(Call &call, const sym_mesh_view &m, const sym_features_view &f,
-                 const double *weights, uint64_t weight_count, const sym_options &o,
-                 sym_rng *rng, std::vector<int32_t> &sample, std::vector<int32_t> &pruned) {
+void select_device(Call &call, const sym_mesh_view &m, const sym_features_view &f,
+                   const double *weights, uint64_t weight_count, const sym_options &o,
+                   sym_rng *rng, std::vector<int32_t> &sample, std::vector<int32_t> &pruned) {
   if (weight_count != m.vertices.count || f.count != weight_count)
     fail(SYM_INVALID_ARGUMENT, "SoA component lengths differ");
-  auto engine = load_rng(rng);
-  sample = sample_vertices(weights, weight_count, o.sample_ratio, engine);
-  store_rng(engine, rng);
+  const uint64_t n = weight_count;
+  double *w = call.upload(weights, n);
+  int32_t *dsample = call.alloc<int32_t>(n);
+  const uint64_t count = sample_device(call, w, n, o.sample_ratio, *rng, dsample);
+  sample.resize(count);
   pruned.clear();
-  uint64_t n = weight_count, count = sample.size();
   if (!count) return;
   double *kmin = call.upload(f.kmin, n);
   double *kmax = call.upload(f.kmax, n);
   uint8_t *valid = call.upload(f.valid, n);
-  int32_t *dsample = call.upload(sample.data(), count);
   int32_t *dpruned = call.alloc<int32_t>(count);
   uint64_t *dcount = call.alloc<uint64_t>(1);
   prune_device(call, dsample, count, kmin, kmax, valid, o.prune, dpruned, dcount);
   uint64_t kept = 0;
+  call.d2h(sample.data(), dsample, count * 4);
   call.d2h(&kept, dcount, 8);
   call.sync();
   pruned.resize(kept);

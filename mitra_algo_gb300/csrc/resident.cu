@@ -19,6 +19,7 @@
 #include "primitives.cuh"
 #include "meanshift_fast.cuh"
 #include "rng.hpp"
+#include "sampling.cuh"
 #include "verification.cuh"
 #include "prepare.cuh"
 
@@ -375,8 +376,11 @@ private:
   cudaEvent_t ev_[10];
 };
 
+// `sample` (ns host ids) is the area-weighted sample; with sample_rng set it
+// is drawn here instead, on the device from the mesh's weights (sampling.cu).
 void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t ns,
-                 const sym_options &o, const sym_fast_options &fo, sym_fast_result &r) {
+                 const sym_options &o, const sym_fast_options &fo, sym_fast_result &r,
+                 sym_rng *sample_rng = nullptr) {
   r = sym_fast_result{};
   cudaStream_t st = call.stream();
   StageClock clock(st);
@@ -394,14 +398,21 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   curvature_device(call, h.xyz, nv, h.fn, h.nf, h.vn, h.nbr_off, h.nbr, h.nbr_count, h.edges, h.ne,
                    o.smoothing, f, h.host_edges.data());
   clock.mark(1);
-  // ---- prune of the host sample
-  int32_t *dsample = call.upload(sample, ns);
+  // ---- area-weighted sample and its prune
+  int32_t *dsample = nullptr;
+  if (sample_rng) {
+    dsample = call.alloc<int32_t>(nv);
+    ns = sample_device(call, h.w, nv, o.sample_ratio, *sample_rng, dsample);
+  } else {
+    dsample = call.upload(sample, ns);
+  }
   int32_t *pruned = call.alloc<int32_t>(ns);
   uint64_t *pcount = call.alloc<uint64_t>(1);
   prune_device(call, dsample, ns, f.kmin, f.kmax, valid, o.prune, pruned, pcount);
   uint64_t s = 0;
   call.d2h(&s, pcount, 8);
   call.sync();
+  r.sampled = ns;
   r.pruned = s;
   clock.mark(2);
   // ---- (b) pairing + 6-D votes
@@ -975,6 +986,27 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh, const int32_
       if (sample[i] < 0 || uint64_t(sample[i]) >= mesh->nv)
         sym::fail(SYM_INVALID_ARGUMENT, "sample vertex index out of range");
     sym::detect_fast(call, *mesh, sample, sample_count, *options, *fast, *out);
+    out->launches = ctx->metrics.current.custom_launches;
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
+  }
+}
+
+sym_status sym_detect_fast_sampled(sym_context *ctx, sym_mesh_handle *mesh,
+                                   const sym_options *options, const sym_fast_options *fast,
+                                   sym_fast_result *out) {
+  if (!ctx || !mesh || !options || !fast || !out) return SYM_INVALID_ARGUMENT;
+  try {
+    sym::Call call(ctx, "detect_fast");
+    sym::validate_prepare_options(*options);
+    sym_rng rng;
+    sym_rng_seed(&rng, options->seed);  // the engine detect() seeds (pipeline.cpp:25)
+    sym::detect_fast(call, *mesh, nullptr, 0, *options, *fast, *out, &rng);
     out->launches = ctx->metrics.current.custom_launches;
     return SYM_OK;
   } catch (const sym::Error &e) {

@@ -467,6 +467,18 @@ uint64_t oracle_rng_next(sym_rng *r) {
   return x;
 }
 
+// The reference's sample_vertices alone (src/core/sampling.cpp:5-24);
+// `out` has room for n ids.
+int oracle_sample_vertices(const double *w, uint64_t n, double ratio, sym_rng *r, int32_t *out,
+                           uint64_t *count) {
+  auto e = load_rng(r);
+  auto s = sample_vertices(w, n, ratio, e);
+  store_rng(e, r);
+  std::copy(s.begin(), s.end(), out);
+  *count = s.size();
+  return 0;
+}
+
 double oracle_triangle_distance2(const double *q) {
   return triangle_d2({q[0], q[1], q[2]}, {q[3], q[4], q[5]}, {q[6], q[7], q[8]},
                      {q[9], q[10], q[11]});

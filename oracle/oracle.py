@@ -37,6 +37,8 @@ _PROTOS = [
     ("oracle_rng_seed", None, [_P(abi.Rng), C.c_uint64]),
     ("oracle_rng_next", C.c_uint64, [_P(abi.Rng)]),
     ("oracle_triangle_distance2", C.c_double, [_P(C.c_double)]),
+    ("oracle_sample_vertices", C.c_int, [_P(C.c_double), C.c_uint64, C.c_double, _P(abi.Rng),
+                                         _P(C.c_int32), _P(C.c_uint64)]),
     ("oracle_curvature", C.c_int, [_P(abi.MeshView), _P(abi.TopologyView), _P(abi.Options),
                                    _P(abi.FeaturesOut)]),
     ("oracle_select", C.c_int, [_P(abi.MeshView), _P(abi.FeaturesView), _P(C.c_double),
@@ -118,6 +120,16 @@ class OracleBackend:
         _check(lib().oracle_curvature(C.byref(mesh.view()), C.byref(topo.view()),
                                       C.byref(options.to_c()), C.byref(f.out_view())))
         return f
+
+    def sample_vertices(self, weights, ratio: float, rng: Rng) -> np.ndarray:
+        """The reference's sample_vertices (src/core/sampling.cpp:5-24)."""
+        w = np.ascontiguousarray(weights, np.float64)
+        out = np.empty(max(1, w.size), np.int32)
+        count = C.c_uint64()
+        lib().oracle_sample_vertices(w.ctypes.data_as(_P(C.c_double)), w.size, float(ratio),
+                                     C.byref(rng.state), out.ctypes.data_as(_P(C.c_int32)),
+                                     C.byref(count))
+        return out[:count.value].copy()
 
     def select(self, mesh: Mesh, features: Features, weights, options: Options, rng: Rng):
         w = np.ascontiguousarray(weights, np.float64)

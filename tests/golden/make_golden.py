@@ -397,6 +397,49 @@ def select_cases():
     save("stage_select", record)
 
 
+def sampling_draw_logs(n, seed=42):
+    """-log(u) of the first n draws of std::mt19937_64(seed), u as
+    src/core/sampling.cpp:12-13 forms it."""
+    r = oracle.rng(seed)
+    return np.array([-math.log(((r.next() >> 11) + 0.5) / 9007199254740992.0)
+                     for _ in range(n)])
+
+
+def sampling_cases():
+    """Area-weighted sampling alone (src/core/sampling.cpp:5-24) through the
+    reference's select(): mixed weights (zero, negative, NaN and infinite
+    ones), ratio edges, all-zero weights, and keys packed closer than 2^-32
+    of each other around the selection boundary (weights -log(u) (1 + i
+    2^-46), so the keys fall in i order, 128 ulps apart)."""
+    g = np.random.default_rng(2024)
+    mixed = g.lognormal(0.0, 1.0, 6000)
+    mixed[::10] = 0.0
+    mixed[3::17] = -1.0
+    mixed[5], mixed[7] = np.nan, np.inf
+    uniform = g.uniform(0.5, 2.0, 1000)
+    tight = sampling_draw_logs(4000) * (1.0 + np.arange(4000) * 2.0 ** -46)
+    cases = [("mixed_weights", mixed, 0.3), ("ratio_one", uniform, 1.0),
+             ("ratio_tiny", uniform, 0.001), ("ratio_zero", uniform, 0.0),
+             ("all_zero", np.zeros(500), 0.5), ("tight_keys", tight, 0.4)]
+    record = {}
+    for idx, (name, w, ratio) in enumerate(cases):
+        n = w.size
+        inputs = {"vx": np.zeros(n), "vy": np.zeros(n), "vz": np.zeros(n),
+                  "valid": np.ones(n, np.uint8), "kmin": np.full(n, 0.1), "kmax": np.ones(n),
+                  "weights": w, **options(sample_ratio=ratio, seed=42)}
+        out = oracle.run_reference("select", inputs)
+        p = f"c{idx}_"
+        record[p + "name"] = np.array(name)
+        record[p + "in_weights"] = w
+        record[p + "in_sample_ratio"] = inputs["sample_ratio"]
+        record[p + "in_seed"] = inputs["seed"]
+        record[p + "sample"] = out["sample"]
+        record[p + "rng_after_select"] = np.array(symd.text(out, "rng_after_select"))
+        print(f"  sampling {name}: sample {out['sample'].size} of {n}")
+    record["count"] = np.array(len(cases))
+    save("stage_sampling", record)
+
+
 def triangle_cases():
     """Point-triangle distances: the reference's geometry.cpp KATs and 1,024
     random queries with degenerate triangles (cuda_verification.cpp:79-100)."""
@@ -431,6 +474,7 @@ if __name__ == "__main__":
     rng_case()
     triangle_cases()
     select_cases()
+    sampling_cases()
     pairing_cases()
     transformation_cases()
     clustering_cases()

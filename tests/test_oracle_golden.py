@@ -56,6 +56,15 @@ def test_select(case, oracle_backend):
     assert rng.text() == str(case["out"]["rng_after_select"])
 
 
+@pytest.mark.parametrize("case", golden_cases("stage_sampling"), ids=lambda c: c["name"])
+def test_sampling(case, oracle_backend):
+    d = case["in"]
+    rng = oracle.rng(int(d["seed"][0]))
+    got = oracle_backend.sample_vertices(d["weights"], float(d["sample_ratio"][0]), rng)
+    same_array(got, case["out"]["sample"], "sample")
+    assert rng.text() == str(case["out"]["rng_after_select"])
+
+
 @pytest.mark.parametrize("case", golden_cases("stage_pairing"), ids=lambda c: c["name"])
 def test_pairing(case, oracle_backend):
     d = case["in"]
