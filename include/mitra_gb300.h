@@ -483,6 +483,41 @@ sym_status sym_prune_static(const int32_t *sample, uint64_t count, const double 
                             double prune, int32_t *pruned, uint64_t *pruned_count,
                             void *stream);
 
+/* ------------------------------------------------------- binary tables */
+/* No counterpart in the reference, which writes its results as text
+ * (export_result, src/io/export.cpp:37-98: features.csv, pairs.csv,
+ * votes.csv, descriptors.csv at 17 significant digits, and mesh.off).  Writes
+ * the same tables, with the same columns and derived fields (the sampled /
+ * pruned flags of each vertex, each vote's cluster -- the last cluster that
+ * lists it, -1 for none -- and each descriptor's dimension, 4 for a
+ * reflection vote and 12 for a rigid one), into `directory` as binary column
+ * files: features.symt, pairs.symt, votes.symt, descriptors.symt,
+ * vertices.symt and faces.symt.  A file is a 24-byte header, one 32-byte
+ * record per column, then the columns, each starting at a file offset that
+ * is a multiple of 64:
+ *
+ *   char magic[8] = "SYMTAB01"; uint64 rows; uint32 columns; uint32 0;
+ *   per column: char name[24] (NUL padded); uint32 type (1 int32,
+ *   2 float64, 3 uint8); uint32 0;
+ *   then each column's rows, little-endian.
+ *
+ * The values are the inputs' own bits, so a reader recovers every double
+ * exactly; text at 17 significant digits (the reference's format) can be
+ * rendered from them byte for byte.  Every id is checked against its range;
+ * the directory must exist.  Host memory only: no device work. */
+typedef struct sym_export_view {
+  sym_mesh_view mesh;           /* the prepared mesh (vertices, faces) */
+  sym_features_view features;   /* one row per vertex */
+  const int32_t *sample;        /* sampled vertex ids */
+  uint64_t sample_count;
+  const int32_t *pruned;        /* pruned vertex ids */
+  uint64_t pruned_count;
+  sym_pairs_view pairs;
+  sym_votes_view votes;
+  sym_clusters_view clusters;   /* for each vote's cluster column */
+} sym_export_view;
+sym_status sym_export_tables(const sym_export_view *result, const char *directory);
+
 /* --------------------------------------------------------------- metrics */
 /* Per-stage accounting, the fields of the reference CudaMetric
  * (include/symmetry/cuda.h:7-13, src/cuda/profile.cpp). */

@@ -83,6 +83,12 @@ class ClustersView(C.Structure):
                 ("vote_offsets", _u64), ("vote_indices", _i)]
 
 
+class ExportView(C.Structure):
+    _fields_ = [("mesh", MeshView), ("features", FeaturesView), ("sample", _i),
+                ("sample_count", C.c_uint64), ("pruned", _i), ("pruned_count", C.c_uint64),
+                ("pairs", PairsView), ("votes", VotesView), ("clusters", ClustersView)]
+
+
 class ModelContext(C.Structure):
     _fields_ = [("box_size", C.c_double), ("center", C.c_double * 3)]
 
@@ -241,6 +247,7 @@ PROTOTYPES = [
     ("sym_prune_static_setup", C.c_int, []),
     ("sym_prune_static", C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_uint64, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("sym_export_tables", C.c_int, [P(ExportView), C.c_char_p]),
     ("sym_set_profiling", C.c_int, [C.c_void_p, C.c_int]),
     ("sym_take_metrics", C.c_uint64, [C.c_void_p, P(Metric), C.c_uint64]),
 ]

@@ -291,6 +291,15 @@ void run(const std::string &mode, const Archive &in, Writer &w) {
       write_verification(w, v);
     }
     w.f64("stage_ms", times);
+  } else if (mode == "export") {
+    // The reference's detect() and export_result() (src/core/pipeline.cpp:5-52,
+    // src/io/export.cpp:37-189) into the directory given as text input "dir".
+    const Array &d = in.at("dir");
+    Result r = detect(mesh_from(in), o, *cpu);
+    auto t0 = std::chrono::steady_clock::now();
+    export_result(r, std::string(d.bytes.begin(), d.bytes.end()));
+    w.f64("export_ms", {ms_since(t0)});
+    w.i32("pairs", {int32_t(r.pairs.size())}), w.i32("votes", {int32_t(r.votes.size())});
   } else if (mode == "curvature") {
     Prepared p = prepare(mesh_from(in), o);
     write_topology(w, p);

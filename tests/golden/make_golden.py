@@ -133,6 +133,32 @@ def heightfield():
           "pairs", out["pair_a"].size, "votes", out["vote_pair"].size)
 
 
+def export_cases():
+    """The reference's own text export (detect() then export_result(),
+    src/io/export.cpp:37-189) of the eight example runs: SHA-256 and size of
+    features.csv, pairs.csv, votes.csv, descriptors.csv and mesh.off."""
+    import tempfile
+    record = {}
+    for scene in ["reflection", "rigid", "partial", "single"]:
+        v, f = read_off(EXAMPLES / f"{scene}.off")
+        for ratio in [1, 0.5]:
+            name = f"{scene}_{'1' if ratio == 1 else '05'}"
+            with tempfile.TemporaryDirectory() as d:
+                out = oracle.run_reference("export", {
+                    **mesh_arrays(v, f), "dir": str(Path(d) / "csv"),
+                    **options(sample_ratio=ratio, pair_threshold=0.08, verify_threshold=0.01)})
+                for file in EXPORT_FILES:
+                    data = (Path(d) / "csv" / file).read_bytes()
+                    record[f"{name}:{file}:sha"] = np.array(hashlib.sha256(data).hexdigest())
+                    record[f"{name}:{file}:bytes"] = np.array(len(data))
+            print(f"  export {name}: {int(out['pairs'][0])} pairs, {int(out['votes'][0])} votes, "
+                  f"export_result {out['export_ms'][0]:.2f} ms")
+    save("export_text", record)
+
+
+EXPORT_FILES = ("features.csv", "pairs.csv", "votes.csv", "descriptors.csv", "mesh.off")
+
+
 # ------------------------------------------------------------- stage cases
 def pairing_cases():
     """Shaped like the reference's tests/cuda_pairing.cpp:42-127."""
@@ -480,4 +506,5 @@ if __name__ == "__main__":
     clustering_cases()
     verification_cases()
     examples()
+    export_cases()
     heightfield()
