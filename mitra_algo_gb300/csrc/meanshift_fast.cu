@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
     move += delta[d] * delta[d];
   }
   if (!near) {
-    for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + T(kRelax) * delta[d];
+    for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + delta[d];
     if (move < T(kSwitch2) * h2) state[s] = kNear;
     return;
   }

@@ -29,7 +29,6 @@ constexpr int kChunk = 128;  // votes per chunk = seeds per tile
 // steps that keep being accepted without shrinking) settles too.
 constexpr uint8_t kMoving = 0, kConverged = 1, kExhausted = 2, kNear = 3, kSettled = 4;
 constexpr double kSwitch2 = 1e-4, kNewtonStop2 = 1e-8, kTrust = 0.25;
-constexpr double kRelax = 1.0;
 constexpr int kNewtonCap = 10;
 // Floats (or doubles) per partial sum of one seed: sum w x (6), sum w, pad,
 // then for kNear seeds the unweighted in-window sums of d = v - x: sum d

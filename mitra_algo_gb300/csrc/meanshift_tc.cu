@@ -950,9 +950,10 @@ __global__ void __launch_bounds__(256) ms_update_bulk(float *means, const float 
   }
   float move = 0;
   for (int d = 0; d < 6; ++d) {
-    float x = means[uint64_t(s) * 8 + d], e = acc[d] / acc[6] - x;
+    float nx = acc[d] / acc[6];
+    float e = means[uint64_t(s) * 8 + d] - nx;
     move += e * e;
-    means[uint64_t(s) * 8 + d] = x + float(kRelax) * e;
+    means[uint64_t(s) * 8 + d] = nx;
   }
   if (move < float(kSwitch2) * h2) state[s] = kNear;
 }

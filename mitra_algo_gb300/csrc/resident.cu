@@ -614,6 +614,9 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   for (int pass = 0; pass < 2; ++pass)
     for (uint64_t i = 0; i < k; ++i) {
       if (state[i] == kExhausted || (state[i] == kConverged) != (pass == 0)) continue;
+      bool finite = true;
+      for (int d = 0; d < 6; ++d) finite = finite && std::isfinite(means[i * 8 + d]);
+      if (!finite) continue;  // no mode (and no NaN key in the ordered index)
       double x0 = means[i * 8];
       int64_t hit = -1;
       for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
