@@ -326,6 +326,13 @@ typedef struct sym_fast_options {
    * probability vote_cap / votes by a hash of its index and seed_rng,
    * order preserved (a uniform subsample, the same for every precision) */
   uint64_t vote_cap;
+  /* FP64 refinement passes of the verified modes' motions before their
+   * verification (0: none): each pass pairs every vertex that supports a
+   * mode forward with the closest surface point to its image, then fits the
+   * motion to those pairs by weighted least squares (rigid: Kabsch; reflection:
+   * the plane through the midpoints, normal along the displacements) --
+   * ICP on the device in FP64; the records carry the refined motions */
+  int32_t refine;
 } sym_fast_options;
 
 #define SYM_FAST_MAX_CLUSTERS 32
@@ -374,6 +381,16 @@ sym_status sym_detect_fast(sym_context *ctx, sym_mesh_handle *mesh,
 sym_status sym_detect_fast_sampled(sym_context *ctx, sym_mesh_handle *mesh,
                                    const sym_options *options,
                                    const sym_fast_options *fast, sym_fast_result *out);
+
+/* The refinement and verification of sym_detect_fast on given motions: the
+ * `count` records are refined in place by `iterations` passes (see
+ * sym_fast_options.refine), then verified with options->verify_threshold;
+ * coverage and rms get `count` entries, patches 2 * count (forward, inverse
+ * patch counts). */
+sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
+                                 const sym_options *options, sym_cluster_record *records,
+                                 uint64_t count, int32_t iterations, double *coverage,
+                                 double *rms, uint32_t *patches);
 
 /* GPU mesh preparation: the reference's prepare() (src/core/prepare.cpp:
  * 102-149) without subdivision (options->subdivide must be 0) and its

@@ -150,7 +150,7 @@ class FastOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("seeds", C.c_int32), ("seed_rng", C.c_uint64),
                 ("max_iterations", C.c_int32), ("polish_iterations", C.c_int32),
                 ("reference_seeds", C.c_int32), ("verify", C.c_int32), ("mode", C.c_int32),
-                ("vote_cap", C.c_uint64)]
+                ("vote_cap", C.c_uint64), ("refine", C.c_int32)]
 
 
 FAST_MAX_CLUSTERS = 32
@@ -233,6 +233,8 @@ PROTOTYPES = [
                                   P(FastOptions), P(FastResult)]),
     ("sym_detect_fast_sampled", C.c_int, [C.c_void_p, C.c_void_p, P(Options), P(FastOptions),
                                           P(FastResult)]),
+    ("sym_refine_transforms", C.c_int, [C.c_void_p, C.c_void_p, P(Options), P(ClusterRecord),
+                                        C.c_uint64, C.c_int32, _d, _d, P(C.c_uint32)]),
     ("sym_detect_fast_batch", C.c_int, [P(C.c_void_p), C.c_int32, P(BatchItem), C.c_uint64]),
     ("sym_prepare", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(PreparedOut)]),
     ("sym_prepared_release", None, [P(PreparedOut)]),

@@ -200,24 +200,27 @@ class Gb300Backend:
 
     @staticmethod
     def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                      reference_seeds, verify, mode="rigid", vote_cap=0):
+                      reference_seeds, verify, mode="rigid", vote_cap=0, refine=0):
         if mode not in ("rigid", "reflection"):
             raise ValueError(f"unknown detection mode {mode!r}")
         return abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
                                seed_rng, max_iterations, polish_iterations, reference_seeds,
                                1 if verify else 0, 1 if mode == "reflection" else 0,
-                               int(vote_cap))
+                               int(vote_cap), int(refine))
 
     def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
                     seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
-                    reference_seeds=0, verify=True, mode="rigid", vote_cap=0) -> dict:
+                    reference_seeds=0, verify=True, mode="rigid", vote_cap=0,
+                    refine=0) -> dict:
         """Throughput pipeline on a resident mesh (no reference counterpart);
         mode "rigid" (rotation + translation votes) or "reflection" (plane
         votes); vote_cap > 0 subsamples the votes that enter the mean shift
-        to about that many.  `sample` None draws the area-weighted sample on
-        the device from options.seed, as detect() does (sym_detect_fast_sampled)."""
+        to about that many; refine > 0 runs that many FP64 ICP passes on the
+        verified modes' motions.  `sample` None draws the area-weighted
+        sample on the device from options.seed, as detect() does
+        (sym_detect_fast_sampled)."""
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                                reference_seeds, verify, mode, vote_cap)
+                                reference_seeds, verify, mode, vote_cap, refine)
         res = abi.FastResult()
         if sample is None:
             _check(self._lib.sym_detect_fast_sampled(self._ctx, mesh.handle,
@@ -229,6 +232,35 @@ class Gb300Backend:
                                          sample.ctypes.data_as(C.POINTER(C.c_int32)), sample.size,
                                          C.byref(options.to_c()), C.byref(fo), C.byref(res)))
         return self._fast_dict(res)
+
+    def refine_transforms(self, mesh: "ResidentMesh", options: Options, records,
+                          iterations: int) -> dict:
+        """sym_refine_transforms: `records` = [(reflection, rotation (9),
+        translation (3), plane_normal (3), plane_offset), ...] refined by
+        `iterations` FP64 ICP passes against the resident mesh, then
+        verified.  Returns the refined motions with coverage, rms, patches."""
+        n = len(records)
+        recs = (abi.ClusterRecord * max(n, 1))()
+        for r, (refl, rot, tr, nrm, off) in zip(recs, records):
+            r.reflection = int(refl)
+            for k in range(9):
+                r.rotation[k] = float(rot[k])
+            for k in range(3):
+                r.translation[k] = float(tr[k])
+                r.plane_normal[k] = float(nrm[k])
+            r.plane_offset = float(off)
+        cov, rms = np.zeros(max(n, 1)), np.zeros(max(n, 1))
+        patches = np.zeros(2 * max(n, 1), np.uint32)
+        _check(self._lib.sym_refine_transforms(
+            self._ctx, mesh.handle, C.byref(options.to_c()), recs, n, int(iterations),
+            cov.ctypes.data_as(C.POINTER(C.c_double)), rms.ctypes.data_as(C.POINTER(C.c_double)),
+            patches.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return {"rotation": np.array([list(r.rotation) for r in recs[:n]]).reshape(n, 9),
+                "translation": np.array([list(r.translation) for r in recs[:n]]).reshape(n, 3),
+                "plane_normal": np.array([list(r.plane_normal) for r in recs[:n]]).reshape(n, 3),
+                "plane_offset": np.array([r.plane_offset for r in recs[:n]]),
+                "coverage": cov[:n], "rms": rms[:n],
+                "patches": [(int(patches[2 * i]), int(patches[2 * i + 1])) for i in range(n)]}
 
     def sample_vertices(self, weights, ratio: float, rng: Rng) -> np.ndarray:
         """sym_sample_vertices: the reference's sample_vertices

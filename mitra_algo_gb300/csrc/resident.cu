@@ -41,8 +41,8 @@ void prune_device(Call &, const int32_t *, uint64_t, const double *, const doubl
 uint64_t pairing_device(Call &, const int32_t *, uint64_t, const double *, uint64_t, const double *,
                         const double *, double, double, uint64_t, int32_t **, int32_t **);
 void verification_fast(Call &, const Lbvh &, const double *, const double *, const double *,
-                       const uint64_t *, const int32_t *, const sym_cluster_record *, uint64_t,
-                       double, double *, double *, uint32_t *);
+                       const uint64_t *, const int32_t *, sym_cluster_record *, uint64_t, double,
+                       int, const double *, double *, double *, uint32_t *);
 // BF16 tensor-core bulk iterations (meanshift_tc.cu); returns false when the
 // tensor path cannot run this problem (the caller then stays in FP32).
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
@@ -701,7 +701,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   // ---- (d) verification of the top modes
   if (fo.verify && nc) {
     verification_fast(call, h.lbvh, h.xyz, h.vn, h.w, h.nbr_off, h.nbr, r.records, nc,
-                      o.verify_threshold * h.model.box_size, r.coverage, r.rms, r.patches);
+                      o.verify_threshold * h.model.box_size, fo.refine, h.model.center,
+                      r.coverage, r.rms, r.patches);
   }
   clock.mark(9);
   call.sync();
@@ -721,7 +722,30 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
 extern "C" {
 
 void sym_fast_options_default(sym_fast_options *o) {
-  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0};
+  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0, 0};
+}
+
+sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
+                                 const sym_options *options, sym_cluster_record *records,
+                                 uint64_t count, int32_t iterations, double *coverage,
+                                 double *rms, uint32_t *patches) {
+  if (!ctx || !mesh || !options || (count && (!records || !coverage || !rms || !patches)))
+    return SYM_INVALID_ARGUMENT;
+  try {
+    sym::Call call(ctx, "refine_transforms");
+    if (iterations < 0) sym::fail(SYM_INVALID_ARGUMENT, "negative refinement iterations");
+    sym::verification_fast(call, mesh->lbvh, mesh->xyz, mesh->vn, mesh->w, mesh->nbr_off,
+                           mesh->nbr, records, count,
+                           options->verify_threshold * mesh->model.box_size, iterations,
+                           mesh->model.center, coverage, rms, patches);
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
+  }
 }
 
 sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_topology_view *g,

@@ -264,8 +264,48 @@ __device__ int32_t nearest_face_fast(const BvhView &b, F3 p, float &best, int *s
   return face;
 }
 
-// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction); the
-// motion is applied in FP64, the search runs in FP32.
+// The verification tests of one (mode, vertex, direction) query: returns
+// the nearest face when vertex i supports mode m in that direction (-1
+// otherwise), its FP32 squared distance in `best` (entering as tau^2) and
+// the image of the vertex in q.  The motion is applied in FP64, the search
+// runs in FP32.
+__device__ __forceinline__ int32_t support_query(const BvhView &b, const double *xyz,
+                                                 const double *vn, const Motion32 &m, uint64_t i,
+                                                 bool inverse, double tau, float &best, double q[3],
+                                                 int *status) {
+  const uint64_t nv = b.nv;
+  double r[9];
+  for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
+  const double p[3] = {xyz[i], xyz[nv + i], xyz[2 * nv + i]};
+  double move2 = 0;
+  for (int a = 0; a < 3; ++a) {
+    double s = 0;
+    for (int k = 0; k < 3; ++k) s += r[a * 3 + k] * (inverse ? p[k] - m.t[k] : p[k]);
+    q[a] = inverse ? s : s + m.t[a];
+    move2 += (q[a] - p[a]) * (q[a] - p[a]);
+  }
+  if (move2 < 4 * tau * tau) return -1;
+  if (m.reflection) {
+    double side = m.n[0] * p[0] + m.n[1] * p[1] + m.n[2] * p[2] + m.offset;
+    if (inverse ? side <= tau : side >= -tau) return -1;
+  }
+  const F3 qf{float(q[0]), float(q[1]), float(q[2])};
+  const int32_t face = nearest_face_fast(b, qf, best, status);
+  if (face < 0) return -1;
+  const F3 a = vtx(b, b.faces[face]), bb = vtx(b, b.faces[b.nf + face]),
+           cc = vtx(b, b.faces[2 * b.nf + face]);
+  F3 fn = crossf(bb - a, cc - a);
+  float len = sqrtf(dotf(fn, fn));
+  if (!(len > 0.f)) return -1;
+  const double ni[3] = {vn[i], vn[nv + i], vn[2 * nv + i]};
+  float rn[3];
+  for (int k = 0; k < 3; ++k)
+    rn[k] = float(r[k * 3] * ni[0] + r[k * 3 + 1] * ni[1] + r[k * 3 + 2] * ni[2]);
+  if ((rn[0] * fn.x + rn[1] * fn.y + rn[2] * fn.z) / len < 0.5f) return -1;
+  return face;
+}
+
+// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).
 __global__ void verify_vertices_fast(BvhView b, const double *xyz, const double *vn,
                                      const Motion32 *motions, uint64_t nc, double tau, float tau2,
                                      uint8_t *flags, double *err, int *status) {
@@ -277,38 +317,232 @@ __global__ void verify_vertices_fast(BvhView b, const double *xyz, const double 
   const uint64_t i = rem % nv;
   flags[row] = 0;
   if (!inverse) err[c * nv + i] = 0;
-  const Motion32 &m = motions[c];
-  double r[9];
-  for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
-  const double p[3] = {xyz[i], xyz[nv + i], xyz[2 * nv + i]};
-  double q[3], move2 = 0;
-  for (int a = 0; a < 3; ++a) {
-    double s = 0;
-    for (int k = 0; k < 3; ++k) s += r[a * 3 + k] * (inverse ? p[k] - m.t[k] : p[k]);
-    q[a] = inverse ? s : s + m.t[a];
-    move2 += (q[a] - p[a]) * (q[a] - p[a]);
-  }
-  if (move2 < 4 * tau * tau) return;
-  if (m.reflection) {
-    double side = m.n[0] * p[0] + m.n[1] * p[1] + m.n[2] * p[2] + m.offset;
-    if (inverse ? side <= tau : side >= -tau) return;
-  }
   float best = tau2;
-  const F3 qf{float(q[0]), float(q[1]), float(q[2])};
-  const int32_t face = nearest_face_fast(b, qf, best, status);
-  if (face < 0) return;
-  const F3 a = vtx(b, b.faces[face]), bb = vtx(b, b.faces[b.nf + face]),
-           cc = vtx(b, b.faces[2 * b.nf + face]);
-  F3 fn = crossf(bb - a, cc - a);
-  float len = sqrtf(dotf(fn, fn));
-  if (!(len > 0.f)) return;
-  const double ni[3] = {vn[i], vn[nv + i], vn[2 * nv + i]};
-  float rn[3];
-  for (int k = 0; k < 3; ++k)
-    rn[k] = float(r[k * 3] * ni[0] + r[k * 3 + 1] * ni[1] + r[k * 3 + 2] * ni[2]);
-  if ((rn[0] * fn.x + rn[1] * fn.y + rn[2] * fn.z) / len < 0.5f) return;
+  double q[3];
+  if (support_query(b, xyz, vn, motions[c], i, inverse, tau, best, q, status) < 0) return;
   flags[row] = 1;
   if (!inverse) err[c * nv + i] = double(best);
+}
+
+// ------------------------------------------------ FP64 transform refinement
+// Closest point of triangle abc to p in FP64 (the region tests of Ericson,
+// Real-Time Collision Detection, 2005, section 5.1.5); a triangle without
+// area gives its nearest corner.
+__device__ void closest_point(const double p[3], const double a[3], const double b[3],
+                              const double c[3], double out[3]) {
+  double ab[3], ac[3], ap[3], bp[3], cp[3];
+  for (int k = 0; k < 3; ++k)
+    ab[k] = b[k] - a[k], ac[k] = c[k] - a[k], ap[k] = p[k] - a[k], bp[k] = p[k] - b[k],
+    cp[k] = p[k] - c[k];
+  auto dot3 = [](const double *x, const double *y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+  auto set = [&](const double *base, const double *dir, double t) {
+    for (int k = 0; k < 3; ++k) out[k] = base[k] + dir[k] * t;
+  };
+  const double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+  if (d1 <= 0 && d2 <= 0) return set(a, ab, 0);
+  const double d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+  if (d3 >= 0 && d4 <= d3) return set(b, ab, 0);
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0 && d1 >= 0 && d3 <= 0) return set(a, ab, d1 / (d1 - d3));
+  const double d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+  if (d6 >= 0 && d5 <= d6) return set(c, ab, 0);
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0 && d2 >= 0 && d6 <= 0) return set(a, ac, d2 / (d2 - d6));
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
+    const double bc[3] = {c[0] - b[0], c[1] - b[1], c[2] - b[2]};
+    return set(b, bc, (d4 - d3) / ((d4 - d3) + (d5 - d6)));
+  }
+  const double den = va + vb + vc;
+  if (!(den > 0)) {  // no area: the nearest corner
+    const double da = dot3(ap, ap), db = dot3(bp, bp), dc = dot3(cp, cp);
+    return set(da <= db && da <= dc ? a : (db <= dc ? b : c), ab, 0);
+  }
+  for (int k = 0; k < 3; ++k) out[k] = a[k] + ab[k] * (vb / den) + ac[k] * (vc / den);
+}
+
+struct Origin {
+  double x[3];
+};
+
+// Forward correspondences: for each vertex i that supports mode c forward
+// (the verification's tests), the FP64 closest point of its nearest face to
+// the vertex's image, relative to `o`; ok[c * nv + i] says which.
+__global__ void refine_pairs(BvhView b, const double *xyz, const double *vn,
+                             const Motion32 *motions, uint64_t nc, double tau, float tau2, Origin o,
+                             double *target, uint8_t *ok, int *status) {
+  const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t nv = b.nv;
+  if (row >= nc * nv) return;
+  const uint64_t c = row / nv, i = row % nv;
+  ok[row] = 0;
+  float best = tau2;
+  double q[3];
+  const int32_t face = support_query(b, xyz, vn, motions[c], i, false, tau, best, q, status);
+  if (face < 0) return;
+  double corner[3][3], out[3];
+  for (int k = 0; k < 3; ++k) {
+    const int32_t v = b.faces[uint64_t(k) * b.nf + face];
+    for (int a = 0; a < 3; ++a) corner[k][a] = xyz[uint64_t(a) * nv + v];
+  }
+  closest_point(q, corner[0], corner[1], corner[2], out);
+  for (int a = 0; a < 3; ++a) target[row * 3 + a] = out[a] - o.x[a];
+  ok[row] = 1;
+}
+
+constexpr int kRefineSums = 28, kRefineThreads = 128;
+
+// Block c: the weighted sums of mode c's correspondences (p the vertex, q its
+// target, both relative to o; weights = vertex weights): W, W p, W q,
+// W p q^T (row-major), W p p^T and W q q^T (upper triangles).  Fixed-order
+// strided partials and a fixed tree.
+__global__ void __launch_bounds__(kRefineThreads) refine_sums(const double *xyz, const double *w,
+                                                              uint64_t nv, const uint8_t *ok,
+                                                              const double *target, Origin o,
+                                                              double *sums) {
+  __shared__ double part[kRefineSums][kRefineThreads];
+  const uint64_t c = blockIdx.x;
+  double acc[kRefineSums];
+  for (int k = 0; k < kRefineSums; ++k) acc[k] = 0;
+  for (uint64_t i = threadIdx.x; i < nv; i += kRefineThreads) {
+    if (!ok[c * nv + i]) continue;
+    const double wi = w[i];
+    double p[3], q[3];
+    for (int a = 0; a < 3; ++a) p[a] = xyz[a * nv + i] - o.x[a], q[a] = target[(c * nv + i) * 3 + a];
+    acc[0] += wi;
+    for (int a = 0; a < 3; ++a) acc[1 + a] += wi * p[a], acc[4 + a] += wi * q[a];
+    for (int a = 0; a < 3; ++a)
+      for (int e = 0; e < 3; ++e) acc[7 + a * 3 + e] += wi * p[a] * q[e];
+    for (int a = 0, at = 0; a < 3; ++a)
+      for (int e = a; e < 3; ++e, ++at) acc[16 + at] += wi * p[a] * p[e], acc[22 + at] += wi * q[a] * q[e];
+  }
+  for (int k = 0; k < kRefineSums; ++k) part[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int s = kRefineThreads / 2; s; s >>= 1) {
+    if (int(threadIdx.x) < s)
+      for (int k = 0; k < kRefineSums; ++k) part[k][threadIdx.x] += part[k][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < kRefineSums) sums[c * kRefineSums + threadIdx.x] = part[threadIdx.x][0];
+}
+
+// Eigen-decomposition of a symmetric 3x3 matrix (row-major) by cyclic
+// Jacobi rotations: eigenvalues in `val`, eigenvectors in the columns of
+// `vec`, sorted by decreasing eigenvalue.
+__device__ void jacobi3(const double m[9], double val[3], double vec[9]) {
+  double a[9];
+  for (int k = 0; k < 9; ++k) a[k] = m[k], vec[k] = (k % 4 == 0) ? 1 : 0;
+  for (int sweep = 0; sweep < 32; ++sweep) {
+    const double off = a[1] * a[1] + a[2] * a[2] + a[5] * a[5];
+    const double diag = a[0] * a[0] + a[4] * a[4] + a[8] * a[8];
+    if (!(off > 1e-40 * diag)) break;
+    for (int pi = 0; pi < 2; ++pi)
+      for (int qi = pi + 1; qi < 3; ++qi) {
+        const double apq = a[pi * 3 + qi];
+        if (apq == 0) continue;
+        // the rotation that zeroes a[p][q]: tan of its angle is the smaller
+        // root of t^2 + 2 theta t - 1 = 0, theta = (a_qq - a_pp) / (2 a_pq)
+        const double theta = (a[qi * 4] - a[pi * 4]) / (2 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1));
+        const double cs = 1 / sqrt(t * t + 1), sn = t * cs;
+        for (int k = 0; k < 3; ++k) {  // columns p, q of a
+          const double akp = a[k * 3 + pi], akq = a[k * 3 + qi];
+          a[k * 3 + pi] = cs * akp - sn * akq, a[k * 3 + qi] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < 3; ++k) {  // rows p, q
+          const double apk = a[pi * 3 + k], aqk = a[qi * 3 + k];
+          a[pi * 3 + k] = cs * apk - sn * aqk, a[qi * 3 + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          const double vkp = vec[k * 3 + pi], vkq = vec[k * 3 + qi];
+          vec[k * 3 + pi] = cs * vkp - sn * vkq, vec[k * 3 + qi] = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  for (int k = 0; k < 3; ++k) val[k] = a[k * 4];
+  for (int i = 0; i < 2; ++i)  // sort the columns, largest first
+    for (int j = 0; j < 2 - i; ++j)
+      if (val[j] < val[j + 1]) {
+        double tv = val[j];
+        val[j] = val[j + 1], val[j + 1] = tv;
+        for (int k = 0; k < 3; ++k) {
+          double tc = vec[k * 3 + j];
+          vec[k * 3 + j] = vec[k * 3 + j + 1], vec[k * 3 + j + 1] = tc;
+        }
+      }
+}
+
+// One thread per mode: the least-squares motion of its correspondences.
+// Rigid: the rotation R maximising tr(R H), H = sum w (p - pbar)(q - qbar)^T,
+// from H's singular vectors (Kabsch: H = U S V^T, R = V diag(1, 1, d) U^T
+// with d making det R = +1), t = qbar - R pbar.  Reflection: the plane
+// normal is the top eigenvector of sum w (q - p)(q - p)^T (the displacements
+// run along it), oriented like the previous one, and the plane passes
+// through the weighted mean of the midpoints (p + q) / 2.  A mode with too
+// few or degenerate correspondences keeps its motion.
+__global__ void refine_solve(const double *sums, uint64_t nc, Origin o, Motion32 *motions) {
+  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const double *s = sums + c * kRefineSums;
+  const double W = s[0];
+  if (!(W > 0)) return;
+  double pb[3], qb[3];
+  for (int a = 0; a < 3; ++a) pb[a] = s[1 + a] / W, qb[a] = s[4 + a] / W;
+  Motion32 &m = motions[c];
+  if (!m.reflection) {
+    double H[9], HtH[9], S2[3], V[9];
+    for (int a = 0; a < 3; ++a)
+      for (int e = 0; e < 3; ++e) H[a * 3 + e] = s[7 + a * 3 + e] / W - pb[a] * qb[e];
+    for (int a = 0; a < 3; ++a)
+      for (int e = 0; e < 3; ++e)
+        HtH[a * 3 + e] = H[a] * H[e] + H[3 + a] * H[3 + e] + H[6 + a] * H[6 + e];
+    jacobi3(HtH, S2, V);
+    const double s0 = sqrt(fmax(S2[0], 0.0)), s1 = sqrt(fmax(S2[1], 0.0));
+    if (!(s1 > 1e-9 * s0)) return;  // collinear correspondences: rotation undetermined
+    double U[9];  // U_k = H V_k / s_k for k = 0, 1; U_2 = U_0 x U_1
+    for (int k = 0; k < 2; ++k)
+      for (int a = 0; a < 3; ++a)
+        U[a * 3 + k] = (H[a * 3] * V[k] + H[a * 3 + 1] * V[3 + k] + H[a * 3 + 2] * V[6 + k]) /
+                       (k ? s1 : s0);
+    U[2] = U[3] * U[7] - U[6] * U[4];
+    U[5] = U[6] * U[1] - U[0] * U[7];
+    U[8] = U[0] * U[4] - U[3] * U[1];
+    const double detv = V[0] * (V[4] * V[8] - V[5] * V[7]) - V[1] * (V[3] * V[8] - V[5] * V[6]) +
+                        V[2] * (V[3] * V[7] - V[4] * V[6]);
+    const double d[3] = {1, 1, detv < 0 ? -1.0 : 1.0};
+    double R[9];
+    for (int a = 0; a < 3; ++a)
+      for (int e = 0; e < 3; ++e)
+        R[a * 3 + e] = V[a * 3] * d[0] * U[e * 3] + V[a * 3 + 1] * d[1] * U[e * 3 + 1] +
+                       V[a * 3 + 2] * d[2] * U[e * 3 + 2];
+    for (int k = 0; k < 9; ++k) m.r[k] = R[k];
+    for (int a = 0; a < 3; ++a) {
+      double rp = 0;
+      for (int e = 0; e < 3; ++e) rp += R[a * 3 + e] * (pb[e] + o.x[e]);
+      m.t[a] = qb[a] + o.x[a] - rp;
+    }
+  } else {
+    double C[9], val[3], V[9];
+    const int up[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};  // upper-triangle slots
+    for (int a = 0; a < 3; ++a)
+      for (int e = 0; e < 3; ++e)
+        C[a * 3 + e] = (s[22 + up[a][e]] - s[7 + a * 3 + e] - s[7 + e * 3 + a] + s[16 + up[a][e]]) / W;
+    jacobi3(C, val, V);
+    if (!(val[0] > 0)) return;
+    double n[3] = {V[0], V[3], V[6]};
+    const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    if (!(len > 0)) return;
+    const double sgn = (n[0] * m.n[0] + n[1] * m.n[1] + n[2] * m.n[2]) < 0 ? -1.0 : 1.0;
+    for (int a = 0; a < 3; ++a) n[a] *= sgn / len;
+    double off = 0;
+    for (int a = 0; a < 3; ++a) off -= n[a] * (0.5 * (pb[a] + qb[a]) + o.x[a]);
+    for (int a = 0; a < 3; ++a) {
+      m.n[a] = n[a];
+      m.t[a] = -2 * off * n[a];
+      for (int e = 0; e < 3; ++e) m.r[a * 3 + e] = (a == e ? 1.0 : 0.0) - 2 * n[a] * n[e];
+    }
+    m.offset = off;
+  }
 }
 
 // Block c < nc: sum of the forward errors, supporting weight (both
@@ -415,11 +649,59 @@ void lbvh_free(Lbvh &b) {
   b = Lbvh{};
 }
 
-// Coverage, rms and patch counts of the nc modes (the throughput path).
+namespace {
+
+// `refine` passes of FP64 least-squares refinement of the nc modes' motions
+// against the mesh (ICP: forward correspondences under the current motion,
+// then the motion that fits them best), on the device; dm is updated in
+// place.  `origin` (a point near the mesh) keeps the sums well conditioned.
+void refine_motions(Call &call, const BvhView &view, const double *xyz, const double *vn,
+                    const double *w, Motion32 *dm, uint64_t nc, double tau, int refine,
+                    const double origin[3]) {
+  const uint64_t nv = view.nv;
+  if (refine <= 0 || !nc || !nv || !view.nf) return;
+  cudaStream_t st = call.stream();
+  const Origin o{{origin[0], origin[1], origin[2]}};
+  double *target = call.alloc<double>(nc * nv * 3), *sums = call.alloc<double>(nc * kRefineSums);
+  uint8_t *ok = call.alloc<uint8_t>(nc * nv);
+  for (int it = 0; it < refine; ++it) {
+    refine_pairs<<<blocks_for(nc * nv), kThreads, 0, st>>>(view, xyz, vn, dm, nc, tau,
+                                                           float(tau * tau), o, target, ok,
+                                                           call.status());
+    check_launch();
+    refine_sums<<<unsigned(nc), kRefineThreads, 0, st>>>(xyz, w, nv, ok, target, o, sums);
+    check_launch();
+    refine_solve<<<1, 32, 0, st>>>(sums, nc, o, dm);
+    check_launch();
+    call.launched(3);
+  }
+}
+
+Motion32 motion_of(const sym_cluster_record &r) {
+  Motion32 m{};
+  for (int k = 0; k < 9; ++k) m.r[k] = r.rotation[k];
+  for (int k = 0; k < 3; ++k) m.t[k] = r.translation[k], m.n[k] = r.plane_normal[k];
+  m.offset = r.plane_offset;
+  m.reflection = r.reflection != 0;
+  return m;
+}
+
+void store_motion(const Motion32 &m, sym_cluster_record &r) {
+  for (int k = 0; k < 9; ++k) r.rotation[k] = m.r[k];
+  for (int k = 0; k < 3; ++k) r.translation[k] = m.t[k], r.plane_normal[k] = m.n[k];
+  r.plane_offset = m.offset;
+}
+
+}  // namespace
+
+// Coverage, rms and patch counts of the nc modes (the throughput path),
+// after `refine` FP64 refinement passes of their motions (written back to
+// records).
 void verification_fast(Call &call, const Lbvh &bvh, const double *xyz, const double *vn,
                        const double *w, const uint64_t *nbr_off, const int32_t *nbr,
-                       const sym_cluster_record *records, uint64_t nc, double tau,
-                       double *coverage, double *rms, uint32_t *patches) {
+                       sym_cluster_record *records, uint64_t nc, double tau, int refine,
+                       const double origin[3], double *coverage, double *rms,
+                       uint32_t *patches) {
   const uint64_t nv = bvh.nv;
   if (!nc || !nv) {
     for (uint64_t c = 0; c < nc; ++c) coverage[c] = rms[c] = 0, patches[2 * c] = patches[2 * c + 1] = 0;
@@ -427,18 +709,18 @@ void verification_fast(Call &call, const Lbvh &bvh, const double *xyz, const dou
   }
   cudaStream_t st = call.stream();
   std::vector<Motion32> motions(nc);
-  for (uint64_t c = 0; c < nc; ++c) {
-    const sym_cluster_record &r = records[c];
-    for (int k = 0; k < 9; ++k) motions[c].r[k] = r.rotation[k];
-    for (int k = 0; k < 3; ++k) motions[c].t[k] = r.translation[k], motions[c].n[k] = r.plane_normal[k];
-    motions[c].offset = r.plane_offset;
-    motions[c].reflection = r.reflection != 0;
-  }
+  for (uint64_t c = 0; c < nc; ++c) motions[c] = motion_of(records[c]);
   Motion32 *dm = call.upload(motions.data(), nc);
+  BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
+  if (refine > 0) {
+    refine_motions(call, view, xyz, vn, w, dm, nc, tau, refine, origin);
+    call.d2h(motions.data(), dm, nc * sizeof(Motion32));
+    call.check_status("transform refinement");
+    for (uint64_t c = 0; c < nc; ++c) store_motion(motions[c], records[c]);
+  }
   const uint64_t rows = nc * 2 * nv;
   uint8_t *flags = call.alloc<uint8_t>(rows);
   double *err = call.alloc<double>(nc * nv);
-  BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
   if (bvh.nf) {
     verify_vertices_fast<<<blocks_for(rows), kThreads, 0, st>>>(view, xyz, vn, dm, nc, tau,
                                                                 float(tau * tau), flags, err,
