@@ -671,7 +671,7 @@ void refine_motions(Call &call, const BvhView &view, const double *xyz, const do
     check_launch();
     refine_sums<<<unsigned(nc), kRefineThreads, 0, st>>>(xyz, w, nv, ok, target, o, sums);
     check_launch();
-    refine_solve<<<1, 32, 0, st>>>(sums, nc, o, dm);
+    refine_solve<<<unsigned((nc + 31) / 32), 32, 0, st>>>(sums, nc, o, dm);
     check_launch();
     call.launched(3);
   }
