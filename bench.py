@@ -65,7 +65,9 @@ def reflection_bench(gpu, steps=5):
     CPU-runnable case (128 x 128 grid, 8 bumps mirrored in x, 2,000 samples,
     5% curvature tolerance, bandwidth 0.02): meshes/s of the BF16-refined and
     FP32 forms (host wall clock around synchronous calls, after two warm-up
-    runs) and the plane each finds first."""
+    runs) and the plane each finds first; then the BF16 form with 5 FP64
+    refinement passes (`refine`): its rate and the top plane's distance from
+    the exact mirror plane x = 0 before and after."""
     from mitra_algo_gb300.mesh import mirrored_heightfield, prepare
     from mitra_algo_gb300.types import Options, Rng
     mesh = mirrored_heightfield(size=128, bumps=8, seed=0)
@@ -91,6 +93,25 @@ def reflection_bench(gpu, steps=5):
                    "plane": [round(x, 6) for x in r["plane_normal"][0]] +
                             [round(r["plane_offset"][0], 6)] if r["clusters"] else None,
                    "coverage": round(r["coverage"][0], 4) if r["clusters"] else None}
+
+    def plane_error(r):  # max |n - (+-1, 0, 0)| + |offset| of the top plane
+        n = np.asarray(r["plane_normal"][0])
+        return float(np.abs(np.abs(n) - np.array([1.0, 0.0, 0.0])).max() + abs(r["plane_offset"][0]))
+
+    kw = dict(precision="bf16", seeds=512, max_iterations=100, polish_iterations=POLISH,
+              mode="reflection")
+    plain = gpu.detect_fast(resident, sample, opts, **kw)
+    for _ in range(2):
+        r = gpu.detect_fast(resident, sample, opts, refine=5, **kw)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r = gpu.detect_fast(resident, sample, opts, refine=5, **kw)
+    dt = (time.perf_counter() - t0) / steps
+    if r["clusters"]:
+        out["bf16_refined_transforms"] = {
+            "refine_passes": 5, "meshes_per_s": round(1.0 / dt, 3),
+            "plane_error_before": plane_error(plain), "plane_error_after": plane_error(r),
+            "coverage": round(r["coverage"][0], 4)}
     resident.close()
     return out
 
@@ -100,8 +121,9 @@ def batch_bench(gpu, n, workers):
     drawn so that sizes spread over that range, 2-5 fold rotations, noise
     sigma in [0, 5e-3] of the diagonal): sym_detect_fast one mesh after the
     other on one context, against sym_detect_fast_batch with `workers`
-    contexts.  Host wall clock around each pass (both calls are
-    synchronous); mesh preparation, curvature and sampling are not timed."""
+    contexts, and the batch again with the FP32 mean shift.  Host wall clock
+    around each pass (the calls are synchronous); mesh preparation,
+    curvature and sampling are not timed."""
     import torch
     from mitra_algo_gb300.mesh import motif_sphere, prepare
     from mitra_algo_gb300.types import Options, Rng
@@ -129,8 +151,12 @@ def batch_bench(gpu, n, workers):
     def together():
         return gpu.detect_fast_batch(jobs, workers=workers, **kw)
 
+    def together_fp32():
+        return gpu.detect_fast_batch(jobs, workers=workers, **dict(kw, precision="fp32"))
+
     out = {}
-    for name, fn in (("per_mesh_loop", loop), ("batched", together)):
+    for name, fn in (("per_mesh_loop", loop), ("batched", together),
+                     ("batched_fp32", together_fp32)):
         fn()  # warm-up: workspaces reach their size
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -140,12 +166,15 @@ def batch_bench(gpu, n, workers):
     for m, _, _ in jobs:
         m.close()
     (t_loop, r_loop), (t_batch, r_batch) = out["per_mesh_loop"], out["batched"]
+    t_fp32 = out["batched_fp32"][0]
     same = all(a["pairs"] == b["pairs"] and a["modes"] == b["modes"] and
                a["rotation"] == b["rotation"] for a, b in zip(r_loop, r_batch))
     return {"meshes": n, "vertices": [int(min(sizes)), int(max(sizes))],
             "samples_per_mesh": BATCH_SAMPLES, "seeds": BATCH_SEEDS, "workers": workers,
             "per_mesh_loop_meshes_per_s": round(n / t_loop, 3),
             "batched_meshes_per_s": round(n / t_batch, 3),
+            "batched_fp32_meshes_per_s": round(n / t_fp32, 3),
+            "batched_bf16_over_fp32": round(t_fp32 / t_batch, 3),
             "pairs": int(sum(r["pairs"] for r in r_batch)),
             "results_equal": bool(same), "clock": "host wall clock, synchronous calls"}
 

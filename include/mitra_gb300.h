@@ -333,6 +333,13 @@ typedef struct sym_fast_options {
    * the plane through the midpoints, normal along the displacements) --
    * ICP on the device in FP64; the records carry the refined motions */
   int32_t refine;
+  /* Launch shapes of the mean shift, 0 for the default (mitra_algo_gb300's
+   * autotuner picks them per workload): Morton bits per coordinate of the
+   * vote order (1-10, default 8), SIMT CTAs per SM (1-256, default 64),
+   * tensor-kernel CTAs per SM for the chunk lists (1-8, default 1), tensor
+   * approach iterations between host checks (default 8).  They change the
+   * order of FP32 sums and the work split, not the method. */
+  int32_t vote_bits, simt_blocks_per_sm, tc_ctas_per_sm, check_interval;
 } sym_fast_options;
 
 #define SYM_FAST_MAX_CLUSTERS 32

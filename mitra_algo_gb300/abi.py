@@ -150,7 +150,9 @@ class FastOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("seeds", C.c_int32), ("seed_rng", C.c_uint64),
                 ("max_iterations", C.c_int32), ("polish_iterations", C.c_int32),
                 ("reference_seeds", C.c_int32), ("verify", C.c_int32), ("mode", C.c_int32),
-                ("vote_cap", C.c_uint64), ("refine", C.c_int32)]
+                ("vote_cap", C.c_uint64), ("refine", C.c_int32), ("vote_bits", C.c_int32),
+                ("simt_blocks_per_sm", C.c_int32), ("tc_ctas_per_sm", C.c_int32),
+                ("check_interval", C.c_int32)]
 
 
 FAST_MAX_CLUSTERS = 32

@@ -46,6 +46,10 @@ def _check(status: int):
         _raise(status)
 
 
+# sym_fast_options' launch-shape fields, in their order (0 = the default)
+TUNING_KEYS = ("vote_bits", "simt_blocks_per_sm", "tc_ctas_per_sm", "check_interval")
+
+
 class Gb300Backend:
     """The GB300 backend: one device, one stream, one reusable workspace."""
 
@@ -200,27 +204,32 @@ class Gb300Backend:
 
     @staticmethod
     def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                      reference_seeds, verify, mode="rigid", vote_cap=0, refine=0):
+                      reference_seeds, verify, mode="rigid", vote_cap=0, refine=0, tuning=None):
         if mode not in ("rigid", "reflection"):
             raise ValueError(f"unknown detection mode {mode!r}")
+        t = dict(tuning or {})
+        unknown = set(t) - set(TUNING_KEYS)
+        if unknown:
+            raise ValueError(f"unknown tuning parameters {sorted(unknown)}")
         return abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
                                seed_rng, max_iterations, polish_iterations, reference_seeds,
                                1 if verify else 0, 1 if mode == "reflection" else 0,
-                               int(vote_cap), int(refine))
+                               int(vote_cap), int(refine), *(int(t.get(k, 0)) for k in TUNING_KEYS))
 
     def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
                     seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
                     reference_seeds=0, verify=True, mode="rigid", vote_cap=0,
-                    refine=0) -> dict:
+                    refine=0, tuning=None) -> dict:
         """Throughput pipeline on a resident mesh (no reference counterpart);
         mode "rigid" (rotation + translation votes) or "reflection" (plane
         votes); vote_cap > 0 subsamples the votes that enter the mean shift
         to about that many; refine > 0 runs that many FP64 ICP passes on the
-        verified modes' motions.  `sample` None draws the area-weighted
-        sample on the device from options.seed, as detect() does
-        (sym_detect_fast_sampled)."""
+        verified modes' motions; `tuning` sets the mean shift's launch
+        shapes (keys TUNING_KEYS, see autotune.py).  `sample` None draws the
+        area-weighted sample on the device from options.seed, as detect()
+        does (sym_detect_fast_sampled)."""
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                                reference_seeds, verify, mode, vote_cap, refine)
+                                reference_seeds, verify, mode, vote_cap, refine, tuning)
         res = abi.FastResult()
         if sample is None:
             _check(self._lib.sym_detect_fast_sampled(self._ctx, mesh.handle,
@@ -276,7 +285,7 @@ class Gb300Backend:
 
     def detect_fast_batch(self, jobs, workers=4, precision="bf16", seeds=2048, seed_rng=7,
                           max_iterations=100, polish_iterations=100, verify=True,
-                          mode="rigid") -> list:
+                          mode="rigid", tuning=None) -> list:
         """sym_detect_fast_batch over `jobs` = [(ResidentMesh, sample, Options), ...]:
         `workers` meshes in flight at a time, each on its own context (stream
         and workspace), the contexts kept for later calls.  Returns one result
@@ -286,7 +295,7 @@ class Gb300Backend:
             _check(self._lib.sym_context_create(self._device, C.byref(w)))
             self._workers.append(w)
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations, 0,
-                                verify, mode)
+                                verify, mode, tuning=tuning)
         keep = []
         items = (abi.BatchItem * len(jobs))()
         results = [abi.FastResult() for _ in jobs]
@@ -441,6 +450,11 @@ class ResidentMesh:
                                            C.byref(self._views[1]), C.byref(self._views[2]),
                                            C.byref(h)))
         self.handle = h
+
+    @property
+    def vertex_count(self) -> int:
+        m = self._raw if self.prepared is None else self.prepared.mesh
+        return int(m.vertex_count)
 
     def bytes(self) -> int:
         """Host-to-device bytes of one load."""

@@ -57,16 +57,14 @@ __device__ __forceinline__ uint64_t morton6(const float *x, const float *box, in
   return key;
 }
 
-// Votes are ordered by 8 bits per coordinate: a cell of the vote space is
-// then ~1/256 of its extent (well under the bandwidth on the benchmark
-// workloads), and the 48-bit key sorts in six 8-bit radix passes.
-constexpr int kVoteMortonBits = 8;
-
-__global__ void morton_keys(const float *desc, uint64_t q, const float *box, uint64_t *keys,
-                            int32_t *idx) {
+// Votes are ordered by `bits` bits per coordinate (8 by default: a cell of
+// the vote space is then ~1/256 of its extent, well under the bandwidth on
+// the benchmark workloads, and the 48-bit key sorts in six radix passes).
+__global__ void morton_keys(const float *desc, uint64_t q, const float *box, int bits,
+                            uint64_t *keys, int32_t *idx) {
   uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (v >= q) return;
-  keys[v] = morton6(desc + v * 8, box, kVoteMortonBits);
+  keys[v] = morton6(desc + v * 8, box, bits);
   idx[v] = int32_t(v);
 }
 
@@ -455,10 +453,10 @@ struct Grid {
   uint64_t tiles, splits, cps, slots;
 };
 
-Grid grid_for(uint64_t nactive, uint64_t nchunks) {
+Grid grid_for(uint64_t nactive, uint64_t nchunks, int blocks_per_sm) {
   Grid g;
   g.tiles = (nactive + kChunk - 1) / kChunk;
-  uint64_t want = (64 * 152 + g.tiles - 1) / g.tiles;
+  uint64_t want = (uint64_t(blocks_per_sm) * 152 + g.tiles - 1) / g.tiles;
   g.splits = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, want));
   g.cps = (nchunks + g.splits - 1) / g.splits;
   g.splits = (nchunks + g.cps - 1) / g.cps;
@@ -473,8 +471,9 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
   cudaStream_t st = call.stream();
   int32_t *ids = call.alloc<int32_t>(k);
   unsigned *nact = call.alloc<unsigned>(2);
-  // partial capacity: splits x slots is at most ~64*152*kChunk (+ one tile)
-  uint64_t cap = (64 * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
+  // partial capacity: splits x slots is at most ~blocks*152*kChunk (+ one tile)
+  const int bps = v.tuning.simt_blocks_per_sm;
+  uint64_t cap = (uint64_t(bps) * 152 + 2) * uint64_t(kChunk) + std::max<uint64_t>(k, kChunk) * 2;
   T *partial = call.alloc<T>(cap * kPartial);
   T *red = call.alloc<T>(uint64_t(kGroups) * kPartial * std::max<uint64_t>(k, kChunk) * 2);
   float gap = float(std::sqrt(h2)) + 1e-6f;
@@ -490,7 +489,7 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
     if (!n) break;
     if (seed_iterations) *seed_iterations += n;
     if (trace && it < trace_len) trace[it] = n;
-    Grid g = grid_for(n, v.nchunks);
+    Grid g = grid_for(n, v.nchunks, bps);
     if (g.splits * g.slots > cap) fail(SYM_RUNTIME_ERROR, "mean-shift partial buffer too small");
     const dim3 grid(unsigned(g.tiles), unsigned(g.splits));
     if (counts[1])
@@ -513,9 +512,15 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
 
 }  // namespace
 
-VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_raw, uint64_t q) {
+VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_raw, uint64_t q,
+                       const Tuning &tuning) {
   cudaStream_t st = call.stream();
+  if (tuning.vote_bits < 1 || tuning.vote_bits > 10 || tuning.simt_blocks_per_sm < 1 ||
+      tuning.simt_blocks_per_sm > 256 || tuning.tc_ctas_per_sm < 1 || tuning.tc_ctas_per_sm > 8 ||
+      tuning.check_interval < 1)
+    fail(SYM_INVALID_ARGUMENT, "tuning parameter out of range");
   VoteSet v;
+  v.tuning = tuning;
   v.q = q;
   v.nchunks = (q + kChunk - 1) / kChunk;
   const int kBoxBlocks = 256;
@@ -529,9 +534,9 @@ VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_r
   int32_t *idx = call.alloc<int32_t>(q);
   v.order = call.alloc<int32_t>(q);
   v.rank = call.alloc<int32_t>(q);
-  morton_keys<<<blocks_for(q), kThreads, 0, st>>>(desc_raw, q, v.gbox, keys, idx);
+  morton_keys<<<blocks_for(q), kThreads, 0, st>>>(desc_raw, q, v.gbox, tuning.vote_bits, keys, idx);
   check_launch();
-  radix_sort_pairs(call, keys, idx, skeys, v.order, q, 6 * kVoteMortonBits);
+  radix_sort_pairs(call, keys, idx, skeys, v.order, q, 6 * tuning.vote_bits);
   invert<<<blocks_for(q), kThreads, 0, st>>>(v.order, q, v.rank);
   check_launch();
   v.desc = call.alloc<float>(q * 8);
@@ -605,7 +610,7 @@ void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm
   unsigned *nact = call.alloc<unsigned>(2);
   retile<float><<<1, 1024, 0, st>>>(points, state, nm, v.gbox, false, ids, nact);
   check_launch();
-  Grid g = grid_for(nm, v.nchunks);
+  Grid g = grid_for(nm, v.nchunks, v.tuning.simt_blocks_per_sm);
   float *partial = call.alloc<float>(g.splits * g.slots * 8);
   float gap = float(std::sqrt(h2)) + 1e-6f;
   ms_tile<float, true, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(

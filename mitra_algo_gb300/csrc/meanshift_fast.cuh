@@ -35,7 +35,18 @@ constexpr int kNewtonCap = 10;
 // (6) and sum d d^T (21, upper triangle row by row), pad.
 constexpr int kPartial = 40;
 
+// Launch-shape parameters of the mean shift (an autotuner chooses them; the
+// defaults are its choice on the benchmark workload).  Each changes only the
+// order of FP32 sums, the work split or how often the host looks.
+struct Tuning {
+  int vote_bits = 8;            // Morton bits per coordinate of the vote order
+  int simt_blocks_per_sm = 64;  // CTAs per SM the SIMT kernel's grid aims at
+  int tc_ctas_per_sm = 1;       // tensor-kernel CTAs per SM for the chunk lists
+  int check_interval = 8;       // tensor approach iterations between host checks
+};
+
 struct VoteSet {
+  Tuning tuning;
   uint64_t q = 0, nchunks = 0;
   float *desc = nullptr;      // q x 8, Morton order
   double *desc64 = nullptr;   // q x 8, same order (only when requested)
@@ -46,7 +57,8 @@ struct VoteSet {
 };
 
 // Sorts raw votes (q x 8; desc64_raw may be null) into a VoteSet.
-VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_raw, uint64_t q);
+VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_raw, uint64_t q,
+                       const Tuning &tuning = Tuning());
 
 // Seeds: sorted positions of the seed votes -> initial means (k x 8).
 void init_means(Call &call, const VoteSet &v, const int64_t *seed_rank, uint64_t k, float *means);

@@ -990,7 +990,8 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   int32_t *list = call.alloc<int32_t>(max_tiles * v.nchunks);
   uint64_t *offsets = call.alloc<uint64_t>(max_tiles + 1);
   uint32_t *pieces = call.alloc<uint32_t>(max_tiles + 1);
-  const uint32_t sms = 152;  // one wave: budget + tiles CTAs on the 152 SMs
+  // budget + tiles CTAs: tc_ctas_per_sm waves of the 152 SMs
+  const uint32_t sms = 152 * uint32_t(v.tuning.tc_ctas_per_sm);
   const uint64_t max_grid = std::max<uint64_t>(sms, 2 * max_tiles);
   float *partial = call.alloc<float>(max_grid * kChunk * 8);
   unsigned *nact = call.alloc<unsigned>(2), *iter = call.alloc<unsigned>(1);
@@ -1014,7 +1015,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   // Iterations are launched back to back: each reads the active-seed count
   // that the previous one left on the device, and one whose count is zero
   // returns at once.  The host looks at the count every kCheck iterations.
-  constexpr int kCheck = 8;
+  const int kCheck = v.tuning.check_interval;
   int it = 0;
   for (; it < max_iter; ++it) {
     active_seeds_async(call, v, means, state, k, ids, nact, iter, trace_dev, trace_cap);

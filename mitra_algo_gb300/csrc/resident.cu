@@ -509,7 +509,12 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   }
   clock.mark(4);
   // ---- Morton sort into chunks
-  VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q);
+  Tuning tuning;
+  if (fo.vote_bits) tuning.vote_bits = fo.vote_bits;
+  if (fo.simt_blocks_per_sm) tuning.simt_blocks_per_sm = fo.simt_blocks_per_sm;
+  if (fo.tc_ctas_per_sm) tuning.tc_ctas_per_sm = fo.tc_ctas_per_sm;
+  if (fo.check_interval) tuning.check_interval = fo.check_interval;
+  VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q, tuning);
   clock.mark(5);
   // ---- (c) mean shift from K seeds (uniform draw of distinct votes)
   uint64_t k = std::min<uint64_t>(uint64_t(std::max(fo.seeds, 1)), q);
@@ -722,7 +727,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
 extern "C" {
 
 void sym_fast_options_default(sym_fast_options *o) {
-  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0, 0};
+  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0, 0, 0, 0, 0, 0};
 }
 
 sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
