@@ -335,7 +335,7 @@ typedef struct sym_fast_options {
   int32_t refine;
   /* Launch shapes of the mean shift, 0 for the default (mitra_algo_gb300's
    * autotuner picks them per workload): Morton bits per coordinate of the
-   * vote order (1-10, default 8), SIMT CTAs per SM (1-256, default 64),
+   * vote order (1-10, default 8), SIMT CTAs per SM (1-256, default 128),
    * tensor-kernel CTAs per SM for the chunk lists (1-8, default 1), tensor
    * approach iterations between host checks (default 8).  They change the
    * order of FP32 sums and the work split, not the method. */

@@ -31,10 +31,10 @@ from pathlib import Path
 
 from .backend import TUNING_KEYS
 
-DEFAULTS = {"vote_bits": 8, "simt_blocks_per_sm": 64, "tc_ctas_per_sm": 1, "check_interval": 8}
+DEFAULTS = {"vote_bits": 8, "simt_blocks_per_sm": 128, "tc_ctas_per_sm": 1, "check_interval": 8}
 CANDIDATES = {
     "vote_bits": (6, 7, 8, 9),
-    "simt_blocks_per_sm": (16, 32, 64, 128),
+    "simt_blocks_per_sm": (32, 64, 128, 256),
     "tc_ctas_per_sm": (1, 2, 3),
     "check_interval": (4, 8, 16),
 }

@@ -40,7 +40,7 @@ constexpr int kPartial = 40;
 // order of FP32 sums, the work split or how often the host looks.
 struct Tuning {
   int vote_bits = 8;            // Morton bits per coordinate of the vote order
-  int simt_blocks_per_sm = 64;  // CTAs per SM the SIMT kernel's grid aims at
+  int simt_blocks_per_sm = 128; // CTAs per SM the SIMT kernel's grid aims at
   int tc_ctas_per_sm = 1;       // tensor-kernel CTAs per SM for the chunk lists
   int check_interval = 8;       // tensor approach iterations between host checks
 };

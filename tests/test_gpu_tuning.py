@@ -45,7 +45,7 @@ def test_check_interval_changes_nothing(job):
 
 @pytest.mark.parametrize("precision", ["bf16", "fp32"])
 @pytest.mark.parametrize("tuning", [{"vote_bits": 6}, {"vote_bits": 9},
-                                    {"simt_blocks_per_sm": 16}, {"simt_blocks_per_sm": 128},
+                                    {"simt_blocks_per_sm": 32}, {"simt_blocks_per_sm": 256},
                                     {"tc_ctas_per_sm": 3}])
 def test_shapes_keep_the_results(job, precision, tuning):
     gpu, mesh, o = job
