@@ -461,6 +461,36 @@ def run_gpu(args):
     extra = args.config == "c2"
     batch = batch_bench(gpu, args.batch, args.batch_workers) if args.batch and extra else None
     refl = reflection_bench(gpu) if extra else None
+
+    def gaussian_leg(steps=3):
+        """The same workload with the truncated Gaussian kernel (exp weights,
+        MUFU BF16x2 exponentials in the tensor kernel): both forms' device
+        time per mesh (CUDA events, like the main legs) and mode error."""
+        out = {"kernel": "exp(-4.5 d^2/h^2) for d < h"}
+        for p in ("bf16", "fp32"):
+            kw = dict(precision=p, seeds=SEEDS, max_iterations=ITERATIONS,
+                      polish_iterations=POLISH, vote_cap=VOTE_CAP, tuning=shape(p),
+                      kernel="gaussian")
+            e = gpu.detect_fast(resident, sample, opts, reference_seeds=256, **kw)
+            t = []
+            for _ in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.random_(0, 255)
+                    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                gpu.detect_fast(resident, sample, opts, **kw)
+                with torch.cuda.stream(stream):
+                    b.record(stream)
+                b.synchronize()
+                t.append(a.elapsed_time(b))
+            ms = statistics.mean(t)
+            out[p] = {"meshes_per_s": round(1000.0 / ms, 4), "ms_per_step": round(ms, 3),
+                      "mode_error_max": e["mode_error_max"], "compared": int(e["modes_compared"]),
+                      "within_1e-4": int(e["modes_within"])}
+        out["bf16_over_fp32"] = round(out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"], 3)
+        return out
+
+    gauss = gaussian_leg() if extra else None
     if rank != 0:
         return
     r = res_bf16[-1]
@@ -535,6 +565,8 @@ def run_gpu(args):
         line["batch"] = batch
     if refl:
         line["reflection"] = refl
+    if gauss:
+        line["gaussian_kernel"] = gauss
     if not args.no_cpu and extra:
         line["cpu_baseline"] = cpu_estimate(prepared, opts, sample, r)
     print(json.dumps(line))

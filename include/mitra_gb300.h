@@ -340,7 +340,14 @@ typedef struct sym_fast_options {
    * approach iterations between host checks (default 8).  They change the
    * order of FP32 sums and the work split, not the method. */
   int32_t vote_bits, simt_blocks_per_sm, tc_ctas_per_sm, check_interval;
+  /* Mean-shift weight kernel: SYM_KERNEL_EPANECHNIKOV (1 - d^2/h^2, the
+   * reference's) or SYM_KERNEL_GAUSSIAN (exp(-4.5 d^2/h^2) for d < h, i.e.
+   * sigma = h/3 truncated at h; the tensor kernel makes these weights with
+   * the MUFU's BF16x2 exponential, the polish takes Newton steps with the
+   * Gaussian's Jacobian) */
+  int32_t kernel;
 } sym_fast_options;
+enum { SYM_KERNEL_EPANECHNIKOV = 0, SYM_KERNEL_GAUSSIAN = 1 };
 
 #define SYM_FAST_MAX_CLUSTERS 32
 typedef struct sym_fast_result {
@@ -464,12 +471,13 @@ sym_status sym_detect_fast_batch(sym_context *const *workers, int32_t worker_cou
  * 1 converged, 2 exhausted, 3 near a mode when the iterations ran out,
  * 4 settled) and the approach / polish iteration counts.  `precision`: SYM_MS_FP32,
  * SYM_MS_BF16_REFINED, or SYM_MS_FP64 (the form used to measure mode
- * errors). */
+ * errors); `kernel`: SYM_KERNEL_EPANECHNIKOV or SYM_KERNEL_GAUSSIAN (see
+ * sym_fast_options). */
 enum { SYM_MS_FP64 = 2 };
 sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q,
                           const int64_t *seeds, uint64_t k, double bandwidth,
                           int32_t precision, int32_t max_iterations,
-                          int32_t polish_iterations, double *means_out,
+                          int32_t polish_iterations, int32_t kernel, double *means_out,
                           uint8_t *state_out, int32_t *iterations_out);
 
 /* Test hook for the tensor-core path of the BF16 mean-shift: one tile of

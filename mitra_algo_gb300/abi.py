@@ -152,7 +152,7 @@ class FastOptions(C.Structure):
                 ("reference_seeds", C.c_int32), ("verify", C.c_int32), ("mode", C.c_int32),
                 ("vote_cap", C.c_uint64), ("refine", C.c_int32), ("vote_bits", C.c_int32),
                 ("simt_blocks_per_sm", C.c_int32), ("tc_ctas_per_sm", C.c_int32),
-                ("check_interval", C.c_int32)]
+                ("check_interval", C.c_int32), ("kernel", C.c_int32)]
 
 
 FAST_MAX_CLUSTERS = 32
@@ -243,7 +243,8 @@ PROTOTYPES = [
     ("sym_mesh_load_raw", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(C.c_void_p)]),
     ("sym_context_stream", C.c_void_p, [C.c_void_p]),
     ("sym_meanshift6", C.c_int, [C.c_void_p, _d, C.c_uint64, P(C.c_int64), C.c_uint64, C.c_double,
-                                 C.c_int32, C.c_int32, C.c_int32, _d, _u8, P(C.c_int32)]),
+                                 C.c_int32, C.c_int32, C.c_int32, C.c_int32, _d, _u8,
+                                 P(C.c_int32)]),
     ("sym_tc_selftest", C.c_int, [C.c_void_p, P(C.c_uint16), P(C.c_uint16), P(C.c_uint16),
                                   P(C.c_uint16), _f, _f]),
     # allocation-free prune: device pointers + a cudaStream_t

@@ -46,6 +46,8 @@ def _check(status: int):
         _raise(status)
 
 
+KERNELS = {"epanechnikov": 0, "gaussian": 1}  # SYM_KERNEL_*
+
 # sym_fast_options' launch-shape fields, in their order (0 = the default)
 TUNING_KEYS = ("vote_bits", "simt_blocks_per_sm", "tc_ctas_per_sm", "check_interval")
 
@@ -204,7 +206,8 @@ class Gb300Backend:
 
     @staticmethod
     def _fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                      reference_seeds, verify, mode="rigid", vote_cap=0, refine=0, tuning=None):
+                      reference_seeds, verify, mode="rigid", vote_cap=0, refine=0, tuning=None,
+                      kernel="epanechnikov"):
         if mode not in ("rigid", "reflection"):
             raise ValueError(f"unknown detection mode {mode!r}")
         t = dict(tuning or {})
@@ -214,22 +217,24 @@ class Gb300Backend:
         return abi.FastOptions(abi.MS_BF16_REFINED if precision == "bf16" else abi.MS_FP32, seeds,
                                seed_rng, max_iterations, polish_iterations, reference_seeds,
                                1 if verify else 0, 1 if mode == "reflection" else 0,
-                               int(vote_cap), int(refine), *(int(t.get(k, 0)) for k in TUNING_KEYS))
+                               int(vote_cap), int(refine), *(int(t.get(k, 0)) for k in TUNING_KEYS),
+                               KERNELS[kernel])
 
     def detect_fast(self, mesh: "ResidentMesh", sample, options: Options, precision="bf16",
                     seeds=2048, seed_rng=7, max_iterations=100, polish_iterations=100,
                     reference_seeds=0, verify=True, mode="rigid", vote_cap=0,
-                    refine=0, tuning=None) -> dict:
+                    refine=0, tuning=None, kernel="epanechnikov") -> dict:
         """Throughput pipeline on a resident mesh (no reference counterpart);
         mode "rigid" (rotation + translation votes) or "reflection" (plane
         votes); vote_cap > 0 subsamples the votes that enter the mean shift
         to about that many; refine > 0 runs that many FP64 ICP passes on the
         verified modes' motions; `tuning` sets the mean shift's launch
-        shapes (keys TUNING_KEYS, see autotune.py).  `sample` None draws the
+        shapes (keys TUNING_KEYS, see autotune.py); kernel "epanechnikov"
+        (the reference's weights) or "gaussian" (exp(-4.5 d^2/h^2) cut at h).  `sample` None draws the
         area-weighted sample on the device from options.seed, as detect()
         does (sym_detect_fast_sampled)."""
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                                reference_seeds, verify, mode, vote_cap, refine, tuning)
+                                reference_seeds, verify, mode, vote_cap, refine, tuning, kernel)
         res = abi.FastResult()
         if sample is None:
             _check(self._lib.sym_detect_fast_sampled(self._ctx, mesh.handle,
@@ -342,12 +347,12 @@ class Gb300Backend:
         return out
 
     def meanshift6(self, votes, seeds, bandwidth, precision="fp32", max_iterations=100,
-                   polish_iterations=100):
+                   polish_iterations=100, kernel="epanechnikov"):
         """Mean-shift of the seed votes over 6-D votes (q x 6); returns the
         final means (k x 6), per-seed state and the (approach, polish)
         iteration counts.  precision: "fp32" (FP32 approach), "bf16" (BF16
         tensor-core approach), both followed by the same FP32 polish, or
-        "fp64" (both phases in FP64)."""
+        "fp64" (both phases in FP64); kernel "epanechnikov" or "gaussian"."""
         v = np.ascontiguousarray(votes, np.float64).reshape(-1, 6)
         s = np.ascontiguousarray(seeds, np.int64)
         means = np.zeros((s.size, 6))
@@ -357,6 +362,7 @@ class Gb300Backend:
         _check(self._lib.sym_meanshift6(self._ctx, v.ctypes.data_as(C.POINTER(C.c_double)),
                                         v.shape[0], s.ctypes.data_as(C.POINTER(C.c_int64)), s.size,
                                         bandwidth, code, max_iterations, polish_iterations,
+                                        KERNELS[kernel],
                                         means.ctypes.data_as(C.POINTER(C.c_double)),
                                         state.ctypes.data_as(C.POINTER(C.c_uint8)), iters))
         return means, state, (iters[0], iters[1])

@@ -127,7 +127,7 @@ template <typename T, bool COUNT, bool NEWTON>
 __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cbox, uint64_t nchunks,
                                                   uint64_t q, const T *means, const uint8_t *state,
                                                   const int32_t *ids, uint64_t nactive, T h2,
-                                                  float skip_gap2, uint64_t chunks_per_split,
+                                                  T gk, float skip_gap2, uint64_t chunks_per_split,
                                                   T *partial, unsigned long long *evals) {
   constexpr int stride = COUNT ? 8 : kPartial;
   __shared__ T xs[kChunk * 8];
@@ -202,18 +202,20 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
         if (COUNT) {
           acc[6] += T(1);
         } else {
-          T w = T(1) - d2 / h2;
+          const T w = gk > T(0) ? exp(-gk * (d2 / h2)) : T(1) - d2 / h2;
 #pragma unroll
           for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
           acc[6] += w;
-          if (newton) {
+          if (newton) {  // Epanechnikov: unweighted sums; Gaussian: weighted
+            const T wn = gk > T(0) ? w : T(1);
             T *ns = nsum + threadIdx.x;
             int at = 6;
 #pragma unroll
             for (int d = 0; d < 6; ++d) {
-              ns[d * kChunk] += e[d];
+              const T we = wn * e[d];
+              ns[d * kChunk] += we;
 #pragma unroll
-              for (int l = d; l < 6; ++l, ++at) ns[at * kChunk] += e[d] * e[l];
+              for (int l = d; l < 6; ++l, ++at) ns[at * kChunk] += we * e[l];
             }
           }
         }
@@ -262,10 +264,12 @@ __device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
 }
 
 // One step of a seed from its summed values (ms_reduce): the
-// Epanechnikov mean-shift step m - x for a kMoving seed, the safeguarded
-// Newton step (I - J)^-1 (m - x) for a kNear seed, where
+// mean-shift step m - x for a kMoving seed, the safeguarded Newton step
+// (I - J)^-1 (m - x) for a kNear seed, where for Epanechnikov weights
 //   J = dm/dx = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T),
-// d = v - x over the votes within the bandwidth.  Stopping rules: exhausted
+// d = v - x over the votes within the bandwidth, and for the Gaussian
+// exp(-k d^2 / h^2) (dw/dx = 2 k w d / h^2)
+//   J = 2 k / (h^2 sum w) * (sum w d d^T - (m - x) (sum w d)^T).  Stopping rules: exhausted
 // when the weight is <= 1e-14 (reference, src/cpu/clustering.cpp:169-181),
 // converged when a Newton step^2 < kNewtonStop2 h^2, settled (plain step
 // taken) when the Newton step is rejected, or when an accepted Newton step
@@ -298,7 +302,7 @@ __global__ void __launch_bounds__(kChunk) ms_reduce(const T *partial, uint64_t s
 template <typename T>
 __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint64_t slots,
                                                     const int32_t *ids, uint64_t nactive, T h2,
-                                                    int polish_it, uint8_t *state) {
+                                                    T gk, int polish_it, uint8_t *state) {
   const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
   if (slot >= nactive) return;
   const int32_t s = ids[slot];
@@ -328,7 +332,7 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
   }
   const T *sd = ns, *sdd = ns + 6;
   T M[6][6], step[6];
-  const T g = T(2) / (h2 * acc[6]);
+  const T g = (gk > T(0) ? T(2) * gk : T(2)) / (h2 * acc[6]);
   for (int d = 0, at = 0; d < 6; ++d)
     for (int l = d; l < 6; ++l, ++at) M[d][l] = M[l][d] = sdd[at];
   for (int d = 0; d < 6; ++d) {
@@ -494,16 +498,18 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
     const dim3 grid(unsigned(g.tiles), unsigned(g.splits));
     if (counts[1])
       ms_tile<T, false, true><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state, ids,
-                                                      n, T(h2), gap * gap, g.cps, partial, evals);
+                                                      n, T(h2), T(v.kernel_k), gap * gap, g.cps,
+                                                      partial, evals);
     else
       ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state,
-                                                       ids, n, T(h2), gap * gap, g.cps, partial, evals);
+                                                       ids, n, T(h2), T(v.kernel_k), gap * gap,
+                                                       g.cps, partial, evals);
     check_launch();
     ms_reduce<T><<<dim3(unsigned(g.tiles), counts[1] ? 34u : 7u, kGroups), kChunk, 0, st>>>(
         partial, g.splits, g.slots, n, red);
     check_launch();
     ms_update<T><<<unsigned(g.tiles), kChunk, 0, st>>>(means, red, g.slots, ids, n, T(h2),
-                                                       polish ? it : -1, state);
+                                                       T(v.kernel_k), polish ? it : -1, state);
     check_launch();
     call.launched(3);
   }
@@ -614,8 +620,8 @@ void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm
   float *partial = call.alloc<float>(g.splits * g.slots * 8);
   float gap = float(std::sqrt(h2)) + 1e-6f;
   ms_tile<float, true, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
-      v.desc, v.cbox, v.nchunks, v.q, points, nullptr, ids, nm, float(h2), gap * gap, g.cps, partial,
-      nullptr);
+      v.desc, v.cbox, v.nchunks, v.q, points, nullptr, ids, nm, float(h2), 0.f, gap * gap, g.cps,
+      partial, nullptr);
   check_launch();
   sum_counts<<<blocks_for(nm), kThreads, 0, st>>>(partial, g.splits, g.slots, ids, nm, counts);
   check_launch();

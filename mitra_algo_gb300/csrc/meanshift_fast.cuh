@@ -45,8 +45,16 @@ struct Tuning {
   int check_interval = 8;       // tensor approach iterations between host checks
 };
 
+// The Gaussian kernel of the extension: w = exp(-kGaussK d^2 / h^2) for
+// d < h (sigma = h / 3, weight 0.011 at the cut), 0 beyond, so chunk
+// skipping stays exact.
+constexpr double kGaussK = 4.5;
+
 struct VoteSet {
   Tuning tuning;
+  // weight kernel: 0 Epanechnikov 1 - d^2 / h^2 (the reference's); > 0 the
+  // truncated Gaussian exp(-kernel_k d^2 / h^2)
+  double kernel_k = 0;
   uint64_t q = 0, nchunks = 0;
   float *desc = nullptr;      // q x 8, Morton order
   double *desc64 = nullptr;   // q x 8, same order (only when requested)

@@ -547,6 +547,7 @@ struct TcArgs {
   const int32_t *ids;
   const float *gbox;        // box of all votes; its centre is c_g
   float inv_h;
+  float gauss_k2;           // 0: Epanechnikov weights; > 0: exp2(-gauss_k2 d^2 / h^2)
   float *partial;
   unsigned long long *evals;
   int *status;
@@ -571,6 +572,19 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
 __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
   uint32_t r;
   asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+
+// Truncated Gaussian weights of t = 1 - d^2 / h^2: exp2(k2 (t - 1)) for
+// t > 0 and 0 otherwise (the exponent of -inf), two at a time: the
+// exponents are rounded to BF16 and the MUFU's BF16x2 base-2 exponential
+// makes both BF16 weights in one instruction.
+__device__ __forceinline__ uint32_t gauss_bf16x2(float lo, float hi, float k2) {
+  const float alo = lo > 0.f ? k2 * (lo - 1.f) : -INFINITY;
+  const float ahi = hi > 0.f ? k2 * (hi - 1.f) : -INFINITY;
+  uint32_t a, r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(a) : "f"(ahi), "f"(alo));
+  asm("ex2.approx.ftz.bf16x2 %0, %1;" : "=r"(r) : "r"(a));
   return r;
 }
 
@@ -751,6 +765,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
     const float2 one2 = make_float2(1.f, 1.f);
     const uint32_t lane_base = uint32_t(quad * 32) << 16;
     const uint32_t dcol = tmem + 128 * p + 64 * h, wcol = tmem + kTcColW + 64 * p + 32 * h;
+    const bool gauss = a.gauss_k2 > 0.f;
     bool ok = true;
     uint32_t kth = 0;  // index of chunk i among the pair's chunks
     for (uint32_t i = p; i < n; i += 2, ++kth) {
@@ -776,15 +791,28 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         __syncwarp();
         if (lane == 0) mbar_arrive(&d_free[p]);  // D[p] may be overwritten
         const float2 rowc2 = make_float2(rowc, rowc);
-        for (int j = 0; j < 16; ++j) {
-          float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
-                          one2, rowc2);
-          w[j] = relu_bf16x2(t.x, t.y);
-        }
-        for (int j = 0; j < 16; ++j) {
-          float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
-                          one2, rowc2);
-          w2[j] = relu_bf16x2(t.x, t.y);
+        if (gauss) {
+          for (int j = 0; j < 16; ++j) {
+            float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
+                            one2, rowc2);
+            w[j] = gauss_bf16x2(t.x, t.y, a.gauss_k2);
+          }
+          for (int j = 0; j < 16; ++j) {
+            float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
+                            one2, rowc2);
+            w2[j] = gauss_bf16x2(t.x, t.y, a.gauss_k2);
+          }
+        } else {
+          for (int j = 0; j < 16; ++j) {
+            float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
+                            one2, rowc2);
+            w[j] = relu_bf16x2(t.x, t.y);
+          }
+          for (int j = 0; j < 16; ++j) {
+            float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
+                            one2, rowc2);
+            w2[j] = relu_bf16x2(t.x, t.y);
+          }
         }
       }
       if (kth > 0) {
@@ -1003,7 +1031,8 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   const float gap = float(std::sqrt(h2)) + 1e-6f;
   call.launched();
   TcArgs args{images, v.nchunks, list, offsets, pieces, nact, means, ids, v.gbox,
-              float(1.0 / std::sqrt(h2)), partial, evals, call.status()};
+              float(1.0 / std::sqrt(h2)), float(v.kernel_k * 1.4426950408889634), partial, evals,
+              call.status()};
   // CUDA events around every launch of the tensor kernel (its own time)
   std::vector<cudaEvent_t> marks;
   auto mark_event = [&]() {

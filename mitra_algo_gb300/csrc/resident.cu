@@ -515,6 +515,9 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   if (fo.tc_ctas_per_sm) tuning.tc_ctas_per_sm = fo.tc_ctas_per_sm;
   if (fo.check_interval) tuning.check_interval = fo.check_interval;
   VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q, tuning);
+  if (fo.kernel != SYM_KERNEL_EPANECHNIKOV && fo.kernel != SYM_KERNEL_GAUSSIAN)
+    fail(SYM_INVALID_ARGUMENT, "unknown mean-shift kernel");
+  vs.kernel_k = fo.kernel == SYM_KERNEL_GAUSSIAN ? kGaussK : 0.0;
   clock.mark(5);
   // ---- (c) mean shift from K seeds (uniform draw of distinct votes)
   uint64_t k = std::min<uint64_t>(uint64_t(std::max(fo.seeds, 1)), q);
@@ -727,7 +730,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
 extern "C" {
 
 void sym_fast_options_default(sym_fast_options *o) {
-  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0, 0, 0, 0, 0, 0};
+  *o = sym_fast_options{SYM_MS_BF16_REFINED, 2048, 7, 100, 100, 0, 1, SYM_RIGID, 0, 0, 0, 0, 0, 0,
+                        SYM_KERNEL_EPANECHNIKOV};
 }
 
 sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
@@ -927,14 +931,16 @@ __global__ void pack_votes(const double *in, uint64_t q, float *d32, double *d64
 
 sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q, const int64_t *seeds,
                           uint64_t k, double bandwidth, int32_t precision, int32_t max_iterations,
-                          int32_t polish_iterations, double *means_out, uint8_t *state_out,
-                          int32_t *iterations_out) {
+                          int32_t polish_iterations, int32_t kernel, double *means_out,
+                          uint8_t *state_out, int32_t *iterations_out) {
   if (!ctx || (q && !votes) || (k && (!seeds || !means_out || !state_out)) || !iterations_out)
     return SYM_INVALID_ARGUMENT;
   try {
     sym::Call call(ctx, "mean_shift6");
     if (!(bandwidth > 0) || max_iterations < 1 || polish_iterations < 0)
       sym::fail(SYM_INVALID_ARGUMENT, "Invalid parameter range; see --help");
+    if (kernel != SYM_KERNEL_EPANECHNIKOV && kernel != SYM_KERNEL_GAUSSIAN)
+      sym::fail(SYM_INVALID_ARGUMENT, "unknown mean-shift kernel");
     if (q > uint64_t(std::numeric_limits<int32_t>::max()))
       sym::fail(SYM_OVERFLOW, "vote ids exceed int32 range");
     for (uint64_t i = 0; i < k; ++i)
@@ -949,6 +955,7 @@ sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q, con
     pack_votes<<<sym::blocks_for(q), sym::kThreads, 0, st>>>(raw, q, d32, d64);
     sym::check_launch();
     sym::VoteSet vs = sym::build_vote_set(call, d32, d64, q);
+    vs.kernel_k = kernel == SYM_KERNEL_GAUSSIAN ? sym::kGaussK : 0.0;
     int64_t *dseeds = call.upload(seeds, k);
     int64_t *rank = call.alloc<int64_t>(k);
     sym::ranks_of<<<sym::blocks_for(k), sym::kThreads, 0, st>>>(vs.rank, dseeds, k, rank);

@@ -2,11 +2,14 @@
 mean-shift of the throughput extension (no reference counterpart; parity
 unpinned).
 
-Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2.  A seed takes plain
-mean-shift steps m(x) - x until its squared step is below 1e-4 h^2, then
-safeguarded Newton steps on m(x) = x:
+Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2 (kernel "epanechnikov"),
+or the truncated Gaussian w = exp(-4.5 d^2/h^2) for d^2 < h^2 (kernel
+"gaussian").  A seed takes plain mean-shift steps m(x) - x until its squared
+step is below 1e-4 h^2, then safeguarded Newton steps on m(x) = x:
     (I - J) s = m(x) - x,   J = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T)
-with d = v - x over the votes within the bandwidth.  A Newton step is taken
+with d = v - x over the votes within the bandwidth (Epanechnikov), or
+    J = 2 k / (h^2 sum w) * (sum w d d^T - (m - x) (sum w d)^T),  k = 4.5
+(Gaussian: dw/dx = 2 k w d / h^2).  A Newton step is taken
 when the 6x6 system is regular (pivots above 1e-12), |s| <= h/4 and
 s.(m - x) > 0 (or the step already meets the convergence test); otherwise the
 density is flat along some direction (a ridge, no well-defined mode
@@ -21,6 +24,14 @@ import numpy as np
 
 MOVING, CONVERGED, EXHAUSTED, NEAR, SETTLED = 0, 1, 2, 3, 4
 SWITCH2, NEWTON_STOP2, TRUST, NEWTON_CAP = 1e-4, 1e-8, 0.25, 10
+GAUSS_K = 4.5
+
+
+def weights(d2, h2, kernel):
+    inside = d2 < h2
+    if kernel == "gaussian":
+        return np.where(inside, np.exp(-GAUSS_K * (d2 / h2)), 0.0)
+    return np.where(inside, 1 - d2 / h2, 0.0)
 
 
 def solve6(M, b, tiny=1e-12):
@@ -44,14 +55,20 @@ def solve6(M, b, tiny=1e-12):
     return b
 
 
-def newton_seed(x, m, w, tot, delta, move, h2, polish_it):
+def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov"):
     """The kNear step of one seed from its weights w over all votes x
     (polish_it: the polish iteration, -1 in the approach phase)."""
     inside = w > 0
     di = x[inside] - m
-    sd = di.sum(0)
-    g = 2.0 / (h2 * tot)
-    M = np.eye(6) - g * (di.T @ di - np.outer(delta, sd))
+    if kernel == "gaussian":
+        wi = w[inside][:, None]
+        sd = (wi * di).sum(0)
+        g = 2.0 * GAUSS_K / (h2 * tot)
+        M = np.eye(6) - g * ((wi * di).T @ di - np.outer(delta, sd))
+    else:
+        sd = di.sum(0)
+        g = 2.0 / (h2 * tot)
+        M = np.eye(6) - g * (di.T @ di - np.outer(delta, sd))
     s = solve6(M, delta)
     if (s is not None and np.all(np.isfinite(s)) and s @ s <= TRUST * TRUST * h2
             and (s @ delta > 0 or s @ s < NEWTON_STOP2 * h2)):
@@ -61,7 +78,8 @@ def newton_seed(x, m, w, tot, delta, move, h2, polish_it):
     return m + delta, SETTLED
 
 
-def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=100, block=64):
+def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=100, block=64,
+               kernel="epanechnikov"):
     """Approach phase (at most max_iterations; kMoving seeds only, a seed
     leaves once it is near a mode), then the polish phase (at most
     polish_iterations; kMoving and kNear seeds).  Returns the means, the
@@ -72,11 +90,11 @@ def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=10
     h2 = bandwidth * bandwidth
     counts = []
     for phase, budget in ((False, max_iterations), (True, polish_iterations)):
-        counts.append(_phase(x, means, state, h2, budget, phase, block))
+        counts.append(_phase(x, means, state, h2, budget, phase, block, kernel))
     return means, state, tuple(counts)
 
 
-def _phase(x, means, state, h2, budget, polish, block):
+def _phase(x, means, state, h2, budget, polish, block, kernel):
     iterations = 0
     for it in range(budget):
         act = np.flatnonzero((state == MOVING) | ((state == NEAR) & polish))
@@ -87,7 +105,7 @@ def _phase(x, means, state, h2, budget, polish, block):
             ids = act[b:b + block]
             m = means[ids]
             d2 = ((x[None, :, :] - m[:, None, :]) ** 2).sum(-1)
-            w = np.where(d2 < h2, 1 - d2 / h2, 0.0)
+            w = weights(d2, h2, kernel)
             tot = w.sum(1)
             safe = np.where(tot <= 1e-14, 1.0, tot)
             delta = (w @ x) / safe[:, None] - m
@@ -101,7 +119,7 @@ def _phase(x, means, state, h2, budget, polish, block):
                         state[i] = NEAR
                 else:
                     means[i], state[i] = newton_seed(x, m[j], w[j], tot[j], delta[j], move[j], h2,
-                                                     it if polish else -1)
+                                                     it if polish else -1, kernel)
     return iterations
 
 

@@ -168,3 +168,24 @@ def test_vote_cap_subsamples_uniformly_and_deterministically(fast):
     assert abs(a["votes"] - cap) <= 0.02 * cap            # ~cap votes enter the mean shift
     assert a["votes"] == b["votes"] == c["votes"]         # the same subsample every run
     assert a["rotation"] == b["rotation"] and a["support"] == b["support"]
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp32"])
+def test_gaussian_kernel_pipeline(fast, precision):
+    """The pipeline with the truncated Gaussian kernel (exp weights): the
+    same pairs and votes, every compared mode within 1e-4 of the FP64 run of
+    the same seeds, and the planted 5-fold rotation among the top modes."""
+    gpu, p, opts, runs = fast
+    resident = gpu.load_mesh(p)
+    r = gpu.detect_fast(resident, None, opts, precision=precision, seeds=256, max_iterations=300,
+                        polish_iterations=30, reference_seeds=128, kernel="gaussian")
+    resident.close()
+    assert r["pairs"] == runs[precision]["pairs"] and r["votes"] == runs[precision]["votes"]
+    assert r["modes_compared"] >= 10
+    assert r["modes_within"] == r["modes_compared"], r["mode_error_max"]
+    hits = []
+    for rot in r["rotation"]:
+        angle, axis = rotation_angle_axis(rot)
+        k = angle / (2 * np.pi / 5)
+        hits.append(abs(axis[2]) > 0.99 and abs(k - round(k)) < 0.05 and round(k) in (1, 2))
+    assert any(hits)

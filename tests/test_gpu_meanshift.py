@@ -54,6 +54,38 @@ def test_meanshift6_bf16_mode_error(gpu, case):
     assert np.max(err) <= 1e-4, (np.max(err), iters)
 
 
+@pytest.fixture(scope="module")
+def gauss_case():
+    votes, centers = clustered_votes()
+    rng = np.random.default_rng(4)
+    seeds = np.sort(rng.choice(len(votes), 300, replace=False))
+    ref, state, _ = meanshift6(votes, seeds, 0.06, 200, 200, kernel="gaussian")
+    return votes, seeds, ref, state
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-5)])
+def test_gaussian_kernel_matches_fp64(gpu, gauss_case, precision, tol):
+    """The truncated Gaussian kernel (exp weights, Gaussian Newton steps):
+    FP64 and FP32 follow the restatement's trajectories."""
+    votes, seeds, ref, ref_state = gauss_case
+    means, state, iters = gpu.meanshift6(votes, seeds, 0.06, precision, 200, 200,
+                                         kernel="gaussian")
+    assert np.array_equal(state, ref_state)
+    err = rel(means, ref)
+    assert np.max(err) <= tol, (precision, np.max(err), iters)
+
+
+def test_gaussian_kernel_bf16_mode_error(gpu, gauss_case):
+    """BF16 weights from the MUFU's BF16x2 exponential in the tensor kernel,
+    FP32 Gaussian polish: every mode converged in both runs within 1e-4."""
+    votes, seeds, ref, ref_state = gauss_case
+    means, state, iters = gpu.meanshift6(votes, seeds, 0.06, "bf16", 200, 200, kernel="gaussian")
+    both = (state == 1) & (ref_state == 1)
+    assert both.sum() >= 0.9 * (ref_state == 1).sum()
+    err = rel(means[both], ref[both])
+    assert np.max(err) <= 1e-4, (np.max(err), iters)
+
+
 def test_meanshift6_finds_the_clusters(gpu):
     votes, centers = clustered_votes(seed=5)
     seeds = np.arange(0, len(votes), 97)
