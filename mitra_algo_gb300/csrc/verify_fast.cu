@@ -219,37 +219,25 @@ __device__ __forceinline__ float face_d2(const BvhView &b, F3 p, int32_t f) {
   return triangle_d2f(p, vtx(b, b.faces[f]), vtx(b, b.faces[b.nf + f]), vtx(b, b.faces[2 * b.nf + f]));
 }
 
-// Nearest face within `best` (FP32); -1 when none.  Warp-cooperative: the
-// 32 lanes of a warp (32 consecutive queries, neighbouring vertices under
-// the same motion, so nearby points) walk one traversal together.  A node
-// is entered when it can still improve some lane's best face; when both
-// children can, the one more lanes find nearer goes first.  Each lane keeps
-// its own best face and distance, and tests a leaf's face only when the
-// face's box can improve its own best, so the result is each lane's own
-// nearest face (ties between faces at equal FP32 distance may resolve to
-// another of them).  Every lane of the warp calls it, `active` false for
-// the lanes without a query.
-__device__ int32_t nearest_face_fast(const BvhView &b, F3 p, bool active, float &best,
-                                     int *status) {
-  constexpr unsigned kAll = 0xffffffffu;
+// Nearest face within `best` (FP32), near-first; -1 when none.
+__device__ int32_t nearest_face_fast(const BvhView &b, F3 p, float &best, int *status) {
   int32_t face = -1;
-  if (!active) best = 0.f;  // no distance improves on 0
   if (b.nf == 1) {
-    float d = active ? face_d2(b, p, 0) : INFINITY;
+    float d = face_d2(b, p, 0);
     if (d < best) best = d, face = 0;
     return face;
   }
-  int32_t stack[kStackFast];  // node ids: the same in every lane
-  float dist[kStackFast];     // each lane's distance to the node's box
+  int32_t stack[kStackFast];
+  float dist[kStackFast];
   int top = 0;
   stack[top] = 0, dist[top++] = 0.f;
   while (top) {
     --top;
-    if (!__any_sync(kAll, dist[top] < best)) continue;
+    if (dist[top] >= best) continue;
     const int32_t node = stack[top];
     const float *bx = b.box + int64_t(node) * 12;
     const int32_t c0 = b.child[2 * node], c1 = b.child[2 * node + 1];
-    const float d0 = box_d2f(p, bx), d1 = box_d2f(p, bx + 6);
+    float d0 = box_d2f(p, bx), d1 = box_d2f(p, bx + 6);
     if (c0 < 0 && d0 < best) {
       float d = face_d2(b, p, ~c0);
       if (d < best) best = d, face = ~c0;
@@ -259,20 +247,17 @@ __device__ int32_t nearest_face_fast(const BvhView &b, F3 p, bool active, float 
       if (d < best) best = d, face = ~c1;
     }
     const bool p0 = c0 >= 0 && d0 < best, p1 = c1 >= 0 && d1 < best;
-    const bool any0 = __any_sync(kAll, p0), any1 = __any_sync(kAll, p1);
     if (top + 2 > kStackFast) {
-      if (active) atomicExch(status, DS_CAPACITY);
+      atomicExch(status, DS_CAPACITY);
       return face;
     }
-    if (any0 && any1) {  // the child more lanes find nearer is popped first
-      const int near0 = __popc(__ballot_sync(kAll, p0 && (!p1 || d0 <= d1)));
-      const int near1 = __popc(__ballot_sync(kAll, p1 && (!p0 || d1 < d0)));
-      const bool first0 = near0 >= near1;
+    if (p0 && p1) {  // the nearer child is popped first
+      bool first0 = d0 <= d1;
       stack[top] = first0 ? c1 : c0, dist[top++] = first0 ? d1 : d0;
       stack[top] = first0 ? c0 : c1, dist[top++] = first0 ? d0 : d1;
-    } else if (any0) {
+    } else if (p0) {
       stack[top] = c0, dist[top++] = d0;
-    } else if (any1) {
+    } else if (p1) {
       stack[top] = c1, dist[top++] = d1;
     }
   }
@@ -283,18 +268,15 @@ __device__ int32_t nearest_face_fast(const BvhView &b, F3 p, bool active, float 
 // the nearest face when vertex i supports mode m in that direction (-1
 // otherwise), its FP32 squared distance in `best` (entering as tau^2) and
 // the image of the vertex in q.  The motion is applied in FP64, the search
-// runs in FP32.  Every lane of the warp calls it (the search is
-// warp-cooperative); `valid` false for lanes past the last query.
+// runs in FP32.
 __device__ __forceinline__ int32_t support_query(const BvhView &b, const double *xyz,
                                                  const double *vn, const Motion32 &m, uint64_t i,
-                                                 bool inverse, bool valid, double tau, float &best,
-                                                 double q[3], int *status) {
+                                                 bool inverse, double tau, float &best, double q[3],
+                                                 int *status) {
   const uint64_t nv = b.nv;
   double r[9];
   for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
-  double p[3] = {0, 0, 0};
-  if (valid)
-    for (int a = 0; a < 3; ++a) p[a] = xyz[a * nv + i];
+  const double p[3] = {xyz[i], xyz[nv + i], xyz[2 * nv + i]};
   double move2 = 0;
   for (int a = 0; a < 3; ++a) {
     double s = 0;
@@ -302,13 +284,13 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
     q[a] = inverse ? s : s + m.t[a];
     move2 += (q[a] - p[a]) * (q[a] - p[a]);
   }
-  bool eligible = valid && !(move2 < 4 * tau * tau);
-  if (eligible && m.reflection) {
+  if (move2 < 4 * tau * tau) return -1;
+  if (m.reflection) {
     double side = m.n[0] * p[0] + m.n[1] * p[1] + m.n[2] * p[2] + m.offset;
-    eligible = !(inverse ? side <= tau : side >= -tau);
+    if (inverse ? side <= tau : side >= -tau) return -1;
   }
   const F3 qf{float(q[0]), float(q[1]), float(q[2])};
-  const int32_t face = nearest_face_fast(b, qf, eligible, best, status);
+  const int32_t face = nearest_face_fast(b, qf, best, status);
   if (face < 0) return -1;
   const F3 a = vtx(b, b.faces[face]), bb = vtx(b, b.faces[b.nf + face]),
            cc = vtx(b, b.faces[2 * b.nf + face]);
@@ -327,20 +309,19 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
 __global__ void verify_vertices_fast(BvhView b, const double *xyz, const double *vn,
                                      const Motion32 *motions, uint64_t nc, double tau, float tau2,
                                      uint8_t *flags, double *err, int *status) {
-  const uint64_t nv = b.nv, rows = nc * 2 * nv;
-  const uint64_t row0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (row0 - (threadIdx.x & 31) >= rows) return;  // the whole warp is past the end
-  const bool valid = row0 < rows;
-  const uint64_t row = valid ? row0 : rows - 1;  // lanes past the end mirror the last query
+  uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t nv = b.nv;
+  if (row >= nc * 2 * nv) return;
   const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
+  flags[row] = 0;
+  if (!inverse) err[c * nv + i] = 0;
   float best = tau2;
   double q[3];
-  const bool hit = support_query(b, xyz, vn, motions[c], i, inverse, valid, tau, best, q, status) >= 0;
-  if (!valid) return;
-  flags[row] = hit;
-  if (!inverse) err[c * nv + i] = hit ? double(best) : 0.0;
+  if (support_query(b, xyz, vn, motions[c], i, inverse, tau, best, q, status) < 0) return;
+  flags[row] = 1;
+  if (!inverse) err[c * nv + i] = double(best);
 }
 
 // ------------------------------------------------ FP64 transform refinement
@@ -390,17 +371,14 @@ struct Origin {
 __global__ void refine_pairs(BvhView b, const double *xyz, const double *vn,
                              const Motion32 *motions, uint64_t nc, double tau, float tau2, Origin o,
                              double *target, uint8_t *ok, int *status) {
-  const uint64_t nv = b.nv, rows = nc * nv;
-  const uint64_t row0 = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (row0 - (threadIdx.x & 31) >= rows) return;  // the whole warp is past the end
-  const bool valid = row0 < rows;
-  const uint64_t row = valid ? row0 : rows - 1;
+  const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t nv = b.nv;
+  if (row >= nc * nv) return;
   const uint64_t c = row / nv, i = row % nv;
+  ok[row] = 0;
   float best = tau2;
   double q[3];
-  const int32_t face = support_query(b, xyz, vn, motions[c], i, false, valid, tau, best, q, status);
-  if (!valid) return;
-  ok[row] = 0;
+  const int32_t face = support_query(b, xyz, vn, motions[c], i, false, tau, best, q, status);
   if (face < 0) return;
   double corner[3][3], out[3];
   for (int k = 0; k < 3; ++k) {
