@@ -159,7 +159,7 @@ __device__ __forceinline__ Source load_source(const int32_t *selected, uint64_t 
 // move by less than 5e-7 M with M >= max |k|; each coordinate moves by at
 // most 2^-24 of the largest coordinate magnitude S of the two points, so the
 // distance moves by at most 2.1e-7 S.  Outside those bands (widened further
-// for the FP32 arithmetic) the FP32 verdict is the FP64 one.
+// for the FP32 arithmetic) the FP32 decision is the FP64 one.
 __device__ __forceinline__ bool accept_filtered(const Source &src, const SortedSamples &srt,
                                                 uint64_t k, float tf, float min_dist_f, double t,
                                                 double min_dist) {
