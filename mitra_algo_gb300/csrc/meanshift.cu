@@ -12,10 +12,10 @@
 //   1. one launch runs the trajectory of EVERY vote as a seed, a warp per
 //      seed, and records its final mean, its converged/exhausted flags and
 //      its support as a bitmask over same-kind votes;
-//   2. the host replays the reference driver verbatim (RNG draw per seed,
+//   2. the host replays the reference's host loop verbatim (RNG draw per seed,
 //      visited set, merge test, budgets) on those results - no device round
 //      trip per trajectory;
-//   3. one launch re-runs only the trajectories the driver used and adds
+//   3. one launch re-runs only the trajectories the host loop used and adds
 //      each member's per-iteration hit into its cluster's support counts;
 //      one launch picks each vote's winning cluster (largest count, first
 //      cluster on ties).

@@ -1,5 +1,5 @@
 """ORACLE - test infrastructure only (see oracle/oracle.cpp).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
-this package, and only as the checker; the GPU library never uses it.
+this package, and only to check results; the GPU library never uses it.
 """

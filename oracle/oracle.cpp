@@ -2,8 +2,8 @@
 //
 // ORACLE - test infrastructure only.  This is a CPU restatement of the
 // reference (deoksieze/Mitra_algo) CPU backend for the symmetry hot path, used
-// by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as
-// the checker.  The GPU library never links, loads or calls it.
+// by tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg to
+// check results.  The GPU library never links, loads or calls it.
 //
 // Every function follows the reference algorithm operation by operation, in
 // FP64, so that results agree bit for bit with the reference's own CPU build

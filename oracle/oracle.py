@@ -5,7 +5,7 @@ reference's CPU backend, oracle/oracle.cpp) with the method names of the
 reference's ``Backend`` (include/symmetry/pipeline.h:54-69), plus a runner
 for the reference's own CPU library (oracle/_ref/ref_harness) where it has
 been built.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
-leg use this module, as the checker.
+leg use this module, to check results.
 """
 from __future__ import annotations
 
