@@ -991,7 +991,7 @@ __global__ void __launch_bounds__(256) ms_update_bulk(float *means, const float 
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
                          double h2, int max_iter, int *iterations, double *evaluations,
                          uint32_t *trace, int trace_len, double *kernel_ms,
-                         uint64_t *kernel_launches) {
+                         uint64_t *kernel_launches, double *seed_iterations) {
   *iterations = 0;
   *evaluations = 0;
   if (kernel_ms) *kernel_ms = 0;
@@ -1084,12 +1084,15 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   call.sync();
   *iterations = int(active_iterations);
   *evaluations = double(ev);
-  if (trace && trace_len > 0) {
+  if ((trace && trace_len > 0) || seed_iterations) {
     std::vector<uint32_t> tr(trace_cap);
     call.d2h(tr.data(), trace_dev, trace_cap * sizeof(uint32_t));
     call.sync();
-    for (int i = 0; i < trace_len && i < int(active_iterations) && i < int(trace_cap); ++i)
+    for (int i = 0; trace && i < trace_len && i < int(active_iterations) && i < int(trace_cap); ++i)
       trace[i] = tr[i];
+    // every iteration with active seeds is recorded (trace_cap = max_iter)
+    for (unsigned i = 0; seed_iterations && i < active_iterations && i < trace_cap; ++i)
+      *seed_iterations += tr[i];
   }
   // launches after the last iteration with active seeds found none and
   // returned at once: only the active ones are timed

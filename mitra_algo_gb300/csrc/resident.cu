@@ -45,10 +45,12 @@ void verification_fast(Call &, const Lbvh &, const double *, const double *, con
                        int, const double *, double *, double *, uint32_t *);
 // BF16 tensor-core bulk iterations (meanshift_tc.cu); returns false when the
 // tensor path cannot run this problem (the caller then stays in FP32).
+// seed_iterations (optional) receives the sum over iterations of the
+// active seeds.
 bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k,
                          double h2, int max_iter, int *iterations, double *evaluations,
                          uint32_t *trace = nullptr, int trace_len = 0, double *kernel_ms = nullptr,
-                         uint64_t *kernel_launches = nullptr);
+                         uint64_t *kernel_launches = nullptr, double *seed_iterations = nullptr);
 void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,
                       const uint16_t *b2, float *d_out, float *acc_out);
 }  // namespace sym
@@ -543,7 +545,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   // approaching
   bool tensor = fo.precision == SYM_MS_BF16_REFINED &&
                 meanshift_bf16_bulk(call, vs, m32, st32, k, h2, fo.max_iterations, &bulk, &tc_evals,
-                                    r.bulk_trace, 320, &r.tc_kernel_ms, &r.tc_launches);
+                                    r.bulk_trace, 320, &r.tc_kernel_ms, &r.tc_launches,
+                                    &r.seed_iterations);
   r.tc_evaluations = tc_evals;
   if (!tensor)
     bulk = shift(call, vs, m32, st32, k, h2, fo.max_iterations, false, &r.seed_iterations, evals,
