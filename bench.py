@@ -579,11 +579,14 @@ def run_reference(args):
     prepared, opts = workload(args.small)
     from oracle import oracle
     cpu = oracle.OracleBackend()
-    # the GPU run's mean-shift work counts come from a fixed estimate of the
-    # same workload when no GPU result is at hand: seeds x avg iterations.
+    # the mean-shift work counts of this workload as the GPU run measures
+    # them (no GPU result is at hand here): 1.09e7 pairs, 2.18e7 votes, and
+    # 52.8 iterations per seed over approach and polish (108,139 seed
+    # iterations for 2,048 seeds in both forms) - the reference's own rule
+    # (steps until movement^2 < 1e-6 h^2, up to 100) runs at least as many
     f = cpu.curvature(prepared.mesh, prepared.topology, opts)
     sel = cpu.select(prepared.mesh, f, prepared.topology.weights, opts, oracle.rng(opts.seed))
-    gpu_like = {"pairs": 10_000_000, "votes": 20_000_000, "seed_iterations": SEEDS * 12.0,
+    gpu_like = {"pairs": 10_918_138, "votes": 21_836_276, "seed_iterations": SEEDS * 52.8,
                 "clusters": 20, "rotation": [], "translation": []}
     times = []
     est = None
