@@ -385,6 +385,10 @@ def run_gpu(args):
                                tuning=shape(precision))
 
     if args.once:  # one warm-up and one measured pipeline run (profiler captures)
+        def step(precision, reference_seeds=0):  # noqa: F811 - the --kernel choice applies here
+            return gpu.detect_fast(resident, sample, opts, precision=precision, seeds=SEEDS,
+                                   max_iterations=ITERATIONS, polish_iterations=POLISH,
+                                   vote_cap=VOTE_CAP, kernel=args.kernel)
         step(args.once)
         r = step(args.once)
         print(json.dumps({"precision": args.once, "stage_ms": r["stage_ms"], "pairs": r["pairs"],
@@ -626,6 +630,8 @@ def main():
     ap.add_argument("--bandwidth", type=float, default=None, help="override the bandwidth")
     ap.add_argument("--once", choices=["bf16", "fp32"], default=None,
                     help="run the pipeline once after one warm-up run and print its stages")
+    ap.add_argument("--kernel", choices=["epanechnikov", "gaussian"], default="epanechnikov",
+                    help="weight kernel of the --once runs (profiler captures)")
     ap.add_argument("--small", action="store_true",
                     help="level-5 mesh, 5,000 samples, 256 seeds (profiler captures)")
     args = ap.parse_args()
