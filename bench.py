@@ -467,10 +467,10 @@ def run_gpu(args):
     refl = reflection_bench(gpu) if extra else None
 
     def gaussian_leg(steps=3):
-        """The same workload with the truncated Gaussian kernel (exp weights,
+        """The same workload with the shifted Gaussian kernel (exp weights,
         MUFU BF16x2 exponentials in the tensor kernel): both forms' device
         time per mesh (CUDA events, like the main legs) and mode error."""
-        out = {"kernel": "exp(-4.5 d^2/h^2) for d < h"}
+        out = {"kernel": "2^(-8 d^2/h^2) - 2^-8 for d < h"}
         for p in ("bf16", "fp32"):
             kw = dict(precision=p, seeds=SEEDS, max_iterations=ITERATIONS,
                       polish_iterations=POLISH, vote_cap=VOTE_CAP, tuning=shape(p),

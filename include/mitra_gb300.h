@@ -341,10 +341,10 @@ typedef struct sym_fast_options {
    * order of FP32 sums and the work split, not the method. */
   int32_t vote_bits, simt_blocks_per_sm, tc_ctas_per_sm, check_interval;
   /* Mean-shift weight kernel: SYM_KERNEL_EPANECHNIKOV (1 - d^2/h^2, the
-   * reference's) or SYM_KERNEL_GAUSSIAN (exp(-4.5 d^2/h^2) for d < h, i.e.
-   * sigma = h/3 truncated at h; the tensor kernel makes these weights with
-   * the MUFU's BF16x2 exponential, the polish takes Newton steps with the
-   * Gaussian's Jacobian) */
+   * reference's) or SYM_KERNEL_GAUSSIAN (2^(-8 d^2/h^2) - 2^-8 for d < h: a
+   * Gaussian with sigma = h/3.33 shifted to reach 0 at the cut; the tensor
+   * kernel makes these weights with the MUFU's BF16x2 exponential, the
+   * polish takes Newton steps with the Gaussian's Jacobian) */
   int32_t kernel;
 } sym_fast_options;
 enum { SYM_KERNEL_EPANECHNIKOV = 0, SYM_KERNEL_GAUSSIAN = 1 };

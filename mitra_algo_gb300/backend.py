@@ -230,7 +230,8 @@ class Gb300Backend:
         to about that many; refine > 0 runs that many FP64 ICP passes on the
         verified modes' motions; `tuning` sets the mean shift's launch
         shapes (keys TUNING_KEYS, see autotune.py); kernel "epanechnikov"
-        (the reference's weights) or "gaussian" (exp(-4.5 d^2/h^2) cut at h).  `sample` None draws the
+        (the reference's weights) or "gaussian" (2^(-8 d^2/h^2) - 2^-8, zero
+        at the cut h).  `sample` None draws the
         area-weighted sample on the device from options.seed, as detect()
         does (sym_detect_fast_sampled)."""
         fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,

@@ -202,12 +202,13 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
         if (COUNT) {
           acc[6] += T(1);
         } else {
-          const T w = gk > T(0) ? exp(-gk * (d2 / h2)) : T(1) - d2 / h2;
+          const T floor_w = gk > T(0) ? exp2(-gk) : T(0);
+          const T w = gk > T(0) ? exp2(-gk * (d2 / h2)) - floor_w : T(1) - d2 / h2;
 #pragma unroll
           for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
           acc[6] += w;
-          if (newton) {  // Epanechnikov: unweighted sums; Gaussian: weighted
-            const T wn = gk > T(0) ? w : T(1);
+          if (newton) {  // Epanechnikov: unweighted sums; Gaussian: by 2^(-k d^2/h^2)
+            const T wn = gk > T(0) ? w + floor_w : T(1);
             T *ns = nsum + threadIdx.x;
             int at = 6;
 #pragma unroll
@@ -267,9 +268,9 @@ __device__ bool solve6(T (&M)[6][6], T (&b)[6], T tiny) {
 // mean-shift step m - x for a kMoving seed, the safeguarded Newton step
 // (I - J)^-1 (m - x) for a kNear seed, where for Epanechnikov weights
 //   J = dm/dx = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T),
-// d = v - x over the votes within the bandwidth, and for the Gaussian
-// exp(-k d^2 / h^2) (dw/dx = 2 k w d / h^2)
-//   J = 2 k / (h^2 sum w) * (sum w d d^T - (m - x) (sum w d)^T).  Stopping rules: exhausted
+// d = v - x over the votes within the bandwidth, and for the shifted
+// Gaussian w = g - 2^-k, g = 2^(-k d^2 / h^2) (dw/dx = 2 k ln2 g d / h^2)
+//   J = 2 k ln2 / (h^2 sum w) * (sum g d d^T - (m - x) (sum g d)^T).  Stopping rules: exhausted
 // when the weight is <= 1e-14 (reference, src/cpu/clustering.cpp:169-181),
 // converged when a Newton step^2 < kNewtonStop2 h^2, settled (plain step
 // taken) when the Newton step is rejected, or when an accepted Newton step
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
   }
   const T *sd = ns, *sdd = ns + 6;
   T M[6][6], step[6];
-  const T g = (gk > T(0) ? T(2) * gk : T(2)) / (h2 * acc[6]);
+  const T g = (gk > T(0) ? T(2) * gk * T(0.69314718055994531) : T(2)) / (h2 * acc[6]);
   for (int d = 0, at = 0; d < 6; ++d)
     for (int l = d; l < 6; ++l, ++at) M[d][l] = M[l][d] = sdd[at];
   for (int d = 0; d < 6; ++d) {

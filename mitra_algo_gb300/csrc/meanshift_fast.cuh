@@ -45,15 +45,17 @@ struct Tuning {
   int check_interval = 8;       // tensor approach iterations between host checks
 };
 
-// The Gaussian kernel of the extension: w = exp(-kGaussK d^2 / h^2) for
-// d < h (sigma = h / 3, weight 0.011 at the cut), 0 beyond, so chunk
-// skipping stays exact.
-constexpr double kGaussK = 4.5;
+// The Gaussian kernel of the extension, in base 2 and shifted to reach 0 at
+// the cut: w = 2^(-kGauss2 d^2 / h^2) - 2^-kGauss2 for d < h, 0 beyond
+// (sigma = h / sqrt(2 kGauss2 ln 2) = h / 3.33), so it is continuous and
+// chunk skipping stays exact.  kGauss2 is a power of two: the tensor kernel
+// scales its BF16 seed operand by it exactly.
+constexpr double kGauss2 = 8.0;
 
 struct VoteSet {
   Tuning tuning;
   // weight kernel: 0 Epanechnikov 1 - d^2 / h^2 (the reference's); > 0 the
-  // truncated Gaussian exp(-kernel_k d^2 / h^2)
+  // shifted Gaussian 2^(-kernel_k d^2 / h^2) - 2^-kernel_k
   double kernel_k = 0;
   uint64_t q = 0, nchunks = 0;
   float *desc = nullptr;      // q x 8, Morton order

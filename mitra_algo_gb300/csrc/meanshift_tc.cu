@@ -547,7 +547,7 @@ struct TcArgs {
   const int32_t *ids;
   const float *gbox;        // box of all votes; its centre is c_g
   float inv_h;
-  float gauss_k2;           // 0: Epanechnikov weights; > 0: exp2(-gauss_k2 d^2 / h^2)
+  float gauss_k2;           // 0: Epanechnikov; k > 0 (a power of 2): 2^(-k d^2/h^2) - 2^-k
   float *partial;
   unsigned long long *evals;
   int *status;
@@ -575,17 +575,16 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi) {
   return r;
 }
 
-// Truncated Gaussian weights of t = 1 - d^2 / h^2: exp2(k2 (t - 1)) for
-// t > 0 and 0 otherwise (the exponent of -inf), two at a time: the
-// exponents are rounded to BF16 and the MUFU's BF16x2 base-2 exponential
-// makes both BF16 weights in one instruction.
-__device__ __forceinline__ uint32_t gauss_bf16x2(float lo, float hi, float k2) {
-  const float alo = lo > 0.f ? k2 * (lo - 1.f) : -INFINITY;
-  const float ahi = hi > 0.f ? k2 * (hi - 1.f) : -INFINITY;
-  uint32_t a, r;
-  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(a) : "f"(ahi), "f"(alo));
-  asm("ex2.approx.ftz.bf16x2 %0, %1;" : "=r"(r) : "r"(a));
-  return r;
+// Shifted Gaussian weights 2^a - 2^-k from the exponents a = -k d^2 / h^2
+// (the MMA's D with the seed operand scaled by k, plus -k |u - E|^2), two at
+// a time: the exponents rounded to BF16, one MUFU BF16x2 base-2
+// exponential, one BF16x2 FMA with relu (votes past the cut, a < -k, get 0).
+__device__ __forceinline__ uint32_t gauss_bf16x2(float lo, float hi, uint32_t neg_floor2) {
+  uint32_t x, e, w;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(x) : "f"(hi), "f"(lo));
+  asm("ex2.approx.ftz.bf16x2 %0, %1;" : "=r"(e) : "r"(x));
+  asm("fma.rn.relu.bf16x2 %0, %1, %2, %3;" : "=r"(w) : "r"(e), "r"(0x3F803F80u), "r"(neg_floor2));
+  return w;
 }
 
 // ACC[q % 4] += W[:, 16q..16q+15] . B2[:, 16q..16q+15]^T for the eight
@@ -639,17 +638,20 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
     bool live = slot < nactive;
     int32_t sd = live ? a.ids[slot] : 0;
     __align__(16) __nv_bfloat16 k0[8], k1[8];
-    const __nv_bfloat16 one = __float2bfloat16_rn(1.f);
+    // Gaussian weights: the whole operand scaled by the power of two k
+    // (exact in BF16), so D comes out as k times the Epanechnikov D
+    const float kscale = a.gauss_k2 > 0.f ? a.gauss_k2 : 1.f;
+    const __nv_bfloat16 kone = __float2bfloat16_rn(kscale);
     for (int d = 0; d < 6; ++d) {
       float cg = 0.5f * (a.gbox[d] + a.gbox[6 + d]);
       float u = live ? (a.means[uint64_t(sd) * 8 + d] - cg) * a.inv_h : 0.f;
       __nv_bfloat16 hi, lo;
       split_bf16(u, hi, lo);
       U[tid * 8 + d] = __bfloat162float(hi) + __bfloat162float(lo);
-      k0[d] = __float2bfloat16_rn(2.f * __bfloat162float(hi));  // exact
-      k1[d] = __float2bfloat16_rn(2.f * __bfloat162float(lo));
+      k0[d] = __float2bfloat16_rn(2.f * kscale * __bfloat162float(hi));  // exact
+      k1[d] = __float2bfloat16_rn(2.f * kscale * __bfloat162float(lo));
     }
-    k0[6] = k0[7] = k1[6] = k1[7] = one;
+    k0[6] = k0[7] = k1[6] = k1[7] = kone;
     *reinterpret_cast<uint4 *>(ATILE + kmajor_offset(tid, 0, 128, 256)) = *reinterpret_cast<uint4 *>(k0);
     *reinterpret_cast<uint4 *>(ATILE + kmajor_offset(tid, 8, 128, 256)) = *reinterpret_cast<uint4 *>(k1);
   }
@@ -766,6 +768,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
     const uint32_t lane_base = uint32_t(quad * 32) << 16;
     const uint32_t dcol = tmem + 128 * p + 64 * h, wcol = tmem + kTcColW + 64 * p + 32 * h;
     const bool gauss = a.gauss_k2 > 0.f;
+    uint32_t neg_floor2 = 0;  // -2^-k in both BF16 halves
+    if (gauss) {
+      const uint32_t h16 = __bfloat16_as_ushort(__float2bfloat16_rn(-exp2f(-a.gauss_k2)));
+      neg_floor2 = h16 | (h16 << 16);
+    }
     bool ok = true;
     uint32_t kth = 0;  // index of chunk i among the pair's chunks
     for (uint32_t i = p; i < n; i += 2, ++kth) {
@@ -790,19 +797,21 @@ __global__ void __launch_bounds__(kThreadsTc, 1) ms_tile_tc(TcArgs a) {
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&d_free[p]);  // D[p] may be overwritten
-        const float2 rowc2 = make_float2(rowc, rowc);
-        if (gauss) {
+        if (gauss) {  // a = k D - k |u - E|^2 = -k d^2 / h^2
+          const float rowg = a.gauss_k2 * (rowc - 1.f);
+          const float2 rowg2 = make_float2(rowg, rowg);
           for (int j = 0; j < 16; ++j) {
             float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
-                            one2, rowc2);
-            w[j] = gauss_bf16x2(t.x, t.y, a.gauss_k2);
+                            one2, rowg2);
+            w[j] = gauss_bf16x2(t.x, t.y, neg_floor2);
           }
           for (int j = 0; j < 16; ++j) {
             float2 t = fma2(make_float2(__uint_as_float(d1[2 * j]), __uint_as_float(d1[2 * j + 1])),
-                            one2, rowc2);
-            w2[j] = gauss_bf16x2(t.x, t.y, a.gauss_k2);
+                            one2, rowg2);
+            w2[j] = gauss_bf16x2(t.x, t.y, neg_floor2);
           }
         } else {
+          const float2 rowc2 = make_float2(rowc, rowc);
           for (int j = 0; j < 16; ++j) {
             float2 t = fma2(make_float2(__uint_as_float(d0[2 * j]), __uint_as_float(d0[2 * j + 1])),
                             one2, rowc2);
@@ -1031,8 +1040,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   const float gap = float(std::sqrt(h2)) + 1e-6f;
   call.launched();
   TcArgs args{images, v.nchunks, list, offsets, pieces, nact, means, ids, v.gbox,
-              float(1.0 / std::sqrt(h2)), float(v.kernel_k * 1.4426950408889634), partial, evals,
-              call.status()};
+              float(1.0 / std::sqrt(h2)), float(v.kernel_k), partial, evals, call.status()};
   // CUDA events around every launch of the tensor kernel (its own time)
   std::vector<cudaEvent_t> marks;
   auto mark_event = [&]() {

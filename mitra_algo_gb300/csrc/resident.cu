@@ -519,7 +519,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   VoteSet vs = build_vote_set(call, desc_raw, desc64_raw, q, tuning);
   if (fo.kernel != SYM_KERNEL_EPANECHNIKOV && fo.kernel != SYM_KERNEL_GAUSSIAN)
     fail(SYM_INVALID_ARGUMENT, "unknown mean-shift kernel");
-  vs.kernel_k = fo.kernel == SYM_KERNEL_GAUSSIAN ? kGaussK : 0.0;
+  vs.kernel_k = fo.kernel == SYM_KERNEL_GAUSSIAN ? kGauss2 : 0.0;
   clock.mark(5);
   // ---- (c) mean shift from K seeds (uniform draw of distinct votes)
   uint64_t k = std::min<uint64_t>(uint64_t(std::max(fo.seeds, 1)), q);
@@ -958,7 +958,7 @@ sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q, con
     pack_votes<<<sym::blocks_for(q), sym::kThreads, 0, st>>>(raw, q, d32, d64);
     sym::check_launch();
     sym::VoteSet vs = sym::build_vote_set(call, d32, d64, q);
-    vs.kernel_k = kernel == SYM_KERNEL_GAUSSIAN ? sym::kGaussK : 0.0;
+    vs.kernel_k = kernel == SYM_KERNEL_GAUSSIAN ? sym::kGauss2 : 0.0;
     int64_t *dseeds = call.upload(seeds, k);
     int64_t *rank = call.alloc<int64_t>(k);
     sym::ranks_of<<<sym::blocks_for(k), sym::kThreads, 0, st>>>(vs.rank, dseeds, k, rank);

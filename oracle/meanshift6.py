@@ -3,13 +3,13 @@ mean-shift of the throughput extension (no reference counterpart; parity
 unpinned).
 
 Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2 (kernel "epanechnikov"),
-or the truncated Gaussian w = exp(-4.5 d^2/h^2) for d^2 < h^2 (kernel
-"gaussian").  A seed takes plain mean-shift steps m(x) - x until its squared
+or the shifted Gaussian w = 2^(-8 d^2/h^2) - 2^-8 for d^2 < h^2 (kernel
+"gaussian": zero at the cut).  A seed takes plain mean-shift steps m(x) - x until its squared
 step is below 1e-4 h^2, then safeguarded Newton steps on m(x) = x:
     (I - J) s = m(x) - x,   J = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T)
 with d = v - x over the votes within the bandwidth (Epanechnikov), or
-    J = 2 k / (h^2 sum w) * (sum w d d^T - (m - x) (sum w d)^T),  k = 4.5
-(Gaussian: dw/dx = 2 k w d / h^2).  A Newton step is taken
+    J = 2 k ln2 / (h^2 sum w) * (sum g d d^T - (m - x) (sum g d)^T)
+with g = w + 2^-k = 2^(-k d^2/h^2), k = 8 (Gaussian: dw/dx = 2 k ln2 g d / h^2).  A Newton step is taken
 when the 6x6 system is regular (pivots above 1e-12), |s| <= h/4 and
 s.(m - x) > 0 (or the step already meets the convergence test); otherwise the
 density is flat along some direction (a ridge, no well-defined mode
@@ -24,13 +24,13 @@ import numpy as np
 
 MOVING, CONVERGED, EXHAUSTED, NEAR, SETTLED = 0, 1, 2, 3, 4
 SWITCH2, NEWTON_STOP2, TRUST, NEWTON_CAP = 1e-4, 1e-8, 0.25, 10
-GAUSS_K = 4.5
+GAUSS_K = 8.0  # base-2 exponent scale of the Gaussian kernel
 
 
 def weights(d2, h2, kernel):
     inside = d2 < h2
     if kernel == "gaussian":
-        return np.where(inside, np.exp(-GAUSS_K * (d2 / h2)), 0.0)
+        return np.where(inside, np.exp2(-GAUSS_K * (d2 / h2)) - 2.0 ** -GAUSS_K, 0.0)
     return np.where(inside, 1 - d2 / h2, 0.0)
 
 
@@ -61,10 +61,10 @@ def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov")
     inside = w > 0
     di = x[inside] - m
     if kernel == "gaussian":
-        wi = w[inside][:, None]
-        sd = (wi * di).sum(0)
-        g = 2.0 * GAUSS_K / (h2 * tot)
-        M = np.eye(6) - g * ((wi * di).T @ di - np.outer(delta, sd))
+        gi = (w[inside] + 2.0 ** -GAUSS_K)[:, None]
+        sd = (gi * di).sum(0)
+        g = 2.0 * GAUSS_K * np.log(2.0) / (h2 * tot)
+        M = np.eye(6) - g * ((gi * di).T @ di - np.outer(delta, sd))
     else:
         sd = di.sum(0)
         g = 2.0 / (h2 * tot)

@@ -172,7 +172,7 @@ def test_vote_cap_subsamples_uniformly_and_deterministically(fast):
 
 @pytest.mark.parametrize("precision", ["bf16", "fp32"])
 def test_gaussian_kernel_pipeline(fast, precision):
-    """The pipeline with the truncated Gaussian kernel (exp weights): the
+    """The pipeline with the shifted Gaussian kernel (exp weights): the
     same pairs and votes, the compared modes within 1e-4 of the FP64 run of
     the same seeds (a BF16 approach may leave one seed in 50 at a nearby
     fixed point: measured 101 of 102 within, the other at 2.8e-4), and the

@@ -65,7 +65,7 @@ def gauss_case():
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("fp32", 1e-5)])
 def test_gaussian_kernel_matches_fp64(gpu, gauss_case, precision, tol):
-    """The truncated Gaussian kernel (exp weights, Gaussian Newton steps):
+    """The shifted Gaussian kernel (exp weights, Gaussian Newton steps):
     FP64 and FP32 follow the restatement's trajectories."""
     votes, seeds, ref, ref_state = gauss_case
     means, state, iters = gpu.meanshift6(votes, seeds, 0.06, precision, 200, 200,

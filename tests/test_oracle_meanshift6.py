@@ -42,12 +42,12 @@ def test_solve6_matches_numpy():
 
 def gauss_target(votes, m, h):
     d2 = ((votes - m) ** 2).sum(1)
-    w = np.where(d2 < h * h, np.exp(-4.5 * d2 / (h * h)), 0.0)
+    w = np.where(d2 < h * h, np.exp2(-8.0 * d2 / (h * h)) - 2.0 ** -8, 0.0)
     return (w @ votes) / w.sum()
 
 
 def test_gaussian_restatement_converges_to_fixed_points():
-    """Truncated Gaussian kernel: seeds near the cluster centres converge
+    """Shifted Gaussian kernel: seeds near the cluster centres converge
     with the Gaussian Newton steps to fixed points of the Gaussian map."""
     votes, centers = clustered_votes(clusters=3, per_cluster=500, noise=2000, seed=1)
     start = np.min(np.linalg.norm(votes[:, None, :] - centers[None], axis=2), axis=1)
