@@ -340,6 +340,24 @@ def ctypes_sizeof_result():
     return ctypes.sizeof(abi.FastResult)
 
 
+# ----------------------------------------------------------- multi-rank
+def max_over_ranks(values, device, world):
+    """The slowest rank's value of each entry (ranks time their replica of
+    the workload; the job takes as long as its slowest rank): an all-reduce
+    MAX when more than one rank runs.  No data moves between ranks - every
+    rank detects on its own copy of the mesh (replicas only)."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_rate(ms_per_step, world):
+    """Whole-job meshes/s: every rank finishes one mesh per step."""
+    return world * 1000.0 / ms_per_step
+
+
 # --------------------------------------------------------------- GPU arm
 def run_gpu(args):
     import torch
@@ -458,10 +476,8 @@ def run_gpu(args):
             h2d = mesh_i.bytes() + r["h2d_bytes"]
             d2h = r["d2h_bytes"] + ctypes_sizeof_result()
     barrier()
-    ms = torch.tensor([ms_bf16, ms_fp32, statistics.mean(e2e_ms)], device=f"cuda:{local}")
-    if world > 1:
-        torch.distributed.all_reduce(ms, op=torch.distributed.ReduceOp.MAX)
-    ms_bf16, ms_fp32, ms_e2e = ms.tolist()
+    ms_bf16, ms_fp32, ms_e2e = max_over_ranks([ms_bf16, ms_fp32, statistics.mean(e2e_ms)],
+                                              f"cuda:{local}", world)
     extra = args.config == "c2"
     batch = batch_bench(gpu, args.batch, args.batch_workers) if args.batch and extra else None
     refl = reflection_bench(gpu) if extra else None
@@ -498,7 +514,7 @@ def run_gpu(args):
     if rank != 0:
         return
     r = res_bf16[-1]
-    meshes = world * 1000.0 / ms_bf16
+    meshes = job_rate(ms_bf16, world)
     votes_per_s = world * r["votes"] * 1000.0 / ms_bf16
     pk, pk_kind = peaks()
     evals = statistics.mean(x["mean_shift_pairs"] for x in res_bf16)
@@ -519,7 +535,7 @@ def run_gpu(args):
         "data": "synthetic (seeded motif icosphere, generated in-process)",
         "config": config(prepared, r),
         "pair_votes_per_s": round(votes_per_s, 1),
-        "fp32": {"meshes_per_s": round(world * 1000.0 / ms_fp32, 4), "ms_per_step": round(ms_fp32, 3)},
+        "fp32": {"meshes_per_s": round(job_rate(ms_fp32, world), 4), "ms_per_step": round(ms_fp32, 3)},
         "bf16_over_fp32": round(ms_fp32 / ms_bf16, 3),
         "mode_error": {pr: {"max": e["mode_error_max"], "mean": e["mode_error_mean"],
                             "reference_seeds": 256, "compared": e["modes_compared"],
@@ -534,7 +550,7 @@ def run_gpu(args):
         "modes": r["modes"], "evaluations": evals,
         "stage_ms": {k: round(statistics.mean(x["stage_ms"][k] for x in res_bf16), 3)
                      for k in r["stage_ms"]},
-        "e2e": {"value": round(world * 1000.0 / ms_e2e, 4), "unit": "meshes/s",
+        "e2e": {"value": round(job_rate(ms_e2e, world), 4), "unit": "meshes/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "path": "raw vertices and faces in pinned host memory -> sym_mesh_load_raw "
                         "(GPU prepare, resident mesh) -> sym_detect_fast_sampled (GPU "
