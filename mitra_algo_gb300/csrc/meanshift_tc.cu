@@ -374,10 +374,7 @@ constexpr int kListThreads = 256;  // chunks per block of the list kernels
 // chunk c's box (tested against the tile's box, then each group's box, then
 // the group's 16 seeds).  Exact for Epanechnikov weights: every vote of a
 // skipped chunk is farther than the bandwidth from every seed of the tile.
-// bcount[t * gridDim.x + blockIdx.x] = the block's kept chunks.  One block
-// per 256 chunks takes every active tile in turn: the chunk boxes are read
-// once, and a tile's seeds are loaded only when some chunk of the block
-// passes the tile-box test.
+// bcount[t * gridDim.x + blockIdx.x] = the block's kept chunks.
 __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, const float *means,
                                                            const int32_t *ids, const unsigned *nact,
                                                            const float *cbox, uint64_t nchunks,
@@ -385,45 +382,39 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
                                                            uint32_t *bcount) {
   __shared__ float seed[kChunk * 6];
   __shared__ float gb[kBoxFloats];
-  const uint32_t tiles = active_tiles(nact);
+  const uint64_t t = blockIdx.y;
+  if (t >= active_tiles(nact)) return;
   const unsigned nactive = nact[0];
-  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool real = c < nchunks;
-  float cb[12];
-  for (int d = 0; d < 12; ++d) cb[d] = real ? cbox[c * 12 + d] : 0.f;
-  for (uint32_t t = 0; t < tiles; ++t) {
-    __syncthreads();  // the previous tile's boxes and seeds are no longer read
-    if (threadIdx.x < kBoxFloats) gb[threadIdx.x] = boxes[uint64_t(t) * kBoxFloats + threadIdx.x];
-    __syncthreads();
-    const bool near = real && box_gap2_tc(gb, gb + 6, cb) <= skip_gap2;
-    bool keep = false;
-    if (__syncthreads_or(near)) {
-      for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
-        const uint64_t slot = uint64_t(t) * kChunk + i;
-        const bool live = slot < nactive;
-        for (int d = 0; d < 6; ++d)
-          seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
-      }
-      __syncthreads();
-      if (near)
-        for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
-          const float *b = gb + 12 + 12 * g;
-          if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
-          for (int i = kGroupSeeds * g; i < kGroupSeeds * (g + 1) && !keep; ++i) {
-            float q = 0;
-            for (int d = 0; d < 6; ++d) {
-              const float x = seed[i * 6 + d];
-              const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
-              q += e * e;
-            }
-            keep = q <= skip_gap2;
-          }
-        }
-    }
-    if (real) need[uint64_t(t) * nchunks + c] = keep;
-    const int kept = __syncthreads_count(keep);
-    if (threadIdx.x == 0) bcount[uint64_t(t) * gridDim.x + blockIdx.x] = uint32_t(kept);
+  for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
+    const uint64_t slot = t * kChunk + i;
+    const bool live = slot < nactive;
+    for (int d = 0; d < 6; ++d) seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
   }
+  if (threadIdx.x < kBoxFloats) gb[threadIdx.x] = boxes[t * kBoxFloats + threadIdx.x];
+  __syncthreads();
+  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  bool keep = false;
+  if (c < nchunks) {
+    float cb[12];
+    for (int d = 0; d < 12; ++d) cb[d] = cbox[c * 12 + d];
+    if (box_gap2_tc(gb, gb + 6, cb) <= skip_gap2)
+      for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
+        const float *b = gb + 12 + 12 * g;
+        if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
+        for (int i = kGroupSeeds * g; i < kGroupSeeds * (g + 1) && !keep; ++i) {
+          float q = 0;
+          for (int d = 0; d < 6; ++d) {
+            const float x = seed[i * 6 + d];
+            const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
+            q += e * e;
+          }
+          keep = q <= skip_gap2;
+        }
+      }
+    need[t * nchunks + c] = keep;
+  }
+  const int kept = __syncthreads_count(keep);
+  if (threadIdx.x == 0) bcount[t * gridDim.x + blockIdx.x] = uint32_t(kept);
 }
 
 // One block: boff = exclusive scan of the active tiles' block counts,
@@ -1067,7 +1058,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     active_seeds_async(call, v, means, state, k, ids, nact, iter, trace_dev, trace_cap);
     tile_boxes<<<unsigned(max_tiles), kChunk, 0, st>>>(means, ids, nact, boxes);
     check_launch();
-    tile_count<<<nblk, kListThreads, 0, st>>>(
+    tile_count<<<dim3(nblk, unsigned(max_tiles)), kListThreads, 0, st>>>(
         boxes, means, ids, nact, v.cbox, v.nchunks, gap * gap, need, bcount);
     check_launch();
     scan_lists<<<1, 1024, 0, st>>>(bcount, nact, nblk, sms, boff, offsets, pieces);
