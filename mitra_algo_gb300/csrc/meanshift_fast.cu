@@ -458,17 +458,10 @@ struct Grid {
   uint64_t tiles, splits, cps, slots;
 };
 
-// Splits of the chunk range per seed tile: blocks_per_sm CTAs per SM over
-// all tiles, but at least kMinChunksPerSplit chunks per split, so that with
-// few tiles the per-split partial sums (read back by ms_reduce for every
-// split) stay few.
-constexpr uint64_t kMinChunksPerSplit = 64;
-
 Grid grid_for(uint64_t nactive, uint64_t nchunks, int blocks_per_sm) {
   Grid g;
   g.tiles = (nactive + kChunk - 1) / kChunk;
   uint64_t want = (uint64_t(blocks_per_sm) * 152 + g.tiles - 1) / g.tiles;
-  want = std::min<uint64_t>(want, (nchunks + kMinChunksPerSplit - 1) / kMinChunksPerSplit);
   g.splits = std::max<uint64_t>(1, std::min<uint64_t>(nchunks, want));
   g.cps = (nchunks + g.splits - 1) / g.splits;
   g.splits = (nchunks + g.cps - 1) / g.cps;
