@@ -586,18 +586,6 @@ int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t 
                             seed_iterations, evals);
 }
 
-unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
-                      uint64_t k, int32_t *ids) {
-  unsigned *nact = call.alloc<unsigned>(2);
-  retile<float><<<1, 1024, 0, call.stream()>>>(means, state, k, v.gbox, false, ids, nact);
-  check_launch();
-  call.launched();
-  unsigned n = 0;
-  SYM_CUDA(cudaMemcpyAsync(&n, nact, sizeof(unsigned), cudaMemcpyDeviceToHost, call.stream()));
-  call.sync();
-  return n;
-}
-
 void active_seeds_async(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
                         uint64_t k, int32_t *ids, unsigned *nact, unsigned *iter, uint32_t *trace,
                         unsigned trace_cap) {

@@ -87,13 +87,10 @@ int shift(Call &call, const VoteSet &v, float *means, uint8_t *state, uint64_t k
 int shift(Call &call, const VoteSet &v, double *means, uint8_t *state, uint64_t k, double h2,
           int max_iter, bool polish, double *seed_iterations, unsigned long long *evals);
 
-// kMoving seeds, Morton-sorted by position when k <= 2048; returns their
-// number (synchronises).
-unsigned active_seeds(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
-                      uint64_t k, int32_t *ids);
-// The same list with its size left on the device (nact[0]); an iteration
-// that finds active seeds records their number in trace[*iter] (while
-// *iter < trace_cap) and increments *iter.  No synchronisation.
+// kMoving seeds, Morton-sorted by position when k <= 2048, with their
+// number left on the device (nact[0]); an iteration that finds active seeds
+// records their number in trace[*iter] (while *iter < trace_cap) and
+// increments *iter.  No synchronisation.
 void active_seeds_async(Call &call, const VoteSet &v, const float *means, const uint8_t *state,
                         uint64_t k, int32_t *ids, unsigned *nact, unsigned *iter, uint32_t *trace,
                         unsigned trace_cap);
