@@ -10,7 +10,7 @@ Each class mirrors one storage type of the reference
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass, field, replace
+from dataclasses import dataclass, replace
 
 import numpy as np
 
