@@ -268,14 +268,11 @@ __device__ int32_t nearest_face_fast(const BvhView &b, F3 p, float &best, int *s
 // the nearest face when vertex i supports mode m in that direction (-1
 // otherwise), its FP32 squared distance in `best` (entering as tau^2) and
 // the image of the vertex in q.  The motion is applied in FP64, the search
-// runs in FP32.  `hint` (in/out) is a face to try first -- the previous
-// query's nearest face, usually next to this one -- whose distance, when
-// under tau^2, bounds the search from the start; it returns this query's
-// nearest face.
+// runs in FP32.
 __device__ __forceinline__ int32_t support_query(const BvhView &b, const double *xyz,
                                                  const double *vn, const Motion32 &m, uint64_t i,
                                                  bool inverse, double tau, float &best, double q[3],
-                                                 int32_t &hint, int *status) {
+                                                 int *status) {
   const uint64_t nv = b.nv;
   double r[9];
   for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
@@ -293,14 +290,7 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
     if (inverse ? side <= tau : side >= -tau) return -1;
   }
   const F3 qf{float(q[0]), float(q[1]), float(q[2])};
-  int32_t face = -1;
-  if (hint >= 0) {
-    const float d = face_d2(b, qf, hint);
-    if (d < best) best = d, face = hint;
-  }
-  const int32_t found = nearest_face_fast(b, qf, best, status);  // strictly nearer only
-  if (found >= 0) face = found;
-  hint = face;
+  const int32_t face = nearest_face_fast(b, qf, best, status);
   if (face < 0) return -1;
   const F3 a = vtx(b, b.faces[face]), bb = vtx(b, b.faces[b.nf + face]),
            cc = vtx(b, b.faces[2 * b.nf + face]);
@@ -315,30 +305,23 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
   return face;
 }
 
-// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).  A
-// thread takes kVerifyRun consecutive vertices of one mode and direction,
-// each search starting from the previous vertex's nearest face.
-constexpr uint64_t kVerifyRun = 4;
-
+// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).
 __global__ void verify_vertices_fast(BvhView b, const double *xyz, const double *vn,
                                      const Motion32 *motions, uint64_t nc, double tau, float tau2,
                                      uint8_t *flags, double *err, int *status) {
-  const uint64_t nv = b.nv, runs = (nv + kVerifyRun - 1) / kVerifyRun;
-  const uint64_t job = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (job >= nc * 2 * runs) return;
-  const uint64_t set = job / runs, c = set / 2;  // set = c * 2 + dir
-  const bool inverse = set % 2 == 1;
-  const uint64_t i0 = (job % runs) * kVerifyRun, i1 = i0 + kVerifyRun < nv ? i0 + kVerifyRun : nv;
-  const Motion32 m = motions[c];
-  int32_t hint = -1;
-  for (uint64_t i = i0; i < i1; ++i) {
-    const uint64_t row = set * nv + i;
-    float best = tau2;
-    double q[3];
-    const bool hit = support_query(b, xyz, vn, m, i, inverse, tau, best, q, hint, status) >= 0;
-    flags[row] = hit;
-    if (!inverse) err[c * nv + i] = hit ? double(best) : 0.0;
-  }
+  uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t nv = b.nv;
+  if (row >= nc * 2 * nv) return;
+  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  const bool inverse = rem >= nv;
+  const uint64_t i = rem % nv;
+  flags[row] = 0;
+  if (!inverse) err[c * nv + i] = 0;
+  float best = tau2;
+  double q[3];
+  if (support_query(b, xyz, vn, motions[c], i, inverse, tau, best, q, status) < 0) return;
+  flags[row] = 1;
+  if (!inverse) err[c * nv + i] = double(best);
 }
 
 // ------------------------------------------------ FP64 transform refinement
@@ -395,8 +378,7 @@ __global__ void refine_pairs(BvhView b, const double *xyz, const double *vn,
   ok[row] = 0;
   float best = tau2;
   double q[3];
-  int32_t hint = -1;
-  const int32_t face = support_query(b, xyz, vn, motions[c], i, false, tau, best, q, hint, status);
+  const int32_t face = support_query(b, xyz, vn, motions[c], i, false, tau, best, q, status);
   if (face < 0) return;
   double corner[3][3], out[3];
   for (int k = 0; k < 3; ++k) {
@@ -740,8 +722,7 @@ void verification_fast(Call &call, const Lbvh &bvh, const double *xyz, const dou
   uint8_t *flags = call.alloc<uint8_t>(rows);
   double *err = call.alloc<double>(nc * nv);
   if (bvh.nf) {
-    const uint64_t jobs = nc * 2 * ((nv + kVerifyRun - 1) / kVerifyRun);
-    verify_vertices_fast<<<blocks_for(jobs), kThreads, 0, st>>>(view, xyz, vn, dm, nc, tau,
+    verify_vertices_fast<<<blocks_for(rows), kThreads, 0, st>>>(view, xyz, vn, dm, nc, tau,
                                                                 float(tau * tau), flags, err,
                                                                 call.status());
   } else {
