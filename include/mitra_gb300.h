@@ -446,14 +446,15 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
  * own status and message). */
 typedef struct sym_batch_item {
   sym_mesh_handle *mesh;
-  const int32_t *sample;
-  uint64_t sample_count;
+  const int32_t *sample; /* NULL with SYM_SAMPLE_ON_DEVICE: the item runs as */
+  uint64_t sample_count; /* sym_detect_fast_sampled (sample from options->seed) */
   const sym_options *options;
   const sym_fast_options *fast;
   sym_fast_result *out; /* caller-owned */
   sym_status status;    /* written by the call */
   char message[256];    /* the item's error message, "" on success */
 } sym_batch_item;
+#define SYM_SAMPLE_ON_DEVICE UINT64_MAX
 sym_status sym_detect_fast_batch(sym_context *const *workers, int32_t worker_count,
                                  sym_batch_item *items, uint64_t count);
 

@@ -47,6 +47,7 @@ def _check(status: int):
 
 
 KERNELS = {"epanechnikov": 0, "gaussian": 1}  # SYM_KERNEL_*
+SAMPLE_ON_DEVICE = 2 ** 64 - 1  # SYM_SAMPLE_ON_DEVICE
 
 # sym_fast_options' launch-shape fields, in their order (0 = the default)
 TUNING_KEYS = ("vote_bits", "simt_blocks_per_sm", "tc_ctas_per_sm", "check_interval")
@@ -292,7 +293,8 @@ class Gb300Backend:
     def detect_fast_batch(self, jobs, workers=4, precision="bf16", seeds=2048, seed_rng=7,
                           max_iterations=100, polish_iterations=100, verify=True,
                           mode="rigid", tuning=None) -> list:
-        """sym_detect_fast_batch over `jobs` = [(ResidentMesh, sample, Options), ...]:
+        """sym_detect_fast_batch over `jobs` = [(ResidentMesh, sample, Options), ...]
+        (a sample None is drawn on the device, as detect_fast does it):
         `workers` meshes in flight at a time, each on its own context (stream
         and workspace), the contexts kept for later calls.  Returns one result
         dict per job, as detect_fast gives it."""
@@ -306,12 +308,17 @@ class Gb300Backend:
         items = (abi.BatchItem * len(jobs))()
         results = [abi.FastResult() for _ in jobs]
         for it, (mesh, sample, options), res in zip(items, jobs, results):
-            sample = np.ascontiguousarray(sample, np.int32)
             opts = options.to_c()
-            keep += [sample, opts]
+            keep.append(opts)
             it.mesh = mesh.handle
-            it.sample = sample.ctypes.data_as(C.POINTER(C.c_int32))
-            it.sample_count = sample.size
+            if sample is None:  # drawn on the device from options.seed
+                it.sample = None
+                it.sample_count = SAMPLE_ON_DEVICE
+            else:
+                sample = np.ascontiguousarray(sample, np.int32)
+                keep.append(sample)
+                it.sample = sample.ctypes.data_as(C.POINTER(C.c_int32))
+                it.sample_count = sample.size
             it.options = C.pointer(opts)
             it.fast = C.pointer(fo)
             it.out = C.pointer(res)

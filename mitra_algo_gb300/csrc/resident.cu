@@ -1074,8 +1074,10 @@ sym_status sym_detect_fast_batch(sym_context *const *workers, int32_t worker_cou
   auto run = [&](sym_context *ctx) {
     for (uint64_t i = next++; i < count; i = next++) {
       sym_batch_item &it = items[i];
-      it.status = sym_detect_fast(ctx, it.mesh, it.sample, it.sample_count, it.options, it.fast,
-                                  it.out);
+      it.status = it.sample_count == SYM_SAMPLE_ON_DEVICE && !it.sample
+                      ? sym_detect_fast_sampled(ctx, it.mesh, it.options, it.fast, it.out)
+                      : sym_detect_fast(ctx, it.mesh, it.sample, it.sample_count, it.options,
+                                        it.fast, it.out);
       if (it.status != SYM_OK) {
         std::snprintf(it.message, sizeof(it.message), "%s", sym_error_text.c_str());
         if (!it.message[0]) std::snprintf(it.message, sizeof(it.message), "invalid argument");

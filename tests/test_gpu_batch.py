@@ -74,3 +74,18 @@ def test_batch_reports_a_failing_item(batch):
     with pytest.raises(Exception, match="sample vertex index out of range"):
         gpu.detect_fast_batch([jobs[1], (mesh, bad, opts), jobs[2]], workers=2, seeds=64,
                               max_iterations=20, polish_iterations=5)
+
+
+def test_batch_items_may_sample_on_the_device(batch):
+    """An item without a sample draws it on the device from its options'
+    seed (sym_detect_fast_sampled): the results equal detect_fast with the
+    sample None, and also with the host-drawn sample of the fixture."""
+    gpu, jobs = batch
+    kw = dict(precision="bf16", seeds=128, max_iterations=60, polish_iterations=20)
+    alone = [gpu.detect_fast(m, None, o, **kw) for m, _, o in jobs[:3]]
+    with_host_sample = [gpu.detect_fast(m, s, o, **kw) for m, s, o in jobs[:3]]
+    together = gpu.detect_fast_batch([(m, None, o) for m, _, o in jobs[:3]], workers=2, **kw)
+    for a, b, c in zip(alone, together, with_host_sample):
+        same(a, b)
+        same(a, c)
+        assert a["sampled"] == b["sampled"] > 0
