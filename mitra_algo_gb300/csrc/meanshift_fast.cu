@@ -128,8 +128,7 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
                                                   uint64_t q, const T *means, const uint8_t *state,
                                                   const int32_t *ids, uint64_t nactive, T h2,
                                                   T gk, float skip_gap2, uint64_t chunks_per_split,
-                                                  T *partial, unsigned long long *evals,
-                                                  const uint8_t *frozen = nullptr) {
+                                                  T *partial, unsigned long long *evals) {
   constexpr int stride = COUNT ? 8 : kPartial;
   __shared__ T xs[kChunk * 8];
   __shared__ float tlo[6][4], thi[6][4];
@@ -140,8 +139,7 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
   uint64_t slots = uint64_t(gridDim.x) * kChunk;
   bool live = slot < nactive;
   int32_t seed = live ? ids[slot] : 0;
-  const bool newton =
-      NEWTON && !COUNT && live && state[seed] == kNear && !(frozen && frozen[seed]);
+  const bool newton = NEWTON && !COUNT && live && state[seed] == kNear;
   T m[6];
   for (int d = 0; d < 6; ++d) m[d] = live ? means[uint64_t(seed) * 8 + d] : T(0);
   float lo[6], hi[6];
@@ -305,17 +303,15 @@ __global__ void __launch_bounds__(kChunk) ms_reduce(const T *partial, uint64_t s
 template <typename T>
 __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint64_t slots,
                                                     const int32_t *ids, uint64_t nactive, T h2,
-                                                    T gk, int polish_it, uint8_t *state,
-                                                    T *mstore = nullptr, uint8_t *frozen = nullptr) {
+                                                    T gk, int polish_it, uint8_t *state) {
   const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
   if (slot >= nactive) return;
   const int32_t s = ids[slot];
   const bool near = state[s] == kNear;
-  const bool reuse = near && frozen && frozen[s];  // Newton matrix kept from before
   T acc[7] = {0, 0, 0, 0, 0, 0, 0}, ns[27];
   for (int g = 0; g < kGroups; ++g)
     for (int d = 0; d < 7; ++d) acc[d] += red[(uint64_t(g) * kPartial + d) * slots + slot];
-  if (near && !reuse)
+  if (near)
     for (int j = 0; j < 27; ++j) {
       ns[j] = 0;
       for (int g = 0; g < kGroups; ++g) ns[j] += red[(uint64_t(g) * kPartial + 8 + j) * slots + slot];
@@ -335,24 +331,15 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
     if (move < T(kSwitch2) * h2) state[s] = kNear;
     return;
   }
+  const T *sd = ns, *sdd = ns + 6;
   T M[6][6], step[6];
-  if (reuse) {
-    for (int d = 0; d < 6; ++d)
-      for (int l = 0; l < 6; ++l) M[d][l] = mstore[uint64_t(s) * 36 + d * 6 + l];
-  } else {
-    const T *sd = ns, *sdd = ns + 6;
-    const T g = (gk > T(0) ? T(2) * gk * T(0.69314718055994531) : T(2)) / (h2 * acc[6]);
-    for (int d = 0, at = 0; d < 6; ++d)
-      for (int l = d; l < 6; ++l, ++at) M[d][l] = M[l][d] = sdd[at];
-    for (int d = 0; d < 6; ++d)
-      for (int l = 0; l < 6; ++l) M[d][l] = (d == l ? T(1) : T(0)) - g * (M[d][l] - delta[d] * sd[l]);
-    if (frozen) {  // kept for the seed's later Newton steps
-      for (int d = 0; d < 6; ++d)
-        for (int l = 0; l < 6; ++l) mstore[uint64_t(s) * 36 + d * 6 + l] = M[d][l];
-      frozen[s] = 1;
-    }
+  const T g = (gk > T(0) ? T(2) * gk * T(0.69314718055994531) : T(2)) / (h2 * acc[6]);
+  for (int d = 0, at = 0; d < 6; ++d)
+    for (int l = d; l < 6; ++l, ++at) M[d][l] = M[l][d] = sdd[at];
+  for (int d = 0; d < 6; ++d) {
+    for (int l = 0; l < 6; ++l) M[d][l] = (d == l ? T(1) : T(0)) - g * (M[d][l] - delta[d] * sd[l]);
+    step[d] = delta[d];
   }
-  for (int d = 0; d < 6; ++d) step[d] = delta[d];
   bool ok = solve6(M, step, T(sizeof(T) == 4 ? 1e-6 : 1e-12));
   T len = 0, along = 0;
   for (int d = 0; d < 6; ++d) len += step[d] * step[d], along += step[d] * delta[d];
@@ -373,16 +360,14 @@ constexpr int kRetile = 2048;  // seeds sorted in one block (static shared memor
 // Active seeds (kMoving, and kNear when include_near) in seed order, then
 // sorted by the Morton key of
 // their current mean (ties by seed id) when k <= kRetile.  nactive[0] = the
-// number of active seeds, nactive[1] = how many of them are kNear and still
-// need the sums of a Newton matrix (none kept in `frozen`).  With
+// number of active seeds, nactive[1] = how many of them are kNear.  With
 // `iter`, an iteration that finds active seeds records their number in
 // trace[*iter] (while *iter < trace_cap) and counts itself in *iter.
 template <typename T>
 __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *state, uint64_t k,
                                                const float *box, bool include_near, int32_t *ids,
                                                unsigned *nactive, unsigned *iter = nullptr,
-                                               uint32_t *trace = nullptr, unsigned trace_cap = 0,
-                                               const uint8_t *frozen = nullptr) {
+                                               uint32_t *trace = nullptr, unsigned trace_cap = 0) {
   __shared__ unsigned long long keys[kRetile];
   __shared__ int32_t vals[kRetile];
   __shared__ unsigned warp_tot[32];
@@ -403,7 +388,7 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
       total += warp_tot[w];
     }
     unsigned pos = base_s + before + __popc(bal & ((1u << lane) - 1));
-    if (act && state[s] == kNear && !(frozen && frozen[s])) atomicAdd(&near_s, 1u);
+    if (act && state[s] == kNear) atomicAdd(&near_s, 1u);
     if (act) {
       if (sort) {
         float x[6];
@@ -497,20 +482,9 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
   T *partial = call.alloc<T>(cap * kPartial);
   T *red = call.alloc<T>(uint64_t(kGroups) * kPartial * std::max<uint64_t>(k, kChunk) * 2);
   float gap = float(std::sqrt(h2)) + 1e-6f;
-  // polish: each seed's Newton matrix I - J is formed at its first Newton
-  // step and kept for the later ones (the fixed point m(x) = x does not
-  // depend on it; later iterations skip the Jacobian sums)
-  T *mstore = nullptr;
-  uint8_t *frozen = nullptr;
-  if (polish) {
-    mstore = call.alloc<T>(k * 36);
-    frozen = call.alloc<uint8_t>(k);
-    SYM_CUDA(cudaMemsetAsync(frozen, 0, k, st));
-  }
   int it = 0;
   for (; it < max_iter; ++it) {
-    retile<T><<<1, 1024, 0, st>>>(means, state, k, v.gbox, polish, ids, nact, nullptr, nullptr, 0,
-                                  frozen);
+    retile<T><<<1, 1024, 0, st>>>(means, state, k, v.gbox, polish, ids, nact);
     check_launch();
     unsigned counts[2] = {0, 0};
     SYM_CUDA(cudaMemcpyAsync(counts, nact, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -526,7 +500,7 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
     if (counts[1])
       ms_tile<T, false, true><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state, ids,
                                                       n, T(h2), T(v.kernel_k), gap * gap, g.cps,
-                                                      partial, evals, frozen);
+                                                      partial, evals);
     else
       ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state,
                                                        ids, n, T(h2), T(v.kernel_k), gap * gap,
@@ -536,8 +510,7 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
         partial, g.splits, g.slots, n, red);
     check_launch();
     ms_update<T><<<unsigned(g.tiles), kChunk, 0, st>>>(means, red, g.slots, ids, n, T(h2),
-                                                       T(v.kernel_k), polish ? it : -1, state,
-                                                       mstore, frozen);
+                                                       T(v.kernel_k), polish ? it : -1, state);
     check_launch();
     call.launched(3);
   }

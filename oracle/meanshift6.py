@@ -5,9 +5,7 @@ unpinned).
 Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2 (kernel "epanechnikov"),
 or the shifted Gaussian w = 2^(-8 d^2/h^2) - 2^-8 for d^2 < h^2 (kernel
 "gaussian": zero at the cut).  A seed takes plain mean-shift steps m(x) - x until its squared
-step is below 1e-4 h^2, then safeguarded Newton steps on m(x) = x (the matrix I - J formed at a seed's
-first Newton step and kept for its later ones; the fixed point does not
-depend on it):
+step is below 1e-4 h^2, then safeguarded Newton steps on m(x) = x:
     (I - J) s = m(x) - x,   J = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T)
 with d = v - x over the votes within the bandwidth (Epanechnikov), or
     J = 2 k ln2 / (h^2 sum w) * (sum g d d^T - (m - x) (sum g d)^T)
@@ -57,26 +55,20 @@ def solve6(M, b, tiny=1e-12):
     return b
 
 
-def newton_matrix(x, m, w, tot, delta, h2, kernel="epanechnikov"):
-    """I - J at m from the weights w over all votes x."""
+def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov"):
+    """The kNear step of one seed from its weights w over all votes x
+    (polish_it: the polish iteration, -1 in the approach phase)."""
     inside = w > 0
     di = x[inside] - m
     if kernel == "gaussian":
         gi = (w[inside] + 2.0 ** -GAUSS_K)[:, None]
         sd = (gi * di).sum(0)
         g = 2.0 * GAUSS_K * np.log(2.0) / (h2 * tot)
-        return np.eye(6) - g * ((gi * di).T @ di - np.outer(delta, sd))
-    sd = di.sum(0)
-    g = 2.0 / (h2 * tot)
-    return np.eye(6) - g * (di.T @ di - np.outer(delta, sd))
-
-
-def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov", M=None):
-    """The kNear step of one seed from its weights w over all votes x
-    (polish_it: the polish iteration, -1 in the approach phase); M, when
-    given, is the Newton matrix kept from the seed's first Newton step."""
-    if M is None:
-        M = newton_matrix(x, m, w, tot, delta, h2, kernel)
+        M = np.eye(6) - g * ((gi * di).T @ di - np.outer(delta, sd))
+    else:
+        sd = di.sum(0)
+        g = 2.0 / (h2 * tot)
+        M = np.eye(6) - g * (di.T @ di - np.outer(delta, sd))
     s = solve6(M, delta)
     if (s is not None and np.all(np.isfinite(s)) and s @ s <= TRUST * TRUST * h2
             and (s @ delta > 0 or s @ s < NEWTON_STOP2 * h2)):
@@ -104,7 +96,6 @@ def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=10
 
 def _phase(x, means, state, h2, budget, polish, block, kernel):
     iterations = 0
-    kept = {}  # polish: each seed's Newton matrix from its first Newton step
     for it in range(budget):
         act = np.flatnonzero((state == MOVING) | ((state == NEAR) & polish))
         if act.size == 0:
@@ -127,11 +118,8 @@ def _phase(x, means, state, h2, budget, polish, block, kernel):
                     if move[j] < SWITCH2 * h2:
                         state[i] = NEAR
                 else:
-                    if polish and i not in kept:
-                        kept[i] = newton_matrix(x, m[j], w[j], tot[j], delta[j], h2, kernel)
                     means[i], state[i] = newton_seed(x, m[j], w[j], tot[j], delta[j], move[j], h2,
-                                                     it if polish else -1, kernel,
-                                                     kept.get(i) if polish else None)
+                                                     it if polish else -1, kernel)
     return iterations
 
 
