@@ -66,3 +66,27 @@ def test_bad_ids_are_rejected(tmp_path):
     a[-1] = -1
     with pytest.raises(RuntimeError, match="pair index out of range"):
         export_tables(tmp_path, mesh, f, sample, pruned, Pairs(a, pairs.b), votes, clusters)
+
+
+def test_empty_result_exports_headers_only(tmp_path):
+    """No pairs, votes or clusters: the tables have zero rows and the text
+    files hold the reference's header lines only (features and the mesh
+    still list every vertex)."""
+    g, mesh, f, sample, pruned, pairs, votes, clusters = golden_result("single_05")
+    empty_pairs = Pairs(np.zeros(0, np.int32), np.zeros(0, np.int32))
+    empty_votes = votes_from({**g, "vote_pair": np.zeros(0, np.int32),
+                              "vote_kind": np.zeros(0, np.uint8), "poff": np.zeros(0)})
+    from mitra_algo_gb300.types import ClusterOutput, Csr
+    no_clusters = ClusterOutput(np.zeros(0, np.uint8), np.zeros((0, 9)), np.zeros((0, 3)),
+                                np.zeros((0, 3)), np.zeros(0),
+                                Csr(np.zeros(1, np.uint64), np.zeros(0, np.int32)))
+    export_tables(tmp_path / "bin", mesh, f, sample, pruned, empty_pairs, empty_votes, no_clusters)
+    t = read_tables(tmp_path / "bin")
+    assert len(t["pairs"]["a"]) == 0 and len(t["votes"]["pair"]) == 0
+    assert len(t["features"]["x"]) == mesh.vertex_count
+    render_text(tmp_path / "bin", tmp_path / "text")
+    assert (tmp_path / "text" / "pairs.csv").read_text() == "pair,a,b\n"
+    assert (tmp_path / "text" / "votes.csv").read_text().count("\n") == 1
+    assert (tmp_path / "text" / "descriptors.csv").read_text().startswith("vote,dimension,component0")
+    lines = (tmp_path / "text" / "features.csv").read_text().splitlines()
+    assert len(lines) == mesh.vertex_count + 1
