@@ -58,7 +58,7 @@ void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const 
 struct sym_mesh_handle {
   sym_context *ctx = nullptr;
   sym_mesh_view host{};
-  std::vector<sym_edge> host_edges;
+  std::vector<sym_edge> host_edges;  // sym_mesh_load only (an edge table in any order)
   sym_model_context model{};
   uint64_t nv = 0, nf = 0, ne = 0, nbr_count = 0;
   char *block = nullptr;
@@ -398,7 +398,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   f.valid = valid;
   f.count = nv;
   curvature_device(call, h.xyz, nv, h.fn, h.nf, h.vn, h.nbr_off, h.nbr, h.nbr_count, h.edges, h.ne,
-                   o.smoothing, f, h.host_edges.data());
+                   o.smoothing, f, h.host_edges.empty() ? nullptr : h.host_edges.data());
   clock.mark(1);
   // ---- area-weighted sample and its prune
   int32_t *dsample = nullptr;
@@ -849,7 +849,8 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
     h->host = sym_mesh_view{};  // the vertices and faces live on the device only
     h->model = p.context;
     h->nv = p.nv, h->nf = p.nf, h->ne = p.ne, h->nbr_count = p.nbr_count;
-    h->host_edges.resize(p.ne);
+    // no host copy of the edge table: the GPU prepare emits it sorted by
+    // (lo, hi), so the curvature never needs the host-side reordering
     const uint64_t nv = p.nv, nf = p.nf, ne = p.ne;
     auto pad = [](uint64_t b) { return (b + 255) & ~uint64_t(255); };
     uint64_t sizes[8] = {pad(24 * nv), pad(24 * nf), pad(24 * nv), pad(8 * nv), pad(12 * nf),
@@ -879,7 +880,6 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
     d2d(h->nbr_off, p.nbr_off, 8 * (nv + 1));
     d2d(h->nbr, p.nbr, 4 * h->nbr_count);
     d2d(h->edges, p.edges, 24 * ne);
-    call.d2h(h->host_edges.data(), p.edges, 24 * ne);
     if (nf >= (uint64_t(1) << 30)) sym::fail(SYM_INVALID_ARGUMENT, "too many faces for the LBVH");
     h->lbvh = sym::lbvh_build(call, h->xyz, nv, h->faces, nf);
     call.check_status("mesh_load_raw");
