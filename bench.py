@@ -55,7 +55,7 @@ VOTE_CAP = 0      # votes entering the mean shift (0: all)
 WORKLOAD = "motif icosphere L6, rigid mode, 6-D votes"
 # DRAM bytes (read + write) per (seed tile, vote chunk) pair of ms_tile_tc,
 # from the ncu capture summarised in profiles/ms_tile_tc.md
-TRAFFIC_PER_CHUNK_PAIR = 8309.0
+TRAFFIC_PER_CHUNK_PAIR = 8300.0
 IMAGE_BYTES = 8224.0  # one chunk image: the algorithmic bytes of a (tile, chunk) pair
 BATCH_SAMPLES, BATCH_SEEDS = 4000, 512  # per mesh of the uneven batch
 
