@@ -290,17 +290,18 @@ sym_status sym_triangle_distances(sym_context *ctx, const double *queries,
  * No counterpart in the reference (it processes one mesh per detect() with
  * every stage re-uploading its inputs).  A mesh is loaded once into device
  * memory, then sym_detect_fast runs the whole hot path on it with device-
- * resident intermediates: curvature, prune of a host sample, exact pairing,
- * 6-D rigid votes (axis-angle/2 + centred translation/box, FP32 transforms,
- * FP64 log map near pi), a spatially sorted vote set, mean-shift from K seeds
- * with Epanechnikov weights, mode merging, and verification of the top
- * modes.  The mean-shift approach phase runs in FP32 (SIMT) or BF16 (tensor
+ * resident intermediates: curvature, prune of the area-weighted sample (the
+ * caller's, or drawn on the device by sym_detect_fast_sampled), exact
+ * pairing, 6-D rigid votes (axis-angle/2 + centred translation/box, FP32
+ * transforms, FP64 log map near pi) or plane votes, a spatially sorted vote
+ * set, mean-shift from K seeds with Epanechnikov or exp (Gaussian) weights,
+ * mode merging, and verification of the top modes on a device LBVH.  The mean-shift approach phase runs in FP32 (SIMT) or BF16 (tensor
  * cores); both forms then share the same FP32 polish phase (Newton steps near
  * the modes, see sym_meanshift6); a subset of seeds can be re-run in FP64 to
  * report the mode error. */
 typedef struct sym_mesh_handle sym_mesh_handle;
-/* Uploads the mesh and its topology; the host views must stay valid while
- * the handle is used (the verification BVH is built from them). */
+/* Uploads the mesh and its topology (the views are read during the call
+ * only) and builds the verification LBVH on the device. */
 sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh,
                          const sym_topology_view *topology,
                          const sym_model_context *model, sym_mesh_handle **out);
