@@ -325,9 +325,22 @@ __global__ void verify_vertices_fast(BvhView b, const double *xyz, const double 
 }
 
 // ------------------------------------------------ FP64 transform refinement
-// Closest point of triangle abc to p in FP64 (the region tests of Ericson,
-// Real-Time Collision Detection, 2005, section 5.1.5); a triangle without
-// area gives its nearest corner.
+// Closest point of triangle abc to p in FP64: the region tests of Ericson,
+// Real-Time Collision Detection, 2005, section 5.1.5, and for a triangle
+// without area (|ab x ac|^2 < 1e-28) the nearest of its three segments, the
+// rule of the verification's distance (the reference's
+// point_triangle_distance2).
+__device__ void closest_on_segment(const double p[3], const double a[3], const double b[3],
+                                   double out[3]) {
+  double d[3], l = 0, t = 0;
+  for (int k = 0; k < 3; ++k) d[k] = b[k] - a[k], l += d[k] * d[k];
+  if (l > 1e-14) {
+    t = ((p[0] - a[0]) * d[0] + (p[1] - a[1]) * d[1] + (p[2] - a[2]) * d[2]) / l;
+    t = t < 0.0 ? 0.0 : (1.0 < t ? 1.0 : t);
+  }
+  for (int k = 0; k < 3; ++k) out[k] = a[k] + d[k] * t;
+}
+
 __device__ void closest_point(const double p[3], const double a[3], const double b[3],
                               const double c[3], double out[3]) {
   double ab[3], ac[3], ap[3], bp[3], cp[3];
@@ -335,6 +348,22 @@ __device__ void closest_point(const double p[3], const double a[3], const double
     ab[k] = b[k] - a[k], ac[k] = c[k] - a[k], ap[k] = p[k] - a[k], bp[k] = p[k] - b[k],
     cp[k] = p[k] - c[k];
   auto dot3 = [](const double *x, const double *y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+  const double n[3] = {ab[1] * ac[2] - ab[2] * ac[1], ab[2] * ac[0] - ab[0] * ac[2],
+                       ab[0] * ac[1] - ab[1] * ac[0]};
+  if (dot3(n, n) < 1e-14 * 1e-14) {  // no area: the nearest of the three segments
+    double s[3][3], e[3];
+    closest_on_segment(p, a, b, s[0]);
+    closest_on_segment(p, a, c, s[1]);
+    closest_on_segment(p, b, c, s[2]);
+    for (int j = 0; j < 3; ++j) {
+      const double r[3] = {p[0] - s[j][0], p[1] - s[j][1], p[2] - s[j][2]};
+      e[j] = dot3(r, r);
+    }
+    const int m01 = e[1] < e[0] ? 1 : 0;
+    const int pick = e[2] < e[m01] ? 2 : m01;
+    for (int k = 0; k < 3; ++k) out[k] = s[pick][k];
+    return;
+  }
   auto set = [&](const double *base, const double *dir, double t) {
     for (int k = 0; k < 3; ++k) out[k] = base[k] + dir[k] * t;
   };
@@ -354,10 +383,6 @@ __device__ void closest_point(const double p[3], const double a[3], const double
     return set(b, bc, (d4 - d3) / ((d4 - d3) + (d5 - d6)));
   }
   const double den = va + vb + vc;
-  if (!(den > 0)) {  // no area: the nearest corner
-    const double da = dot3(ap, ap), db = dot3(bp, bp), dc = dot3(cp, cp);
-    return set(da <= db && da <= dc ? a : (db <= dc ? b : c), ab, 0);
-  }
   for (int k = 0; k < 3; ++k) out[k] = a[k] + ab[k] * (vb / den) + ac[k] * (vc / den);
 }
 

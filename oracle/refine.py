@@ -19,8 +19,21 @@ from __future__ import annotations
 import numpy as np
 
 
+def closest_on_segments(p, a, b):
+    """Closest points of segments ab to points p (the clamp of the
+    reference's segment distance: no parameter for a segment shorter than
+    1e-7)."""
+    d = b - a
+    ln = np.einsum("ij,ij->i", d, d)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t = np.where(ln > 1e-14, np.einsum("ij,ij->i", p - a, d) / np.where(ln > 1e-14, ln, 1.0), 0.0)
+    return a + d * np.clip(t, 0.0, 1.0)[:, None]
+
+
 def closest_on_triangles(p, a, b, c):
-    """Closest points of triangles (a, b, c) to points p, all (m, 3)."""
+    """Closest points of triangles (a, b, c) to points p, all (m, 3): the
+    region tests, and for a triangle without area (|ab x ac|^2 < 1e-28) the
+    nearest of its three segments."""
     ab, ac, ap = b - a, c - a, p - a
     bp, cp = p - b, p - c
     dot = lambda x, y: np.einsum("ij,ij->i", x, y)  # noqa: E731
@@ -28,15 +41,11 @@ def closest_on_triangles(p, a, b, c):
     vc, vb, va = d1 * d4 - d3 * d2, d5 * d2 - d1 * d6, d3 * d6 - d5 * d4
     with np.errstate(divide="ignore", invalid="ignore"):
         den = va + vb + vc
-        inner = a + ab * (vb / den)[:, None] + ac * (vc / den)[:, None]
-        out = inner
+        out = a + ab * (vb / den)[:, None] + ac * (vc / den)[:, None]
         e_bc = b + (c - b) * ((d4 - d3) / ((d4 - d3) + (d5 - d6)))[:, None]
         e_ac = a + ac * (d2 / (d2 - d6))[:, None]
         e_ab = a + ab * (d1 / (d1 - d3))[:, None]
     # region tests in the order they are made; the first that holds wins
-    da, db, dc = dot(ap, ap), dot(bp, bp), dot(cp, cp)
-    corner = np.where((da <= db) & (da <= dc), 0, np.where(db <= dc, 1, 2))
-    nearest_corner = np.stack([a, b, c])[corner, np.arange(len(p))]
     choices = [
         ((d1 <= 0) & (d2 <= 0), a),
         ((d3 >= 0) & (d4 <= d3), b),
@@ -44,13 +53,22 @@ def closest_on_triangles(p, a, b, c):
         ((d6 >= 0) & (d5 <= d6), c),
         ((vb <= 0) & (d2 >= 0) & (d6 <= 0), e_ac),
         ((va <= 0) & ((d4 - d3) >= 0) & ((d5 - d6) >= 0), e_bc),
-        (~(den > 0), nearest_corner),
     ]
     taken = np.zeros(len(p), bool)
     for cond, val in choices:
         use = cond & ~taken
         out = np.where(use[:, None], val, out)
         taken |= use
+    n = np.cross(ab, ac)
+    flat = dot(n, n) < 1e-14 * 1e-14
+    if flat.any():
+        s = [closest_on_segments(p, a, b), closest_on_segments(p, a, c),
+             closest_on_segments(p, b, c)]
+        e = [((p - x) ** 2).sum(1) for x in s]
+        m01 = np.where(e[1] < e[0], 1, 0)
+        pick = np.where(e[2] < np.where(m01 == 1, e[1], e[0]), 2, m01)
+        seg = np.stack(s)[pick, np.arange(len(p))]
+        out = np.where(flat[:, None], seg, out)
     return out
 
 
