@@ -509,7 +509,8 @@ sym_status sym_tc_selftest(sym_context *ctx, const uint16_t *a1, const uint16_t 
  * race and must be ordered by the caller.  sym_prune_static_setup() resolves
  * the array's address for the current device; call it once per device, with
  * that device current, before any stream capture (the first
- * sym_prune_static on a device otherwise does it). */
+ * sym_prune_static on a device otherwise does it), and again after the
+ * device's context was reset (cudaDeviceReset), which moves the array. */
 uint64_t sym_prune_static_max_samples(void);
 sym_status sym_prune_static_setup(void);
 sym_status sym_prune_static(const int32_t *sample, uint64_t count, const double *kmin,

@@ -21,7 +21,9 @@
 //                         writes the total (or UINT64_MAX on a bad index)
 //   3. prune_scatter      each block re-evaluates its samples, ranks the kept
 //                         ones inside the block and writes them at
-//                         offsets[tile] + rank
+//                         offsets[tile] + rank (it leaves the status word to
+//                         prune_tile_counts, which already reported any bad
+//                         index before the scan read the word)
 #include "common.cuh"
 
 #include <cstring>
@@ -54,12 +56,13 @@ __device__ __forceinline__ bool keep_vertex(int32_t v, const double *kmin, const
 }
 
 // Keep flags of this thread's kPrunePerThread consecutive samples (bit j =
-// sample base + j); an index outside [0, vertex_count) is not kept and
-// raises the status word.
+// sample base + j); an index outside [0, vertex_count) is not kept and, when
+// `report` is set, raises the status word.
 __device__ __forceinline__ uint32_t thread_flags(const int32_t *sample, uint64_t count,
                                                  const double *kmin, const double *kmax,
                                                  const uint8_t *valid, uint64_t vertex_count,
-                                                 double threshold, uint32_t *scratch) {
+                                                 double threshold, uint32_t *scratch,
+                                                 bool report) {
   uint64_t base = uint64_t(blockIdx.x) * kPruneTile + uint64_t(threadIdx.x) * kPrunePerThread;
   uint32_t bits = 0;
   for (uint32_t j = 0; j < kPrunePerThread; ++j) {
@@ -67,7 +70,7 @@ __device__ __forceinline__ uint32_t thread_flags(const int32_t *sample, uint64_t
     if (i >= count) break;
     int32_t v = sample[i];
     if (v < 0 || uint64_t(v) >= vertex_count) {
-      atomicOr(&scratch[kStatusWord], 1u);
+      if (report) atomicOr(&scratch[kStatusWord], 1u);
       continue;
     }
     if (keep_vertex(v, kmin, kmax, valid, threshold)) bits |= 1u << j;
@@ -100,7 +103,8 @@ __device__ __forceinline__ uint32_t block_exclusive(uint32_t value, uint32_t *to
 __global__ void __launch_bounds__(kPruneThreads) prune_tile_counts(
     const int32_t *sample, uint64_t count, const double *kmin, const double *kmax,
     const uint8_t *valid, uint64_t vertex_count, double threshold, uint32_t *scratch) {
-  uint32_t bits = thread_flags(sample, count, kmin, kmax, valid, vertex_count, threshold, scratch);
+  uint32_t bits =
+      thread_flags(sample, count, kmin, kmax, valid, vertex_count, threshold, scratch, true);
   uint32_t total;
   block_exclusive(__popc(bits), &total);
   if (threadIdx.x == 0) scratch[blockIdx.x] = total;
@@ -145,7 +149,8 @@ __global__ void __launch_bounds__(kPruneThreads) prune_scatter(
     const int32_t *sample, uint64_t count, const double *kmin, const double *kmax,
     const uint8_t *valid, uint64_t vertex_count, double threshold, uint32_t *scratch,
     int32_t *pruned) {
-  uint32_t bits = thread_flags(sample, count, kmin, kmax, valid, vertex_count, threshold, scratch);
+  uint32_t bits =
+      thread_flags(sample, count, kmin, kmax, valid, vertex_count, threshold, scratch, false);
   uint32_t total;
   uint32_t rank = block_exclusive(__popc(bits), &total);
   uint64_t out = uint64_t(scratch[blockIdx.x]) + rank;
@@ -169,15 +174,17 @@ sym_status cuda_fail(cudaError_t e, const char *what) {
   return SYM_CUDA_ERROR;
 }
 
-// Scratch address on the current device (setting it up on first use).
-sym_status scratch_for_current_device(uint32_t **out) {
+// Scratch address on the current device.  The first use on a device looks
+// it up; `refresh` looks it up again (after cudaDeviceReset the device's
+// context, and with it the array's address, is new).
+sym_status scratch_for_current_device(uint32_t **out, bool refresh) {
   int device = -1;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (device < 0 || device >= kMaxDevices)
     return fail_with(SYM_RUNTIME_ERROR, "device ordinal beyond the static scratch table");
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (!g_scratch_ptr[device]) {
+  if (refresh || !g_scratch_ptr[device]) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_prune_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_prune_scratch)");
@@ -195,7 +202,7 @@ uint64_t sym_prune_static_max_samples(void) { return kPruneMaxSamples; }
 
 sym_status sym_prune_static_setup(void) {
   uint32_t *p = nullptr;
-  return scratch_for_current_device(&p);
+  return scratch_for_current_device(&p, true);
 }
 
 sym_status sym_prune_static(const int32_t *sample, uint64_t count, const double *kmin,
@@ -211,7 +218,7 @@ sym_status sym_prune_static(const int32_t *sample, uint64_t count, const double 
   if (!(prune > 0 && prune < 1))
     return fail_with(SYM_INVALID_ARGUMENT, "prune must lie in (0, 1)");
   uint32_t *scratch = nullptr;
-  sym_status s = scratch_for_current_device(&scratch);
+  sym_status s = scratch_for_current_device(&scratch, false);
   if (s != SYM_OK) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(scratch + kStatusWord, 0, sizeof(uint32_t), st);

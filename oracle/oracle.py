@@ -28,7 +28,23 @@ from . import symd
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_HARNESS = HERE / "_ref" / "ref_harness"
-REFERENCE_TREE = Path("/root/reference")
+
+
+def reference_tree():
+    """The reference's source tree, or None where it is absent: the
+    MITRA_REFERENCE_DIR environment variable, else the default that
+    oracle/Makefile's recipe records (REF)."""
+    path = os.environ.get("MITRA_REFERENCE_DIR")
+    if not path:
+        try:
+            path = subprocess.run(["make", "-s", "--no-print-directory", "-C", str(HERE),
+                                   "print-ref"], check=True, capture_output=True,
+                                  text=True).stdout.strip()
+        except (OSError, subprocess.CalledProcessError):
+            return None
+    tree = Path(path)
+    return tree if (tree / "include" / "symmetry").is_dir() else None
+
 
 _P = C.POINTER
 _PROTOS = [
@@ -64,8 +80,9 @@ def build(reference=False):
     """Compile the oracle (and, when the reference tree is present and
     `reference` is set, the reference harness) with oracle/Makefile."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    if reference and REFERENCE_TREE.exists():
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_TREE}"], check=True)
+    tree = reference_tree() if reference else None
+    if tree:
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={tree}"], check=True)
 
 
 def lib():

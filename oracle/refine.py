@@ -21,8 +21,9 @@ import numpy as np
 
 def closest_on_segments(p, a, b):
     """Closest points of segments ab to points p (the clamp of the
-    reference's segment distance: no parameter for a segment shorter than
-    1e-7)."""
+    reference's segment distance, src/core/math.cpp: the parameter is used
+    only when the segment's squared length exceeds 1e-14, the reference's
+    eps; otherwise the closest point is a)."""
     d = b - a
     ln = np.einsum("ij,ij->i", d, d)
     with np.errstate(divide="ignore", invalid="ignore"):

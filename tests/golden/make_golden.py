@@ -21,7 +21,8 @@ need neither the reference nor this script at test time.  Large FP64 arrays
 are stored as SHA-256 digests of their bytes: the oracle is bit-exact, so a
 digest comparison is an exact comparison.
 
-Usage:  python tests/golden/make_golden.py   (needs /root/reference)
+Usage:  python tests/golden/make_golden.py   (needs the reference tree: the
+        MITRA_REFERENCE_DIR environment variable, else oracle/Makefile's REF)
 """
 from __future__ import annotations
 
@@ -39,7 +40,7 @@ from mitra_algo_gb300.mesh import mirrored_heightfield  # noqa: E402
 from oracle import oracle, symd  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-EXAMPLES = oracle.REFERENCE_TREE / "examples"
+EXAMPLES = (oracle.reference_tree() or Path("reference-tree-not-found")) / "examples"
 
 
 def digest(a) -> str:

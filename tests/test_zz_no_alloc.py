@@ -61,10 +61,45 @@ def test_matches_select_on_golden_cases(gpu, case):
     f = features_from(d, mesh.vertex_count)
     o = options_from(d)
     s = gpu.select(mesh, f, d["weights"], o, Rng(int(d["seed"][0])))
-    for kept, count in prune_static(s.sample, f, o.prune):
-        assert count == len(s.pruned)
-        assert np.array_equal(kept[:count], s.pruned)
+    want = case["out"]["pruned"]  # the reference's own select() on this case
+    assert np.array_equal(s.pruned, want)
+    for kept, count in prune_static(case["out"]["sample"], f, o.prune):
+        assert count == len(want)
+        assert np.array_equal(kept[:count], want)
         assert np.all(kept[count:] == -7)  # nothing written past the kept entries
+
+
+def test_call_allocates_no_device_memory(gpu):
+    """The defining property: a call (after the set-up) takes no device
+    memory.  The device's free memory is read right before and right after
+    a call whose inputs and outputs were allocated beforehand."""
+    lib = abi.library()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(3)
+    n = 200_000
+    d_sample = torch.from_numpy(rng.integers(0, n, n // 2).astype(np.int32)).to(dev)
+    d_kmin = torch.from_numpy(rng.normal(size=n)).to(dev)
+    d_kmax = torch.from_numpy(rng.normal(size=n)).to(dev)
+    d_valid = torch.ones(n, dtype=torch.uint8, device=dev)
+    d_pruned = torch.empty(n // 2, dtype=torch.int32, device=dev)
+    d_count = torch.empty(1, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    assert lib.sym_prune_static_setup() == abi.OK, lib.sym_last_error()
+
+    def call():
+        assert lib.sym_prune_static(d_sample.data_ptr(), n // 2, d_kmin.data_ptr(),
+                                    d_kmax.data_ptr(), d_valid.data_ptr(), n, 0.85,
+                                    d_pruned.data_ptr(), d_count.data_ptr(),
+                                    stream) == abi.OK, lib.sym_last_error()
+        torch.cuda.synchronize(dev)
+
+    call()  # first call: kernels loaded
+    for _ in range(2):
+        free_before, _ = torch.cuda.mem_get_info(dev)
+        call()
+        free_after, _ = torch.cuda.mem_get_info(dev)
+        assert free_after == free_before
+    assert 0 < int(d_count.cpu()[0]) <= n // 2
 
 
 def test_matches_select_many_tiles(gpu):
