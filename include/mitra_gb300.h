@@ -491,6 +491,23 @@ sym_status sym_tc_selftest(sym_context *ctx, const uint16_t *a1, const uint16_t 
                            const uint16_t *a2, const uint16_t *b2, float *d_out,
                            float *acc_out);
 
+/* Test hook for the throughput path's vote descriptors (the records
+ * sym_detect_fast feeds to its mean shift), on host inputs: `positions` and
+ * `features` (one row per vertex, as the reference's FeaturesView) and
+ * `pairs`.  SYM_RIGID: two records per pair, in the order of the reference's
+ * two rigid votes (transformations.cpp:53-70: b's frame with sign +1, then
+ * -1), each [log(R)/2, (R c + t - c)/box, |d|^2, 0] in FP32 -- the rotation
+ * part is the axis-angle vector of the reference's rotation, the translation
+ * part its descriptor[9..11]; SYM_REFLECTION: one record per pair whose
+ * mirrored frames agree (the reference's test, transformations.cpp:31-48),
+ * [n, (d + n.c)/box, 0, 0, |d|^2, 0].  `out` has room for 16 floats per
+ * pair, `pair_of` for 2 ids per pair (the pair of each record); `count`
+ * receives the number of records. */
+sym_status sym_fast_votes(sym_context *ctx, const sym_points_view *positions,
+                          const sym_features_view *features, const sym_pairs_view *pairs,
+                          const sym_model_context *model, int32_t mode, float *out,
+                          int32_t *pair_of, uint64_t *count);
+
 /* ------------------------------------------------ allocation-free prune */
 /* No counterpart in the reference: an allocation-free form of the prune half
  * of select() (src/cpu/selection.cpp:20-27, src/cuda/backend.cu:21-30).

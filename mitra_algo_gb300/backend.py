@@ -22,7 +22,7 @@ from . import abi
 from .mesh import Prepared, prepare
 from .types import (ClusterOutput, Csr, Features, Mesh, ModelContext, Options, Pairs, Rng,
                     Selection, Topology, Verification, Votes, clusters_from_c, pairs_from_c,
-                    selection_from_c, verification_from_c, votes_from_c)
+                    points_view, selection_from_c, verification_from_c, votes_from_c)
 
 
 class DeviceTimeout(RuntimeError):
@@ -374,6 +374,26 @@ class Gb300Backend:
                                         means.ctypes.data_as(C.POINTER(C.c_double)),
                                         state.ctypes.data_as(C.POINTER(C.c_uint8)), iters))
         return means, state, (iters[0], iters[1])
+
+    def fast_votes(self, mesh: Mesh, features: Features, pairs: Pairs, context: ModelContext,
+                   mode="rigid"):
+        """The throughput path's FP32 vote records for `pairs` (sym_fast_votes):
+        (records (q, 8) float32, pair index of each record (q,))."""
+        if mode not in ("rigid", "reflection"):
+            raise ValueError(f"unknown detection mode {mode!r}")
+        n = len(pairs)
+        out = np.zeros((max(2 * n, 1), 8), np.float32)
+        pair_of = np.zeros(max(2 * n, 1), np.int32)
+        count = C.c_uint64(0)
+        pts = points_view(mesh.vertices)
+        _check(self._lib.sym_fast_votes(self._ctx, C.byref(pts), C.byref(features.view()),
+                                        C.byref(pairs.view()), C.byref(context.to_c()),
+                                        1 if mode == "reflection" else 0,
+                                        out.ctypes.data_as(C.POINTER(C.c_float)),
+                                        pair_of.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        C.byref(count)))
+        q = int(count.value)
+        return out[:q].copy(), pair_of[:q].copy()
 
     def tc_selftest(self, a1, b1, a2, b2):
         """Tensor-core path check: returns (A1 . B1^T, A2 . B2^T) computed by

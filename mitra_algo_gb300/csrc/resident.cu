@@ -72,38 +72,41 @@ struct sym_mesh_handle {
 namespace sym {
 
 // --------------------------------------------------------------- 6-D votes
-// Rotation log map: axis-angle w with |w| = theta in [0, pi].  Near pi the
-// axis comes from the symmetric part in FP64.
+// Rotation log map: the axis-angle vector w of R (|w| = theta in [0, pi]).
+// theta = atan2(|s| / 2, c) from c = (tr R - 1) / 2 and the antisymmetric
+// part s = (R21 - R12, R02 - R20, R10 - R01) = 2 sin(theta) n, which is well
+// conditioned at every angle (acos(c) amplifies the rounding of c by
+// 1 / sin(theta) near 0 and pi).  Away from pi the axis is s / |s|.  For
+// c <= -0.99 (theta within about 8 degrees of pi, where s vanishes) the axis
+// comes, in FP64, from the symmetric part (R + R^T) / 2 = c I + (1 - c) n n^T
+// through its largest diagonal entry, normalised, with the sign of s.
 template <typename T>
 __device__ void log_map(const T r[9], T w[3]) {
-  T c = (r[0] + r[4] + r[8] - T(1)) * T(0.5);
-  c = c > T(1) ? T(1) : (c < T(-1) ? T(-1) : c);
-  T sx = r[7] - r[5], sy = r[2] - r[6], sz = r[3] - r[1];  // 2 sin(theta) n
-  if (c > T(0.9999)) {
-    T theta2 = T(2) * (T(1) - c);  // theta^2 to leading order
-    T f = T(0.5) * (T(1) + theta2 / T(6));
+  const T c = (r[0] + r[4] + r[8] - T(1)) * T(0.5);
+  const T sx = r[7] - r[5], sy = r[2] - r[6], sz = r[3] - r[1];  // 2 sin(theta) n
+  if (c > T(-0.99)) {
+    const T sn = sqrt(sx * sx + sy * sy + sz * sz);
+    const T f = sn > T(0) ? atan2(T(0.5) * sn, c) / sn : T(0.5);
     w[0] = f * sx, w[1] = f * sy, w[2] = f * sz;
-  } else if (c > T(-0.99)) {
-    T theta = acos(c);
-    T f = theta / (T(2) * sin(theta));
-    w[0] = f * sx, w[1] = f * sy, w[2] = f * sz;
-  } else {
-    double rd[9];
-    for (int i = 0; i < 9; ++i) rd[i] = double(r[i]);
-    double cd = (rd[0] + rd[4] + rd[8] - 1) * 0.5;
-    cd = cd > 1 ? 1 : (cd < -1 ? -1 : cd);
-    double theta = acos(cd), one_c = 1 - cd;
-    int k = 0;
-    if (rd[4] > rd[k * 4]) k = 1;
-    if (rd[8] > rd[k * 4]) k = 2;
-    double n[3];
-    n[k] = sqrt(fmax((rd[k * 4] - cd) / one_c, 0.0));
-    for (int j = 0; j < 3; ++j)
-      if (j != k) n[j] = (rd[k * 3 + j] + rd[j * 3 + k]) / (2 * one_c * n[k]);
-    double s[3] = {rd[7] - rd[5], rd[2] - rd[6], rd[3] - rd[1]};
-    if (n[0] * s[0] + n[1] * s[1] + n[2] * s[2] < 0) n[0] = -n[0], n[1] = -n[1], n[2] = -n[2];
-    w[0] = T(theta * n[0]), w[1] = T(theta * n[1]), w[2] = T(theta * n[2]);
+    return;
   }
+  double rd[9];
+  for (int i = 0; i < 9; ++i) rd[i] = double(r[i]);
+  const double cd = (rd[0] + rd[4] + rd[8] - 1) * 0.5;
+  const double s[3] = {rd[7] - rd[5], rd[2] - rd[6], rd[3] - rd[1]};
+  const double theta = atan2(0.5 * sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]), cd);
+  const double one_c = 1 - cd;
+  int k = 0;
+  if (rd[4] > rd[k * 4]) k = 1;
+  if (rd[8] > rd[k * 4]) k = 2;
+  double n[3];
+  n[k] = sqrt(fmax((rd[k * 4] - cd) / one_c, 0.0));
+  for (int j = 0; j < 3; ++j)
+    if (j != k) n[j] = (rd[k * 3 + j] + rd[j * 3 + k]) / (2 * one_c * n[k]);
+  const double len = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const double sign = n[0] * s[0] + n[1] * s[1] + n[2] * s[2] < 0 ? -1.0 : 1.0;
+  const double g = sign * theta / len;
+  w[0] = T(g * n[0]), w[1] = T(g * n[1]), w[2] = T(g * n[2]);
 }
 
 // Two rigid votes per pair (b's frame with sign +1, then -1) as the
@@ -202,9 +205,8 @@ __device__ __forceinline__ void finish_vote(const float r[9], float d[8], const 
 }
 
 __device__ __forceinline__ bool near_pi(const float r[9]) {
-  float c = (r[0] + r[4] + r[8] - 1.f) * 0.5f;
-  c = c > 1.f ? 1.f : (c < -1.f ? -1.f : c);
-  return !(c > 0.9999f) && !(c > -0.99f);  // log_map's FP64 branch
+  const float c = (r[0] + r[4] + r[8] - 1.f) * 0.5f;
+  return !(c > -0.99f);  // log_map's FP64 branch
 }
 
 __global__ void votes6_f32(const float4 *frames, const int32_t *pa, const int32_t *pb, uint64_t np,
@@ -307,6 +309,49 @@ __global__ void plane_votes(const double *pos, uint64_t nv, const int32_t *pa, c
   T out[8] = {n[0], n[1], n[2], (d + n[0] * T(cx) + n[1] * T(cy) + n[2] * T(cz)) / T(box), 0, 0, 0, 0};
   out[6] = out[0] * out[0] + out[1] * out[1] + out[2] * out[2] + out[3] * out[3];
   for (int k = 0; k < 8; ++k) desc[v * 8 + k] = out[k];
+}
+
+// The FP32 rigid votes of np pairs into desc (2 np records of 8 floats):
+// frames_f32, votes6_f32, then votes6_near_pi for the votes near pi.
+void rigid_votes_f32(Call &call, const double *xyz, const double *nrm, const double *dmn,
+                     const double *dmx, uint64_t nv, const int32_t *pa, const int32_t *pb,
+                     uint64_t np, const sym_model_context &model, float *desc) {
+  if (!np) return;
+  cudaStream_t st = call.stream();
+  const double *c = model.center;
+  float4 *frames = call.alloc<float4>(3 * nv);
+  unsigned long long *near_list = call.alloc<unsigned long long>(2 * np);
+  unsigned long long *near_count = call.alloc<unsigned long long>(1);
+  SYM_CUDA(cudaMemsetAsync(near_count, 0, 8, st));
+  frames_f32<<<blocks_for(nv), kThreads, 0, st>>>(xyz, nrm, dmn, dmx, nv, frames);
+  check_launch();
+  votes6_f32<<<blocks_for(np), kThreads, 0, st>>>(frames, pa, pb, np, model.box_size, c[0], c[1],
+                                                   c[2], desc, near_list, near_count);
+  check_launch();
+  votes6_near_pi<<<152 * 8, kThreads, 0, st>>>(frames, pa, pb, model.box_size, c[0], c[1], c[2],
+                                               desc, near_list, near_count);
+  check_launch();
+  call.launched(3);
+}
+
+// Reflection mode: the indices of the np pairs whose mirrored frames agree
+// (plane_flags, in FP64), in pair order, into list; returns their number.
+uint64_t plane_vote_pairs(Call &call, const double *xyz, const double *nrm, const double *dmn,
+                          uint64_t nv, const int32_t *pa, const int32_t *pb, uint64_t np,
+                          int32_t *list) {
+  cudaStream_t st = call.stream();
+  uint8_t *flags = call.alloc<uint8_t>(std::max<uint64_t>(np, 1));
+  uint64_t *count = call.alloc<uint64_t>(1);
+  if (np) {
+    plane_flags<<<blocks_for(np), kThreads, 0, st>>>(xyz, nrm, dmn, nv, pa, pb, np, flags);
+    check_launch();
+    call.launched();
+  }
+  compact_indices(call, flags, np, list, count);
+  uint64_t q = 0;
+  call.d2h(&q, count, 8);
+  call.sync();
+  return q;
 }
 
 // keep[i]: item i of n enters the subsample (probability p, from a hash of
@@ -448,18 +493,8 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   int32_t *plane_list = nullptr;
   uint64_t q = 2 * np;
   if (reflection) {  // one vote per pair whose mirrored frames agree
-    uint8_t *flags = call.alloc<uint8_t>(std::max<uint64_t>(np, 1));
     plane_list = call.alloc<int32_t>(std::max<uint64_t>(np, 1));
-    uint64_t *count = call.alloc<uint64_t>(1);
-    if (np) {
-      plane_flags<<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, nv, pa, pb, np,
-                                                       flags);
-      check_launch();
-      call.launched();
-    }
-    compact_indices(call, flags, np, plane_list, count);
-    call.d2h(&q, count, 8);
-    call.sync();
+    q = plane_vote_pairs(call, h.xyz, f.normal_x, f.dmin_x, nv, pa, pb, np, plane_list);
     int32_t *none = nullptr;
     q = subsample(q, 1, plane_list, none);
   }
@@ -487,20 +522,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     }
     call.launched(want64 ? 2 : 1);
   } else {
-    float4 *frames = call.alloc<float4>(3 * nv);
-    unsigned long long *near_list = call.alloc<unsigned long long>(q);
-    unsigned long long *near_count = call.alloc<unsigned long long>(1);
-    SYM_CUDA(cudaMemsetAsync(near_count, 0, 8, st));
-    frames_f32<<<blocks_for(nv), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x, nv,
-                                                     frames);
-    check_launch();
-    votes6_f32<<<blocks_for(np), kThreads, 0, st>>>(frames, pa, pb, np, h.model.box_size, c[0],
-                                                     c[1], c[2], desc_raw, near_list, near_count);
-    check_launch();
-    votes6_near_pi<<<152 * 8, kThreads, 0, st>>>(frames, pa, pb, h.model.box_size, c[0], c[1], c[2],
-                                                 desc_raw, near_list, near_count);
-    check_launch();
-    call.launched(3);
+    rigid_votes_f32(call, h.xyz, f.normal_x, f.dmin_x, f.dmax_x, nv, pa, pb, np, h.model, desc_raw);
     if (want64) {
       votes6<double><<<blocks_for(np), kThreads, 0, st>>>(h.xyz, f.normal_x, f.dmin_x, f.dmax_x,
                                                           nv, pa, pb, np, h.model.box_size, c[0],
@@ -726,6 +748,46 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   r.stage_ms[5] = clock.ms(5, 6);
   r.stage_ms[6] = clock.ms(7, 8);
   r.stage_ms[7] = clock.ms(8, 9);
+}
+
+// The vote records of the throughput path for given pairs (sym_fast_votes).
+uint64_t fast_votes_host(Call &call, const sym_points_view &pos, const sym_features_view &fv,
+                         const sym_pairs_view &pr, const sym_model_context &model, int mode,
+                         float *out, int32_t *pair_of) {
+  const uint64_t nv = pos.count, np = pr.count;
+  if (fv.count != nv || fv.normal.count != nv || fv.dmin.count != nv || fv.dmax.count != nv)
+    fail(SYM_INVALID_ARGUMENT, "SoA component lengths differ");
+  if (mode != SYM_RIGID && mode != SYM_REFLECTION) fail(SYM_INVALID_ARGUMENT, "unknown detection mode");
+  for (uint64_t i = 0; i < np; ++i)
+    if (pr.a[i] < 0 || pr.b[i] < 0 || uint64_t(pr.a[i]) >= nv || uint64_t(pr.b[i]) >= nv)
+      fail(SYM_INVALID_ARGUMENT, "pair vertex index out of range");
+  if (!np) return 0;
+  const double *xyz = upload_points(call, pos), *nrm = upload_points(call, fv.normal),
+               *dmn = upload_points(call, fv.dmin), *dmx = upload_points(call, fv.dmax);
+  const int32_t *pa = call.upload(pr.a, np), *pb = call.upload(pr.b, np);
+  uint64_t q = 0;
+  if (mode == SYM_RIGID) {
+    q = 2 * np;
+    float *desc = call.alloc<float>(q * 8);
+    rigid_votes_f32(call, xyz, nrm, dmn, dmx, nv, pa, pb, np, model, desc);
+    call.d2h(out, desc, q * 32);
+    for (uint64_t v = 0; v < q; ++v) pair_of[v] = int32_t(v / 2);
+  } else {
+    int32_t *list = call.alloc<int32_t>(np);
+    q = plane_vote_pairs(call, xyz, nrm, dmn, nv, pa, pb, np, list);
+    if (q) {
+      float *desc = call.alloc<float>(q * 8);
+      const double *c = model.center;
+      plane_votes<float><<<blocks_for(q), kThreads, 0, call.stream()>>>(
+          xyz, nv, pa, pb, list, q, model.box_size, c[0], c[1], c[2], desc);
+      check_launch();
+      call.launched();
+      call.d2h(out, desc, q * 32);
+      call.d2h(pair_of, list, q * 4);
+    }
+  }
+  call.check_status("fast_votes");
+  return q;
 }
 
 }  // namespace sym
@@ -1015,6 +1077,26 @@ sym_status sym_tc_selftest(sym_context *ctx, const uint16_t *a1, const uint16_t 
   } catch (const sym::Error &e) {
     sym_error_text = e.what();
     return e.status;
+  }
+}
+
+sym_status sym_fast_votes(sym_context *ctx, const sym_points_view *positions,
+                          const sym_features_view *features, const sym_pairs_view *pairs,
+                          const sym_model_context *model, int32_t mode, float *out,
+                          int32_t *pair_of, uint64_t *count) {
+  if (!ctx || !positions || !features || !pairs || !model || !count ||
+      (pairs->count && (!out || !pair_of)))
+    return SYM_INVALID_ARGUMENT;
+  try {
+    sym::Call call(ctx, "fast_votes");
+    *count = sym::fast_votes_host(call, *positions, *features, *pairs, *model, mode, out, pair_of);
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
   }
 }
 
