@@ -381,6 +381,10 @@ typedef struct sym_fast_result {
    * events around each launch) and the seed-vote evaluations it made */
   uint64_t tc_launches;
   double tc_kernel_ms, tc_evaluations;
+  /* verification queries that the FP32 search and its FP64 rechecks left
+   * to the reference-order BVH (an exact FP64 distance tie between faces
+   * that disagree on the normal test, or too many candidate faces) */
+  uint64_t verify_undecided;
 } sym_fast_result;
 void sym_fast_options_default(sym_fast_options *out);
 /* `sample` is a host array of vertex ids (the area-weighted sample). */
@@ -406,6 +410,19 @@ sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
                                  const sym_options *options, sym_cluster_record *records,
                                  uint64_t count, int32_t iterations, double *coverage,
                                  double *rms, uint32_t *patches);
+
+/* Backend::verification (pipeline.h:67-68; src/cpu/verification.cpp:50-110)
+ * on a resident mesh: the same side lists, patches, coverage and rms as
+ * sym_verification gives for the mesh and records, bit for bit.  The
+ * closest-point searches run in FP32 on the mesh's LBVH and every decision
+ * is rechecked in FP64 with the reference's expressions; queries whose FP64
+ * nearest distance is shared by faces that disagree on the normal test
+ * (the reference keeps the face its median-split BVH visits first) go
+ * through that BVH, built on the host once per resident mesh when first
+ * needed.  `undecided` (may be NULL) receives the number of such queries. */
+sym_status sym_verification_resident(sym_context *ctx, sym_mesh_handle *mesh,
+                                     const sym_clusters_view *clusters, const sym_options *options,
+                                     sym_verification_result *out, uint64_t *undecided);
 
 /* GPU mesh preparation: the reference's prepare() (src/core/prepare.cpp:
  * 102-149) without subdivision (options->subdivide must be 0) and its

@@ -176,7 +176,7 @@ class FastResult(C.Structure):
                 ("patches", C.c_uint32 * (2 * FAST_MAX_CLUSTERS)),
                 ("precise", C.c_uint8 * FAST_MAX_CLUSTERS),
                 ("tc_launches", C.c_uint64), ("tc_kernel_ms", C.c_double),
-                ("tc_evaluations", C.c_double)]
+                ("tc_evaluations", C.c_double), ("verify_undecided", C.c_uint64)]
 
 
 class PreparedOut(C.Structure):
@@ -238,6 +238,8 @@ PROTOTYPES = [
     ("sym_refine_transforms", C.c_int, [C.c_void_p, C.c_void_p, P(Options), P(ClusterRecord),
                                         C.c_uint64, C.c_int32, _d, _d, P(C.c_uint32)]),
     ("sym_detect_fast_batch", C.c_int, [P(C.c_void_p), C.c_int32, P(BatchItem), C.c_uint64]),
+    ("sym_verification_resident", C.c_int, [C.c_void_p, C.c_void_p, P(ClustersView), P(Options),
+                                            P(VerificationOut), P(C.c_uint64)]),
     ("sym_prepare", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(PreparedOut)]),
     ("sym_prepared_release", None, [P(PreparedOut)]),
     ("sym_mesh_load_raw", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(C.c_void_p)]),

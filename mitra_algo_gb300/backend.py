@@ -152,6 +152,23 @@ class Gb300Backend:
         finally:
             self._lib.sym_verification_release(C.byref(out))
 
+    def verification_resident(self, mesh: "ResidentMesh", clusters: ClusterOutput,
+                              options: Options):
+        """Backend::verification on a resident mesh (sym_verification_resident):
+        the same result as verification() on the mesh's host arrays; also
+        returns how many queries went to the reference-order BVH."""
+        view, keep = clusters.view()
+        out = abi.VerificationOut()
+        undecided = C.c_uint64(0)
+        _check(self._lib.sym_verification_resident(self._ctx, mesh.handle, C.byref(view),
+                                                   C.byref(options.to_c()), C.byref(out),
+                                                   C.byref(undecided)))
+        del keep
+        try:
+            return verification_from_c(out), int(undecided.value)
+        finally:
+            self._lib.sym_verification_release(C.byref(out))
+
     def triangle_distances(self, queries) -> np.ndarray:
         q = np.ascontiguousarray(queries, np.float64).reshape(-1)
         n = q.size // 12
@@ -347,6 +364,7 @@ class Gb300Backend:
         out["tc_launches"] = int(res.tc_launches)
         out["tc_kernel_ms"] = float(res.tc_kernel_ms)
         out["tc_evaluations"] = float(res.tc_evaluations)
+        out["verify_undecided"] = int(res.verify_undecided)
         out["rotation"] = [list(res.records[i].rotation) for i in range(n)]
         out["translation"] = [list(res.records[i].translation) for i in range(n)]
         out["reflection"] = [bool(res.records[i].reflection) for i in range(n)]

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <limits>
 #include <map>
@@ -40,9 +41,6 @@ void prune_device(Call &, const int32_t *, uint64_t, const double *, const doubl
                   const uint8_t *, double, int32_t *, uint64_t *);
 uint64_t pairing_device(Call &, const int32_t *, uint64_t, const double *, uint64_t, const double *,
                         const double *, double, double, uint64_t, int32_t **, int32_t **);
-void verification_fast(Call &, const Lbvh &, const double *, const double *, const double *,
-                       const uint64_t *, const int32_t *, sym_cluster_record *, uint64_t, double,
-                       int, const double *, double *, double *, uint32_t *);
 // BF16 tensor-core bulk iterations (meanshift_tc.cu); returns false when the
 // tensor path cannot run this problem (the caller then stays in FP32).
 // seed_iterations (optional) receives the sum over iterations of the
@@ -67,6 +65,16 @@ struct sym_mesh_handle {
   uint64_t *nbr_off = nullptr;
   sym_edge *edges = nullptr;
   sym::Lbvh lbvh;  // FP32 linear BVH of the faces (verification of the fast path)
+  sym::RefBvh ref;  // the reference-order BVH, built when a verification first needs it
+  sym::ResidentSurface surface() {
+    return {&lbvh, xyz, vn, w, faces, nbr_off, nbr, nv, nf, &ref};
+  }
+  void release() {  // the device memory (after the context's stream is idle)
+    sym::lbvh_free(lbvh);
+    sym::ref_bvh_free(ref);
+    if (block) cudaFree(block);
+    block = nullptr;
+  }
 };
 
 namespace sym {
@@ -733,9 +741,9 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   clock.mark(8);
   // ---- (d) verification of the top modes
   if (fo.verify && nc) {
-    verification_fast(call, h.lbvh, h.xyz, h.vn, h.w, h.nbr_off, h.nbr, r.records, nc,
-                      o.verify_threshold * h.model.box_size, fo.refine, h.model.center,
-                      r.coverage, r.rms, r.patches);
+    verification_fast(call, h.surface(), r.records, nc, o.verify_threshold * h.model.box_size,
+                      fo.refine, h.model.center, r.coverage, r.rms, r.patches,
+                      &r.verify_undecided);
   }
   clock.mark(9);
   call.sync();
@@ -808,10 +816,39 @@ sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
   try {
     sym::Call call(ctx, "refine_transforms");
     if (iterations < 0) sym::fail(SYM_INVALID_ARGUMENT, "negative refinement iterations");
-    sym::verification_fast(call, mesh->lbvh, mesh->xyz, mesh->vn, mesh->w, mesh->nbr_off,
-                           mesh->nbr, records, count,
+    sym::verification_fast(call, mesh->surface(), records, count,
                            options->verify_threshold * mesh->model.box_size, iterations,
-                           mesh->model.center, coverage, rms, patches);
+                           mesh->model.center, coverage, rms, patches, nullptr);
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
+  }
+}
+
+sym_status sym_verification_resident(sym_context *ctx, sym_mesh_handle *mesh,
+                                     const sym_clusters_view *clusters, const sym_options *options,
+                                     sym_verification_result *out, uint64_t *undecided) {
+  if (!ctx || !mesh || !clusters || !options || !out || (clusters->count && !clusters->records))
+    return SYM_INVALID_ARGUMENT;
+  *out = sym_verification_result{};
+  try {
+    sym::Call call(ctx, "verification");
+    const uint64_t nc = clusters->count;
+    if (nc && (!mesh->nv || !mesh->nf))
+      sym::fail(SYM_INVALID_ARGUMENT, "verification requires a nonempty surface");
+    std::vector<std::vector<int32_t>> side;
+    std::vector<std::vector<std::vector<int32_t>>> patches;
+    std::vector<double> coverage, rms;
+    uint64_t n = 0;
+    sym::verification_resident(call, mesh->surface(), clusters->records, nc,
+                               options->verify_threshold * mesh->model.box_size, side, patches,
+                               coverage, rms, &n);
+    if (undecided) *undecided = n;
+    sym::fill_verification_result(nc, side, patches, coverage, rms, *out, std::malloc);
     return SYM_OK;
   } catch (const sym::Error &e) {
     sym_error_text = e.what();
@@ -885,8 +922,7 @@ sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_
       h->lbvh = sym::lbvh_build(call, h->xyz, nv, h->faces, nf);
       call.check_status("mesh_load");
     } catch (...) {
-      sym::lbvh_free(h->lbvh);
-      cudaFree(h->block);
+      h->release();
       delete h;
       throw;
     }
@@ -950,8 +986,7 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
   } catch (const sym::Error &e) {
     if (h) {
       cudaStreamSynchronize(ctx->stream);
-      sym::lbvh_free(h->lbvh);
-      cudaFree(h->block);
+      h->release();
       delete h;
     }
     sym_error_text = e.what();
@@ -959,8 +994,7 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
   } catch (const std::exception &e) {
     if (h) {
       cudaStreamSynchronize(ctx->stream);
-      sym::lbvh_free(h->lbvh);
-      cudaFree(h->block);
+      h->release();
       delete h;
     }
     sym_error_text = e.what();
@@ -972,8 +1006,7 @@ void sym_mesh_free(sym_mesh_handle *h) {
   if (!h) return;
   cudaSetDevice(h->ctx->device);
   cudaStreamSynchronize(h->ctx->stream);
-  sym::lbvh_free(h->lbvh);
-  cudaFree(h->block);
+  h->release();
   delete h;
 }
 

@@ -31,183 +31,71 @@
 
 namespace sym {
 
-__host__ __device__ inline double segment_d2(D3 p, D3 a, D3 b) {
-  D3 d = b - a;
-  double l = dot(d, d);
-  double t = 0;
-  if (l > 1e-14) {
-    t = dot(p - a, d) / l;
-    t = t < 0.0 ? 0.0 : (1.0 < t ? 1.0 : t);
-  }
-  D3 e = p - (a + d * t);
-  return dot(e, e);
+HostBvh::HostBvh(const sym_mesh_view &m) {
+  ids.resize(m.faces.count);
+  for (uint64_t i = 0; i < ids.size(); ++i) ids[i] = int32_t(i);
+  auto coord = [&](int f, int corner, int axis) {
+    const int32_t *col = corner == 0 ? m.faces.v0 : (corner == 1 ? m.faces.v1 : m.faces.v2);
+    const double *c = axis == 0 ? m.vertices.x : (axis == 1 ? m.vertices.y : m.vertices.z);
+    return c[col[f]];
+  };
+  struct Builder {
+    HostBvh &t;
+    decltype(coord) &co;
+    int build(int begin, int end, int level) {
+      t.depth = std::max(t.depth, level);
+      BvhNode n;
+      for (int k = 0; k < 3; ++k) n.lo[k] = 1e300, n.hi[k] = -1e300;
+      for (int i = begin; i < end; ++i)
+        for (int corner = 0; corner < 3; ++corner)
+          for (int k = 0; k < 3; ++k) {
+            double x = co(t.ids[i], corner, k);
+            n.lo[k] = std::min(n.lo[k], x);
+            n.hi[k] = std::max(n.hi[k], x);
+          }
+      n.begin = begin, n.end = end, n.left = -1, n.right = -1;
+      int index = int(t.nodes.size());
+      t.nodes.push_back(n);
+      if (end - begin > 8) {
+        double ext[3] = {n.hi[0] - n.lo[0], n.hi[1] - n.lo[1], n.hi[2] - n.lo[2]};
+        int axis = ext[1] > ext[0] ? 1 : 0;
+        if (ext[2] > ext[axis]) axis = 2;
+        int mid = (begin + end) / 2;
+        auto centroid = [&](int f) { return (co(f, 0, axis) + co(f, 1, axis) + co(f, 2, axis)) / 3; };
+        std::nth_element(t.ids.begin() + begin, t.ids.begin() + mid, t.ids.begin() + end,
+                         [&](int a, int b) { return centroid(a) < centroid(b); });
+        int l = build(begin, mid, level + 1), r = build(mid, end, level + 1);
+        t.nodes[index].left = l;
+        t.nodes[index].right = r;
+      }
+      return index;
+    }
+  } builder{*this, coord};
+  if (!ids.empty()) builder.build(0, int(ids.size()), 0);
 }
 
-// Ericson, "Real-Time Collision Detection" 5.1.5 region test; degenerate
-// triangles use the nearest of their three segments (reference math.cpp).
-__host__ __device__ inline double triangle_d2(D3 p, D3 a, D3 b, D3 c) {
-  D3 ab = b - a, ac = c - a, ap = p - a;
-  D3 n = cross(ab, ac);
-  if (dot(n, n) < 1e-14 * 1e-14) {
-    double s0 = segment_d2(p, a, b), s1 = segment_d2(p, a, c), s2 = segment_d2(p, b, c);
-    double m = s1 < s0 ? s1 : s0;
-    return s2 < m ? s2 : m;
-  }
-  double d1 = dot(ab, ap), d2 = dot(ac, ap);
-  if (d1 <= 0 && d2 <= 0) return dot(ap, ap);
-  D3 bp = p - b;
-  double d3 = dot(ab, bp), d4 = dot(ac, bp);
-  if (d3 >= 0 && d4 <= d3) return dot(bp, bp);
-  double vc = d1 * d4 - d3 * d2;
-  if (vc <= 0 && d1 >= 0 && d3 <= 0) {
-    D3 e = p - (a + ab * (d1 / (d1 - d3)));
-    return dot(e, e);
-  }
-  D3 cp = p - c;
-  double d5 = dot(ab, cp), d6 = dot(ac, cp);
-  if (d6 >= 0 && d5 <= d6) return dot(cp, cp);
-  double vb = d5 * d2 - d1 * d6;
-  if (vb <= 0 && d2 >= 0 && d6 <= 0) {
-    D3 e = p - (a + ac * (d2 / (d2 - d6)));
-    return dot(e, e);
-  }
-  double va = d3 * d6 - d5 * d4;
-  if (va <= 0 && (d4 - d3) >= 0 && (d5 - d6) >= 0) {
-    D3 e = p - (b + (c - b) * ((d4 - d3) / ((d4 - d3) + (d5 - d6))));
-    return dot(e, e);
-  }
-  D3 e = p - (a + ab * (vb / (va + vb + vc)) + ac * (vc / (va + vb + vc)));
-  double r = dot(e, e);
-  return r > 0.0 ? r : 0.0;
+RefBvh ref_bvh_upload(const HostBvh &bvh, cudaStream_t stream) {
+  RefBvh b;
+  b.depth = bvh.depth;
+  const size_t node_bytes = (bvh.nodes.size() * sizeof(BvhNode) + 255) & ~size_t(255);
+  const size_t id_bytes = bvh.ids.size() * sizeof(int32_t);
+  SYM_CUDA(cudaMalloc(&b.block, node_bytes + id_bytes + 256));
+  b.nodes = reinterpret_cast<const BvhNode *>(b.block);
+  b.ids = reinterpret_cast<const int32_t *>(b.block + node_bytes);
+  SYM_CUDA(cudaMemcpyAsync(b.block, bvh.nodes.data(), bvh.nodes.size() * sizeof(BvhNode),
+                           cudaMemcpyHostToDevice, stream));
+  SYM_CUDA(cudaMemcpyAsync(b.block + node_bytes, bvh.ids.data(), id_bytes, cudaMemcpyHostToDevice,
+                           stream));
+  SYM_CUDA(cudaStreamSynchronize(stream));
+  return b;
+}
+
+void ref_bvh_free(RefBvh &b) {
+  if (b.block) cudaFree(b.block);
+  b = RefBvh{};
 }
 
 namespace {
-
-struct Node {
-  double lo[3], hi[3];
-  int32_t left, right, begin, end;
-};
-
-// Host BVH with the reference's construction order.
-class HostBvh {
-public:
-  std::vector<Node> nodes;
-  std::vector<int32_t> ids;
-  HostBvh(const sym_mesh_view &m) : m_(m) {
-    ids.resize(m.faces.count);
-    std::iota(ids.begin(), ids.end(), 0);
-    if (!ids.empty()) build(0, int(ids.size()), 0);
-  }
-  int depth = 0;
-
-private:
-  const sym_mesh_view &m_;
-  double coord(int f, int corner, int axis) const {
-    const int32_t *col = corner == 0 ? m_.faces.v0 : (corner == 1 ? m_.faces.v1 : m_.faces.v2);
-    int32_t v = col[f];
-    const double *c = axis == 0 ? m_.vertices.x : (axis == 1 ? m_.vertices.y : m_.vertices.z);
-    return c[v];
-  }
-  int build(int begin, int end, int level) {
-    depth = std::max(depth, level);
-    Node n;
-    for (int k = 0; k < 3; ++k) n.lo[k] = 1e300, n.hi[k] = -1e300;
-    for (int i = begin; i < end; ++i)
-      for (int corner = 0; corner < 3; ++corner)
-        for (int k = 0; k < 3; ++k) {
-          double x = coord(ids[i], corner, k);
-          n.lo[k] = std::min(n.lo[k], x);
-          n.hi[k] = std::max(n.hi[k], x);
-        }
-    n.begin = begin, n.end = end, n.left = -1, n.right = -1;
-    int index = int(nodes.size());
-    nodes.push_back(n);
-    if (end - begin > 8) {
-      double ext[3] = {n.hi[0] - n.lo[0], n.hi[1] - n.lo[1], n.hi[2] - n.lo[2]};
-      int axis = ext[1] > ext[0] ? 1 : 0;
-      if (ext[2] > ext[axis]) axis = 2;
-      int mid = (begin + end) / 2;
-      auto centroid = [&](int f) {
-        return (coord(f, 0, axis) + coord(f, 1, axis) + coord(f, 2, axis)) / 3;
-      };
-      std::nth_element(ids.begin() + begin, ids.begin() + mid, ids.begin() + end,
-                       [&](int a, int b) { return centroid(a) < centroid(b); });
-      int l = build(begin, mid, level + 1), r = build(mid, end, level + 1);
-      nodes[index].left = l;
-      nodes[index].right = r;
-    }
-    return index;
-  }
-};
-
-__device__ double box_d2(D3 p, const Node &n) {
-  double s = 0, a[3] = {p.x, p.y, p.z};
-  for (int k = 0; k < 3; ++k) {
-    double d = fmax(fmax(n.lo[k] - a[k], 0.0), a[k] - n.hi[k]);
-    s += d * d;
-  }
-  return s;
-}
-
-struct Surface {
-  const double *xyz;
-  uint64_t nv;
-  const int32_t *faces;  // 3 x nf
-  uint64_t nf;
-  const Node *nodes;
-  const int32_t *ids;
-};
-
-__device__ D3 vertex(const Surface &s, int32_t v) { return {s.xyz[v], s.xyz[s.nv + v], s.xyz[2 * s.nv + v]}; }
-__device__ D3 corner(const Surface &s, int32_t f, int k) { return vertex(s, s.faces[uint64_t(k) * s.nf + f]); }
-
-constexpr int kStack = 96;
-
-// Near-first search identical to the reference's recursion: a node is
-// skipped when its box is farther than the best so far, the nearer child
-// is searched first, faces win only with a strictly smaller distance.
-// The search starts from `limit` (the next double above tau^2) instead of
-// infinity: the caller rejects every distance above tau^2, nodes farther
-// than the limit can hold no face the reference would accept, and the
-// visiting order of the nodes that remain is unchanged, so an accepted
-// query finds the reference's face and distance.  Rejected queries report
-// no face.
-__device__ double nearest_face(const Surface &s, D3 p, double limit, int32_t &face, int *status) {
-  double best = limit;
-  face = -1;
-  int stack[kStack], top = 0;
-  stack[top++] = 0;
-  while (top) {
-    const Node &n = s.nodes[stack[--top]];
-    if (box_d2(p, n) > best) continue;
-    if (n.left < 0) {
-      for (int i = n.begin; i < n.end; ++i) {
-        int32_t f = s.ids[i];
-        double d = triangle_d2(p, corner(s, f, 0), corner(s, f, 1), corner(s, f, 2));
-        if (d < best) best = d, face = f;
-      }
-    } else {
-      int first = n.left, second = n.right;
-      if (box_d2(p, s.nodes[first]) > box_d2(p, s.nodes[second])) {
-        int t = first;
-        first = second;
-        second = t;
-      }
-      if (top + 2 > kStack) {
-        atomicExch(status, DS_CAPACITY);
-        return best;
-      }
-      stack[top++] = second;
-      stack[top++] = first;
-    }
-  }
-  return best;
-}
-
-struct ClusterMotion {
-  double r[9], t[3], n[3], offset;
-  int32_t reflection;
-};
 
 // flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).
 __global__ void verify_vertices(Surface s, const double *vn, const ClusterMotion *clusters,
@@ -221,55 +109,72 @@ __global__ void verify_vertices(Surface s, const double *vn, const ClusterMotion
   uint64_t i = rem % nv;
   flags[row] = 0;
   if (!inverse) err[c * nv + i] = 0;
-  const ClusterMotion &m = clusters[c];
-  M3 r;
-  for (int k = 0; k < 9; ++k) r.m[k] = m.r[k];
-  if (inverse) r = transpose(r);
-  D3 t{m.t[0], m.t[1], m.t[2]}, pn{m.n[0], m.n[1], m.n[2]};
-  D3 p = vertex(s, int32_t(i));
-  D3 q = inverse ? mul(r, p - t) : mul(r, p) + t;
-  if (norm(q - p) < tau * 2) return;
-  if (m.reflection) {
-    double side = dot(pn, p) + m.offset;
-    if (inverse ? side <= tau : side >= -tau) return;
-  }
-  int32_t face;
-  double d = nearest_face(s, q, limit, face, status);
-  if (d > tau * tau || face < 0) return;
-  D3 a = corner(s, face, 0), b = corner(s, face, 1), cc = corner(s, face, 2);
-  D3 fnorm = unit(cross(b - a, cc - a));
-  D3 ni{vn[i], vn[nv + i], vn[2 * nv + i]};
-  if (dot(mul(r, ni), fnorm) < 0.5) return;
+  double d = 0;
+  if (!exact_query(s, vn, clusters[c], inverse, i, tau, limit, d, status)) return;
   flags[row] = 1;
   if (!inverse) err[c * nv + i] = d;
 }
 
-// Serial sums in the reference's order: thread c < nc handles cluster c,
-// thread nc the total weight.
-__global__ void ordered_sums(const uint8_t *flags, const double *err, const double *w, uint64_t nv,
-                             uint64_t nc, double *error, double *area, uint64_t *side_a_size,
-                             double *total) {
-  uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (c > nc) return;
+// One warp per cluster (block c < nc) or for the total weight (block nc):
+// rows are staged 32 at a time in shared memory and lane 0 adds them in
+// vertex order; a group of 32 rows with no flag set is skipped (adding
+// nothing leaves the sums unchanged).
+__global__ void __launch_bounds__(32) ordered_sums_warp(const uint8_t *flags, const double *err,
+                                                         const double *w, uint64_t nv, uint64_t nc,
+                                                         double *error, double *area,
+                                                         uint64_t *count, double *total) {
+  __shared__ double sv[32], sw[32];
+  const uint64_t c = blockIdx.x;
+  const unsigned lane = threadIdx.x;
   if (c == nc) {
     double t = 0;
-    for (uint64_t i = 0; i < nv; ++i) t += w[i];
-    *total = t;
+    for (uint64_t base = 0; base < nv; base += 32) {
+      const uint64_t i = base + lane;
+      sw[lane] = i < nv ? w[i] : 0.0;
+      __syncwarp();
+      if (lane == 0) {
+        const unsigned m = nv - base < 32 ? unsigned(nv - base) : 32u;
+        for (unsigned j = 0; j < m; ++j) t += sw[j];
+      }
+      __syncwarp();
+    }
+    if (lane == 0) *total = t;
     return;
   }
   double e = 0, a = 0;
-  uint64_t na = 0;
-  const uint8_t *fa = flags + c * 2 * nv, *fb = fa + nv;
-  for (uint64_t i = 0; i < nv; ++i)
-    if (fa[i]) e += err[c * nv + i], a += w[i], ++na;
-  for (uint64_t i = 0; i < nv; ++i)
-    if (fb[i]) a += w[i];
-  error[c] = e;
-  area[c] = a;
-  side_a_size[c] = na;
+  unsigned long long n = 0;
+  for (int dir = 0; dir < 2; ++dir) {
+    const uint8_t *f = flags + (c * 2 + dir) * nv;
+    for (uint64_t base = 0; base < nv; base += 32) {
+      const uint64_t i = base + lane;
+      const bool on = i < nv && f[i];
+      const unsigned mask = __ballot_sync(0xffffffffu, on);
+      if (!mask) continue;
+      sw[lane] = on ? w[i] : 0.0;
+      if (dir == 0) sv[lane] = on ? err[c * nv + i] : 0.0;
+      __syncwarp();
+      if (lane == 0)
+        for (unsigned j = 0; j < 32; ++j)
+          if (mask >> j & 1u) {
+            if (dir == 0) e += sv[j], ++n;
+            a += sw[j];
+          }
+      __syncwarp();
+    }
+  }
+  if (lane == 0) error[c] = e, area[c] = a, count[c] = n;
 }
 
 }  // namespace
+
+void ordered_verification_sums(Call &call, const uint8_t *flags, const double *err,
+                               const double *w, uint64_t nv, uint64_t nc, double *error,
+                               double *area, uint64_t *count, double *total) {
+  ordered_sums_warp<<<unsigned(nc + 1), 32, 0, call.stream()>>>(flags, err, w, nv, nc, error, area,
+                                                                 count, total);
+  check_launch();
+  call.launched();
+}
 
 // Union-find over (set, vertex) rows (find_root: verification.cuh).
 // parent index space: (c * 2 + dir) * nv + i ; -1 marks excluded vertices.
@@ -355,52 +260,30 @@ void triangle_distances_host(Call &call, const double *queries, uint64_t count, 
   call.sync();
 }
 
-// Device core shared by the ABI entry point and the resident pipeline.
-// Mesh arrays are device pointers; `m` is the host mesh (the BVH is built on
-// the host with the reference's construction order).  Fills per (cluster,
-// side) vertex lists, patches, rms and coverage.
-void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, const int32_t *faces,
-                       const double *vn, const double *w, const uint64_t *nbr_off,
-                       const int32_t *nbr, const sym_cluster_record *records, uint64_t nc,
-                       double tau, std::vector<std::vector<int32_t>> &side,
-                       std::vector<std::vector<std::vector<int32_t>>> &patches,
-                       std::vector<double> &coverage, std::vector<double> &rms) {
-  const uint64_t nv = m.vertices.count, nf = m.faces.count;
+ClusterMotion cluster_motion(const sym_cluster_record &r) {
+  ClusterMotion m{};
+  for (int k = 0; k < 9; ++k) m.r[k] = r.rotation[k];
+  for (int k = 0; k < 3; ++k) m.t[k] = r.translation[k], m.n[k] = r.plane_normal[k];
+  m.offset = r.plane_offset;
+  m.reflection = r.reflection != 0;
+  return m;
+}
+
+void finish_verification(Call &call, const uint8_t *flags, const double *err, const double *w,
+                         const uint64_t *nbr_off, const int32_t *nbr, uint64_t nv, uint64_t nc,
+                         std::vector<std::vector<int32_t>> &side,
+                         std::vector<std::vector<std::vector<int32_t>>> &patches,
+                         std::vector<double> &coverage, std::vector<double> &rms) {
   cudaStream_t st = call.stream();
   side.assign(2 * nc, {});
   patches.assign(2 * nc, {});
   coverage.assign(nc, 0);
   rms.assign(nc, 0);
   if (!nc) return;
-  HostBvh bvh(m);
-  if (2 * bvh.depth + 4 > kStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
-  Surface s;
-  s.xyz = xyz;
-  s.nv = nv;
-  s.faces = faces;
-  s.nf = nf;
-  s.nodes = call.upload(bvh.nodes.data(), bvh.nodes.size());
-  s.ids = call.upload(bvh.ids.data(), bvh.ids.size());
-  std::vector<ClusterMotion> motions(nc);
-  for (uint64_t c = 0; c < nc; ++c) {
-    const sym_cluster_record &r = records[c];
-    for (int k = 0; k < 9; ++k) motions[c].r[k] = r.rotation[k];
-    for (int k = 0; k < 3; ++k) motions[c].t[k] = r.translation[k], motions[c].n[k] = r.plane_normal[k];
-    motions[c].offset = r.plane_offset;
-    motions[c].reflection = r.reflection != 0;
-  }
-  ClusterMotion *dm = call.upload(motions.data(), nc);
-  uint64_t rows = nc * 2 * nv;
-  uint8_t *flags = call.alloc<uint8_t>(rows);
-  double *err = call.alloc<double>(nc * nv);
-  double limit = std::nextafter(tau * tau, std::numeric_limits<double>::infinity());
-  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, limit, flags, err,
-                                                         call.status());
-  check_launch();
+  const uint64_t rows = nc * 2 * nv;
   double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
   uint64_t *na = call.alloc<uint64_t>(nc);
-  ordered_sums<<<blocks_for(nc + 1, 64), 64, 0, st>>>(flags, err, w, nv, nc, error, area, na, total);
-  check_launch();
+  ordered_verification_sums(call, flags, err, w, nv, nc, error, area, na, total);
   int32_t *parent = call.alloc<int32_t>(rows);
   init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
   check_launch();
@@ -417,7 +300,7 @@ void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, co
   uint64_t nkept = 0;
   call.d2h(&nkept, kept, 8);
   call.sync();
-  call.launched(5);
+  call.launched(3);
   std::vector<uint64_t> hkeys(nkept);
   std::vector<int32_t> hvals(nkept);
   if (nkept) {
@@ -425,6 +308,7 @@ void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, co
     int32_t *dv = call.alloc<int32_t>(nkept);
     gather_kept<<<blocks_for(nkept), kThreads, 0, st>>>(pos, nkept, keys, nv, dk, dv);
     check_launch();
+    call.launched();
     int bits = 32;
     while ((uint64_t(1) << (bits - 32)) < 2 * nc) ++bits;
     radix_sort_pairs(call, dk, dv, skeys, svals, nkept, bits);
@@ -452,37 +336,49 @@ void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, co
   }
 }
 
-void verification_host(Call &call, const sym_mesh_view &m, const sym_topology_view &g,
-                       const sym_clusters_view &cl, const sym_model_context &ctx,
-                       const sym_options &o, sym_verification_result &out,
-                       void *(*allocate)(size_t)) {
-  const uint64_t nv = m.vertices.count, nf = m.faces.count, nc = cl.count;
-  std::vector<std::vector<int32_t>> side;
-  std::vector<std::vector<std::vector<int32_t>>> patches;
-  std::vector<double> coverage, rms;
-  if (nc) {
-    if (!nv || !nf) fail(SYM_INVALID_ARGUMENT, "verification requires a nonempty surface");
-    if (g.normals.count != nv || g.weight_count != nv || g.neighbors.rows != nv)
-      fail(SYM_INVALID_ARGUMENT, "SoA component lengths differ");
-    validate_csr(g.neighbors, nv, nv, "neighbors");
-    for (uint64_t f = 0; f < nf; ++f)
-      if (m.faces.v0[f] < 0 || m.faces.v1[f] < 0 || m.faces.v2[f] < 0 ||
-          uint64_t(m.faces.v0[f]) >= nv || uint64_t(m.faces.v1[f]) >= nv ||
-          uint64_t(m.faces.v2[f]) >= nv)
-        fail(SYM_INVALID_ARGUMENT, "Face index out of range");
-    double *xyz = upload_points(call, m.vertices);
-    int32_t *faces = upload_faces(call, m.faces);
-    double *vn = upload_points(call, g.normals);
-    double *w = call.upload(g.weights, nv);
-    uint64_t nbr_count = g.neighbors.offsets[nv];
-    uint64_t *nbr_off = call.upload(g.neighbors.offsets, nv + 1);
-    int32_t *nbr = call.upload(g.neighbors.indices, nbr_count);
-    verification_core(call, m, xyz, faces, vn, w, nbr_off, nbr, cl.records, nc,
-                      o.verify_threshold * ctx.box_size, side, patches, coverage, rms);
-  } else {
-    side.assign(0, {});
-    patches.assign(0, {});
+// Device core of sym_verification.  Mesh arrays are device pointers; `m` is
+// the host mesh (the BVH is built on the host with the reference's
+// construction order).  Fills per (cluster, side) vertex lists, patches,
+// rms and coverage.
+void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, const int32_t *faces,
+                       const double *vn, const double *w, const uint64_t *nbr_off,
+                       const int32_t *nbr, const sym_cluster_record *records, uint64_t nc,
+                       double tau, std::vector<std::vector<int32_t>> &side,
+                       std::vector<std::vector<std::vector<int32_t>>> &patches,
+                       std::vector<double> &coverage, std::vector<double> &rms) {
+  const uint64_t nv = m.vertices.count, nf = m.faces.count;
+  cudaStream_t st = call.stream();
+  if (!nc) {
+    finish_verification(call, nullptr, nullptr, w, nbr_off, nbr, nv, 0, side, patches, coverage, rms);
+    return;
   }
+  HostBvh bvh(m);
+  if (2 * bvh.depth + 4 > kRefStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
+  Surface s;
+  s.xyz = xyz;
+  s.nv = nv;
+  s.faces = faces;
+  s.nf = nf;
+  s.nodes = call.upload(bvh.nodes.data(), bvh.nodes.size());
+  s.ids = call.upload(bvh.ids.data(), bvh.ids.size());
+  std::vector<ClusterMotion> motions(nc);
+  for (uint64_t c = 0; c < nc; ++c) motions[c] = cluster_motion(records[c]);
+  ClusterMotion *dm = call.upload(motions.data(), nc);
+  uint64_t rows = nc * 2 * nv;
+  uint8_t *flags = call.alloc<uint8_t>(rows);
+  double *err = call.alloc<double>(nc * nv);
+  double limit = std::nextafter(tau * tau, std::numeric_limits<double>::infinity());
+  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, limit, flags, err,
+                                                         call.status());
+  check_launch();
+  call.launched();
+  finish_verification(call, flags, err, w, nbr_off, nbr, nv, nc, side, patches, coverage, rms);
+}
+
+void fill_verification_result(uint64_t nc, const std::vector<std::vector<int32_t>> &side,
+                              const std::vector<std::vector<std::vector<int32_t>>> &patches,
+                              const std::vector<double> &coverage, const std::vector<double> &rms,
+                              sym_verification_result &out, void *(*allocate)(size_t)) {
   uint64_t na = 0, nb = 0, ra = 0, rb = 0;
   for (uint64_t c = 0; c < nc; ++c) {
     na += side[2 * c].size(), nb += side[2 * c + 1].size();
@@ -531,6 +427,37 @@ void verification_host(Call &call, const sym_mesh_view &m, const sym_topology_vi
   fill(1, out.side_b_offsets, out.side_b, out.patches_b);
   std::copy(coverage.begin(), coverage.end(), out.coverage);
   std::copy(rms.begin(), rms.end(), out.rms);
+}
+
+void verification_host(Call &call, const sym_mesh_view &m, const sym_topology_view &g,
+                       const sym_clusters_view &cl, const sym_model_context &ctx,
+                       const sym_options &o, sym_verification_result &out,
+                       void *(*allocate)(size_t)) {
+  const uint64_t nv = m.vertices.count, nf = m.faces.count, nc = cl.count;
+  std::vector<std::vector<int32_t>> side;
+  std::vector<std::vector<std::vector<int32_t>>> patches;
+  std::vector<double> coverage, rms;
+  if (nc) {
+    if (!nv || !nf) fail(SYM_INVALID_ARGUMENT, "verification requires a nonempty surface");
+    if (g.normals.count != nv || g.weight_count != nv || g.neighbors.rows != nv)
+      fail(SYM_INVALID_ARGUMENT, "SoA component lengths differ");
+    validate_csr(g.neighbors, nv, nv, "neighbors");
+    for (uint64_t f = 0; f < nf; ++f)
+      if (m.faces.v0[f] < 0 || m.faces.v1[f] < 0 || m.faces.v2[f] < 0 ||
+          uint64_t(m.faces.v0[f]) >= nv || uint64_t(m.faces.v1[f]) >= nv ||
+          uint64_t(m.faces.v2[f]) >= nv)
+        fail(SYM_INVALID_ARGUMENT, "Face index out of range");
+    double *xyz = upload_points(call, m.vertices);
+    int32_t *faces = upload_faces(call, m.faces);
+    double *vn = upload_points(call, g.normals);
+    double *w = call.upload(g.weights, nv);
+    uint64_t nbr_count = g.neighbors.offsets[nv];
+    uint64_t *nbr_off = call.upload(g.neighbors.offsets, nv + 1);
+    int32_t *nbr = call.upload(g.neighbors.indices, nbr_count);
+    verification_core(call, m, xyz, faces, vn, w, nbr_off, nbr, cl.records, nc,
+                      o.verify_threshold * ctx.box_size, side, patches, coverage, rms);
+  }
+  fill_verification_result(nc, side, patches, coverage, rms, out, allocate);
 }
 
 }  // namespace sym

@@ -1,6 +1,7 @@
 // SPDX-License-Identifier: MPL-2.0
-// Stage (d) on the throughput path: verification of sym_detect_fast's top
-// modes with a linear BVH built on the GPU and FP32 closest-point queries.
+// Stage (d) on the throughput path: verification of resident meshes with a
+// linear BVH built on the GPU, FP32 closest-point searches and FP64
+// rechecks, with results identical to the reference's.
 //
 // The tests are the reference's (src/cpu/verification.cpp:22-110): a vertex
 // supports a mode in one direction when its image under the mode's motion
@@ -9,18 +10,27 @@
 // 60 degrees of the nearest face's normal; coverage is the supporting
 // vertices' weight over the total, rms the root mean square of the forward
 // distances; patches are the connected components of the supporting
-// vertices (region growing), counted here.  What differs from the exact
-// path (verification.cu): the BVH is an LBVH (Karras 2012: 30-bit Morton
-// codes of the face centroids, radix sort, longest-common-prefix splits,
-// boxes merged bottom-up), built on the device once per resident mesh; the
-// closest-point search runs in FP32 (the nearest face can differ from the
-// reference's on ties closer than FP32 resolves); the sums are fixed-order
-// block reductions instead of the reference's serial loop.
+// vertices (region growing).
+//
+// How the decisions stay the reference's: the LBVH (Karras 2012: 30-bit
+// Morton codes of the face centroids, radix sort, longest-common-prefix
+// splits, boxes merged bottom-up, built once per resident mesh) is searched
+// in FP32 for every face whose FP32 distance lies within a margin of the
+// nearest one -- a margin several hundred times the FP32 error of a
+// distance, so the face of smallest FP64 distance is always among them.
+// Those candidates are re-evaluated with the reference's FP64 distance, and
+// the FP64 nearest face takes the reference's FP64 distance and normal
+// tests.  A query whose FP64 minimum is shared by faces that disagree on the
+// normal test (the reference then keeps the face its BVH visits first), or
+// whose candidates overflow the list, is re-run through the reference-order
+// BVH (verification.cuh), built on the host once per resident mesh when the
+// first such query appears.  Sums use the reference's serial order.
 #include "primitives.cuh"
 #include "verification.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <limits>
 #include <vector>
 
 namespace sym {
@@ -190,11 +200,6 @@ __global__ void lbvh_boxes(const float *xyz, uint64_t nv, const int32_t *faces, 
 }
 
 // ------------------------------------------------------------ verification
-struct Motion32 {
-  double r[9], t[3], n[3], offset;
-  int32_t reflection;
-};
-
 constexpr int kStackFast = 96;
 
 __device__ __forceinline__ float box_d2f(F3 p, const float *b) {
@@ -264,15 +269,15 @@ __device__ int32_t nearest_face_fast(const BvhView &b, F3 p, float &best, int *s
   return face;
 }
 
-// The verification tests of one (mode, vertex, direction) query: returns
-// the nearest face when vertex i supports mode m in that direction (-1
-// otherwise), its FP32 squared distance in `best` (entering as tau^2) and
-// the image of the vertex in q.  The motion is applied in FP64, the search
-// runs in FP32.
+// The verification tests of one (mode, vertex, direction) query with the
+// FP32 search (the refinement's correspondences): returns the nearest face
+// when vertex i supports mode m in that direction (-1 otherwise), its FP32
+// squared distance in `best` (entering as tau^2) and the image of the vertex
+// in q.  The motion is applied in FP64.
 __device__ __forceinline__ int32_t support_query(const BvhView &b, const double *xyz,
-                                                 const double *vn, const Motion32 &m, uint64_t i,
-                                                 bool inverse, double tau, float &best, double q[3],
-                                                 int *status) {
+                                                 const double *vn, const ClusterMotion &m,
+                                                 uint64_t i, bool inverse, double tau, float &best,
+                                                 double q[3], int *status) {
   const uint64_t nv = b.nv;
   double r[9];
   for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
@@ -305,23 +310,187 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
   return face;
 }
 
-// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).
-__global__ void verify_vertices_fast(BvhView b, const double *xyz, const double *vn,
-                                     const Motion32 *motions, uint64_t nc, double tau, float tau2,
-                                     uint8_t *flags, double *err, int *status) {
-  uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+// ------------------------------------------- exact decisions, FP32 search
+// Margin of the FP32 search, in distance units: kMargin times the largest
+// coordinate magnitude of the query and the mesh.  The FP32 distance of a
+// face whose smallest corner-pair angle has sin^2 >= kWellShaped differs from
+// its FP64 distance by a few tens of FP32 units of that magnitude at most
+// (inputs rounded to FP32, region tests whose conditioning is that angle's
+// 1/sin^2), far below the margin; other faces enter the candidates by the
+// distance of their box instead of their FP32 distance.
+constexpr float kMargin = 1.0f / 16384.0f;
+constexpr float kWellShaped = 0.05f;
+constexpr int kCandidates = 8;
+
+// sin^2 of the smallest angle of triangle abc: |ab x ac|^2 over the product
+// of the two longest squared edges.
+__device__ __forceinline__ float shape_quality(F3 a, F3 b, F3 c) {
+  const F3 ab = b - a, ac = c - a, bc = c - b;
+  const float l0 = dotf(ab, ab), l1 = dotf(ac, ac), l2 = dotf(bc, bc);
+  const F3 n = crossf(ab, ac);
+  const float lo = fminf(l0, fminf(l1, l2));
+  const float prod = (l0 * l1 * l2) / fmaxf(lo, 1e-37f);
+  return prod > 0.f ? dotf(n, n) / prod : 0.f;
+}
+
+// Faces whose FP64 distance to p can be the smallest: every face whose FP32
+// distance (or, for a badly shaped face, box distance) is within 3 margins
+// of min(best FP32 distance, tau + margin).  Returns the count (kCandidates
+// + 1 on overflow); `best` receives the smallest FP32 distance of a
+// well-shaped face (INFINITY when none lies within tau + 4 margins).
+__device__ int candidate_faces(const BvhView &b, F3 p, float tau_margin, float margin,
+                               int32_t *faces, float *keys, float &best, int *status) {
+  best = INFINITY;
+  float lim = (tau_margin + 3.f * margin) * (tau_margin + 3.f * margin);
+  int n = 0;
+  bool overflow = false;
+  auto consider = [&](int32_t f, float box) {
+    const F3 a = vtx(b, b.faces[f]), bb = vtx(b, b.faces[b.nf + f]), cc = vtx(b, b.faces[2 * b.nf + f]);
+    float key;
+    if (shape_quality(a, bb, cc) >= kWellShaped) {
+      key = triangle_d2f(p, a, bb, cc);
+      if (key < best) {
+        best = key;
+        const float r = fminf(tau_margin, sqrtf(best)) + 3.f * margin;
+        lim = r * r;
+      }
+    } else {
+      key = box;
+    }
+    if (key > lim) return;
+    if (n == kCandidates) {  // drop entries beyond the current limit
+      int m = 0;
+      for (int j = 0; j < n; ++j)
+        if (keys[j] <= lim) faces[m] = faces[j], keys[m++] = keys[j];
+      n = m;
+    }
+    if (n == kCandidates) {
+      overflow = true;
+      return;
+    }
+    faces[n] = f, keys[n++] = key;
+  };
+  if (b.nf == 1) {
+    consider(0, 0.f);
+  } else {
+    int32_t stack[kStackFast];
+    float dist[kStackFast];
+    int top = 0;
+    stack[top] = 0, dist[top++] = 0.f;
+    while (top) {
+      --top;
+      if (dist[top] > lim) continue;
+      const int32_t node = stack[top];
+      const float *bx = b.box + int64_t(node) * 12;
+      const int32_t c0 = b.child[2 * node], c1 = b.child[2 * node + 1];
+      const float d0 = box_d2f(p, bx), d1 = box_d2f(p, bx + 6);
+      if (c0 < 0 && d0 <= lim) consider(~c0, d0);
+      if (c1 < 0 && d1 <= lim) consider(~c1, d1);
+      const bool p0 = c0 >= 0 && d0 <= lim, p1 = c1 >= 0 && d1 <= lim;
+      if (top + 2 > kStackFast) {
+        atomicExch(status, DS_CAPACITY);
+        return kCandidates + 1;
+      }
+      if (p0 && p1) {  // the nearer child is popped first
+        const bool first0 = d0 <= d1;
+        stack[top] = first0 ? c1 : c0, dist[top++] = first0 ? d1 : d0;
+        stack[top] = first0 ? c0 : c1, dist[top++] = first0 ? d0 : d1;
+      } else if (p0) {
+        stack[top] = c0, dist[top++] = d0;
+      } else if (p1) {
+        stack[top] = c1, dist[top++] = d1;
+      }
+    }
+  }
+  if (overflow) return kCandidates + 1;
+  int m = 0;
+  for (int j = 0; j < n; ++j)
+    if (keys[j] <= lim) faces[m] = faces[j], keys[m++] = keys[j];
+  return m;
+}
+
+// One query of the reference's verification, decided with the FP32
+// candidates and FP64 rechecks.  Returns 1 (supports; `d2` = the reference's
+// FP64 squared distance), 0 (does not), or 2 (undecided here: an FP64 tie
+// between faces that disagree on the normal test, or too many candidates).
+__device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn,
+                            const ClusterMotion &m, bool inverse, uint64_t i, double tau,
+                            float scale, double &d2, int *status) {
+  const M3 r = query_rotation(m, inverse);
+  const D3 p = vertex(s, int32_t(i));
+  D3 q;
+  if (query_skipped(m, r, inverse, p, tau, q)) return 0;
+  const F3 qf{float(q.x), float(q.y), float(q.z)};
+  const float mag = fmaxf(scale, fmaxf(fabsf(qf.x), fmaxf(fabsf(qf.y), fabsf(qf.z))));
+  const float margin = kMargin * mag;
+  int32_t faces[kCandidates];
+  float keys[kCandidates];
+  float best;
+  const int n = candidate_faces(b, qf, float(tau) + margin, margin, faces, keys, best, status);
+  if (n > kCandidates) return 2;
+  // the FP64 distances of the candidates: their minimum is the reference's
+  double dmin = INFINITY;
+  double dist[kCandidates];
+  for (int j = 0; j < n; ++j) {
+    dist[j] = triangle_d2(q, corner(s, faces[j], 0), corner(s, faces[j], 1), corner(s, faces[j], 2));
+    dmin = fmin(dmin, dist[j]);
+  }
+  if (!(dmin <= tau * tau)) return 0;
+  // the normal test of every face at (or within a few units of rounding of)
+  // the minimum: one outcome decides, two leave the reference's tie order
+  // to decide
+  const D3 ni{vn[i], vn[s.nv + i], vn[2 * s.nv + i]};
+  const double near = dmin + dmin * 1e-14;
+  int agree = 0, disagree = 0;
+  bool exact_tie_only = true;
+  for (int j = 0; j < n; ++j) {
+    if (dist[j] > near) continue;
+    exact_tie_only = exact_tie_only && dist[j] == dmin;
+    if (normal_agrees(s, faces[j], r, ni)) ++agree;
+    else ++disagree;
+  }
+  if (agree && disagree) return 2;
+  if (!exact_tie_only && agree) return 2;  // the reference's distance is one of several
+  if (!agree) return 0;
+  d2 = dmin;
+  return 1;
+}
+
+// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction); rows
+// left undecided are listed in `undecided` (count in *undecided_count).
+__global__ void verify_vertices_hybrid(BvhView b, Surface s, const double *vn,
+                                       const ClusterMotion *motions, uint64_t nc, double tau,
+                                       float scale, uint8_t *flags, double *err,
+                                       uint32_t *undecided, unsigned long long *undecided_count,
+                                       int *status) {
+  const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t nv = b.nv;
   if (row >= nc * 2 * nv) return;
   const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
-  flags[row] = 0;
-  if (!inverse) err[c * nv + i] = 0;
-  float best = tau2;
-  double q[3];
-  if (support_query(b, xyz, vn, motions[c], i, inverse, tau, best, q, status) < 0) return;
-  flags[row] = 1;
-  if (!inverse) err[c * nv + i] = double(best);
+  double d = 0;
+  const int v = hybrid_query(b, s, vn, motions[c], inverse, i, tau, scale, d, status);
+  flags[row] = v == 1;
+  if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
+  if (v == 2) undecided[atomicAdd(undecided_count, 1ull)] = uint32_t(row);
+}
+
+// The listed rows through the reference-order BVH (exact_query).
+__global__ void verify_listed_ref(Surface s, const double *vn, const ClusterMotion *motions,
+                                  double tau, double limit, const uint32_t *rows,
+                                  unsigned long long count, uint8_t *flags, double *err,
+                                  int *status) {
+  const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint64_t row = rows[k], nv = s.nv;
+  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  const bool inverse = rem >= nv;
+  const uint64_t i = rem % nv;
+  double d = 0;
+  const bool ok = exact_query(s, vn, motions[c], inverse, i, tau, limit, d, status);
+  flags[row] = ok;
+  if (!inverse) err[c * nv + i] = ok ? d : 0.0;
 }
 
 // ------------------------------------------------ FP64 transform refinement
@@ -394,7 +563,7 @@ struct Origin {
 // (the verification's tests), the FP64 closest point of its nearest face to
 // the vertex's image, relative to `o`; ok[c * nv + i] says which.
 __global__ void refine_pairs(BvhView b, const double *xyz, const double *vn,
-                             const Motion32 *motions, uint64_t nc, double tau, float tau2, Origin o,
+                             const ClusterMotion *motions, uint64_t nc, double tau, float tau2, Origin o,
                              double *target, uint8_t *ok, int *status) {
   const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t nv = b.nv;
@@ -505,7 +674,7 @@ __device__ void jacobi3(const double m[9], double val[3], double vec[9]) {
 // run along it), oriented like the previous one, and the plane passes
 // through the weighted mean of the midpoints (p + q) / 2.  A mode with too
 // few or degenerate correspondences keeps its motion.
-__global__ void refine_solve(const double *sums, uint64_t nc, Origin o, Motion32 *motions) {
+__global__ void refine_solve(const double *sums, uint64_t nc, Origin o, ClusterMotion *motions) {
   const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const double *s = sums + c * kRefineSums;
@@ -513,7 +682,7 @@ __global__ void refine_solve(const double *sums, uint64_t nc, Origin o, Motion32
   if (!(W > 0)) return;
   double pb[3], qb[3];
   for (int a = 0; a < 3; ++a) pb[a] = s[1 + a] / W, qb[a] = s[4 + a] / W;
-  Motion32 &m = motions[c];
+  ClusterMotion &m = motions[c];
   if (!m.reflection) {
     double H[9], HtH[9], S2[3], V[9];
     for (int a = 0; a < 3; ++a)
@@ -570,47 +739,6 @@ __global__ void refine_solve(const double *sums, uint64_t nc, Origin o, Motion32
   }
 }
 
-// Block c < nc: sum of the forward errors, supporting weight (both
-// directions) and forward count of cluster c; block nc: the total weight.
-// Fixed-order strided partials and a fixed tree, so the result is
-// reproducible.
-__global__ void __launch_bounds__(256) block_sums(const uint8_t *flags, const double *err,
-                                                  const double *w, uint64_t nv, uint64_t nc,
-                                                  double *error, double *area, uint64_t *count,
-                                                  double *total) {
-  __shared__ double se[256], sa[256];
-  __shared__ unsigned long long sn[256];
-  const uint64_t c = blockIdx.x;
-  double e = 0, a = 0;
-  unsigned long long n = 0;
-  if (c == nc) {
-    for (uint64_t i = threadIdx.x; i < nv; i += 256) a += w[i];
-  } else {
-    const uint8_t *fa = flags + c * 2 * nv, *fb = fa + nv;
-    for (uint64_t i = threadIdx.x; i < nv; i += 256) {
-      if (fa[i]) e += err[c * nv + i], a += w[i], ++n;
-      if (fb[i]) a += w[i];
-    }
-  }
-  se[threadIdx.x] = e, sa[threadIdx.x] = a, sn[threadIdx.x] = n;
-  __syncthreads();
-  for (int s = 128; s; s >>= 1) {
-    if (int(threadIdx.x) < s) {
-      se[threadIdx.x] += se[threadIdx.x + s];
-      sa[threadIdx.x] += sa[threadIdx.x + s];
-      sn[threadIdx.x] += sn[threadIdx.x + s];
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    if (c == nc) {
-      *total = sa[0];
-    } else {
-      error[c] = se[0], area[c] = sa[0], count[c] = sn[0];
-    }
-  }
-}
-
 // patches[set] += 1 for every component root of the set.
 __global__ void count_roots(int32_t *parent_all, uint64_t nv, uint64_t sets, unsigned *patches) {
   uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -647,6 +775,7 @@ Lbvh lbvh_build(Call &call, const double *xyz, uint64_t nv, const int32_t *faces
     lo[a] = *mm.first, hi[a] = *mm.second;
   }
   float ext = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-30f});
+  for (int a = 0; a < 3; ++a) b.scale = std::max({b.scale, std::fabs(lo[a]), std::fabs(hi[a])});
   uint64_t *keys = call.alloc<uint64_t>(nf), *skeys = call.alloc<uint64_t>(nf);
   int32_t *ids = call.alloc<int32_t>(nf), *sids = call.alloc<int32_t>(nf);
   lbvh_keys<<<blocks_for(nf), kThreads, 0, st>>>(b.xyz, nv, faces, nf, make_float3(lo[0], lo[1], lo[2]),
@@ -681,7 +810,7 @@ namespace {
 // then the motion that fits them best), on the device; dm is updated in
 // place.  `origin` (a point near the mesh) keeps the sums well conditioned.
 void refine_motions(Call &call, const BvhView &view, const double *xyz, const double *vn,
-                    const double *w, Motion32 *dm, uint64_t nc, double tau, int refine,
+                    const double *w, ClusterMotion *dm, uint64_t nc, double tau, int refine,
                     const double origin[3]) {
   const uint64_t nv = view.nv;
   if (refine <= 0 || !nc || !nv || !view.nf) return;
@@ -702,16 +831,7 @@ void refine_motions(Call &call, const BvhView &view, const double *xyz, const do
   }
 }
 
-Motion32 motion_of(const sym_cluster_record &r) {
-  Motion32 m{};
-  for (int k = 0; k < 9; ++k) m.r[k] = r.rotation[k];
-  for (int k = 0; k < 3; ++k) m.t[k] = r.translation[k], m.n[k] = r.plane_normal[k];
-  m.offset = r.plane_offset;
-  m.reflection = r.reflection != 0;
-  return m;
-}
-
-void store_motion(const Motion32 &m, sym_cluster_record &r) {
+void store_motion(const ClusterMotion &m, sym_cluster_record &r) {
   for (int k = 0; k < 9; ++k) r.rotation[k] = m.r[k];
   for (int k = 0; k < 3; ++k) r.translation[k] = m.t[k], r.plane_normal[k] = m.n[k];
   r.plane_offset = m.offset;
@@ -719,56 +839,103 @@ void store_motion(const Motion32 &m, sym_cluster_record &r) {
 
 }  // namespace
 
-// Coverage, rms and patch counts of the nc modes (the throughput path),
-// after `refine` FP64 refinement passes of their motions (written back to
-// records).
-void verification_fast(Call &call, const Lbvh &bvh, const double *xyz, const double *vn,
-                       const double *w, const uint64_t *nbr_off, const int32_t *nbr,
-                       sym_cluster_record *records, uint64_t nc, double tau, int refine,
-                       const double origin[3], double *coverage, double *rms,
-                       uint32_t *patches) {
-  const uint64_t nv = bvh.nv;
+// The reference-order BVH of a resident mesh, built on the host from the
+// device's vertices and faces when the first undecided query needs it.
+void ensure_ref_bvh(Call &call, const ResidentSurface &m) {
+  if (m.ref->block) return;
+  std::vector<double> x(3 * m.nv);
+  std::vector<int32_t> f(3 * m.nf);
+  call.d2h(x.data(), m.xyz, 24 * m.nv);
+  call.d2h(f.data(), m.faces, 12 * m.nf);
+  call.sync();
+  const sym_mesh_view mv{{x.data(), x.data() + m.nv, x.data() + 2 * m.nv, m.nv},
+                         {f.data(), f.data() + m.nf, f.data() + 2 * m.nf, m.nf}};
+  const HostBvh bvh(mv);
+  if (2 * bvh.depth + 4 > kRefStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
+  *m.ref = ref_bvh_upload(bvh, call.stream());
+}
+
+uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *dm, uint64_t nc,
+                     double tau, uint8_t *flags, double *err) {
+  const uint64_t nv = m.nv, rows = nc * 2 * nv;
+  cudaStream_t st = call.stream();
+  if (!rows) return 0;
+  if (rows >= (uint64_t(1) << 32)) fail(SYM_INVALID_ARGUMENT, "verification: too many queries");
+  if (!m.nf) {
+    SYM_CUDA(cudaMemsetAsync(flags, 0, rows, st));
+    SYM_CUDA(cudaMemsetAsync(err, 0, nc * nv * 8, st));
+    return 0;
+  }
+  const Lbvh &bvh = *m.lbvh;
+  uint32_t *undecided = call.alloc<uint32_t>(rows);
+  unsigned long long *count = call.alloc<unsigned long long>(1);
+  SYM_CUDA(cudaMemsetAsync(count, 0, 8, st));
+  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
+  Surface s{m.xyz, nv, m.faces, m.nf, nullptr, nullptr};
+  verify_vertices_hybrid<<<blocks_for(rows), kThreads, 0, st>>>(view, s, m.vn, dm, nc, tau,
+                                                                bvh.scale, flags, err, undecided,
+                                                                count, call.status());
+  check_launch();
+  call.launched();
+  unsigned long long n = 0;
+  call.d2h(&n, count, 8);
+  call.sync();
+  if (n) {
+    ensure_ref_bvh(call, m);
+    s.nodes = m.ref->nodes, s.ids = m.ref->ids;
+    const double limit = std::nextafter(tau * tau, std::numeric_limits<double>::infinity());
+    verify_listed_ref<<<blocks_for(n), kThreads, 0, st>>>(s, m.vn, dm, tau, limit, undecided, n,
+                                                           flags, err, call.status());
+    check_launch();
+    call.launched();
+  }
+  return n;
+}
+
+// Coverage, rms and patch counts of the nc modes (sym_detect_fast), after
+// `refine` FP64 refinement passes of their motions (written back to
+// records); the same coverage, rms and patches as the reference's
+// verification of the records.
+void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record *records,
+                       uint64_t nc, double tau, int refine, const double origin[3],
+                       double *coverage, double *rms, uint32_t *patches, uint64_t *undecided) {
+  const uint64_t nv = m.nv;
+  if (undecided) *undecided = 0;
   if (!nc || !nv) {
     for (uint64_t c = 0; c < nc; ++c) coverage[c] = rms[c] = 0, patches[2 * c] = patches[2 * c + 1] = 0;
     return;
   }
   cudaStream_t st = call.stream();
-  std::vector<Motion32> motions(nc);
-  for (uint64_t c = 0; c < nc; ++c) motions[c] = motion_of(records[c]);
-  Motion32 *dm = call.upload(motions.data(), nc);
-  BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
-  if (refine > 0) {
-    refine_motions(call, view, xyz, vn, w, dm, nc, tau, refine, origin);
-    call.d2h(motions.data(), dm, nc * sizeof(Motion32));
+  std::vector<ClusterMotion> motions(nc);
+  for (uint64_t c = 0; c < nc; ++c) motions[c] = cluster_motion(records[c]);
+  ClusterMotion *dm = call.upload(motions.data(), nc);
+  if (refine > 0 && m.nf) {
+    const Lbvh &bvh = *m.lbvh;
+    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
+    refine_motions(call, view, m.xyz, m.vn, m.w, dm, nc, tau, refine, origin);
+    call.d2h(motions.data(), dm, nc * sizeof(ClusterMotion));
     call.check_status("transform refinement");
     for (uint64_t c = 0; c < nc; ++c) store_motion(motions[c], records[c]);
   }
   const uint64_t rows = nc * 2 * nv;
   uint8_t *flags = call.alloc<uint8_t>(rows);
   double *err = call.alloc<double>(nc * nv);
-  if (bvh.nf) {
-    verify_vertices_fast<<<blocks_for(rows), kThreads, 0, st>>>(view, xyz, vn, dm, nc, tau,
-                                                                float(tau * tau), flags, err,
-                                                                call.status());
-  } else {
-    SYM_CUDA(cudaMemsetAsync(flags, 0, rows, st));
-    SYM_CUDA(cudaMemsetAsync(err, 0, nc * nv * 8, st));
-  }
-  check_launch();
+  const uint64_t n = exact_flags(call, m, dm, nc, tau, flags, err);
+  if (undecided) *undecided = n;
   double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
   uint64_t *na = call.alloc<uint64_t>(nc);
-  block_sums<<<unsigned(nc + 1), 256, 0, st>>>(flags, err, w, nv, nc, error, area, na, total);
-  check_launch();
+  ordered_verification_sums(call, flags, err, m.w, nv, nc, error, area, na, total);
   int32_t *parent = call.alloc<int32_t>(rows);
   unsigned *dpatch = call.alloc<unsigned>(2 * nc);
   SYM_CUDA(cudaMemsetAsync(dpatch, 0, 8 * nc, st));
   init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
   check_launch();
-  unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(nbr_off, nbr, nv, 2 * nc, parent, call.status());
+  unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(m.nbr_off, m.nbr, nv, 2 * nc, parent,
+                                                      call.status());
   check_launch();
   count_roots<<<blocks_for(rows), kThreads, 0, st>>>(parent, nv, 2 * nc, dpatch);
   check_launch();
-  call.launched(6);
+  call.launched(3);
   std::vector<double> herr(nc), harea(nc);
   std::vector<uint64_t> hna(nc);
   std::vector<unsigned> hp(2 * nc);
@@ -784,6 +951,30 @@ void verification_fast(Call &call, const Lbvh &bvh, const double *xyz, const dou
     coverage[c] = htotal > 0 ? std::min(1.0, harea[c] / htotal) : 0;
     patches[2 * c] = hp[2 * c], patches[2 * c + 1] = hp[2 * c + 1];
   }
+}
+
+// The reference's verification of `records` on a resident mesh: side
+// lists, patches, coverage and rms identical to verification_core's.
+void verification_resident(Call &call, const ResidentSurface &m, const sym_cluster_record *records,
+                           uint64_t nc, double tau, std::vector<std::vector<int32_t>> &side,
+                           std::vector<std::vector<std::vector<int32_t>>> &patches,
+                           std::vector<double> &coverage, std::vector<double> &rms,
+                           uint64_t *undecided) {
+  const uint64_t nv = m.nv;
+  if (undecided) *undecided = 0;
+  if (!nc) {
+    finish_verification(call, nullptr, nullptr, m.w, m.nbr_off, m.nbr, nv, 0, side, patches,
+                        coverage, rms);
+    return;
+  }
+  std::vector<ClusterMotion> motions(nc);
+  for (uint64_t c = 0; c < nc; ++c) motions[c] = cluster_motion(records[c]);
+  ClusterMotion *dm = call.upload(motions.data(), nc);
+  uint8_t *flags = call.alloc<uint8_t>(nc * 2 * nv);
+  double *err = call.alloc<double>(nc * nv);
+  const uint64_t n = exact_flags(call, m, dm, nc, tau, flags, err);
+  if (undecided) *undecided = n;
+  finish_verification(call, flags, err, m.w, m.nbr_off, m.nbr, nv, nc, side, patches, coverage, rms);
 }
 
 }  // namespace sym
