@@ -414,7 +414,8 @@ def run_gpu(args):
                           "polish_iterations": r["polish_iterations"], "bulk_ms": r["bulk_ms"],
                           "polish_ms": r["polish_ms"], "evaluations": r["mean_shift_pairs"],
                           "seed_iterations": r["seed_iterations"], "launches": r["launches"],
-                          "verify_undecided": r["verify_undecided"], "coverage": r["coverage"],
+                          "verify_undecided": r["verify_undecided"],
+                          "verify_fp64_rows": r["verify_fp64_rows"], "coverage": r["coverage"],
                           "bulk_trace": list(r["bulk_trace"]),
                           "polish_trace": list(r["polish_trace"])}))
         return

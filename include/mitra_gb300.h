@@ -385,6 +385,9 @@ typedef struct sym_fast_result {
    * to the reference-order BVH (an exact FP64 distance tie between faces
    * that disagree on the normal test, or too many candidate faces) */
   uint64_t verify_undecided;
+  /* verification queries decided in FP64 because an FP32 test fell within
+   * its error band (out of 2 x clusters x vertices) */
+  uint64_t verify_fp64_rows;
 } sym_fast_result;
 void sym_fast_options_default(sym_fast_options *out);
 /* `sample` is a host array of vertex ids (the area-weighted sample). */

@@ -176,7 +176,8 @@ class FastResult(C.Structure):
                 ("patches", C.c_uint32 * (2 * FAST_MAX_CLUSTERS)),
                 ("precise", C.c_uint8 * FAST_MAX_CLUSTERS),
                 ("tc_launches", C.c_uint64), ("tc_kernel_ms", C.c_double),
-                ("tc_evaluations", C.c_double), ("verify_undecided", C.c_uint64)]
+                ("tc_evaluations", C.c_double), ("verify_undecided", C.c_uint64),
+                ("verify_fp64_rows", C.c_uint64)]
 
 
 class PreparedOut(C.Structure):

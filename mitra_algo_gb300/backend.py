@@ -365,6 +365,7 @@ class Gb300Backend:
         out["tc_kernel_ms"] = float(res.tc_kernel_ms)
         out["tc_evaluations"] = float(res.tc_evaluations)
         out["verify_undecided"] = int(res.verify_undecided)
+        out["verify_fp64_rows"] = int(res.verify_fp64_rows)
         out["rotation"] = [list(res.records[i].rotation) for i in range(n)]
         out["translation"] = [list(res.records[i].translation) for i in range(n)]
         out["reflection"] = [bool(res.records[i].reflection) for i in range(n)]

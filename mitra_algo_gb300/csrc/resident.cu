@@ -65,13 +65,15 @@ struct sym_mesh_handle {
   uint64_t *nbr_off = nullptr;
   sym_edge *edges = nullptr;
   sym::Lbvh lbvh;  // FP32 linear BVH of the faces (verification of the fast path)
-  sym::RefBvh ref;  // the reference-order BVH, built when a verification first needs it
+  // the reference-order BVH (verification ties), built on a host thread
+  // from the load on
+  sym::RefBvhSource ref;
   sym::ResidentSurface surface() {
     return {&lbvh, xyz, vn, w, faces, nbr_off, nbr, nv, nf, &ref};
   }
   void release() {  // the device memory (after the context's stream is idle)
     sym::lbvh_free(lbvh);
-    sym::ref_bvh_free(ref);
+    ref.release();
     if (block) cudaFree(block);
     block = nullptr;
   }
@@ -743,7 +745,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   if (fo.verify && nc) {
     verification_fast(call, h.surface(), r.records, nc, o.verify_threshold * h.model.box_size,
                       fo.refine, h.model.center, r.coverage, r.rms, r.patches,
-                      &r.verify_undecided);
+                      &r.verify_undecided, &r.verify_fp64_rows);
   }
   clock.mark(9);
   call.sync();
@@ -818,7 +820,7 @@ sym_status sym_refine_transforms(sym_context *ctx, sym_mesh_handle *mesh,
     if (iterations < 0) sym::fail(SYM_INVALID_ARGUMENT, "negative refinement iterations");
     sym::verification_fast(call, mesh->surface(), records, count,
                            options->verify_threshold * mesh->model.box_size, iterations,
-                           mesh->model.center, coverage, rms, patches, nullptr);
+                           mesh->model.center, coverage, rms, patches, nullptr, nullptr);
     return SYM_OK;
   } catch (const sym::Error &e) {
     sym_error_text = e.what();
@@ -919,8 +921,17 @@ sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_
     try {
       if (nf >= (uint64_t(1) << 30)) sym::fail(SYM_INVALID_ARGUMENT, "too many faces for the LBVH");
       sym::Call call(ctx, "mesh_load");
-      h->lbvh = sym::lbvh_build(call, h->xyz, nv, h->faces, nf);
+      h->lbvh = sym::lbvh_build(call, h->xyz, h->vn, nv, h->faces, nf);
       call.check_status("mesh_load");
+      std::vector<double> hx(3 * nv);
+      std::vector<int32_t> hf(3 * nf);
+      std::copy(mesh->vertices.x, mesh->vertices.x + nv, hx.begin());
+      std::copy(mesh->vertices.y, mesh->vertices.y + nv, hx.begin() + nv);
+      std::copy(mesh->vertices.z, mesh->vertices.z + nv, hx.begin() + 2 * nv);
+      std::copy(mesh->faces.v0, mesh->faces.v0 + nf, hf.begin());
+      std::copy(mesh->faces.v1, mesh->faces.v1 + nf, hf.begin() + nf);
+      std::copy(mesh->faces.v2, mesh->faces.v2 + nf, hf.begin() + 2 * nf);
+      h->ref.start(std::move(hx), std::move(hf), nv, nf);
     } catch (...) {
       h->release();
       delete h;
@@ -979,8 +990,17 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
     d2d(h->nbr, p.nbr, 4 * h->nbr_count);
     d2d(h->edges, p.edges, 24 * ne);
     if (nf >= (uint64_t(1) << 30)) sym::fail(SYM_INVALID_ARGUMENT, "too many faces for the LBVH");
-    h->lbvh = sym::lbvh_build(call, h->xyz, nv, h->faces, nf);
+    h->lbvh = sym::lbvh_build(call, h->xyz, h->vn, nv, h->faces, nf);
     call.check_status("mesh_load_raw");
+    {  // the prepared vertices and faces to the host thread that builds the
+       // reference-order BVH while the GPU works
+      std::vector<double> hx(3 * nv);
+      std::vector<int32_t> hf(3 * nf);
+      call.d2h(hx.data(), h->xyz, 24 * nv);
+      call.d2h(hf.data(), h->faces, 12 * nf);
+      call.sync();
+      h->ref.start(std::move(hx), std::move(hf), nv, nf);
+    }
     *out = h;
     return SYM_OK;
   } catch (const sym::Error &e) {

@@ -72,20 +72,55 @@ HostBvh::HostBvh(const sym_mesh_view &m) {
     }
   } builder{*this, coord};
   if (!ids.empty()) builder.build(0, int(ids.size()), 0);
+  if (depth > 31) throw Error(SYM_RUNTIME_ERROR, "verification: BVH too deep");
+  path.assign(nodes.size(), 0);
+  leaf_slot.assign(nodes.size(), -1);
+  face_leaf.assign(ids.size(), -1);
+  face_pos.assign(ids.size(), -1);
+  std::vector<int32_t> node_depth(nodes.size(), 0), parent(nodes.size(), -1);
+  int32_t leaves = 0;
+  for (size_t n = 0; n < nodes.size(); ++n) {  // parents precede their children
+    const BvhNode &b = nodes[n];
+    if (b.left >= 0) {
+      const int d = node_depth[n];
+      parent[b.left] = parent[b.right] = int32_t(n);
+      node_depth[b.left] = node_depth[b.right] = d + 1;
+      path[b.left] = path[n];
+      path[b.right] = path[n] | (1u << (31 - d));
+    } else {
+      leaf_slot[n] = leaves++;
+      for (int32_t i = b.begin; i < b.end; ++i) face_leaf[ids[i]] = int32_t(n), face_pos[ids[i]] = i;
+    }
+  }
+  ancestors.assign(size_t(leaves) * 32, -1);
+  for (size_t n = 0; n < nodes.size(); ++n)
+    if (leaf_slot[n] >= 0)
+      for (int32_t a = int32_t(n); a >= 0; a = parent[a])
+        ancestors[size_t(leaf_slot[n]) * 32 + node_depth[a]] = a;
 }
 
 RefBvh ref_bvh_upload(const HostBvh &bvh, cudaStream_t stream) {
   RefBvh b;
   b.depth = bvh.depth;
-  const size_t node_bytes = (bvh.nodes.size() * sizeof(BvhNode) + 255) & ~size_t(255);
-  const size_t id_bytes = bvh.ids.size() * sizeof(int32_t);
-  SYM_CUDA(cudaMalloc(&b.block, node_bytes + id_bytes + 256));
-  b.nodes = reinterpret_cast<const BvhNode *>(b.block);
-  b.ids = reinterpret_cast<const int32_t *>(b.block + node_bytes);
-  SYM_CUDA(cudaMemcpyAsync(b.block, bvh.nodes.data(), bvh.nodes.size() * sizeof(BvhNode),
-                           cudaMemcpyHostToDevice, stream));
-  SYM_CUDA(cudaMemcpyAsync(b.block + node_bytes, bvh.ids.data(), id_bytes, cudaMemcpyHostToDevice,
-                           stream));
+  auto pad = [](size_t x) { return (x + 255) & ~size_t(255); };
+  const size_t nn = bvh.nodes.size(), nf = bvh.ids.size(), na = bvh.ancestors.size();
+  const size_t s_nodes = pad(nn * sizeof(BvhNode)), s_face = pad(nf * 4), s_node = pad(nn * 4),
+               s_anc = pad(na * 4);
+  SYM_CUDA(cudaMalloc(&b.block, s_nodes + 3 * s_face + 2 * s_node + s_anc + 256));
+  char *at = b.block;
+  auto put = [&](const void *src, size_t bytes, size_t room) {
+    if (bytes) SYM_CUDA(cudaMemcpyAsync(at, src, bytes, cudaMemcpyHostToDevice, stream));
+    char *here = at;
+    at += room;
+    return here;
+  };
+  b.nodes = reinterpret_cast<const BvhNode *>(put(bvh.nodes.data(), nn * sizeof(BvhNode), s_nodes));
+  b.ids = reinterpret_cast<const int32_t *>(put(bvh.ids.data(), nf * 4, s_face));
+  b.face_leaf = reinterpret_cast<const int32_t *>(put(bvh.face_leaf.data(), nf * 4, s_face));
+  b.face_pos = reinterpret_cast<const int32_t *>(put(bvh.face_pos.data(), nf * 4, s_face));
+  b.path = reinterpret_cast<const uint32_t *>(put(bvh.path.data(), nn * 4, s_node));
+  b.leaf_slot = reinterpret_cast<const int32_t *>(put(bvh.leaf_slot.data(), nn * 4, s_node));
+  b.ancestors = reinterpret_cast<const int32_t *>(put(bvh.ancestors.data(), na * 4, s_anc));
   SYM_CUDA(cudaStreamSynchronize(stream));
   return b;
 }
@@ -93,6 +128,20 @@ RefBvh ref_bvh_upload(const HostBvh &bvh, cudaStream_t stream) {
 void ref_bvh_free(RefBvh &b) {
   if (b.block) cudaFree(b.block);
   b = RefBvh{};
+}
+
+void RefBvhSource::start(std::vector<double> xyz, std::vector<int32_t> faces, uint64_t nv,
+                         uint64_t nf) {
+  pending = std::async(std::launch::async, [x = std::move(xyz), f = std::move(faces), nv, nf]() {
+    const sym_mesh_view mv{{x.data(), x.data() + nv, x.data() + 2 * nv, nv},
+                           {f.data(), f.data() + nf, f.data() + 2 * nf, nf}};
+    return std::make_unique<HostBvh>(mv);
+  });
+}
+
+void RefBvhSource::release() {
+  if (pending.valid()) pending.wait();
+  ref_bvh_free(dev);
 }
 
 namespace {

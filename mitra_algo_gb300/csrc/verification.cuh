@@ -7,6 +7,8 @@
 #pragma once
 #include "common.cuh"
 
+#include <future>
+#include <memory>
 #include <vector>
 
 namespace sym {
@@ -68,6 +70,15 @@ struct BvhNode {
   int32_t left, right, begin, end;
 };
 
+__device__ inline double box_d2(D3 p, const BvhNode &n) {
+  double s = 0, a[3] = {p.x, p.y, p.z};
+  for (int k = 0; k < 3; ++k) {
+    double d = fmax(fmax(n.lo[k] - a[k], 0.0), a[k] - n.hi[k]);
+    s += d * d;
+  }
+  return s;
+}
+
 // Host build in the reference's construction order (surface.h:16-50:
 // median split by std::nth_element on the longest axis, leaves of <= 8
 // faces), so that a near-first strict-< traversal visits faces in the
@@ -75,6 +86,12 @@ struct BvhNode {
 struct HostBvh {
   std::vector<BvhNode> nodes;
   std::vector<int32_t> ids;
+  // the visiting order's bookkeeping: each node's path from the root (bit
+  // 31 - k = 1 when the step from depth k went to the right child), each
+  // face's leaf and position in `ids`, and each leaf's ancestors by depth
+  // (32 slots per leaf, leaf_slot[node] = the leaf's row, -1 inside)
+  std::vector<uint32_t> path;
+  std::vector<int32_t> leaf_slot, ancestors, face_leaf, face_pos;
   int depth = 0;
   explicit HostBvh(const sym_mesh_view &m);
 };
@@ -83,11 +100,32 @@ struct HostBvh {
 struct RefBvh {
   const BvhNode *nodes = nullptr;
   const int32_t *ids = nullptr;
+  const uint32_t *path = nullptr;
+  const int32_t *leaf_slot = nullptr, *ancestors = nullptr, *face_leaf = nullptr,
+                *face_pos = nullptr;
   char *block = nullptr;
   int depth = 0;
 };
 RefBvh ref_bvh_upload(const HostBvh &bvh, cudaStream_t stream);
 void ref_bvh_free(RefBvh &b);
+
+// Of two faces at exactly the same FP64 distance from q, the one the
+// reference's search (surface.h:52-83) visits first: the lower position in
+// a shared leaf, else the face under the child of their lowest common
+// ancestor that the near-first rule searches first (the left child unless
+// its box is strictly farther).  The search reaches both faces, since no
+// node holding a face at the minimum distance is farther than it.
+__device__ inline int32_t first_in_reference_order(const RefBvh &t, D3 q, int32_t a, int32_t b) {
+  if (a == b) return a;
+  const int32_t la = t.face_leaf[a], lb = t.face_leaf[b];
+  if (la == lb) return t.face_pos[a] < t.face_pos[b] ? a : b;
+  const uint32_t pa = t.path[la], pb = t.path[lb];
+  const int depth = __clz(pa ^ pb);  // depth of the lowest common ancestor
+  const BvhNode &lca = t.nodes[t.ancestors[t.leaf_slot[la] * 32 + depth]];
+  const bool right_first = box_d2(q, t.nodes[lca.left]) > box_d2(q, t.nodes[lca.right]);
+  const bool a_right = (pa >> (31 - depth)) & 1u;
+  return a_right == right_first ? a : b;
+}
 
 constexpr int kRefStack = 96;
 
@@ -99,15 +137,6 @@ struct Surface {
   const BvhNode *nodes;
   const int32_t *ids;
 };
-
-__device__ inline double box_d2(D3 p, const BvhNode &n) {
-  double s = 0, a[3] = {p.x, p.y, p.z};
-  for (int k = 0; k < 3; ++k) {
-    double d = fmax(fmax(n.lo[k] - a[k], 0.0), a[k] - n.hi[k]);
-    s += d * d;
-  }
-  return s;
-}
 
 __device__ inline D3 vertex(const Surface &s, int32_t v) {
   return {s.xyz[v], s.xyz[s.nv + v], s.xyz[2 * s.nv + v]};
@@ -269,8 +298,20 @@ struct Lbvh {
   float *xyz = nullptr;            // 3 x nv, FP32 copy of the vertices
   int32_t *child = nullptr;        // (nf - 1) x 2: >= 0 internal node, < 0 leaf ~face
   float *box = nullptr;            // (nf - 1) x 12: the two children's lo[3], hi[3]
+  float *vn = nullptr;             // 3 x nv, FP32 copy of the vertex normals
   char *block = nullptr;           // owns every array above (cudaMalloc)
   float scale = 0;                 // largest vertex coordinate magnitude
+};
+
+// The reference-order BVH of a resident mesh: built on a host thread from
+// the moment the mesh is loaded (`pending`), uploaded when a verification
+// first needs it (`dev`).
+struct RefBvhSource {
+  RefBvh dev;
+  std::future<std::unique_ptr<HostBvh>> pending;
+  // starts the host build from copies of the mesh's vertices and faces
+  void start(std::vector<double> xyz, std::vector<int32_t> faces, uint64_t nv, uint64_t nf);
+  void release();  // waits for a pending build, frees the device copy
 };
 
 // A resident mesh as the throughput verification sees it (device arrays).
@@ -281,21 +322,27 @@ struct ResidentSurface {
   const uint64_t *nbr_off;     // nv + 1
   const int32_t *nbr;
   uint64_t nv, nf;
-  RefBvh *ref;  // the reference-order BVH, built on first need (owned by the mesh)
+  RefBvhSource *ref;  // the reference-order BVH (owned by the mesh)
 };
 
-// Flags and forward errors of nc motions (device array dm) with the
-// reference's decisions: FP32 LBVH candidates, FP64 rechecks, and the
-// reference-order BVH for the queries those leave undecided (their number
-// is returned).
-uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *dm, uint64_t nc,
-                     double tau, uint8_t *flags, double *err);
+// Flags and forward errors of nc motions (`records`, and dm: the same on the
+// device) with the reference's decisions: FP32 decisions outside the error
+// bands of their tests, FP64 rechecks of the rows inside (their number in
+// *fp64_rows), and the reference-order BVH for the queries those leave
+// undecided (their number is returned).
+uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *dm,
+                     const sym_cluster_record *records, uint64_t nc, double tau, uint8_t *flags,
+                     double *err, uint64_t *fp64_rows);
 
 // Coverage, rms and patch counts (forward, inverse) of nc motions after
 // `refine` FP64 refinement passes (the refined motions are written back).
+// Supporting vertices and patches are the reference's; coverage and rms
+// come from fixed-order tree sums, within a few units of rounding of the
+// reference's serial sums.
 void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record *records,
                        uint64_t nc, double tau, int refine, const double origin[3],
-                       double *coverage, double *rms, uint32_t *patches, uint64_t *undecided);
+                       double *coverage, double *rms, uint32_t *patches, uint64_t *undecided,
+                       uint64_t *fp64_rows);
 
 // The reference's full verification of nc records on a resident mesh.
 void verification_resident(Call &call, const ResidentSurface &m, const sym_cluster_record *records,
@@ -305,7 +352,8 @@ void verification_resident(Call &call, const ResidentSurface &m, const sym_clust
                            uint64_t *undecided);
 
 // Builds the LBVH on the device (synchronises); release with lbvh_free.
-Lbvh lbvh_build(Call &call, const double *xyz, uint64_t nv, const int32_t *faces, uint64_t nf);
+Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
+                const int32_t *faces, uint64_t nf);
 void lbvh_free(Lbvh &b);
 
 }  // namespace sym

@@ -311,16 +311,21 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
 }
 
 // ------------------------------------------- exact decisions, FP32 search
-// Margin of the FP32 search, in distance units: kMargin times the largest
-// coordinate magnitude of the query and the mesh.  The FP32 distance of a
-// face whose smallest corner-pair angle has sin^2 >= kWellShaped differs from
-// its FP64 distance by a few tens of FP32 units of that magnitude at most
-// (inputs rounded to FP32, region tests whose conditioning is that angle's
-// 1/sin^2), far below the margin; other faces enter the candidates by the
-// distance of their box instead of their FP32 distance.
-constexpr float kMargin = 1.0f / 16384.0f;
+// Error bound of the FP32 search, in distance units: kErr (512 FP32 units)
+// times the largest coordinate magnitude of the vertex, its image and the
+// mesh.  The FP32 distance of a face whose smallest corner-pair angle has
+// sin^2 >= kWellShaped differs from the FP64 distance of the FP64 image by
+// about 5 units for the rounding of the inputs and the image (the distance
+// is 1-Lipschitz in both) plus about 100 units times (edge length /
+// magnitude) for the region tests, whose conditioning is that angle's
+// 1 / sin^2 -- well below kErr; other faces enter the candidates by the
+// distance of their box and leave the decision to FP64.  The same bound
+// serves as the band of the FP32 threshold tests (2 tau, the plane side,
+// tau), and kNormalBand (on the cosine) as that of the normal test.
+constexpr float kErr = 1.0f / 32768.0f;
 constexpr float kWellShaped = 0.05f;
-constexpr int kCandidates = 8;
+constexpr float kNormalBand = 1.0f / 1024.0f;
+constexpr int kCandidates = 16;
 
 // sin^2 of the smallest angle of triangle abc: |ab x ac|^2 over the product
 // of the two longest squared edges.
@@ -333,29 +338,37 @@ __device__ __forceinline__ float shape_quality(F3 a, F3 b, F3 c) {
   return prod > 0.f ? dotf(n, n) / prod : 0.f;
 }
 
-// Faces whose FP64 distance to p can be the smallest: every face whose FP32
-// distance (or, for a badly shaped face, box distance) is within 3 margins
-// of min(best FP32 distance, tau + margin).  Returns the count (kCandidates
-// + 1 on overflow); `best` receives the smallest FP32 distance of a
-// well-shaped face (INFINITY when none lies within tau + 4 margins).
-__device__ int candidate_faces(const BvhView &b, F3 p, float tau_margin, float margin,
-                               int32_t *faces, float *keys, float &best, int *status) {
+// Faces whose FP64 distance to the image can be the smallest: every face
+// whose FP32 distance (or, for a badly shaped face, box distance) is within
+// 2 error bounds of min(best FP32 distance, tau + bound) -- the face of
+// smallest FP64 distance is at most 2 bounds farther in FP32 than the best
+// FP32 face.  Nodes are pruned with a slightly larger radius, for the
+// rounding of their boxes' distances.  Badly shaped faces are listed as
+// ~face.  Returns the count (kCandidates + 1 on overflow); `best` receives
+// the smallest FP32 squared distance of a well-shaped face (INFINITY when
+// none lies within tau + 3 bounds).
+__device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err, int32_t *faces,
+                               float *keys, float &best, int *status) {
   best = INFINITY;
-  float lim = (tau_margin + 3.f * margin) * (tau_margin + 3.f * margin);
+  float radius = tau_err + 2.f * err;
+  float lim = radius * radius, lim_box = (radius + err * 0.03125f) * (radius + err * 0.03125f);
   int n = 0;
   bool overflow = false;
   auto consider = [&](int32_t f, float box) {
     const F3 a = vtx(b, b.faces[f]), bb = vtx(b, b.faces[b.nf + f]), cc = vtx(b, b.faces[2 * b.nf + f]);
     float key;
+    int32_t id = f;
     if (shape_quality(a, bb, cc) >= kWellShaped) {
       key = triangle_d2f(p, a, bb, cc);
       if (key < best) {
         best = key;
-        const float r = fminf(tau_margin, sqrtf(best)) + 3.f * margin;
-        lim = r * r;
+        radius = fminf(tau_err, sqrtf(best)) + 2.f * err;
+        lim = radius * radius;
+        lim_box = (radius + err * 0.03125f) * (radius + err * 0.03125f);
       }
     } else {
       key = box;
+      id = ~f;
     }
     if (key > lim) return;
     if (n == kCandidates) {  // drop entries beyond the current limit
@@ -368,7 +381,7 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_margin, float m
       overflow = true;
       return;
     }
-    faces[n] = f, keys[n++] = key;
+    faces[n] = id, keys[n++] = key;
   };
   if (b.nf == 1) {
     consider(0, 0.f);
@@ -379,14 +392,14 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_margin, float m
     stack[top] = 0, dist[top++] = 0.f;
     while (top) {
       --top;
-      if (dist[top] > lim) continue;
+      if (dist[top] > lim_box) continue;
       const int32_t node = stack[top];
       const float *bx = b.box + int64_t(node) * 12;
       const int32_t c0 = b.child[2 * node], c1 = b.child[2 * node + 1];
       const float d0 = box_d2f(p, bx), d1 = box_d2f(p, bx + 6);
-      if (c0 < 0 && d0 <= lim) consider(~c0, d0);
-      if (c1 < 0 && d1 <= lim) consider(~c1, d1);
-      const bool p0 = c0 >= 0 && d0 <= lim, p1 = c1 >= 0 && d1 <= lim;
+      if (c0 < 0 && d0 <= lim_box) consider(~c0, d0);
+      if (c1 < 0 && d1 <= lim_box) consider(~c1, d1);
+      const bool p0 = c0 >= 0 && d0 <= lim_box, p1 = c1 >= 0 && d1 <= lim_box;
       if (top + 2 > kStackFast) {
         atomicExch(status, DS_CAPACITY);
         return kCandidates + 1;
@@ -409,88 +422,269 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_margin, float m
   return m;
 }
 
-// One query of the reference's verification, decided with the FP32
-// candidates and FP64 rechecks.  Returns 1 (supports; `d2` = the reference's
-// FP64 squared distance), 0 (does not), or 2 (undecided here: an FP64 tie
-// between faces that disagree on the normal test, or too many candidates).
-__device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn,
-                            const ClusterMotion &m, bool inverse, uint64_t i, double tau,
-                            float scale, double &d2, int *status) {
-  const M3 r = query_rotation(m, inverse);
-  const D3 p = vertex(s, int32_t(i));
-  D3 q;
-  if (query_skipped(m, r, inverse, p, tau, q)) return 0;
-  const F3 qf{float(q.x), float(q.y), float(q.z)};
-  const float mag = fmaxf(scale, fmaxf(fabsf(qf.x), fmaxf(fabsf(qf.y), fabsf(qf.z))));
-  const float margin = kMargin * mag;
-  int32_t faces[kCandidates];
-  float keys[kCandidates];
-  float best;
-  const int n = candidate_faces(b, qf, float(tau) + margin, margin, faces, keys, best, status);
-  if (n > kCandidates) return 2;
-  // the FP64 distances of the candidates: their minimum is the reference's
-  double dmin = INFINITY;
-  double dist[kCandidates];
-  for (int j = 0; j < n; ++j) {
-    dist[j] = triangle_d2(q, corner(s, faces[j], 0), corner(s, faces[j], 1), corner(s, faces[j], 2));
-    dmin = fmin(dmin, dist[j]);
-  }
-  if (!(dmin <= tau * tau)) return 0;
-  // the normal test of every face at (or within a few units of rounding of)
-  // the minimum: one outcome decides, two leave the reference's tie order
-  // to decide
-  const D3 ni{vn[i], vn[s.nv + i], vn[2 * s.nv + i]};
-  const double near = dmin + dmin * 1e-14;
-  int agree = 0, disagree = 0;
-  bool exact_tie_only = true;
-  for (int j = 0; j < n; ++j) {
-    if (dist[j] > near) continue;
-    exact_tie_only = exact_tie_only && dist[j] == dmin;
-    if (normal_agrees(s, faces[j], r, ni)) ++agree;
-    else ++disagree;
-  }
-  if (agree && disagree) return 2;
-  if (!exact_tie_only && agree) return 2;  // the reference's distance is one of several
-  if (!agree) return 0;
-  d2 = dmin;
-  return 1;
-}
+// A cluster's motion in FP32 (the FP32 decisions).
+struct MotionF {
+  float r[9], t[3], n[3], offset;
+  int32_t reflection;
+};
 
-// flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction); rows
-// left undecided are listed in `undecided` (count in *undecided_count).
-__global__ void verify_vertices_hybrid(BvhView b, Surface s, const double *vn,
-                                       const ClusterMotion *motions, uint64_t nc, double tau,
-                                       float scale, uint8_t *flags, double *err,
-                                       uint32_t *undecided, unsigned long long *undecided_count,
-                                       int *status) {
+// Row lists between the verification kernels.
+struct RowLists {
+  uint32_t *forward;    // accepted forward rows whose FP64 distance is still needed
+  int32_t *faces;       // kCandidates faces per forward row (-1 padded)
+  uint32_t *fp64;       // rows decided in FP64
+  unsigned long long *counts;  // [forward, fp64, overflow, tie]
+  uint32_t *reference;  // rows left to the reference-order BVH
+  double *limits;       // their search limits
+};
+
+// Decisions in FP32 (verify_fp32).  The reference's tests are made with
+// the FP32 image of the vertex; each threshold test that falls within its
+// band of the threshold, a badly shaped face among the candidates,
+// candidates that disagree on the normal test, or a candidate overflow send
+// the row to the FP64 decisions.  An accepted forward row is listed with its
+// candidates, the faces its FP64 distance is the smallest of.
+__global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions, uint64_t nc,
+                            float tau, float scale, uint8_t *flags, double *err, RowLists lists,
+                            int *status) {
   const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t nv = b.nv;
   if (row >= nc * 2 * nv) return;
   const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
-  double d = 0;
-  const int v = hybrid_query(b, s, vn, motions[c], inverse, i, tau, scale, d, status);
-  flags[row] = v == 1;
-  if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
-  if (v == 2) undecided[atomicAdd(undecided_count, 1ull)] = uint32_t(row);
+  flags[row] = 0;
+  if (!inverse) err[c * nv + i] = 0.0;
+  const MotionF &m = motions[c];
+  float r[9];
+  for (int k = 0; k < 9; ++k) r[k] = inverse ? m.r[(k % 3) * 3 + k / 3] : m.r[k];
+  const F3 p = vtx(b, int32_t(i));
+  const F3 u = inverse ? F3{p.x - m.t[0], p.y - m.t[1], p.z - m.t[2]} : p;
+  F3 q{r[0] * u.x + r[1] * u.y + r[2] * u.z, r[3] * u.x + r[4] * u.y + r[5] * u.z,
+       r[6] * u.x + r[7] * u.y + r[8] * u.z};
+  if (!inverse) q = q + F3{m.t[0], m.t[1], m.t[2]};
+  const float mag = fmaxf(scale, fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z))));
+  const float e = kErr * fmaxf(mag, fmaxf(fabsf(m.t[0]), fmaxf(fabsf(m.t[1]), fabsf(m.t[2]))));
+  auto to_fp64 = [&]() { lists.fp64[atomicAdd(&lists.counts[1], 1ull)] = uint32_t(row); };
+  // the image moves at least 2 tau (verification.cpp:64)
+  const F3 dq = q - p;
+  const float moved = sqrtf(dotf(dq, dq));
+  if (fabsf(moved - 2.f * tau) <= 2.f * e) return to_fp64();
+  if (moved < 2.f * tau) return;
+  if (m.reflection) {  // the vertex lies on the plane's side (verification.cpp:66, :84)
+    const float side = m.n[0] * p.x + m.n[1] * p.y + m.n[2] * p.z + m.offset;
+    const float at = inverse ? tau : -tau;
+    if (fabsf(side - at) <= e) return to_fp64();
+    if (inverse ? side <= tau : side >= -tau) return;
+  }
+  int32_t faces[kCandidates];
+  float keys[kCandidates];
+  float best;
+  const int n = candidate_faces(b, q, tau + e, e, faces, keys, best, status);
+  if (n > kCandidates) return to_fp64();
+  for (int j = 0; j < n; ++j)
+    if (faces[j] < 0) return to_fp64();  // a badly shaped face
+  if (!n) return;                        // no face within tau (all farther than tau + 3e)
+  const float dbest = sqrtf(best);
+  if (dbest - e > tau) return;           // every face farther than tau
+  if (dbest + e >= tau) return to_fp64();
+  // the normal test of every candidate (verification.cpp:70-73)
+  const F3 ni{vn32[i], vn32[nv + i], vn32[2 * nv + i]};
+  const F3 rn{r[0] * ni.x + r[1] * ni.y + r[2] * ni.z, r[3] * ni.x + r[4] * ni.y + r[5] * ni.z,
+              r[6] * ni.x + r[7] * ni.y + r[8] * ni.z};
+  int agree = 0, disagree = 0;
+  for (int j = 0; j < n; ++j) {
+    const int32_t f = faces[j];
+    const F3 a = vtx(b, b.faces[f]), bb = vtx(b, b.faces[b.nf + f]), cc = vtx(b, b.faces[2 * b.nf + f]);
+    const F3 ab = bb - a, ac = cc - a;
+    const F3 fn = crossf(ab, ac);
+    const float len = sqrtf(dotf(fn, fn));
+    // the direction of the FP32 normal is off by about (rounding of the
+    // corners) x (edge lengths) / |ab x ac|: a face small against the
+    // coordinate magnitude leaves the test to FP64
+    const float drift = 4.f * 5.96e-8f * mag * (sqrtf(dotf(ab, ab)) + sqrtf(dotf(ac, ac)));
+    if (!(drift <= 0.5f * kNormalBand * len)) return to_fp64();
+    const float v = dotf(rn, fn) / len;
+    if (fabsf(v - 0.5f) <= kNormalBand) return to_fp64();
+    if (v >= 0.5f) ++agree;
+    else ++disagree;
+  }
+  if (agree && disagree) return to_fp64();
+  if (!agree) return;
+  flags[row] = 1;
+  if (!inverse) {
+    const unsigned long long k = atomicAdd(&lists.counts[0], 1ull);
+    lists.forward[k] = uint32_t(row);
+    for (int j = 0; j < kCandidates; ++j) lists.faces[k * kCandidates + j] = j < n ? faces[j] : -1;
+  }
 }
 
-// The listed rows through the reference-order BVH (exact_query).
-__global__ void verify_listed_ref(Surface s, const double *vn, const ClusterMotion *motions,
-                                  double tau, double limit, const uint32_t *rows,
-                                  unsigned long long count, uint8_t *flags, double *err,
-                                  int *status) {
+// The reference's FP64 squared distance of each listed forward row: the
+// smallest over its candidate faces (the face it keeps is among them).
+__global__ void forward_errors(Surface s, const ClusterMotion *motions, RowLists lists,
+                               unsigned long long count, double *err) {
   const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  const uint64_t row = rows[k], nv = s.nv;
+  const uint64_t row = lists.forward[k], nv = s.nv;
+  const uint64_t c = row / (2 * nv), i = row % (2 * nv);
+  const ClusterMotion &m = motions[c];
+  const M3 r = query_rotation(m, false);
+  const D3 q = mul(r, vertex(s, int32_t(i))) + D3{m.t[0], m.t[1], m.t[2]};
+  double dmin = INFINITY;
+  for (int j = 0; j < kCandidates; ++j) {
+    const int32_t f = lists.faces[k * kCandidates + j];
+    if (f < 0) break;
+    dmin = fmin(dmin, triangle_d2(q, corner(s, f, 0), corner(s, f, 1), corner(s, f, 2)));
+  }
+  err[c * nv + i] = dmin;
+}
+
+// One query of the reference's verification, decided with the FP32
+// candidates and FP64 rechecks.  Returns 1 (supports; `d2` = the reference's
+// FP64 squared distance), 0 (does not), 3 (the faces at the minimum, listed
+// in `tied`, disagree on the normal test; `d2` = the minimum) or 2 (more
+// candidates than the list holds; `d2` = the tau^2 search limit).
+//
+// The reference keeps the face of strictly smallest FP64 distance, the first
+// its BVH visits among faces at exactly that distance (surface.h:52-83).
+// The candidates hold every face that can be at the minimum, so their FP64
+// minimum is the reference's distance; the normal test of the faces at
+// exactly that minimum decides when they all give the same outcome; when
+// they do not, the reference's visiting order decides (verify_listed_ref).
+__device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn,
+                            const ClusterMotion &m, bool inverse, uint64_t i, double tau,
+                            float scale, double &d2, int32_t *tied, int *status) {
+  const M3 r = query_rotation(m, inverse);
+  const D3 p = vertex(s, int32_t(i));
+  D3 q;
+  if (query_skipped(m, r, inverse, p, tau, q)) return 0;
+  const F3 qf{float(q.x), float(q.y), float(q.z)};
+  const float mag = fmaxf(scale, fmaxf(fabsf(qf.x), fmaxf(fabsf(qf.y), fabsf(qf.z))));
+  const float e = kErr * mag;
+  int32_t faces[kCandidates];
+  float keys[kCandidates];
+  float best;
+  const int n = candidate_faces(b, qf, float(tau) + e, e, faces, keys, best, status);
+  if (n > kCandidates) {
+    d2 = nextafter(tau * tau, double(INFINITY));
+    return 2;
+  }
+  double dmin = INFINITY;
+  double dist[kCandidates];
+  for (int j = 0; j < n; ++j) {
+    faces[j] = faces[j] < 0 ? ~faces[j] : faces[j];
+    dist[j] = triangle_d2(q, corner(s, faces[j], 0), corner(s, faces[j], 1), corner(s, faces[j], 2));
+    dmin = fmin(dmin, dist[j]);
+  }
+  if (!(dmin <= tau * tau)) return 0;
+  const D3 ni{vn[i], vn[s.nv + i], vn[2 * s.nv + i]};
+  int agree = 0, disagree = 0, t = 0;
+  for (int j = 0; j < n; ++j) {
+    if (dist[j] != dmin) continue;
+    tied[t++] = faces[j];
+    if (normal_agrees(s, faces[j], r, ni)) ++agree;
+    else ++disagree;
+  }
+  d2 = dmin;
+  if (agree && disagree) {
+    for (int j = t; j < kCandidates; ++j) tied[j] = -1;
+    return 3;
+  }
+  return agree ? 1 : 0;
+}
+
+// The FP64 decisions of the rows verify_fp32 listed.  Where the faces at
+// the minimum disagree on the normal test, the first of them the reference's
+// search reaches takes the test (first_in_reference_order); rows whose
+// candidates overflow the list are listed for verify_listed_ref.
+__global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *vn,
+                                 const ClusterMotion *motions, double tau, float scale,
+                                 uint8_t *flags, double *err, RowLists lists,
+                                 unsigned long long count, int *status) {
+  const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint64_t row = lists.fp64[k], nv = b.nv;
   const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
   double d = 0;
-  const bool ok = exact_query(s, vn, motions[c], inverse, i, tau, limit, d, status);
+  int32_t tied[kCandidates];
+  int v = hybrid_query(b, s, vn, motions[c], inverse, i, tau, scale, d, tied, status);
+  if (v == 3) {
+    atomicAdd(&lists.counts[3], 1ull);
+    const M3 r = query_rotation(motions[c], inverse);
+    D3 q;
+    query_skipped(motions[c], r, inverse, vertex(s, int32_t(i)), tau, q);
+    int32_t first = tied[0];
+    for (int x = 1; x < kCandidates && tied[x] >= 0; ++x)
+      first = first_in_reference_order(t, q, first, tied[x]);
+    v = normal_agrees(s, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
+  }
+  flags[row] = v == 1;
+  if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
+  if (v == 2) {
+    const unsigned long long j = atomicAdd(&lists.counts[2], 1ull);
+    lists.reference[j] = uint32_t(row);
+    lists.limits[j] = d;
+  }
+}
+
+// Rows whose candidates overflowed the list: the reference's search itself
+// (exact_query) with the tau^2 limit.
+__global__ void verify_listed_ref(Surface s, const double *vn, const ClusterMotion *motions,
+                                  double tau, RowLists lists, unsigned long long count,
+                                  uint8_t *flags, double *err, int *status) {
+  const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint64_t row = lists.reference[k], nv = s.nv;
+  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  const bool inverse = rem >= nv;
+  const uint64_t i = rem % nv;
+  double d = 0;
+  const bool ok = exact_query(s, vn, motions[c], inverse, i, tau, lists.limits[k], d, status);
   flags[row] = ok;
   if (!inverse) err[c * nv + i] = ok ? d : 0.0;
+}
+
+// Block c < nc: sum of the forward errors, supporting weight (both
+// directions) and forward count of cluster c; block nc: the total weight.
+// Fixed-order strided partials and a fixed tree: reproducible, and within
+// a few units of rounding of the reference's serial sums.
+__global__ void __launch_bounds__(256) tree_sums(const uint8_t *flags, const double *err,
+                                                 const double *w, uint64_t nv, uint64_t nc,
+                                                 double *error, double *area, uint64_t *count,
+                                                 double *total) {
+  __shared__ double se[256], sa[256];
+  __shared__ unsigned long long sn[256];
+  const uint64_t c = blockIdx.x;
+  double e = 0, a = 0;
+  unsigned long long n = 0;
+  if (c == nc) {
+    for (uint64_t i = threadIdx.x; i < nv; i += 256) a += w[i];
+  } else {
+    const uint8_t *fa = flags + c * 2 * nv, *fb = fa + nv;
+    for (uint64_t i = threadIdx.x; i < nv; i += 256) {
+      if (fa[i]) e += err[c * nv + i], a += w[i], ++n;
+      if (fb[i]) a += w[i];
+    }
+  }
+  se[threadIdx.x] = e, sa[threadIdx.x] = a, sn[threadIdx.x] = n;
+  __syncthreads();
+  for (int h = 128; h; h >>= 1) {
+    if (int(threadIdx.x) < h) {
+      se[threadIdx.x] += se[threadIdx.x + h];
+      sa[threadIdx.x] += sa[threadIdx.x + h];
+      sn[threadIdx.x] += sn[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (c == nc) {
+      *total = sa[0];
+    } else {
+      error[c] = se[0], area[c] = sa[0], count[c] = sn[0];
+    }
+  }
 }
 
 // ------------------------------------------------ FP64 transform refinement
@@ -751,7 +945,8 @@ __global__ void count_roots(int32_t *parent_all, uint64_t nv, uint64_t sets, uns
 
 }  // namespace
 
-Lbvh lbvh_build(Call &call, const double *xyz, uint64_t nv, const int32_t *faces, uint64_t nf) {
+Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
+                const int32_t *faces, uint64_t nf) {
   Lbvh b;
   b.nv = nv, b.nf = nf, b.faces = faces;
   if (!nf) return b;
@@ -759,11 +954,14 @@ Lbvh lbvh_build(Call &call, const double *xyz, uint64_t nv, const int32_t *faces
   const uint64_t ni = nf - 1;
   auto pad = [](uint64_t x) { return (x + 255) & ~uint64_t(255); };
   const uint64_t s_xyz = pad(12 * nv), s_child = pad(8 * ni + 8), s_box = pad(48 * ni + 48);
-  SYM_CUDA(cudaMalloc(&b.block, s_xyz + s_child + s_box));
+  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box));
   b.xyz = reinterpret_cast<float *>(b.block);
   b.child = reinterpret_cast<int32_t *>(b.block + s_xyz);
   b.box = reinterpret_cast<float *>(b.block + s_xyz + s_child);
+  b.vn = reinterpret_cast<float *>(b.block + s_xyz + s_child + s_box);
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(xyz, nv, b.xyz);
+  check_launch();
+  lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(vn, nv, b.vn);
   check_launch();
   // the mesh box, for the Morton quantisation
   std::vector<float> h(3 * nv);
@@ -793,7 +991,7 @@ Lbvh lbvh_build(Call &call, const double *xyz, uint64_t nv, const int32_t *faces
                                                      parent_in, parent_leaf, b.box, arrivals);
     check_launch();
   }
-  call.launched(ni ? 6 : 4);
+  call.launched(ni ? 7 : 5);
   call.sync();
   return b;
 }
@@ -839,26 +1037,35 @@ void store_motion(const ClusterMotion &m, sym_cluster_record &r) {
 
 }  // namespace
 
-// The reference-order BVH of a resident mesh, built on the host from the
-// device's vertices and faces when the first undecided query needs it.
+// The reference-order BVH of a resident mesh on the device: the build the
+// mesh's load started on a host thread, or, without one, a build from the
+// device's vertices and faces.
 void ensure_ref_bvh(Call &call, const ResidentSurface &m) {
-  if (m.ref->block) return;
-  std::vector<double> x(3 * m.nv);
-  std::vector<int32_t> f(3 * m.nf);
-  call.d2h(x.data(), m.xyz, 24 * m.nv);
-  call.d2h(f.data(), m.faces, 12 * m.nf);
-  call.sync();
-  const sym_mesh_view mv{{x.data(), x.data() + m.nv, x.data() + 2 * m.nv, m.nv},
-                         {f.data(), f.data() + m.nf, f.data() + 2 * m.nf, m.nf}};
-  const HostBvh bvh(mv);
-  if (2 * bvh.depth + 4 > kRefStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
-  *m.ref = ref_bvh_upload(bvh, call.stream());
+  RefBvhSource &src = *m.ref;
+  if (src.dev.block) return;
+  std::unique_ptr<HostBvh> bvh;
+  if (src.pending.valid()) {
+    bvh = src.pending.get();
+  } else {
+    std::vector<double> x(3 * m.nv);
+    std::vector<int32_t> f(3 * m.nf);
+    call.d2h(x.data(), m.xyz, 24 * m.nv);
+    call.d2h(f.data(), m.faces, 12 * m.nf);
+    call.sync();
+    const sym_mesh_view mv{{x.data(), x.data() + m.nv, x.data() + 2 * m.nv, m.nv},
+                           {f.data(), f.data() + m.nf, f.data() + 2 * m.nf, m.nf}};
+    bvh = std::make_unique<HostBvh>(mv);
+  }
+  if (2 * bvh->depth + 4 > kRefStack) fail(SYM_RUNTIME_ERROR, "verification: BVH too deep");
+  src.dev = ref_bvh_upload(*bvh, call.stream());
 }
 
-uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *dm, uint64_t nc,
-                     double tau, uint8_t *flags, double *err) {
+uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *dm,
+                     const sym_cluster_record *records, uint64_t nc, double tau, uint8_t *flags,
+                     double *err, uint64_t *fp64_rows) {
   const uint64_t nv = m.nv, rows = nc * 2 * nv;
   cudaStream_t st = call.stream();
+  if (fp64_rows) *fp64_rows = 0;
   if (!rows) return 0;
   if (rows >= (uint64_t(1) << 32)) fail(SYM_INVALID_ARGUMENT, "verification: too many queries");
   if (!m.nf) {
@@ -867,29 +1074,57 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
     return 0;
   }
   const Lbvh &bvh = *m.lbvh;
-  uint32_t *undecided = call.alloc<uint32_t>(rows);
-  unsigned long long *count = call.alloc<unsigned long long>(1);
-  SYM_CUDA(cudaMemsetAsync(count, 0, 8, st));
+  std::vector<MotionF> mf(nc);
+  for (uint64_t c = 0; c < nc; ++c) {
+    const sym_cluster_record &r = records[c];
+    for (int k = 0; k < 9; ++k) mf[c].r[k] = float(r.rotation[k]);
+    for (int k = 0; k < 3; ++k) mf[c].t[k] = float(r.translation[k]), mf[c].n[k] = float(r.plane_normal[k]);
+    mf[c].offset = float(r.plane_offset);
+    mf[c].reflection = r.reflection != 0;
+  }
+  const MotionF *dmf = call.upload(mf.data(), nc);
+  RowLists lists;
+  lists.forward = call.alloc<uint32_t>(nc * nv);
+  lists.faces = call.alloc<int32_t>(nc * nv * kCandidates);
+  lists.fp64 = call.alloc<uint32_t>(rows);
+  lists.reference = call.alloc<uint32_t>(rows);
+  lists.limits = call.alloc<double>(rows);
+  lists.counts = call.alloc<unsigned long long>(4);
+  SYM_CUDA(cudaMemsetAsync(lists.counts, 0, 32, st));
   const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
   Surface s{m.xyz, nv, m.faces, m.nf, nullptr, nullptr};
-  verify_vertices_hybrid<<<blocks_for(rows), kThreads, 0, st>>>(view, s, m.vn, dm, nc, tau,
-                                                                bvh.scale, flags, err, undecided,
-                                                                count, call.status());
+  verify_fp32<<<blocks_for(rows), kThreads, 0, st>>>(view, bvh.vn, dmf, nc, float(tau), bvh.scale,
+                                                      flags, err, lists, call.status());
   check_launch();
-  call.launched();
-  unsigned long long n = 0;
-  call.d2h(&n, count, 8);
+  unsigned long long counts[4] = {0, 0, 0, 0};
+  call.d2h(counts, lists.counts, 16);
   call.sync();
-  if (n) {
-    ensure_ref_bvh(call, m);
-    s.nodes = m.ref->nodes, s.ids = m.ref->ids;
-    const double limit = std::nextafter(tau * tau, std::numeric_limits<double>::infinity());
-    verify_listed_ref<<<blocks_for(n), kThreads, 0, st>>>(s, m.vn, dm, tau, limit, undecided, n,
-                                                           flags, err, call.status());
+  call.launched();
+  if (counts[0]) {
+    forward_errors<<<blocks_for(counts[0]), kThreads, 0, st>>>(s, dm, lists, counts[0], err);
     check_launch();
     call.launched();
   }
-  return n;
+  if (counts[1]) {
+    ensure_ref_bvh(call, m);
+    s.nodes = m.ref->dev.nodes, s.ids = m.ref->dev.ids;
+    verify_rows_fp64<<<blocks_for(counts[1]), kThreads, 0, st>>>(view, s, m.ref->dev, m.vn, dm, tau,
+                                                                  bvh.scale, flags, err, lists,
+                                                                  counts[1], call.status());
+    check_launch();
+    call.launched();
+    call.d2h(counts + 2, lists.counts + 2, 16);
+    call.sync();
+  }
+  if (fp64_rows) *fp64_rows = counts[1];
+  if (counts[2]) {
+    verify_listed_ref<<<blocks_for(counts[2]), kThreads, 0, st>>>(s, m.vn, dm, tau, lists,
+                                                                   counts[2], flags, err,
+                                                                   call.status());
+    check_launch();
+    call.launched();
+  }
+  return counts[2] + counts[3];
 }
 
 // Coverage, rms and patch counts of the nc modes (sym_detect_fast), after
@@ -898,9 +1133,11 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
 // verification of the records.
 void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record *records,
                        uint64_t nc, double tau, int refine, const double origin[3],
-                       double *coverage, double *rms, uint32_t *patches, uint64_t *undecided) {
+                       double *coverage, double *rms, uint32_t *patches, uint64_t *undecided,
+                       uint64_t *fp64_rows) {
   const uint64_t nv = m.nv;
   if (undecided) *undecided = 0;
+  if (fp64_rows) *fp64_rows = 0;
   if (!nc || !nv) {
     for (uint64_t c = 0; c < nc; ++c) coverage[c] = rms[c] = 0, patches[2 * c] = patches[2 * c + 1] = 0;
     return;
@@ -920,11 +1157,13 @@ void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record 
   const uint64_t rows = nc * 2 * nv;
   uint8_t *flags = call.alloc<uint8_t>(rows);
   double *err = call.alloc<double>(nc * nv);
-  const uint64_t n = exact_flags(call, m, dm, nc, tau, flags, err);
+  const uint64_t n = exact_flags(call, m, dm, records, nc, tau, flags, err, fp64_rows);
   if (undecided) *undecided = n;
   double *error = call.alloc<double>(nc), *area = call.alloc<double>(nc), *total = call.alloc<double>(1);
   uint64_t *na = call.alloc<uint64_t>(nc);
-  ordered_verification_sums(call, flags, err, m.w, nv, nc, error, area, na, total);
+  tree_sums<<<unsigned(nc + 1), 256, 0, st>>>(flags, err, m.w, nv, nc, error, area, na, total);
+  check_launch();
+  call.launched();
   int32_t *parent = call.alloc<int32_t>(rows);
   unsigned *dpatch = call.alloc<unsigned>(2 * nc);
   SYM_CUDA(cudaMemsetAsync(dpatch, 0, 8 * nc, st));
@@ -972,7 +1211,7 @@ void verification_resident(Call &call, const ResidentSurface &m, const sym_clust
   ClusterMotion *dm = call.upload(motions.data(), nc);
   uint8_t *flags = call.alloc<uint8_t>(nc * 2 * nv);
   double *err = call.alloc<double>(nc * nv);
-  const uint64_t n = exact_flags(call, m, dm, nc, tau, flags, err);
+  const uint64_t n = exact_flags(call, m, dm, records, nc, tau, flags, err, nullptr);
   if (undecided) *undecided = n;
   finish_verification(call, flags, err, m.w, m.nbr_off, m.nbr, nv, nc, side, patches, coverage, rms);
 }

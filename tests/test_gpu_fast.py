@@ -1,13 +1,15 @@
 """The throughput pipeline (sym_mesh_load + sym_detect_fast, no reference
 counterpart) on the 256-seed motif-sphere case: it finds the planted 5-fold
-rotation about z, its LBVH verification (FP32 search, FP64 rechecks) gives
-exactly the coverage, rms and patch counts of the exact verification
+rotation about z, its LBVH verification (FP32 decisions, FP64 rechecks) gives
+the patch counts, coverage and rms of the exact verification
 (sym_verification, the reference's algorithm) of the same modes, and the
 BF16-refined and FP32 forms report the same top modes.
 
-Tolerances: none between the two verifications (bit-identical coverage and
-rms, equal patch counts); top modes of the two mean-shift forms agree to
-1e-4 relative (the mode-error target)."""
+Tolerances: patch counts equal; coverage and rms within 1e-12 relative (the
+throughput path sums in a fixed tree instead of the reference's serial
+order; the reference's own CPU/GPU comparison allows 2e-10,
+tests/compare_cuda.py:20-21); top modes of the two mean-shift forms agree
+to 1e-4 relative (the mode-error target)."""
 import numpy as np
 import pytest
 
@@ -64,8 +66,8 @@ def test_fast_verification_matches_exact(fast):
                              np.array(r["translation"]), np.zeros((n, 3)), np.zeros(n),
                              Csr(np.zeros(n + 1, np.uint64), np.zeros(0, np.int32)))
     exact = gpu.verification(p.mesh, p.topology, clusters, p.context, opts)
-    assert np.array_equal(np.array(r["coverage"]), exact.coverage), (r["coverage"], exact.coverage)
-    assert np.array_equal(np.array(r["rms"]), exact.rms), (r["rms"], exact.rms)
+    assert np.allclose(r["coverage"], exact.coverage, rtol=1e-12, atol=0), (r["coverage"], exact.coverage)
+    assert np.allclose(r["rms"], exact.rms, rtol=1e-12, atol=0), (r["rms"], exact.rms)
     pa = np.diff(exact.patches_a_groups.astype(np.int64))
     pb = np.diff(exact.patches_b_groups.astype(np.int64))
     got = np.array(r["patches"]).reshape(n, 2)
@@ -146,8 +148,8 @@ def test_reflection_fast_verification_matches_exact(refl):
                              np.array(r["plane_offset"]),
                              Csr(np.zeros(n + 1, np.uint64), np.zeros(0, np.int32)))
     exact = gpu.verification(p.mesh, p.topology, clusters, p.context, opts)
-    assert np.array_equal(np.array(r["coverage"]), exact.coverage), (r["coverage"], exact.coverage)
-    assert np.array_equal(np.array(r["rms"]), exact.rms), (r["rms"], exact.rms)
+    assert np.allclose(r["coverage"], exact.coverage, rtol=1e-12, atol=0), (r["coverage"], exact.coverage)
+    assert np.allclose(r["rms"], exact.rms, rtol=1e-12, atol=0), (r["rms"], exact.rms)
     got = np.array(r["patches"]).reshape(n, 2)
     assert np.array_equal(got[:, 0], np.diff(exact.patches_a_groups.astype(np.int64)))
     assert np.array_equal(got[:, 1], np.diff(exact.patches_b_groups.astype(np.int64)))
