@@ -356,7 +356,9 @@ typedef struct sym_fast_result {
   int32_t iterations, polish_iterations;
   /* relative error of each mode against FP64, over the reference seeds that
    * converged (Newton, a well-defined mode) in both runs (modes_compared of
-   * them); modes_within counts those within 1e-4 */
+   * them); modes_within counts those within 1e-4.  The seeds_* and
+   * mode_error_all_* / _settled_ / _unconverged_ fields below cover every
+   * reference seed. */
   double mode_error_max, mode_error_mean;
   uint64_t modes_compared, modes_within;
   /* device time per stage: curvature, prune, pairing, votes, vote sort,
@@ -388,6 +390,21 @@ typedef struct sym_fast_result {
   /* verification queries decided in FP64 because an FP32 test fell within
    * its error band (out of 2 x clusters x vertices) */
   uint64_t verify_fp64_rows;
+  /* mode error over every one of the seeds_compared reference seeds (none
+   * dropped): max and mean relative error of the final position against the
+   * FP64 run's, seeds_within of them within 1e-4; by the pair of final
+   * states, modes_compared were Newton-converged in both runs, seeds_settled
+   * ended on a ridge (settled) in one or both, seeds_unconverged were still
+   * approaching, or lost their weight, in one or both */
+  uint64_t seeds_compared, seeds_within, seeds_settled, seeds_unconverged;
+  double mode_error_all_max, mode_error_all_mean;
+  double mode_error_settled_max, mode_error_unconverged_max;
+  /* per reported mode (with reference_seeds > 0): the relative error of its
+   * motion [R, t / box] against the FP64 mode that the FP64 mean shift
+   * reaches from the same position; with `refine`, the error of the refined
+   * motion against the same refinement of the FP64 motion */
+  double transform_error[SYM_FAST_MAX_CLUSTERS], transform_error_max;
+  double transform_error_refined[SYM_FAST_MAX_CLUSTERS], transform_error_refined_max;
 } sym_fast_result;
 void sym_fast_options_default(sym_fast_options *out);
 /* `sample` is a host array of vertex ids (the area-weighted sample). */

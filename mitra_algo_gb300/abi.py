@@ -177,7 +177,14 @@ class FastResult(C.Structure):
                 ("precise", C.c_uint8 * FAST_MAX_CLUSTERS),
                 ("tc_launches", C.c_uint64), ("tc_kernel_ms", C.c_double),
                 ("tc_evaluations", C.c_double), ("verify_undecided", C.c_uint64),
-                ("verify_fp64_rows", C.c_uint64)]
+                ("verify_fp64_rows", C.c_uint64),
+                ("seeds_compared", C.c_uint64), ("seeds_within", C.c_uint64),
+                ("seeds_settled", C.c_uint64), ("seeds_unconverged", C.c_uint64),
+                ("mode_error_all_max", C.c_double), ("mode_error_all_mean", C.c_double),
+                ("mode_error_settled_max", C.c_double), ("mode_error_unconverged_max", C.c_double),
+                ("transform_error", C.c_double * FAST_MAX_CLUSTERS), ("transform_error_max", C.c_double),
+                ("transform_error_refined", C.c_double * FAST_MAX_CLUSTERS),
+                ("transform_error_refined_max", C.c_double)]
 
 
 class PreparedOut(C.Structure):

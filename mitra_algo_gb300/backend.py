@@ -366,6 +366,14 @@ class Gb300Backend:
         out["tc_evaluations"] = float(res.tc_evaluations)
         out["verify_undecided"] = int(res.verify_undecided)
         out["verify_fp64_rows"] = int(res.verify_fp64_rows)
+        for k in ("seeds_compared", "seeds_within", "seeds_settled", "seeds_unconverged"):
+            out[k] = int(getattr(res, k))
+        for k in ("mode_error_all_max", "mode_error_all_mean", "mode_error_settled_max",
+                  "mode_error_unconverged_max", "transform_error_max",
+                  "transform_error_refined_max"):
+            out[k] = float(getattr(res, k))
+        out["transform_error"] = list(res.transform_error)[:n]
+        out["transform_error_refined"] = list(res.transform_error_refined)[:n]
         out["rotation"] = [list(res.records[i].rotation) for i in range(n)]
         out["translation"] = [list(res.records[i].translation) for i in range(n)]
         out["reflection"] = [bool(res.records[i].reflection) for i in range(n)]

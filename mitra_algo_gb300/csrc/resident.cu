@@ -623,23 +623,45 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     call.d2h(hm.data(), m64, k64 * 8 * 8);
     call.d2h(hs64.data(), st64, k64);
     call.sync();
-    double emax = 0, esum = 0;
-    uint64_t compared = 0, within = 0;
+    // every reference seed is compared; the pair of final states puts it
+    // in one of three groups: Newton-converged in both runs (a mode with a
+    // well-defined position), settled on a ridge in either run, or still
+    // unconverged (or without weight) in either
+    double emax = 0, esum = 0, all_max = 0, all_sum = 0, settled_max = 0, open_max = 0;
+    uint64_t compared = 0, within = 0, within_all = 0, settled = 0, open = 0;
     for (uint64_t i = 0; i < k64; ++i) {
-      if (hs64[i] != kConverged || state[i] != kConverged) continue;  // a well-defined mode in both
       double num = 0, den = 0;
       for (int d = 0; d < 6; ++d) {
         double e = double(means[i * 8 + d]) - hm[i * 8 + d];
         num += e * e, den += hm[i * 8 + d] * hm[i * 8 + d];
       }
       double rel = std::sqrt(num) / std::max(std::sqrt(den), 1e-300);
-      emax = std::max(emax, rel), esum += rel, ++compared;
-      within += rel <= 1e-4;
+      if (!std::isfinite(rel)) rel = std::numeric_limits<double>::infinity();
+      all_max = std::max(all_max, rel), all_sum += rel, within_all += rel <= 1e-4;
+      const bool both = hs64[i] == kConverged && state[i] == kConverged;
+      const bool ridge = !both && (hs64[i] == kConverged || hs64[i] == kSettled) &&
+                         (state[i] == kConverged || state[i] == kSettled);
+      if (both) {
+        emax = std::max(emax, rel), esum += rel, ++compared;
+        within += rel <= 1e-4;
+      } else if (ridge) {
+        settled_max = std::max(settled_max, rel), ++settled;
+      } else {
+        open_max = std::max(open_max, rel), ++open;
+      }
     }
     r.mode_error_max = emax;
     r.mode_error_mean = compared ? esum / compared : 0;
     r.modes_compared = compared;
     r.modes_within = within;
+    r.seeds_compared = k64;
+    r.seeds_within = within_all;
+    r.seeds_settled = settled;
+    r.seeds_unconverged = open;
+    r.mode_error_all_max = all_max;
+    r.mode_error_all_mean = k64 ? all_sum / k64 : 0;
+    r.mode_error_settled_max = settled_max;
+    r.mode_error_unconverged_max = open_max;
   }
   clock.mark(7);
   // ---- modes: greedy merge (h^2/4, first mode wins) + support
@@ -712,9 +734,7 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   std::stable_sort(rank.begin(), rank.end(), [&](uint64_t a, uint64_t b) { return support[a] > support[b]; });
   uint64_t nc = std::min<uint64_t>({nm, uint64_t(std::max(o.max_clusters, 0)), SYM_FAST_MAX_CLUSTERS});
   r.clusters = nc;
-  for (uint64_t i = 0; i < nc; ++i) {
-    const double *d = &mode_pos[rank[i] * 6];
-    sym_cluster_record &rec = r.records[i];
+  auto decode = [&](const double *d, sym_cluster_record &rec) {
     rec = sym_cluster_record{};
     if (reflection) {  // the reference's decode, clustering.cpp:117-124
       const D3 nr{d[0], d[1], d[2]};
@@ -737,8 +757,49 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
         rec.translation[x] = d[3 + x] * h.model.box_size + c[x] - rc;
       }
     }
+  };
+  for (uint64_t i = 0; i < nc; ++i) {
+    decode(&mode_pos[rank[i] * 6], r.records[i]);
     r.support[i] = support[rank[i]];
     r.precise[i] = mode_precise[rank[i]];
+  }
+  // each reported motion against FP64: the FP64 mean shift restarted from
+  // the mode's position (approach and polish as above) reaches the FP64 mode
+  // the GPU's approximates; the relative error of the motion [R, t / box]
+  sym_cluster_record rec64[SYM_FAST_MAX_CLUSTERS];
+  auto motion_error = [&](const sym_cluster_record &a, const sym_cluster_record &b) {
+    double num = 0, den = 0;
+    for (int j = 0; j < 12; ++j) {
+      const double x = j < 9 ? a.rotation[j] : a.translation[j - 9] / h.model.box_size;
+      const double y = j < 9 ? b.rotation[j] : b.translation[j - 9] / h.model.box_size;
+      num += (x - y) * (x - y), den += y * y;
+    }
+    return std::sqrt(num) / std::max(std::sqrt(den), 1e-300);
+  };
+  if (want64 && nc) {
+    std::vector<double> start(nc * 8, 0.0);
+    for (uint64_t i = 0; i < nc; ++i) {
+      double n2 = 0;
+      for (int d = 0; d < 6; ++d) {
+        start[i * 8 + d] = mode_pos[rank[i] * 6 + d];
+        n2 += start[i * 8 + d] * start[i * 8 + d];
+      }
+      start[i * 8 + 6] = n2;
+    }
+    double *m64 = call.upload(start.data(), nc * 8);
+    uint8_t *st64 = call.alloc<uint8_t>(nc);
+    SYM_CUDA(cudaMemsetAsync(st64, 0, nc, st));
+    shift(call, vs, m64, st64, nc, h2, fo.max_iterations, false, nullptr, nullptr);
+    shift(call, vs, m64, st64, nc, h2, fo.polish_iterations, true, nullptr, nullptr);
+    call.d2h(start.data(), m64, nc * 64);
+    call.sync();
+    for (uint64_t i = 0; i < nc; ++i) {
+      double d6[6];
+      for (int d = 0; d < 6; ++d) d6[d] = start[i * 8 + d];
+      decode(d6, rec64[i]);
+      r.transform_error[i] = motion_error(r.records[i], rec64[i]);
+      r.transform_error_max = std::max(r.transform_error_max, r.transform_error[i]);
+    }
   }
   clock.mark(8);
   // ---- (d) verification of the top modes
@@ -746,6 +807,17 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     verification_fast(call, h.surface(), r.records, nc, o.verify_threshold * h.model.box_size,
                       fo.refine, h.model.center, r.coverage, r.rms, r.patches,
                       &r.verify_undecided, &r.verify_fp64_rows);
+    if (want64 && fo.refine > 0) {  // the same refinement of the FP64 motions
+      double cov[SYM_FAST_MAX_CLUSTERS], rms[SYM_FAST_MAX_CLUSTERS];
+      uint32_t patches[2 * SYM_FAST_MAX_CLUSTERS];
+      verification_fast(call, h.surface(), rec64, nc, o.verify_threshold * h.model.box_size,
+                        fo.refine, h.model.center, cov, rms, patches, nullptr, nullptr);
+      for (uint64_t i = 0; i < nc; ++i) {
+        r.transform_error_refined[i] = motion_error(r.records[i], rec64[i]);
+        r.transform_error_refined_max =
+            std::max(r.transform_error_refined_max, r.transform_error_refined[i]);
+      }
+    }
   }
   clock.mark(9);
   call.sync();
