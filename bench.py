@@ -401,22 +401,61 @@ def c1_exact(gpu, steps=3):
         return sum(v for k, v in result.timings if k != "prepare") / 1e3
     s_gpu = statistics.mean(stages_s(x) for x in runs)
     s_cpu = stages_s(c)
-    same = (np.array_equal(g.pairs.a, c.pairs.a) and np.array_equal(g.pairs.b, c.pairs.b)
-            and np.array_equal(g.votes.descriptor, c.votes.descriptor)
-            and np.array_equal(g.clusters.votes.indices, c.clusters.votes.indices)
-            and np.array_equal(g.verification.side_a.indices, c.verification.side_a.indices)
-            and np.array_equal(g.verification.patches_b.indices, c.verification.patches_b.indices))
+    parity = c1_parity(g, c)
     return {"workload": "mirrored height field 128 x 128, 2,000 samples, reflection and rigid "
                         "votes, the reference's options otherwise (its CPU-runnable case)",
             "gpu_meshes_per_s": round(1.0 / t_gpu, 3), "cpu_meshes_per_s": round(1.0 / t_cpu, 4),
             "gpu_over_cpu": round(t_cpu / t_gpu, 1),
-            "stages_gpu_over_cpu": round(s_cpu / s_gpu, 1), "identical_results": bool(same),
+            "stages_gpu_over_cpu": round(s_cpu / s_gpu, 1), "parity": parity,
             "pairs": int(len(c.pairs)), "votes": int(len(c.votes)),
             "clusters": int(len(c.clusters.reflection)),
             "gpu_stage_ms": {k: round(v, 2) for k, v in g.timings},
             "cpu_stage_ms": {k: round(v, 1) for k, v in c.timings},
             "cpu": "oracle port of the reference's CPU backend, one core",
             "clock": "host wall clock around detect(); GPU: mean of 3 after one warm-up"}
+
+
+def c1_parity(g, c):
+    """How the GPU's detect() result `g` compares with the CPU port's `c`:
+    every id (pairs, vote pairs and kinds, cluster memberships, supporting
+    vertices, patches) must be equal; FP64 values (features, vote
+    descriptors, cluster motions, coverage, rms) are within the reference's
+    own CPU/GPU bound 2e-10 (1 + |cpu|) (tests/compare_cuda.py:20-21) -- the
+    GPU's curvature rounds its transcendentals differently in the last
+    bits, which every later FP64 value inherits."""
+    def ids(*pairs):
+        return all(np.array_equal(np.asarray(a), np.asarray(b)) for a, b in pairs)
+
+    def fp_excess(*pairs):  # largest |gpu - cpu| / (2e-10 (1 + |cpu|)); <= 1 passes
+        worst = 0.0
+        for a, b in pairs:
+            a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+            if a.shape != b.shape:
+                return float("inf")
+            if a.size:
+                worst = max(worst, float(np.max(np.abs(a - b) / (2e-10 * (1 + np.abs(b))))))
+        return worst
+    gv, cv = g.verification, c.verification
+    out = {
+        "features": fp_excess((g.features.kmin, c.features.kmin), (g.features.kmax, c.features.kmax),
+                              (g.features.normal, c.features.normal)) <= 1 and
+        ids((g.features.valid, c.features.valid)),
+        "pairs": ids((g.pairs.a, c.pairs.a), (g.pairs.b, c.pairs.b)),
+        "votes": ids((g.votes.pair, c.votes.pair), (g.votes.kind, c.votes.kind)) and
+        fp_excess((g.votes.descriptor, c.votes.descriptor), (g.votes.rotation, c.votes.rotation),
+                  (g.votes.translation, c.votes.translation)) <= 1,
+        "clusters": ids((g.clusters.votes.offsets, c.clusters.votes.offsets),
+                        (g.clusters.votes.indices, c.clusters.votes.indices)) and
+        fp_excess((g.clusters.rotation, c.clusters.rotation),
+                  (g.clusters.translation, c.clusters.translation)) <= 1,
+        "verification": ids((gv.side_a.indices, cv.side_a.indices),
+                            (gv.side_b.indices, cv.side_b.indices),
+                            (gv.patches_a.indices, cv.patches_a.indices),
+                            (gv.patches_b.indices, cv.patches_b.indices)) and
+        fp_excess((gv.coverage, cv.coverage), (gv.rms, cv.rms)) <= 1}
+    out["all"] = all(out.values())
+    out["rule"] = "ids equal; FP64 values within 2e-10 (1 + |cpu|)"
+    return out
 
 
 def stage_rooflines(prepared, opts, r, peak_gbs):

@@ -545,6 +545,19 @@ sym_status sym_fast_votes(sym_context *ctx, const sym_points_view *positions,
                           const sym_model_context *model, int32_t mode, float *out,
                           int32_t *pair_of, uint64_t *count);
 
+/* Test hook for the device's bounded waits (no reference counterpart).
+ * which = 0: the tensor-core kernels' barrier wait, with a limit of `limit`
+ * nanoseconds in place of 2 s, on a barrier nothing signals, in a kernel that
+ * holds tensor memory as the mean-shift kernel does; the wait runs out, the
+ * kernel frees its tensor memory and returns, and the call returns
+ * SYM_DEVICE_TIMEOUT.  which = 1: the verification's union-find retry loop
+ * on a path of 64 vertices with at most `limit` retries per union;
+ * SYM_DEVICE_TIMEOUT when a union ran out of retries, else SYM_OK with the
+ * number of components in *components (may be NULL).  The context stays
+ * usable after either. */
+sym_status sym_wait_selftest(sym_context *ctx, int32_t which, uint64_t limit,
+                             uint64_t *components);
+
 /* ------------------------------------------------ allocation-free prune */
 /* No counterpart in the reference: an allocation-free form of the prune half
  * of select() (src/cpu/selection.cpp:20-27, src/cuda/backend.cu:21-30).

@@ -257,6 +257,7 @@ PROTOTYPES = [
                                  P(C.c_int32)]),
     ("sym_tc_selftest", C.c_int, [C.c_void_p, P(C.c_uint16), P(C.c_uint16), P(C.c_uint16),
                                   P(C.c_uint16), _f, _f]),
+    ("sym_wait_selftest", C.c_int, [C.c_void_p, C.c_int32, C.c_uint64, P(C.c_uint64)]),
     ("sym_fast_votes", C.c_int, [C.c_void_p, P(PointsView), P(FeaturesView), P(PairsView),
                                  P(ModelContext), C.c_int32, _f, _i, P(C.c_uint64)]),
     # allocation-free prune: device pointers + a cudaStream_t

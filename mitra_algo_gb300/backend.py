@@ -422,6 +422,16 @@ class Gb300Backend:
         q = int(count.value)
         return out[:q].copy(), pair_of[:q].copy()
 
+    def wait_selftest(self, which: str, limit: int):
+        """sym_wait_selftest: which = "tensor" (the tensor kernels' barrier
+        wait, limit in ns) or "union" (the verification's union-find retries);
+        raises DeviceTimeout when the wait runs out, else returns the
+        union-find's component count (None for "tensor")."""
+        comps = C.c_uint64(0)
+        _check(self._lib.sym_wait_selftest(self._ctx, {"tensor": 0, "union": 1}[which],
+                                           int(limit), C.byref(comps)))
+        return int(comps.value) if which == "union" else None
+
     def tc_selftest(self, a1, b1, a2, b2):
         """Tensor-core path check: returns (A1 . B1^T, A2 . B2^T) computed by
         tcgen05 from BF16 bit patterns (uint16 arrays 128x16, 128x16, 128x128,

@@ -6,6 +6,7 @@
 #include "rng.hpp"
 #include "sampling.cuh"
 
+#include <algorithm>
 #include <cstdlib>
 #include <new>
 #include <vector>
@@ -28,6 +29,8 @@ void verification_host(Call &, const sym_mesh_view &, const sym_topology_view &,
                        const sym_clusters_view &, const sym_model_context &, const sym_options &,
                        sym_verification_result &, void *(*)(size_t));
 void triangle_distances_host(Call &, const double *, uint64_t, double *);
+void wait_selftest_host(Call &, uint64_t);
+uint64_t unite_selftest_host(Call &, int);
 }  // namespace sym
 
 // Message of the last failing call on this thread (read by sym_last_error).
@@ -263,6 +266,21 @@ sym_status sym_triangle_distances(sym_context *ctx, const double *queries, uint6
   return guarded([&] {
     sym::Call call(ctx, "triangle_distances");
     sym::triangle_distances_host(call, queries, count, out);
+  });
+}
+
+sym_status sym_wait_selftest(sym_context *ctx, int32_t which, uint64_t limit,
+                             uint64_t *components) {
+  if (!ctx || (which != 0 && which != 1)) return null_args();
+  return guarded([&] {
+    sym::Call call(ctx, "wait_selftest");
+    if (which == 0) {
+      sym::wait_selftest_host(call, limit);
+    } else {
+      const uint64_t roots =
+          sym::unite_selftest_host(call, int(std::min<uint64_t>(limit, uint64_t(1) << 30)));
+      if (components) *components = roots;
+    }
   });
 }
 

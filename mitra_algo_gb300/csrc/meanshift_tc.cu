@@ -77,13 +77,15 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Bounded wait: false when the barrier phase did not complete in time.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait: false when the barrier phase did not complete within
+// limit_ns.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity,
+                                          uint64_t limit_ns = kWaitLimitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   do {
     if (mbar_try_wait(bar, parity)) return true;
-  } while (global_ns() - t0 < kWaitLimitNs);
+  } while (global_ns() - t0 < limit_ns);
   return false;
 }
 
@@ -961,6 +963,30 @@ __global__ void __launch_bounds__(256, 1) tc_selftest(const __nv_bfloat16 *a1, c
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
+// The kernels' bounded wait made to run out: one warp holds TMEM as the
+// mean-shift kernel does, waits with mbar_wait on a barrier nothing arrives
+// at, with a limit of limit_ns instead of 2 s, then records DS_SPIN_LIMIT,
+// frees its TMEM and returns -- the path a real kernel takes when a copy or
+// an MMA never completes.  No copy or MMA is issued.
+__global__ void __launch_bounds__(32, 1) wait_selftest(uint64_t limit_ns, int *status) {
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  tmem_alloc(&tmem_slot, 32);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const bool ok = __all_sync(0xffffffffu, mbar_wait(&bar, 0, limit_ns));
+  if (!ok && threadIdx.x == 0) atomicExch(status, DS_SPIN_LIMIT);
+  tc_fence_before();
+  __syncthreads();
+  tmem_dealloc(tmem, 32);
+}
+
 // Sum of a seed's pieces (fixed order), then the mean-shift step; a seed
 // leaves the bulk (kNear: the FP32 polish takes it on with Newton steps)
 // when its squared move falls under kSwitch2 h^2.
@@ -1112,6 +1138,13 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   if (kernel_launches) *kernel_launches = std::min<uint64_t>(marks.size() / 2, active_iterations);
   for (auto e : marks) cudaEventDestroy(e);
   return true;
+}
+
+void wait_selftest_host(Call &call, uint64_t limit_ns) {
+  wait_selftest<<<1, 32, 0, call.stream()>>>(limit_ns, call.status());
+  check_launch();
+  call.launched();
+  call.check_status("tensor-kernel wait self-test");
 }
 
 void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const uint16_t *a2,

@@ -233,7 +233,7 @@ __global__ void init_parents(const uint8_t *flags, uint64_t n, int32_t *parent, 
 }
 
 __global__ void unite_edges(const uint64_t *nbr_off, const int32_t *nbr, uint64_t nv, uint64_t sets,
-                            int32_t *parent_all, int *status) {
+                            int32_t *parent_all, int *status, int retry_limit) {
   uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= sets * nv) return;
   uint64_t set = k / nv;
@@ -244,7 +244,7 @@ __global__ void unite_edges(const uint64_t *nbr_off, const int32_t *nbr, uint64_
     int32_t u = nbr[e];
     if (u <= i || parent[u] < 0) continue;  // each edge once, allowed ends only
     for (int guard = 0;; ++guard) {
-      if (guard > (1 << 20)) {
+      if (guard >= retry_limit) {
         atomicExch(status, DS_SPIN_LIMIT);
         return;
       }
@@ -298,6 +298,40 @@ __global__ void triangle_query(const double *q, uint64_t n, double *out) {
 
 }  // namespace
 
+// The union-find's bounded retry loop on a path of 64 vertices (every
+// vertex supporting one set) with `retry_limit` retries: with 0 every union
+// gives up at once and the call ends in the device-status error that a
+// retry loop running out raises; with the regular limit the path becomes
+// one component.  Returns the number of components.
+uint64_t unite_selftest_host(Call &call, int retry_limit) {
+  constexpr uint64_t n = 64;
+  std::vector<uint64_t> off(n + 1);
+  std::vector<int32_t> idx;
+  for (uint64_t i = 0; i < n; ++i) {
+    off[i] = idx.size();
+    if (i > 0) idx.push_back(int32_t(i - 1));
+    if (i + 1 < n) idx.push_back(int32_t(i + 1));
+  }
+  off[n] = idx.size();
+  std::vector<uint8_t> flags(n, 1);
+  cudaStream_t st = call.stream();
+  const uint64_t *doff = call.upload(off.data(), n + 1);
+  const int32_t *didx = call.upload(idx.data(), idx.size());
+  const uint8_t *dflags = call.upload(flags.data(), n);
+  int32_t *parent = call.alloc<int32_t>(n);
+  init_parents<<<1, 64, 0, st>>>(dflags, n, parent, n);
+  check_launch();
+  unite_edges<<<1, 64, 0, st>>>(doff, didx, n, 1, parent, call.status(), retry_limit);
+  check_launch();
+  call.launched(2);
+  std::vector<int32_t> h(n);
+  call.d2h(h.data(), parent, n * 4);
+  call.check_status("union-find self-test");
+  uint64_t roots = 0;
+  for (uint64_t i = 0; i < n; ++i) roots += h[i] == int32_t(i);
+  return roots;
+}
+
 void triangle_distances_host(Call &call, const double *queries, uint64_t count, double *out) {
   if (!count) return;
   double *q = call.upload(queries, count * 12);
@@ -336,7 +370,8 @@ void finish_verification(Call &call, const uint8_t *flags, const double *err, co
   int32_t *parent = call.alloc<int32_t>(rows);
   init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
   check_launch();
-  unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(nbr_off, nbr, nv, 2 * nc, parent, call.status());
+  unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(nbr_off, nbr, nv, 2 * nc, parent, call.status(),
+                                                      kUniteRetries);
   check_launch();
   uint64_t *keys = call.alloc<uint64_t>(rows), *skeys = call.alloc<uint64_t>(rows);
   int32_t *vals = call.alloc<int32_t>(rows), *svals = call.alloc<int32_t>(rows);

@@ -261,8 +261,12 @@ __device__ __forceinline__ int32_t find_root(int32_t *parent, int32_t x) {
   return -1;
 }
 __global__ void init_parents(const uint8_t *flags, uint64_t n, int32_t *parent, uint64_t nv);
+// A union that keeps losing its compare-and-swap retries at most
+// retry_limit times, then records DS_SPIN_LIMIT and stops (kUniteRetries in
+// regular calls).
+constexpr int kUniteRetries = 1 << 20;
 __global__ void unite_edges(const uint64_t *nbr_off, const int32_t *nbr, uint64_t nv, uint64_t sets,
-                            int32_t *parent_all, int *status);
+                            int32_t *parent_all, int *status, int retry_limit);
 
 // Sums of the reference's verification in its serial order
 // (verification.cpp:75-77, :93-96, :98-99): per cluster the forward

@@ -1170,7 +1170,7 @@ void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record 
   init_parents<<<blocks_for(rows), kThreads, 0, st>>>(flags, rows, parent, nv);
   check_launch();
   unite_edges<<<blocks_for(rows), kThreads, 0, st>>>(m.nbr_off, m.nbr, nv, 2 * nc, parent,
-                                                      call.status());
+                                                      call.status(), kUniteRetries);
   check_launch();
   count_roots<<<blocks_for(rows), kThreads, 0, st>>>(parent, nv, 2 * nc, dpatch);
   check_launch();

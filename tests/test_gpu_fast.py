@@ -95,6 +95,31 @@ def test_forms_agree_on_the_top_modes(fast):
         assert err <= 1e-4, (i, err)
 
 
+def test_every_reference_seed_and_mode_is_reported(fast):
+    """With reference seeds, every one of them is compared with its FP64 run
+    (none dropped: Newton-converged in both, settled on a ridge, or
+    unconverged), and every reported mode's motion carries its error against
+    the FP64 mode reached from the same position: within 1e-4 for modes
+    formed by Newton-converged seeds (measured: under 5e-6), finite for
+    ridge modes, whose FP64 restart may slide along the ridge."""
+    gpu, p, opts, _ = fast
+    resident = gpu.load_mesh(p)
+    r = gpu.detect_fast(resident, None, opts, precision="bf16", seeds=256, max_iterations=300,
+                        polish_iterations=30, reference_seeds=64, refine=2)
+    resident.close()
+    assert r["seeds_compared"] == 64
+    assert r["modes_compared"] + r["seeds_settled"] + r["seeds_unconverged"] == 64
+    assert r["mode_error_all_max"] >= r["mode_error_max"]
+    assert r["seeds_within"] >= r["modes_within"]
+    n = r["clusters"]
+    assert n > 0 and len(r["transform_error"]) == n and len(r["transform_error_refined"]) == n
+    assert all(np.isfinite(r["transform_error"])) and all(np.isfinite(r["transform_error_refined"]))
+    for err, precise in zip(r["transform_error"], r["precise"]):
+        if precise:
+            assert err <= 1e-4, (err, r["transform_error"])
+    assert r["transform_error_max"] == max(r["transform_error"])
+
+
 # --------------------------------------------------------- reflection mode
 # The mirrored height field (128 x 128 grid, 8 bumps mirrored in x, 2,000
 # samples, 5% curvature tolerance, bandwidth 0.02) has one plane of symmetry,
