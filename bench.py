@@ -383,7 +383,7 @@ def c1_exact(gpu, steps=3):
     (wall clock, synchronous calls, host prepare included on both sides),
     and their results compared."""
     from mitra_algo_gb300.backend import detect
-    from mitra_algo_gb300.mesh import mirrored_heightfield
+    from mitra_algo_gb300.mesh import mirrored_heightfield, prepare
     from mitra_algo_gb300.types import Options
     from oracle import oracle
     mesh = mirrored_heightfield(size=128, bumps=8, seed=0)
@@ -402,6 +402,16 @@ def c1_exact(gpu, steps=3):
     s_gpu = statistics.mean(stages_s(x) for x in runs)
     s_cpu = stages_s(c)
     parity = c1_parity(g, c)
+    # the verification alone on the same motions (the CPU run's clusters)
+    p = prepare(mesh, o)
+    v_same = gpu.verification(p.mesh, p.topology, c.clusters, p.context, o)
+    parity["verification_on_cpu_clusters"] = bool(
+        all(np.array_equal(getattr(v_same, k).indices, getattr(c.verification, k).indices)
+            for k in ("side_a", "side_b", "patches_a", "patches_b"))
+        and np.array_equal(v_same.coverage, c.verification.coverage)
+        and np.allclose(v_same.rms, c.verification.rms, rtol=1e-12, atol=0))
+    parity["verification_end_to_end_differing_vertices"] = differing_sides(g.verification,
+                                                                         c.verification)
     return {"workload": "mirrored height field 128 x 128, 2,000 samples, reflection and rigid "
                         "votes, the reference's options otherwise (its CPU-runnable case)",
             "gpu_meshes_per_s": round(1.0 / t_gpu, 3), "cpu_meshes_per_s": round(1.0 / t_cpu, 4),
@@ -413,6 +423,19 @@ def c1_exact(gpu, steps=3):
             "cpu_stage_ms": {k: round(v, 1) for k, v in c.timings},
             "cpu": "oracle port of the reference's CPU backend, one core",
             "clock": "host wall clock around detect(); GPU: mean of 3 after one warm-up"}
+
+
+def differing_sides(a, b):
+    """Number of (cluster, side, vertex) memberships in one verification's
+    side lists but not the other's."""
+    n = 0
+    for side in ("side_a", "side_b"):
+        x, y = getattr(a, side), getattr(b, side)
+        for c in range(len(x.offsets) - 1):
+            r1 = set(x.indices[x.offsets[c]:x.offsets[c + 1]].tolist())
+            r2 = set(y.indices[y.offsets[c]:y.offsets[c + 1]].tolist())
+            n += len(r1 ^ r2)
+    return n
 
 
 def c1_parity(g, c):
@@ -436,6 +459,8 @@ def c1_parity(g, c):
                 worst = max(worst, float(np.max(np.abs(a - b) / (2e-10 * (1 + np.abs(b))))))
         return worst
     gv, cv = g.verification, c.verification
+    # verification's ids follow the motions it is given, which differ in the
+    # last bits: exact equality is checked on identical motions (the caller)
     out = {
         "features": fp_excess((g.features.kmin, c.features.kmin), (g.features.kmax, c.features.kmax),
                               (g.features.normal, c.features.normal)) <= 1 and
