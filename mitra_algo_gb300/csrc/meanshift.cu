@@ -19,10 +19,16 @@
 //      each member's per-iteration hit into its cluster's support counts;
 //      one launch picks each vote's winning cluster (largest count, first
 //      cluster on ties).
-// Distances and weights are the reference's FP64 expressions in its order
-// (no FMA contraction), so membership decisions match; the weighted sums use
-// a fixed warp-butterfly order (deterministic, within an ulp-level of the
-// reference's serial sum).
+// Distances, weights and products are the reference's FP64 expressions (no
+// FMA contraction), and the weighted sums add the members' contributions in
+// vote order, as the reference's serial loop does: each lane evaluates one
+// vote of a group of 32, then every lane adds the members' shuffled weights
+// and products in lane order.  The means are therefore the reference's bit
+// for bit, and so is every decision that depends on them (d^2 < h^2, the
+// stop test, the merge test): no rounding band exists to be checked.
+// Memory: seeds run in batches whose support bitmasks fit a fixed device
+// budget (the supports go to the host as sparse member lists), and the
+// members' hit counts are accumulated over batches of clusters.
 #include "common.cuh"
 #include "primitives.cuh"
 #include "rng.hpp"
@@ -78,13 +84,15 @@ __global__ void __launch_bounds__(128) trajectories(const double *desc, uint64_t
   bool converged = false, exhausted = false;
   const double stop = 1e-6 * h2;
   for (int it = 0; it < max_iter; ++it) {
-    double wt = 0, ws[D];
+    double wt = 0, ws[D];  // the same values in every lane
     for (int k = 0; k < D; ++k) ws[k] = 0;
     for (uint64_t base = 0; base < n; base += 32) {
       uint64_t j = base + lane;
       bool in = false;
+      double w = 0, x[D];
+      for (int k = 0; k < D; ++k) x[k] = 0;
       if (j < n) {
-        double x[D], dist = 0;
+        double dist = 0;
         for (int k = 0; k < D; ++k) {
           x[k] = desc[j * D + k];
           double d = mean[k] - x[k];
@@ -92,21 +100,21 @@ __global__ void __launch_bounds__(128) trajectories(const double *desc, uint64_t
         }
         if (dist < h2) {
           in = true;
-          double w = 1 - dist / h2;
-          wt += w;
-          for (int k = 0; k < D; ++k) ws[k] += w * x[k];
+          w = 1 - dist / h2;
         }
       }
+      const unsigned bits = __ballot_sync(0xffffffffu, in);
+      // the members of this group in vote order: weight, then w * x
+      for (unsigned m = bits; m; m &= m - 1) {
+        const int src = __ffs(int(m)) - 1;
+        wt += __shfl_sync(0xffffffffu, w, src);
+        for (int k = 0; k < D; ++k) ws[k] += __shfl_sync(0xffffffffu, w * x[k], src);
+      }
       if (RECORD) {
-        unsigned bits = __ballot_sync(0xffffffffu, in);
         if (lane == 0 && bits) support[si * words + base / 32] |= bits;
       } else if (in) {
         atomicAdd(&counts[crow + j], 1u);
       }
-    }
-    for (int o = 16; o; o >>= 1) {
-      wt += __shfl_xor_sync(0xffffffffu, wt, o);
-      for (int k = 0; k < D; ++k) ws[k] += __shfl_xor_sync(0xffffffffu, ws[k], o);
     }
     if (wt <= kExhausted) {
       exhausted = true;
@@ -130,20 +138,25 @@ __global__ void __launch_bounds__(128) trajectories(const double *desc, uint64_t
   }
 }
 
-// Winner per vote: the cluster (in creation order) with the largest count,
-// the first one on ties; -1 if no cluster counted the vote.
+// Winner per vote over one batch of clusters (in creation order): the
+// cluster with the largest count so far, the earliest one on ties (a later
+// cluster must count strictly more); best/winner carry over batches.
 __global__ void winners(const uint32_t *counts, uint64_t nclusters, uint64_t n,
-                        const int32_t *cluster_id, int32_t *winner) {
+                        const int32_t *cluster_id, uint32_t *best, int32_t *winner) {
   uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (j >= n) return;
-  uint32_t best = 0;
-  int32_t w = -1;
+  uint32_t b = best[j];
+  int32_t w = winner[j];
   for (uint64_t c = 0; c < nclusters; ++c) {
     uint32_t v = counts[c * n + j];
-    if (v > best) best = v, w = cluster_id[c];
+    if (v > b) b = v, w = cluster_id[c];
   }
-  winner[j] = w;
+  best[j] = b, winner[j] = w;
 }
+
+// Device bytes for one batch of seeds' support bitmasks, and for one batch
+// of clusters' hit counts.
+constexpr uint64_t kBatchBytes = uint64_t(1) << 30;
 
 struct KindData {
   int dim = 0;
@@ -152,7 +165,8 @@ struct KindData {
   double *desc = nullptr;            // device AoS
   std::vector<double> mean;          // n x dim final means
   std::vector<uint8_t> flags;        // bit0 converged, bit1 exhausted
-  std::vector<uint32_t> support;     // n x words
+  std::vector<uint64_t> sup_off;     // n + 1: each seed's support (kind-local
+  std::vector<uint32_t> sup_idx;     //   member ids, ascending)
 };
 
 template <int D>
@@ -160,68 +174,82 @@ void run_all_seeds(Call &call, KindData &k, double h2, int max_iter) {
   if (!k.n) return;
   cudaStream_t st = call.stream();
   k.words = (k.n + 31) / 32;
-  int32_t *seeds = call.alloc<int32_t>(k.n);
-  std::vector<int32_t> iota(k.n);
-  for (uint64_t i = 0; i < k.n; ++i) iota[i] = int32_t(i);
-  call.h2d(seeds, iota.data(), k.n * 4);
-  double *mean = call.alloc<double>(k.n * D);
-  uint8_t *flags = call.alloc<uint8_t>(k.n);
-  uint32_t *support = call.alloc<uint32_t>(k.n * k.words);
-  SYM_CUDA(cudaMemsetAsync(support, 0, k.n * k.words * 4, st));
-  unsigned blocks = unsigned((k.n * 32 + 127) / 128);
-  trajectories<D, true><<<blocks, 128, 0, st>>>(k.desc, k.n, seeds, nullptr, k.n, h2, max_iter,
-                                                mean, flags, support, k.words, nullptr);
-  check_launch();
-  call.launched();
+  const uint64_t batch = std::max<uint64_t>(1, std::min<uint64_t>(k.n, kBatchBytes / (k.words * 4)));
+  int32_t *seeds = call.alloc<int32_t>(batch);
+  double *mean = call.alloc<double>(batch * D);
+  uint8_t *flags = call.alloc<uint8_t>(batch);
+  uint32_t *support = call.alloc<uint32_t>(batch * k.words);
   k.mean.resize(k.n * D);
   k.flags.resize(k.n);
-  k.support.resize(k.n * k.words);
-  call.d2h(k.mean.data(), mean, k.n * D * 8);
-  call.d2h(k.flags.data(), flags, k.n);
-  call.d2h(k.support.data(), support, k.n * k.words * 4);
+  k.sup_off.assign(1, 0);
+  k.sup_idx.clear();
+  std::vector<int32_t> iota(batch);
+  std::vector<uint32_t> rows(batch * k.words);
+  for (uint64_t first = 0; first < k.n; first += batch) {
+    const uint64_t cnt = std::min(batch, k.n - first);
+    for (uint64_t i = 0; i < cnt; ++i) iota[i] = int32_t(first + i);
+    call.h2d(seeds, iota.data(), cnt * 4);
+    SYM_CUDA(cudaMemsetAsync(support, 0, cnt * k.words * 4, st));
+    const unsigned blocks = unsigned((cnt * 32 + 127) / 128);
+    trajectories<D, true><<<blocks, 128, 0, st>>>(k.desc, k.n, seeds, nullptr, cnt, h2, max_iter,
+                                                  mean, flags, support, k.words, nullptr);
+    check_launch();
+    call.launched();
+    call.d2h(k.mean.data() + first * D, mean, cnt * D * 8);
+    call.d2h(k.flags.data() + first, flags, cnt);
+    call.d2h(rows.data(), support, cnt * k.words * 4);
+    call.sync();
+    for (uint64_t i = 0; i < cnt; ++i) {
+      const uint32_t *row = &rows[i * k.words];
+      for (uint64_t w = 0; w < k.words; ++w)
+        for (uint32_t m = row[w]; m; m &= m - 1)
+          k.sup_idx.push_back(uint32_t(w * 32 + __builtin_ctz(m)));
+      k.sup_off.push_back(k.sup_idx.size());
+    }
+  }
 }
 
 struct Center {
   double v[12];
   int kind;                    // index into kinds[]
-  std::vector<uint32_t> keys;  // union of supports, kind-local bitmask
+  std::vector<uint64_t> keys;  // union of supports, kind-local bitmask
   uint64_t key_count = 0;
   std::vector<int32_t> seeds;  // kind-local seeds merged into this cluster
 };
 
-uint64_t popcount_row(const uint32_t *row, uint64_t words) {
-  uint64_t c = 0;
-  for (uint64_t w = 0; w < words; ++w) c += __builtin_popcount(row[w]);
-  return c;
-}
-
 template <int D>
 void count_members(Call &call, KindData &k, const std::vector<Center> &centers, int kind_index,
                    double h2, int max_iter, std::vector<int32_t> &winner_global) {
-  std::vector<int32_t> seeds, cluster, cluster_ids;
-  for (size_t c = 0; c < centers.size(); ++c) {
-    if (centers[c].kind != kind_index) continue;
-    int32_t local = int32_t(cluster_ids.size());
-    cluster_ids.push_back(int32_t(c));
-    for (int32_t s : centers[c].seeds) seeds.push_back(s), cluster.push_back(local);
-  }
-  if (seeds.empty()) return;
-  uint64_t nc = cluster_ids.size();
+  std::vector<int32_t> cluster_ids;
+  for (size_t c = 0; c < centers.size(); ++c)
+    if (centers[c].kind == kind_index) cluster_ids.push_back(int32_t(c));
+  if (cluster_ids.empty()) return;
   cudaStream_t st = call.stream();
-  uint64_t cells = nc * k.n;
-  uint32_t *counts = call.alloc<uint32_t>(cells);
-  SYM_CUDA(cudaMemsetAsync(counts, 0, cells * 4, st));
-  int32_t *dseeds = call.upload(seeds.data(), seeds.size());
-  int32_t *dcluster = call.upload(cluster.data(), cluster.size());
-  int32_t *dids = call.upload(cluster_ids.data(), nc);
-  unsigned blocks = unsigned((seeds.size() * 32 + 127) / 128);
-  trajectories<D, false><<<blocks, 128, 0, st>>>(k.desc, k.n, dseeds, dcluster, seeds.size(), h2,
-                                                 max_iter, nullptr, nullptr, nullptr, 0, counts);
-  check_launch();
+  const uint64_t batch = std::max<uint64_t>(1, std::min<uint64_t>(cluster_ids.size(),
+                                                                   kBatchBytes / (k.n * 4)));
+  uint32_t *counts = call.alloc<uint32_t>(batch * k.n);
+  uint32_t *best = call.alloc<uint32_t>(k.n);
   int32_t *win = call.alloc<int32_t>(k.n);
-  winners<<<blocks_for(k.n), kThreads, 0, st>>>(counts, nc, k.n, dids, win);
-  check_launch();
-  call.launched(2);
+  SYM_CUDA(cudaMemsetAsync(best, 0, k.n * 4, st));
+  SYM_CUDA(cudaMemsetAsync(win, 0xff, k.n * 4, st));  // -1: no cluster counted the vote
+  for (uint64_t first = 0; first < cluster_ids.size(); first += batch) {
+    const uint64_t nc = std::min<uint64_t>(batch, cluster_ids.size() - first);
+    std::vector<int32_t> seeds, cluster;
+    for (uint64_t c = 0; c < nc; ++c)
+      for (int32_t s : centers[cluster_ids[first + c]].seeds)
+        seeds.push_back(s), cluster.push_back(int32_t(c));
+    SYM_CUDA(cudaMemsetAsync(counts, 0, nc * k.n * 4, st));
+    int32_t *dseeds = call.upload(seeds.data(), seeds.size());
+    int32_t *dcluster = call.upload(cluster.data(), cluster.size());
+    int32_t *dids = call.upload(cluster_ids.data() + first, nc);
+    const unsigned blocks = unsigned((seeds.size() * 32 + 127) / 128);
+    trajectories<D, false><<<blocks, 128, 0, st>>>(k.desc, k.n, dseeds, dcluster, seeds.size(), h2,
+                                                   max_iter, nullptr, nullptr, nullptr, 0, counts);
+    check_launch();
+    winners<<<blocks_for(k.n), kThreads, 0, st>>>(counts, nc, k.n, dids, best, win);
+    check_launch();
+    call.launched(2);
+  }
   std::vector<int32_t> local(k.n);
   call.d2h(local.data(), win, k.n * 4);
   call.sync();
@@ -304,39 +332,45 @@ void clustering_host(Call &call, const sym_votes_view &votes, const sym_model_co
     int t = kind_of[seed];
     KindData &k = kinds[t];
     uint64_t s = uint64_t(local_of[seed]);
-    const uint32_t *row = &k.support[s * k.words];
-    for (uint64_t w = 0; w < k.words; ++w)
-      for (uint32_t m = row[w]; m; m &= m - 1) visit(uint64_t(k.ids[w * 32 + __builtin_ctz(m)]));
+    const uint32_t *members = k.sup_idx.data() + k.sup_off[s];
+    const uint64_t size = k.sup_off[s + 1] - k.sup_off[s];
+    for (uint64_t m = 0; m < size; ++m) visit(uint64_t(k.ids[members[m]]));
     bool converged = k.flags[s] & 1, exhausted = k.flags[s] & 2;
     if (exhausted) visit(seed);
     if (!converged) ++limited;
     const double *mean = &k.mean[s * k.dim];
-    uint64_t size = popcount_row(row, k.words);
     int merge = -1;
     for (size_t c = 0; c < centers.size(); ++c)
       if (centers[c].kind == t && desc_d2(mean, centers[c].v, k.dim) < h2 / 4) {
         merge = int(c);
         break;
       }
+    auto add_keys = [&](Center &c) {  // the support's members into the union
+      uint64_t added = 0;
+      for (uint64_t m = 0; m < size; ++m) {
+        uint64_t &w = c.keys[members[m] >> 6];
+        const uint64_t bit = uint64_t(1) << (members[m] & 63);
+        if (!(w & bit)) w |= bit, ++added;
+      }
+      c.key_count += added;
+      return added;
+    };
     if (merge < 0) {
       Center c;
       for (int i = 0; i < 12; ++i) c.v[i] = i < k.dim ? mean[i] : 0;
       c.kind = t;
-      c.keys.assign(row, row + k.words);
-      c.key_count = size;
+      c.keys.assign((k.n + 63) / 64, 0);
+      add_keys(c);
       c.seeds.push_back(int32_t(s));
-      support_entries += size;
+      support_entries += c.key_count;
       centers.push_back(std::move(c));
     } else {
       Center &c = centers[merge];
       double old = double(c.key_count), now = double(size);
       if (old + now > 0)
         for (int i = 0; i < k.dim; ++i) c.v[i] = (old * c.v[i] + now * mean[i]) / (old + now);
-      uint64_t before = c.key_count;
-      for (uint64_t w = 0; w < k.words; ++w) c.keys[w] |= row[w];
-      c.key_count = popcount_row(c.keys.data(), k.words);
+      support_entries += add_keys(c);
       c.seeds.push_back(int32_t(s));
-      support_entries += c.key_count - before;
     }
     if (support_entries > 5000000)
       fail(SYM_RUNTIME_ERROR, "Mean-shift support budget exceeded; lower --sample-ratio");

@@ -36,6 +36,9 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 
+sys.path.insert(0, str(ROOT / "tests"))
+
+from helpers import large_clustering_votes, lattice_clustering_votes  # noqa: E402
 from mitra_algo_gb300.mesh import mirrored_heightfield  # noqa: E402
 from oracle import oracle, symd  # noqa: E402
 
@@ -338,25 +341,57 @@ def clustering_votes(count):
 
 
 def clustering_cases():
+    """The shape of tests/cuda_clustering.cpp:12-18 at four sizes, then
+    votes on lattices whose pitch is the bandwidth and the bandwidth times
+    1 +- 1e-15: neighbours at a squared distance within a few units of
+    rounding of h^2, where the reference's strict d^2 < h^2 is decided by
+    the FP64 rounding."""
     record = {}
     idx = 0
+
+    def add(name, votes, **opts):
+        nonlocal idx
+        inputs = {**votes, "box_size": np.array([10.0]), "center": np.zeros(3), **options(**opts)}
+        out = oracle.run_reference("clustering", inputs)
+        p = f"c{idx}_"
+        record[p + "name"] = np.array(name)
+        for k, val in inputs.items():
+            record[p + "in_" + k] = val
+        for k, val in out.items():
+            record[p + k] = np.array(symd.text(out, k)) if k.startswith(("rng", "error")) else val
+        print(f"  clustering {name}: {out['cl_reflection'].size} clusters")
+        idx += 1
+
     for count in [0, 1, 64, 2048]:
         for iters in [1, 100]:
-            inputs = {**clustering_votes(count), "box_size": np.array([10.0]),
-                      "center": np.zeros(3),
-                      **options(bandwidth=0.03, max_clusters=4, max_iterations=iters, seed=42)}
-            out = oracle.run_reference("clustering", inputs)
-            p = f"c{idx}_"
-            record[p + "name"] = np.array(f"votes{count}_iters{iters}")
-            for k, val in inputs.items():
-                record[p + "in_" + k] = val
-            for k, val in out.items():
-                record[p + k] = np.array(symd.text(out, k)) if k.startswith(("rng", "error")) else val
-            print(f"  clustering votes={count} iters={iters}: "
-                  f"{out['cl_reflection'].size} clusters")
-            idx += 1
+            add(f"votes{count}_iters{iters}", clustering_votes(count), bandwidth=0.03,
+                max_clusters=4, max_iterations=iters, seed=42)
+    for name, scale in (("lattice_h", 1.0), ("lattice_h_plus", 1 + 1e-15),
+                        ("lattice_h_minus", 1 - 1e-15)):
+        add(name, lattice_clustering_votes(0.03 * scale), bandwidth=0.03, max_clusters=50,
+            max_iterations=100, seed=42)
     record["count"] = np.array(idx)
     save("stage_clustering", record)
+
+
+def clustering_large_case():
+    """100,000 votes regenerated from integers by
+    tests/helpers.py:large_clustering_votes (not stored): the reference's
+    memberships (as a digest), cluster sizes, records, RNG state."""
+    votes = large_clustering_votes()
+    inputs = {**votes, "box_size": np.array([10.0]), "center": np.zeros(3),
+              **options(bandwidth=0.03, max_clusters=20, max_iterations=100, seed=42)}
+    out = oracle.run_reference("clustering", inputs)
+    rec = {"votes": np.array(votes["vote_kind"].size), "generator_seed": np.array(7),
+           "bandwidth": np.array(0.03), "max_clusters": np.array(20),
+           "max_iterations": np.array(100), "seed": np.array(42),
+           "sha_cl_vote_indices": np.array(digest(out["cl_vote_indices"]))}
+    for k, val in out.items():
+        if k == "cl_vote_indices":
+            continue
+        rec[k] = np.array(symd.text(out, k)) if k.startswith(("rng", "error")) else val
+    print(f"  clustering large: {out['cl_reflection'].size} clusters")
+    save("stage_clustering_large", rec)
 
 
 def verification_cases():
@@ -498,6 +533,10 @@ def rng_case():
 
 if __name__ == "__main__":
     oracle.build(reference=True)
+    if sys.argv[1:] == ["clustering"]:  # only the clustering fixtures
+        clustering_cases()
+        clustering_large_case()
+        sys.exit(0)
     rng_case()
     triangle_cases()
     select_cases()
@@ -505,6 +544,7 @@ if __name__ == "__main__":
     pairing_cases()
     transformation_cases()
     clustering_cases()
+    clustering_large_case()
     verification_cases()
     examples()
     export_cases()

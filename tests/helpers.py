@@ -125,3 +125,94 @@ def verification_arrays(v):
             "ver_patches_a_indices": v.patches_a.indices, "ver_patches_b_groups": v.patches_b_groups,
             "ver_patches_b_offsets": v.patches_b.offsets, "ver_patches_b_indices": v.patches_b.indices,
             "ver_coverage": v.coverage, "ver_rms": v.rms}
+
+
+def lattice_clustering_votes(spacing):
+    """Votes on lattices of pitch `spacing`: rigid votes on a 13 x 13 grid
+    in descriptor entries 9 and 10 and reflection votes on a chain of 25 in
+    entry 3.  With the pitch at the bandwidth, a seed's lattice neighbours
+    lie at a squared distance within a few units of rounding of h^2, so the
+    reference's strict d^2 < h^2 decides by the FP64 rounding of the
+    distances.  Columns as the golden fixtures store votes."""
+    rigid = [(i, j) for i in range(13) for j in range(13)]
+    refl = list(range(25))
+    q = len(rigid) + len(refl)
+    kind = np.array([0] * len(rigid) + [1] * len(refl), np.uint8)
+    rot = np.zeros((9, q))
+    desc = np.zeros((12, q))
+    tr = np.zeros((3, q))
+    pn = np.zeros((3, q))
+    off = np.zeros(q)
+    ident = np.eye(3).reshape(-1)
+    for v, (i, j) in enumerate(rigid):
+        rot[:, v] = ident
+        desc[:9, v] = ident / 2
+        desc[9, v] = 0.2 + i * spacing
+        desc[10, v] = -0.1 + j * spacing
+        tr[:, v] = [desc[9, v] * 10, desc[10, v] * 10, 0]
+    for u, i in enumerate(refl):
+        v = len(rigid) + u
+        rot[:, v] = np.diag([-1.0, 1, 1]).reshape(-1)
+        pn[:, v] = [1, 0, 0]
+        off[v] = 0.5 + i * spacing * 10
+        tr[:, v] = [-2 * off[v], 0, 0]
+        desc[:4, v] = [1, 0, 0, 0.05 + i * spacing]
+    return {"vote_pair": np.arange(q, dtype=np.int32), "vote_kind": kind,
+            **{f"rot{k}": rot[k] for k in range(9)}, "tx": tr[0], "ty": tr[1], "tz": tr[2],
+            "pnx": pn[0], "pny": pn[1], "pnz": pn[2], "poff": off,
+            **{f"desc{k}": desc[k] for k in range(12)}}
+
+
+def _mix64(z):
+    """splitmix64 finaliser on uint64 arrays (wrapping integer arithmetic,
+    the same bits on every machine)."""
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def large_clustering_votes(q=100_000, modes=8, outliers=200, seed=7):
+    """A large vote set, regenerated bit for bit anywhere from integers:
+    `modes` clusters (the first 3 reflection votes, the others rigid) with
+    offsets uniform in [-0.005, 0.005) in every descriptor entry, and
+    `outliers` votes spread over a wide range.  Uniform values are 20-bit
+    integers over 2^20, exact in FP64.  Columns as the golden fixtures store
+    votes."""
+    with np.errstate(over="ignore"):
+        i = np.arange(q, dtype=np.uint64)
+        base = np.uint64(seed) * np.uint64(0x632BE59BD9B4E019)
+
+        def uniform(k):  # (q,) values k/2^20 in [0, 1), stream k
+            z = _mix64(i * np.uint64(16) + np.uint64(k) + base)
+            return (z >> np.uint64(44)).astype(np.float64) / 1048576.0
+        mode = (i % np.uint64(modes)).astype(np.int64)
+        outlier = np.zeros(q, bool)
+        outlier[(_mix64(i + base) % np.uint64(q)).astype(np.int64)[:outliers]] = True
+        kind = (mode < 3).astype(np.uint8)
+        desc = np.zeros((12, q))
+        for k in range(12):
+            desc[k] = (uniform(k) - 0.5) * 0.01
+        ident = np.eye(3).reshape(-1)
+        rot = np.zeros((9, q))
+        for k in range(9):
+            rot[k] = np.where(kind == 1, np.diag([-1.0, 1, 1]).reshape(-1)[k], ident[k])
+        centre = 0.25 * mode
+        desc[3] = np.where(kind == 1, 0.1 + centre + desc[3], desc[3])
+        desc[:3] = np.where(kind == 1, np.array([[1.0], [0.0], [0.0]]) + desc[:3], desc[:3])
+        for k in range(9):
+            desc[k] = np.where(kind == 0, ident[k] / 2 + desc[k], desc[k])
+        desc[9] = np.where(kind == 0, centre + desc[9], desc[9])
+        wide = (uniform(12) - 0.5) * 40.0
+        desc[9] = np.where(outlier & (kind == 0), wide, desc[9])
+        desc[3] = np.where(outlier & (kind == 1), wide, desc[3])
+        desc[4:] = np.where(kind == 1, 0.0, desc[4:])
+        tr = np.zeros((3, q))
+        tr[0] = np.where(kind == 0, desc[9] * 10, -2 * desc[3] * 10)
+        pn = np.zeros((3, q))
+        pn[0] = np.where(kind == 1, 1.0, 0.0)
+        off = np.where(kind == 1, desc[3] * 10, 0.0)
+    return {"vote_pair": np.arange(q, dtype=np.int32), "vote_kind": kind,
+            **{f"rot{k}": rot[k] for k in range(9)}, "tx": tr[0], "ty": tr[1], "tz": tr[2],
+            "pnx": pn[0], "pny": pn[1], "pnz": pn[2], "poff": off,
+            **{f"desc{k}": desc[k] for k in range(12)}}

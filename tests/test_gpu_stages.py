@@ -215,12 +215,35 @@ def test_clustering(gpu, case):
     same_array(c.votes.offsets, want["cl_vote_offsets"], "offsets")
     same_array(c.votes.indices, want["cl_vote_indices"], "indices")
     same_array(c.reflection, want["cl_reflection"], "reflection")
+    # the means add the members in the reference's order, so the cluster
+    # records are the reference's bit for bit
     for k in ["cl_rotation", "cl_translation", "cl_plane_normal", "cl_plane_offset"]:
-        close(want[k], cluster_arrays(c)[k])
+        same_array(cluster_arrays(c)[k], want[k], k)
     rng2 = Rng(int(d["seed"][0]))
     again = gpu.clustering(votes, context_from(d), options_from(d), rng2)
     same_array(again.votes.indices, c.votes.indices)
     same_array(again.rotation, c.rotation)
+
+
+def test_clustering_large(gpu):
+    """100,000 votes (regenerated from integers, tests/helpers.py): the
+    reference's memberships, cluster order, records and RNG state; the
+    trajectories of every vote run in seed batches of bounded device
+    memory."""
+    from helpers import digest, large_clustering_votes
+    g = load_golden("stage_clustering_large")
+    votes = large_clustering_votes(int(g["votes"]), seed=int(g["generator_seed"]))
+    o = Options(bandwidth=float(g["bandwidth"]), max_clusters=int(g["max_clusters"]),
+                max_iterations=int(g["max_iterations"]))
+    rng = Rng(int(g["seed"]))
+    c = gpu.clustering(votes_from(votes), ModelContext(10.0, (0.0, 0.0, 0.0)), o, rng)
+    got = cluster_arrays(c)
+    assert digest(got["cl_vote_indices"]) == str(g["sha_cl_vote_indices"])
+    for k in ("cl_vote_offsets", "cl_reflection", "cl_rotation", "cl_translation",
+              "cl_plane_normal", "cl_plane_offset"):
+        same_array(got[k], g[k], k)
+    assert c.limited_iterations == int(g["limited_iterations"][0])
+    assert rng.text() == str(g["rng_after_clustering"])
 
 
 # ------------------------------------------------------------- verification

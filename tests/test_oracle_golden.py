@@ -105,6 +105,26 @@ def test_clustering(case, oracle_backend):
     assert rng.text() == str(case["out"]["rng_after_clustering"])
 
 
+def test_clustering_large(oracle_backend):
+    """100,000 regenerated votes (tests/helpers.py:large_clustering_votes)
+    against the reference's clustering of them."""
+    from helpers import digest, large_clustering_votes
+    from mitra_algo_gb300.types import ModelContext, Options
+    g = load_golden("stage_clustering_large")
+    votes = large_clustering_votes(int(g["votes"]), seed=int(g["generator_seed"]))
+    o = Options(bandwidth=float(g["bandwidth"]), max_clusters=int(g["max_clusters"]),
+                max_iterations=int(g["max_iterations"]))
+    rng = oracle.rng(int(g["seed"]))
+    c = oracle_backend.clustering(votes_from(votes), ModelContext(10.0, (0.0, 0.0, 0.0)), o, rng)
+    got = cluster_arrays(c)
+    assert digest(got["cl_vote_indices"]) == str(g["sha_cl_vote_indices"])
+    for k in ("cl_vote_offsets", "cl_reflection", "cl_rotation", "cl_translation",
+              "cl_plane_normal", "cl_plane_offset"):
+        assert np.array_equal(got[k], g[k]), k
+    assert c.limited_iterations == int(g["limited_iterations"][0])
+    assert rng.text() == str(g["rng_after_clustering"])
+
+
 @pytest.mark.parametrize("case", golden_cases("stage_verification"), ids=lambda c: c["name"])
 def test_verification(case, oracle_backend):
     d = case["in"]
