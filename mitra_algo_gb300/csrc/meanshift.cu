@@ -35,6 +35,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <unordered_map>
 #include <vector>
 
 namespace sym {
@@ -59,6 +60,11 @@ __global__ void gather_desc(const double *lanes, uint64_t q, const int32_t *ids,
   for (int k = 0; k < D; ++k) out[j * D + k] = lanes[uint64_t(k) * q + v];
 }
 
+__global__ void round_desc(const double *desc, uint64_t n, float *out) {
+  uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = float(desc[i]);
+}
+
 template <int D>
 struct Traj {
   double mean[D];
@@ -67,8 +73,16 @@ struct Traj {
 
 // One trajectory per warp.  RECORD: write the support bitmask row; else add
 // every member hit to counts[cluster * n + j].
+//
+// Culling: `desc32` holds the descriptors rounded to FP32 and `reach` the
+// bandwidth plus a bound on how far an FP32 distance can fall below the FP64
+// one (the rounding of the mean and of every coordinate, D times 2^-22 of the
+// largest coordinate magnitude, and of the FP32 arithmetic).  A vote whose
+// FP32 squared distance exceeds reach^2 lies outside the bandwidth in FP64
+// as well; only the others take the reference's FP64 test.
 template <int D, bool RECORD>
-__global__ void __launch_bounds__(128) trajectories(const double *desc, uint64_t n,
+__global__ void __launch_bounds__(128) trajectories(const double *desc, const float *desc32,
+                                                    float reach, uint64_t n,
                                                     const int32_t *seeds, const int32_t *cluster,
                                                     uint64_t nseeds, double h2, int max_iter,
                                                     double *final_mean, uint8_t *flags,
@@ -86,12 +100,24 @@ __global__ void __launch_bounds__(128) trajectories(const double *desc, uint64_t
   for (int it = 0; it < max_iter; ++it) {
     double wt = 0, ws[D];  // the same values in every lane
     for (int k = 0; k < D; ++k) ws[k] = 0;
+    float mean32[D];
+    for (int k = 0; k < D; ++k) mean32[k] = float(mean[k]);
+    const float reach2 = reach * reach;
     for (uint64_t base = 0; base < n; base += 32) {
       uint64_t j = base + lane;
       bool in = false;
       double w = 0, x[D];
       for (int k = 0; k < D; ++k) x[k] = 0;
+      bool near = false;
       if (j < n) {
+        float d32 = 0;
+        for (int k = 0; k < D; ++k) {
+          const float e = mean32[k] - desc32[j * D + k];
+          d32 += e * e;
+        }
+        near = !(d32 > reach2);
+      }
+      if (near) {
         double dist = 0;
         for (int k = 0; k < D; ++k) {
           x[k] = desc[j * D + k];
@@ -163,6 +189,8 @@ struct KindData {
   uint64_t n = 0, words = 0;
   std::vector<int32_t> ids;          // global vote id of each local index
   double *desc = nullptr;            // device AoS
+  float *desc32 = nullptr;           // the same rounded to FP32
+  float reach = 0;                   // the culling radius (trajectories)
   std::vector<double> mean;          // n x dim final means
   std::vector<uint8_t> flags;        // bit0 converged, bit1 exhausted
   std::vector<uint64_t> sup_off;     // n + 1: each seed's support (kind-local
@@ -191,7 +219,8 @@ void run_all_seeds(Call &call, KindData &k, double h2, int max_iter) {
     call.h2d(seeds, iota.data(), cnt * 4);
     SYM_CUDA(cudaMemsetAsync(support, 0, cnt * k.words * 4, st));
     const unsigned blocks = unsigned((cnt * 32 + 127) / 128);
-    trajectories<D, true><<<blocks, 128, 0, st>>>(k.desc, k.n, seeds, nullptr, cnt, h2, max_iter,
+    trajectories<D, true><<<blocks, 128, 0, st>>>(k.desc, k.desc32, k.reach, k.n, seeds, nullptr,
+                                                  cnt, h2, max_iter,
                                                   mean, flags, support, k.words, nullptr);
     check_launch();
     call.launched();
@@ -243,7 +272,8 @@ void count_members(Call &call, KindData &k, const std::vector<Center> &centers, 
     int32_t *dcluster = call.upload(cluster.data(), cluster.size());
     int32_t *dids = call.upload(cluster_ids.data() + first, nc);
     const unsigned blocks = unsigned((seeds.size() * 32 + 127) / 128);
-    trajectories<D, false><<<blocks, 128, 0, st>>>(k.desc, k.n, dseeds, dcluster, seeds.size(), h2,
+    trajectories<D, false><<<blocks, 128, 0, st>>>(k.desc, k.desc32, k.reach, k.n, dseeds,
+                                                   dcluster, seeds.size(), h2,
                                                    max_iter, nullptr, nullptr, nullptr, 0, counts);
     check_launch();
     winners<<<blocks_for(k.n), kThreads, 0, st>>>(counts, nc, k.n, dids, best, win);
@@ -255,6 +285,64 @@ void count_members(Call &call, KindData &k, const std::vector<Center> &centers, 
   call.sync();
   for (uint64_t j = 0; j < k.n; ++j) winner_global[k.ids[j]] = local[j];
 }
+
+// Index of the centers for the merge test (clustering.cpp:68-73: the first
+// center, in creation order, of the same kind within h/2).  A center within
+// h/2 lies within h/2 in every coordinate, so on three coordinates it falls
+// in one of the 27 cells of pitch slightly above h/2 around the mean; the
+// lowest-numbered center among those that pass the reference's test is the
+// reference's choice.  Centers with coordinates too large for the grid stay
+// in a list that every query scans.
+class CenterGrid {
+public:
+  CenterGrid(double h, const int dims[3]) : scale_(2.0 / h * (1 - 1e-9)) {
+    for (int i = 0; i < 3; ++i) dims_[i] = dims[i];
+  }
+  void insert(int32_t id, const double *v) {
+    uint64_t key;
+    if (cell(v, 0, 0, 0, key)) map_[key].push_back(id);
+    else loose_.push_back(id);
+  }
+  void erase(int32_t id, const double *v) {
+    uint64_t key;
+    std::vector<int32_t> &list = cell(v, 0, 0, 0, key) ? map_[key] : loose_;
+    list.erase(std::find(list.begin(), list.end(), id));
+  }
+  template <class Test>
+  int32_t first(const double *v, Test &&passes) const {
+    int32_t best = -1;
+    auto scan = [&](const std::vector<int32_t> &list) {
+      for (int32_t id : list)
+        if ((best < 0 || id < best) && passes(id)) best = id;
+    };
+    scan(loose_);
+    uint64_t key;
+    for (int a = -1; a <= 1; ++a)
+      for (int b = -1; b <= 1; ++b)
+        for (int c = -1; c <= 1; ++c)
+          if (cell(v, a, b, c, key)) {
+            auto it = map_.find(key);
+            if (it != map_.end()) scan(it->second);
+          }
+    return best;
+  }
+
+private:
+  bool cell(const double *v, int a, int b, int c, uint64_t &key) const {
+    const int off[3] = {a, b, c};
+    key = 0;
+    for (int i = 0; i < 3; ++i) {
+      const double x = std::floor(v[dims_[i]] * scale_);
+      if (!(std::fabs(x) < double(1 << 20))) return false;
+      key = (key << 21) | uint64_t(int64_t(x) + off[i] + (1 << 20));
+    }
+    return true;
+  }
+  double scale_;
+  int dims_[3];
+  std::unordered_map<uint64_t, std::vector<int32_t>> map_;
+  std::vector<int32_t> loose_;
+};
 
 double desc_d2(const double *a, const double *b, int dim) {
   double s = 0;
@@ -297,7 +385,19 @@ void clustering_host(Call &call, const sym_votes_view &votes, const sym_model_co
       else
         gather_desc<12><<<blocks_for(k.n), kThreads, 0, call.stream()>>>(lanes, q, ids, k.n, k.desc);
       check_launch();
-      call.launched();
+      k.desc32 = call.alloc<float>(k.n * k.dim);
+      round_desc<<<blocks_for(k.n * k.dim), kThreads, 0, call.stream()>>>(k.desc, k.n * k.dim,
+                                                                         k.desc32);
+      check_launch();
+      call.launched(2);
+      // the culling radius: h plus the FP32 shortfall of a distance (rounding
+      // of mean and coordinates, 2^-24 of the largest magnitude each, and of
+      // the FP32 sums), each term taken 4 times over
+      double mag = 0;
+      for (uint64_t j = 0; j < k.n; ++j)
+        for (int c = 0; c < k.dim; ++c) mag = std::max(mag, std::fabs(votes.descriptor[c][k.ids[j]]));
+      const double reach = h + k.dim * std::ldexp(mag, -22) + (k.dim + 2) * std::ldexp(h, -22);
+      k.reach = std::isfinite(mag) && mag < 1e15 ? float(reach * (1 + 1e-6)) : INFINITY;
     }
     run_all_seeds<4>(call, kinds[0], h2, o.max_iterations);
     run_all_seeds<12>(call, kinds[1], h2, o.max_iterations);
@@ -310,6 +410,8 @@ void clustering_host(Call &call, const sym_votes_view &votes, const sym_model_co
   uint64_t unvisited = q, support_entries = 0;
   int limited = 0;
   std::vector<Center> centers;
+  const int refl_dims[3] = {1, 2, 3}, rigid_dims[3] = {9, 10, 11};
+  CenterGrid grids[2] = {CenterGrid(h, refl_dims), CenterGrid(h, rigid_dims)};
   auto visit = [&](uint64_t i) {
     uint64_t &w = visited[i >> 6];
     uint64_t bit = 1ull << (i & 63);
@@ -339,12 +441,9 @@ void clustering_host(Call &call, const sym_votes_view &votes, const sym_model_co
     if (exhausted) visit(seed);
     if (!converged) ++limited;
     const double *mean = &k.mean[s * k.dim];
-    int merge = -1;
-    for (size_t c = 0; c < centers.size(); ++c)
-      if (centers[c].kind == t && desc_d2(mean, centers[c].v, k.dim) < h2 / 4) {
-        merge = int(c);
-        break;
-      }
+    const int merge = grids[t].first(mean, [&](int32_t c) {
+      return desc_d2(mean, centers[c].v, k.dim) < h2 / 4;
+    });
     auto add_keys = [&](Center &c) {  // the support's members into the union
       uint64_t added = 0;
       for (uint64_t m = 0; m < size; ++m) {
@@ -363,12 +462,16 @@ void clustering_host(Call &call, const sym_votes_view &votes, const sym_model_co
       add_keys(c);
       c.seeds.push_back(int32_t(s));
       support_entries += c.key_count;
+      grids[t].insert(int32_t(centers.size()), c.v);
       centers.push_back(std::move(c));
     } else {
       Center &c = centers[merge];
       double old = double(c.key_count), now = double(size);
-      if (old + now > 0)
+      if (old + now > 0) {
+        grids[t].erase(merge, c.v);
         for (int i = 0; i < k.dim; ++i) c.v[i] = (old * c.v[i] + now * mean[i]) / (old + now);
+        grids[t].insert(merge, c.v);
+      }
       support_entries += add_keys(c);
       c.seeds.push_back(int32_t(s));
     }
