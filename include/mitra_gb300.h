@@ -496,6 +496,33 @@ typedef struct sym_batch_item {
 sym_status sym_detect_fast_batch(sym_context *const *workers, int32_t worker_count,
                                  sym_batch_item *items, uint64_t count);
 
+/* Fused batched detection (no reference counterpart).  Runs the stages
+ * before the mean shift mesh by mesh, then ONE mean shift for every mesh's
+ * seeds together -- each mesh's votes are moved to their own cell of a
+ * grid in vote space (pitch 8 per coordinate; votes lie within [-2, 2]), so
+ * votes of different meshes never weigh on each other's seeds, and every
+ * iteration is one launch per kernel for the whole batch -- then the modes
+ * and the verification mesh by mesh.  Each item's result is filled as
+ * sym_detect_fast fills it (its mean-shift iteration counts are the
+ * batch's).  Items must share precision, kernel, iteration counts, launch
+ * shape and bandwidth (below 2), and ask for no FP64 reference seeds; at
+ * most 4,096 items.  Items may use a sample or SYM_SAMPLE_ON_DEVICE.  An
+ * item that fails keeps its status and message and takes no part in the
+ * mean shift; the call returns the first failing item's status. */
+typedef struct sym_fused_stats {
+  uint64_t meshes, votes, seeds;
+  int32_t iterations, polish_iterations;
+  double seed_iterations, tc_evaluations;
+  /* device time (CUDA events): the stages before the mean shift over all
+   * meshes, the vote set and seeds, the approach phase, the polish, then
+   * modes and verification over all meshes */
+  double votes_ms, vote_set_ms, bulk_ms, polish_ms, modes_verification_ms;
+  uint64_t tc_launches, launches;
+  double tc_kernel_ms;
+} sym_fused_stats;
+sym_status sym_detect_fast_fused(sym_context *ctx, sym_batch_item *items, uint64_t count,
+                                 sym_fused_stats *stats);
+
 /* The mean-shift kernels of sym_detect_fast on their own (no reference
  * counterpart): K seeds over Q 6-D votes (host, q x 6 doubles), seeds are
  * vote indices.  Approach phase (at most max_iterations, in the requested

@@ -202,6 +202,16 @@ class BatchItem(C.Structure):
                 ("out", C.POINTER(FastResult)), ("status", C.c_int), ("message", C.c_char * 256)]
 
 
+class FusedStats(C.Structure):
+    _fields_ = [("meshes", C.c_uint64), ("votes", C.c_uint64), ("seeds", C.c_uint64),
+                ("iterations", C.c_int32), ("polish_iterations", C.c_int32),
+                ("seed_iterations", C.c_double), ("tc_evaluations", C.c_double),
+                ("votes_ms", C.c_double), ("vote_set_ms", C.c_double), ("bulk_ms", C.c_double),
+                ("polish_ms", C.c_double), ("modes_verification_ms", C.c_double),
+                ("tc_launches", C.c_uint64), ("launches", C.c_uint64),
+                ("tc_kernel_ms", C.c_double)]
+
+
 MS_FP32, MS_BF16_REFINED, MS_FP64 = 0, 1, 2
 STAGES = ["curvature", "prune", "pairing", "votes", "vote_sort", "mean_shift", "modes",
           "verification"]
@@ -246,6 +256,7 @@ PROTOTYPES = [
     ("sym_refine_transforms", C.c_int, [C.c_void_p, C.c_void_p, P(Options), P(ClusterRecord),
                                         C.c_uint64, C.c_int32, _d, _d, P(C.c_uint32)]),
     ("sym_detect_fast_batch", C.c_int, [P(C.c_void_p), C.c_int32, P(BatchItem), C.c_uint64]),
+    ("sym_detect_fast_fused", C.c_int, [C.c_void_p, P(BatchItem), C.c_uint64, P(FusedStats)]),
     ("sym_verification_resident", C.c_int, [C.c_void_p, C.c_void_p, P(ClustersView), P(Options),
                                             P(VerificationOut), P(C.c_uint64)]),
     ("sym_prepare", C.c_int, [C.c_void_p, P(MeshView), P(Options), P(PreparedOut)]),

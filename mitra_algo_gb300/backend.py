@@ -307,6 +307,40 @@ class Gb300Backend:
                                              C.byref(count)))
         return out[:count.value].copy()
 
+    def detect_fast_fused(self, jobs, precision="bf16", seeds=2048, seed_rng=7,
+                          max_iterations=100, polish_iterations=100, verify=True,
+                          mode="rigid", tuning=None, kernel="epanechnikov"):
+        """sym_detect_fast_fused over `jobs` = [(ResidentMesh, sample, Options), ...]
+        (a sample None is drawn on the device; `mode` may be one mode for all
+        or a list, one per job): one mean shift for every mesh's seeds.
+        Returns (one result dict per job as detect_fast gives it, the batch's
+        statistics)."""
+        modes = mode if isinstance(mode, (list, tuple)) else [mode] * len(jobs)
+        keep = []
+        items = (abi.BatchItem * max(len(jobs), 1))()
+        results = [abi.FastResult() for _ in jobs]
+        for it, (mesh, sample, options), res, md in zip(items, jobs, results, modes):
+            fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
+                                    0, verify, md, tuning=tuning, kernel=kernel)
+            opts = options.to_c()
+            keep += [fo, opts]
+            it.mesh = mesh.handle
+            if sample is None:
+                it.sample = None
+                it.sample_count = SAMPLE_ON_DEVICE
+            else:
+                sample = np.ascontiguousarray(sample, np.int32)
+                keep.append(sample)
+                it.sample = sample.ctypes.data_as(C.POINTER(C.c_int32))
+                it.sample_count = sample.size
+            it.options = C.pointer(opts)
+            it.fast = C.pointer(fo)
+            it.out = C.pointer(res)
+        stats = abi.FusedStats()
+        _check(self._lib.sym_detect_fast_fused(self._ctx, items, len(jobs), C.byref(stats)))
+        return ([self._fast_dict(r) for r in results],
+                {f: getattr(stats, f) for f, _ in abi.FusedStats._fields_})
+
     def detect_fast_batch(self, jobs, workers=4, precision="bf16", seeds=2048, seed_rng=7,
                           max_iterations=100, polish_iterations=100, verify=True,
                           mode="rigid", tuning=None) -> list:

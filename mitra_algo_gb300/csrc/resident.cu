@@ -435,14 +435,136 @@ private:
 
 // `sample` (ns host ids) is the area-weighted sample; with sample_rng set it
 // is drawn here instead, on the device from the mesh's weights (sampling.cu).
-void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t ns,
-                 const sym_options &o, const sym_fast_options &fo, sym_fast_result &r,
-                 sym_rng *sample_rng = nullptr) {
-  r = sym_fast_result{};
+// The motion of a mode position d (6-D): for a reflection vote the
+// reference's decode of a plane cluster (clustering.cpp:117-124), for a
+// rigid one the rotation exp(2 d[0..2]) and the translation that maps the
+// model centre as the centred translation d[3..5] says.
+void decode_mode(const double *d, bool reflection, const sym_model_context &model,
+                 sym_cluster_record &rec) {
+  const double *c = model.center;
+  rec = sym_cluster_record{};
+  if (reflection) {  // the reference's decode, clustering.cpp:117-124
+    const D3 nr{d[0], d[1], d[2]};
+    const double len = norm(nr);
+    const D3 n = unit(nr);
+    const double off = d[3] * model.box_size / len - dot(n, D3{c[0], c[1], c[2]});
+    const M3 R = mirror(n);
+    rec.reflection = 1;
+    rec.plane_normal[0] = n.x, rec.plane_normal[1] = n.y, rec.plane_normal[2] = n.z;
+    rec.plane_offset = off;
+    for (int j = 0; j < 9; ++j) rec.rotation[j] = R.m[j];
+    rec.translation[0] = -2 * off * n.x, rec.translation[1] = -2 * off * n.y;
+    rec.translation[2] = -2 * off * n.z;
+  } else {
+    double w[3] = {2 * d[0], 2 * d[1], 2 * d[2]}, R[9];
+    exp_map(w, R);
+    for (int j = 0; j < 9; ++j) rec.rotation[j] = R[j];
+    for (int x = 0; x < 3; ++x) {
+      double rc = R[x * 3] * c[0] + R[x * 3 + 1] * c[1] + R[x * 3 + 2] * c[2];
+      rec.translation[x] = d[3 + x] * model.box_size + c[x] - rc;
+    }
+  }
+}
+
+// Modes of one mesh from the final seed positions (host, k x 8; any
+// offset of a fused run removed): greedy merge, support counts over the
+// vote set (positions shifted by `offset` when not null), ranking by
+// support, and the top records.  Fills r.modes, r.clusters, r.records,
+// r.support and r.precise; returns the merged positions and the ranking.
+void mode_phase(Call &call, const sym_mesh_handle &h, const VoteSet &vs,
+                const std::vector<float> &means, const std::vector<uint8_t> &state, uint64_t k,
+                double h2, bool reflection, const float *offset, const sym_options &o,
+                sym_fast_result &r, std::vector<double> &mode_pos, std::vector<uint64_t> &rank) {
+  // ---- modes: greedy merge (h^2/4, first mode wins) + support
+  // Greedy merge in seed order: a seed joins the earliest-created mode within
+  // h/2 (squared distance < h^2/4).  Candidates come from a window of the
+  // modes sorted by their first coordinate.  Newton-converged seeds (a mode
+  // with a well-defined position) go first and average into their mode;
+  // the other seeds then join a mode within h/2 without moving it, or start
+  // a mode of their own (averaged only with seeds of the same kind).
+  mode_pos.clear();
+  std::vector<uint64_t> mode_seeds;
+  std::vector<uint8_t> mode_precise;
+  std::multimap<double, uint64_t> by_x;
+  const double half = 0.5 * std::sqrt(h2) * (1 + 1e-12);
+  for (int pass = 0; pass < 2; ++pass)
+    for (uint64_t i = 0; i < k; ++i) {
+      if (state[i] == kExhausted || (state[i] == kConverged) != (pass == 0)) continue;
+      bool finite = true;
+      for (int d = 0; d < 6; ++d) finite = finite && std::isfinite(means[i * 8 + d]);
+      if (!finite) continue;  // no mode (and no NaN key in the ordered index)
+      double x0 = means[i * 8];
+      int64_t hit = -1;
+      for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
+        uint64_t m = it->second;
+        if (hit >= 0 && int64_t(m) > hit) continue;
+        double d2 = 0;
+        for (int d = 0; d < 6; ++d) {
+          double e = double(means[i * 8 + d]) - mode_pos[m * 6 + d];
+          d2 += e * e;
+        }
+        if (d2 < h2 / 4) hit = int64_t(m);
+      }
+      if (hit < 0) {
+        for (int d = 0; d < 6; ++d) mode_pos.push_back(means[i * 8 + d]);
+        mode_seeds.push_back(1);
+        mode_precise.push_back(pass == 0);
+        by_x.emplace(mode_pos[(mode_seeds.size() - 1) * 6], mode_seeds.size() - 1);
+      } else if (bool(mode_precise[hit]) != (pass == 0)) {
+        ++mode_seeds[hit];  // a settled seed in a precise mode: counted, not averaged
+      } else {
+        double n = double(mode_seeds[hit]);
+        double old_x = mode_pos[hit * 6];
+        for (int d = 0; d < 6; ++d)
+          mode_pos[hit * 6 + d] = (n * mode_pos[hit * 6 + d] + means[i * 8 + d]) / (n + 1);
+        ++mode_seeds[hit];
+        auto range = by_x.equal_range(old_x);
+        for (auto it = range.first; it != range.second; ++it)
+          if (it->second == uint64_t(hit)) {
+            by_x.erase(it);
+            break;
+          }
+        by_x.emplace(mode_pos[hit * 6], uint64_t(hit));
+      }
+    }
+  uint64_t nm = mode_seeds.size();
+  r.modes = nm;
+  std::vector<uint64_t> support(nm, 0);
+  if (nm) {
+    std::vector<float> mp(nm * 8, 0.f);
+    for (uint64_t m = 0; m < nm; ++m)
+      for (int d = 0; d < 6; ++d) mp[m * 8 + d] = float(mode_pos[m * 6 + d] + (offset ? offset[d] : 0.f));
+    float *dmodes = call.upload(mp.data(), mp.size());
+    unsigned long long *dsup = call.alloc<unsigned long long>(nm);
+    count_within(call, vs, dmodes, nm, h2, dsup);
+    call.d2h(support.data(), dsup, nm * 8);
+    call.sync();
+  }
+  rank.assign(nm, 0);
+  for (uint64_t m = 0; m < nm; ++m) rank[m] = m;
+  std::stable_sort(rank.begin(), rank.end(), [&](uint64_t a, uint64_t b) { return support[a] > support[b]; });
+  uint64_t nc = std::min<uint64_t>({nm, uint64_t(std::max(o.max_clusters, 0)), SYM_FAST_MAX_CLUSTERS});
+  r.clusters = nc;
+  for (uint64_t i = 0; i < nc; ++i) {
+    decode_mode(&mode_pos[rank[i] * 6], reflection, h.model, r.records[i]);
+    r.support[i] = support[rank[i]];
+    r.precise[i] = mode_precise[rank[i]];
+  }
+}
+
+// The stages before the mean shift on one resident mesh: curvature, the
+// area-weighted sample (the caller's, or drawn on the device with
+// sample_rng) and its prune, exact pairing, and the votes as 8-float records
+// (*desc_out; *desc64_out in FP64 as well when want64).  Fills the counts of
+// `r` and marks the clock at 1-4; returns the number of votes.
+uint64_t vote_phase(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t ns,
+                    const sym_options &o, const sym_fast_options &fo, sym_fast_result &r,
+                    sym_rng *sample_rng, bool want64, StageClock &clock, float **desc_out,
+                    double **desc64_out) {
   cudaStream_t st = call.stream();
-  StageClock clock(st);
   const uint64_t nv = h.nv;
-  clock.mark(0);
+  *desc_out = nullptr;
+  *desc64_out = nullptr;
   // ---- (a) curvature
   double *lanes = call.alloc<double>(11 * nv);
   uint8_t *valid = call.alloc<uint8_t>(nv);
@@ -513,11 +635,10 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
   r.votes = q;
   if (!q) {
     clock.mark(4);
-    return;
+    return 0;
   }
-  const bool want64 = fo.reference_seeds > 0;
-  float *desc_raw = call.alloc<float>(q * 8);
-  double *desc64_raw = want64 ? call.alloc<double>(q * 8) : nullptr;
+  float *desc_raw = *desc_out = call.alloc<float>(q * 8);
+  double *desc64_raw = *desc64_out = want64 ? call.alloc<double>(q * 8) : nullptr;
   const double *c = h.model.center;
   if (reflection) {
     plane_votes<float><<<blocks_for(q), kThreads, 0, st>>>(h.xyz, nv, pa, pb, plane_list, q,
@@ -542,6 +663,23 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     }
   }
   clock.mark(4);
+  return q;
+}
+
+void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t ns,
+                 const sym_options &o, const sym_fast_options &fo, sym_fast_result &r,
+                 sym_rng *sample_rng = nullptr) {
+  r = sym_fast_result{};
+  cudaStream_t st = call.stream();
+  StageClock clock(st);
+  clock.mark(0);
+  const bool reflection = fo.mode == SYM_REFLECTION;
+  const bool want64 = fo.reference_seeds > 0;
+  float *desc_raw = nullptr;
+  double *desc64_raw = nullptr;
+  const uint64_t q = vote_phase(call, h, sample, ns, o, fo, r, sample_rng, want64, clock,
+                                &desc_raw, &desc64_raw);
+  if (!q) return;
   // ---- Morton sort into chunks
   Tuning tuning;
   if (fo.vote_bits) tuning.vote_bits = fo.vote_bits;
@@ -664,105 +802,13 @@ void detect_fast(Call &call, sym_mesh_handle &h, const int32_t *sample, uint64_t
     r.mode_error_unconverged_max = open_max;
   }
   clock.mark(7);
-  // ---- modes: greedy merge (h^2/4, first mode wins) + support
-  // Greedy merge in seed order: a seed joins the earliest-created mode within
-  // h/2 (squared distance < h^2/4).  Candidates come from a window of the
-  // modes sorted by their first coordinate.  Newton-converged seeds (a mode
-  // with a well-defined position) go first and average into their mode;
-  // the other seeds then join a mode within h/2 without moving it, or start
-  // a mode of their own (averaged only with seeds of the same kind).
   std::vector<double> mode_pos;
-  std::vector<uint64_t> mode_seeds;
-  std::vector<uint8_t> mode_precise;
-  std::multimap<double, uint64_t> by_x;
-  const double half = 0.5 * std::sqrt(h2) * (1 + 1e-12);
-  for (int pass = 0; pass < 2; ++pass)
-    for (uint64_t i = 0; i < k; ++i) {
-      if (state[i] == kExhausted || (state[i] == kConverged) != (pass == 0)) continue;
-      bool finite = true;
-      for (int d = 0; d < 6; ++d) finite = finite && std::isfinite(means[i * 8 + d]);
-      if (!finite) continue;  // no mode (and no NaN key in the ordered index)
-      double x0 = means[i * 8];
-      int64_t hit = -1;
-      for (auto it = by_x.lower_bound(x0 - half); it != by_x.end() && it->first <= x0 + half; ++it) {
-        uint64_t m = it->second;
-        if (hit >= 0 && int64_t(m) > hit) continue;
-        double d2 = 0;
-        for (int d = 0; d < 6; ++d) {
-          double e = double(means[i * 8 + d]) - mode_pos[m * 6 + d];
-          d2 += e * e;
-        }
-        if (d2 < h2 / 4) hit = int64_t(m);
-      }
-      if (hit < 0) {
-        for (int d = 0; d < 6; ++d) mode_pos.push_back(means[i * 8 + d]);
-        mode_seeds.push_back(1);
-        mode_precise.push_back(pass == 0);
-        by_x.emplace(mode_pos[(mode_seeds.size() - 1) * 6], mode_seeds.size() - 1);
-      } else if (bool(mode_precise[hit]) != (pass == 0)) {
-        ++mode_seeds[hit];  // a settled seed in a precise mode: counted, not averaged
-      } else {
-        double n = double(mode_seeds[hit]);
-        double old_x = mode_pos[hit * 6];
-        for (int d = 0; d < 6; ++d)
-          mode_pos[hit * 6 + d] = (n * mode_pos[hit * 6 + d] + means[i * 8 + d]) / (n + 1);
-        ++mode_seeds[hit];
-        auto range = by_x.equal_range(old_x);
-        for (auto it = range.first; it != range.second; ++it)
-          if (it->second == uint64_t(hit)) {
-            by_x.erase(it);
-            break;
-          }
-        by_x.emplace(mode_pos[hit * 6], uint64_t(hit));
-      }
-    }
-  uint64_t nm = mode_seeds.size();
-  r.modes = nm;
-  std::vector<uint64_t> support(nm, 0);
-  if (nm) {
-    std::vector<float> mp(nm * 8, 0.f);
-    for (uint64_t m = 0; m < nm; ++m)
-      for (int d = 0; d < 6; ++d) mp[m * 8 + d] = float(mode_pos[m * 6 + d]);
-    float *dmodes = call.upload(mp.data(), mp.size());
-    unsigned long long *dsup = call.alloc<unsigned long long>(nm);
-    count_within(call, vs, dmodes, nm, h2, dsup);
-    call.d2h(support.data(), dsup, nm * 8);
-    call.sync();
-  }
-  std::vector<uint64_t> rank(nm);
-  for (uint64_t m = 0; m < nm; ++m) rank[m] = m;
-  std::stable_sort(rank.begin(), rank.end(), [&](uint64_t a, uint64_t b) { return support[a] > support[b]; });
-  uint64_t nc = std::min<uint64_t>({nm, uint64_t(std::max(o.max_clusters, 0)), SYM_FAST_MAX_CLUSTERS});
-  r.clusters = nc;
+  std::vector<uint64_t> rank;
+  mode_phase(call, h, vs, means, state, k, h2, reflection, nullptr, o, r, mode_pos, rank);
+  const uint64_t nc = r.clusters;
   auto decode = [&](const double *d, sym_cluster_record &rec) {
-    rec = sym_cluster_record{};
-    if (reflection) {  // the reference's decode, clustering.cpp:117-124
-      const D3 nr{d[0], d[1], d[2]};
-      const double len = norm(nr);
-      const D3 n = unit(nr);
-      const double off = d[3] * h.model.box_size / len - dot(n, D3{c[0], c[1], c[2]});
-      const M3 R = mirror(n);
-      rec.reflection = 1;
-      rec.plane_normal[0] = n.x, rec.plane_normal[1] = n.y, rec.plane_normal[2] = n.z;
-      rec.plane_offset = off;
-      for (int j = 0; j < 9; ++j) rec.rotation[j] = R.m[j];
-      rec.translation[0] = -2 * off * n.x, rec.translation[1] = -2 * off * n.y;
-      rec.translation[2] = -2 * off * n.z;
-    } else {
-      double w[3] = {2 * d[0], 2 * d[1], 2 * d[2]}, R[9];
-      exp_map(w, R);
-      for (int j = 0; j < 9; ++j) rec.rotation[j] = R[j];
-      for (int x = 0; x < 3; ++x) {
-        double rc = R[x * 3] * c[0] + R[x * 3 + 1] * c[1] + R[x * 3 + 2] * c[2];
-        rec.translation[x] = d[3 + x] * h.model.box_size + c[x] - rc;
-      }
-    }
+    decode_mode(d, reflection, h.model, rec);
   };
-  for (uint64_t i = 0; i < nc; ++i) {
-    decode(&mode_pos[rank[i] * 6], r.records[i]);
-    r.support[i] = support[rank[i]];
-    r.precise[i] = mode_precise[rank[i]];
-  }
   // each reported motion against FP64: the FP64 mean shift restarted from
   // the mode's position (approach and polish as above) reaches the FP64 mode
   // the GPU's approximates; the relative error of the motion [R, t / box]
@@ -870,6 +916,216 @@ uint64_t fast_votes_host(Call &call, const sym_points_view &pos, const sym_featu
   }
   call.check_status("fast_votes");
   return q;
+}
+
+// ------------------------------------------------- many meshes, one mean shift
+// Vote-space tiling: every mesh's votes (each component within [-2, 2]: a
+// rotation part of at most pi/2, a centred translation of at most 2 boxes,
+// a unit normal and an offset of at most one box) are moved by their own
+// offset on a grid of pitch 8 -- one of {-12, -4, 4, 12} per coordinate,
+// 4,096 cells -- so votes of different meshes lie at least 4 apart, beyond
+// any bandwidth below 2: their weights are exactly zero and the chunk tests
+// never pair a seed with another mesh's chunk.  One mean-shift run then
+// serves every mesh's seeds, one launch per kernel and iteration.
+constexpr uint64_t kFusedMax = 4096;
+
+void fused_offset(uint64_t i, float off[6]) {
+  static const float steps[4] = {-12.f, -4.f, 4.f, 12.f};
+  for (int d = 0; d < 6; ++d) off[d] = steps[(i >> (2 * d)) & 3];
+}
+
+__global__ void place_votes(const float *desc, uint64_t q, float o0, float o1, float o2, float o3,
+                            float o4, float o5, float *out) {
+  const uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= q) return;
+  const float off[6] = {o0, o1, o2, o3, o4, o5};
+  float x[8], n2 = 0;
+  for (int d = 0; d < 6; ++d) x[d] = desc[v * 8 + d] + off[d], n2 += x[d] * x[d];
+  x[6] = n2, x[7] = 0;
+  float4 *o = reinterpret_cast<float4 *>(out + v * 8);
+  o[0] = make_float4(x[0], x[1], x[2], x[3]);
+  o[1] = make_float4(x[4], x[5], x[6], x[7]);
+}
+
+void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fused_stats &stats) {
+  stats = sym_fused_stats{};
+  if (!count) return;
+  if (count > kFusedMax) fail(SYM_INVALID_ARGUMENT, "fused detection takes at most 4,096 meshes");
+  const sym_fast_options &f0 = *items[0].fast;
+  const double h = items[0].options->bandwidth, h2 = h * h;
+  for (uint64_t i = 0; i < count; ++i) {
+    const sym_fast_options &f = *items[i].fast;
+    if (!items[i].mesh || !items[i].options || !items[i].out)
+      fail(SYM_INVALID_ARGUMENT, "batch item without mesh, options or result");
+    if (f.precision != f0.precision || f.kernel != f0.kernel ||
+        f.max_iterations != f0.max_iterations || f.polish_iterations != f0.polish_iterations ||
+        f.vote_bits != f0.vote_bits || f.simt_blocks_per_sm != f0.simt_blocks_per_sm ||
+        f.tc_ctas_per_sm != f0.tc_ctas_per_sm || f.check_interval != f0.check_interval ||
+        items[i].options->bandwidth != h)
+      fail(SYM_INVALID_ARGUMENT, "fused detection needs one precision, kernel, iteration counts, "
+                                 "launch shape and bandwidth for every mesh");
+    if (f.reference_seeds) fail(SYM_INVALID_ARGUMENT, "fused detection runs no FP64 reference seeds");
+    if (f.kernel != SYM_KERNEL_EPANECHNIKOV && f.kernel != SYM_KERNEL_GAUSSIAN)
+      fail(SYM_INVALID_ARGUMENT, "unknown mean-shift kernel");
+  }
+  if (!(h > 0 && h < 2)) fail(SYM_INVALID_ARGUMENT, "fused detection needs a bandwidth below 2");
+  cudaStream_t st = call.stream();
+  StageClock clock(st);
+  cudaEvent_t ev[5];
+  for (auto &e : ev) SYM_CUDA(cudaEventCreate(&e));
+  SYM_CUDA(cudaEventRecord(ev[0], st));
+  // ---- the stages before the mean shift, mesh by mesh
+  struct Part {
+    float *desc = nullptr;
+    uint64_t q = 0, base = 0, k = 0, seed_base = 0;
+    bool ok = false;
+  };
+  std::vector<Part> parts(count);
+  uint64_t total = 0;
+  for (uint64_t i = 0; i < count; ++i) {
+    sym_batch_item &it = items[i];
+    sym_fast_result &r = *it.out;
+    r = sym_fast_result{};
+    it.status = SYM_OK;
+    it.message[0] = 0;
+    try {
+      sym_rng rng;
+      const bool on_device = !it.sample && it.sample_count == SYM_SAMPLE_ON_DEVICE;
+      if (on_device) {
+        validate_prepare_options(*it.options);
+        sym_rng_seed(&rng, it.options->seed);
+      } else {
+        for (uint64_t j = 0; j < it.sample_count; ++j)
+          if (it.sample[j] < 0 || uint64_t(it.sample[j]) >= it.mesh->nv)
+            fail(SYM_INVALID_ARGUMENT, "sample vertex index out of range");
+      }
+      double *unused = nullptr;
+      parts[i].q = vote_phase(call, *it.mesh, on_device ? nullptr : it.sample,
+                              on_device ? 0 : it.sample_count, *it.options, *it.fast, r,
+                              on_device ? &rng : nullptr, false, clock, &parts[i].desc, &unused);
+      parts[i].ok = true;
+      parts[i].base = total;
+      total += parts[i].q;
+    } catch (const Error &e) {
+      it.status = e.status;
+      std::snprintf(it.message, sizeof(it.message), "%s", e.what());
+    }
+  }
+  if (total > uint64_t(std::numeric_limits<int32_t>::max()))
+    fail(SYM_RUNTIME_ERROR, "Vote budget exceeded; lower --sample-ratio or tighten --pair-threshold");
+  SYM_CUDA(cudaEventRecord(ev[1], st));
+  // ---- one vote set, one seed set
+  std::vector<int64_t> seeds;
+  if (total) {
+    float *all = call.alloc<float>(total * 8);
+    for (uint64_t i = 0; i < count; ++i) {
+      Part &pt = parts[i];
+      if (!pt.q) continue;
+      float off[6];
+      fused_offset(i, off);
+      place_votes<<<blocks_for(pt.q), kThreads, 0, st>>>(pt.desc, pt.q, off[0], off[1], off[2],
+                                                         off[3], off[4], off[5],
+                                                         all + pt.base * 8);
+      check_launch();
+      call.launched();
+      pt.k = std::min<uint64_t>(uint64_t(std::max(items[i].fast->seeds, 1)), pt.q);
+      pt.seed_base = seeds.size();
+      for (int64_t v : draw_seeds(pt.q, pt.k, items[i].fast->seed_rng))
+        seeds.push_back(int64_t(pt.base) + v);
+    }
+    Tuning tuning;
+    if (f0.vote_bits) tuning.vote_bits = f0.vote_bits;
+    if (f0.simt_blocks_per_sm) tuning.simt_blocks_per_sm = f0.simt_blocks_per_sm;
+    if (f0.tc_ctas_per_sm) tuning.tc_ctas_per_sm = f0.tc_ctas_per_sm;
+    if (f0.check_interval) tuning.check_interval = f0.check_interval;
+    VoteSet vs = build_vote_set(call, all, nullptr, total, tuning);
+    vs.kernel_k = f0.kernel == SYM_KERNEL_GAUSSIAN ? kGauss2 : 0.0;
+    const uint64_t k = seeds.size();
+    int64_t *dseeds = call.upload(seeds.data(), k);
+    int64_t *seed_rank = call.alloc<int64_t>(k);
+    ranks_of<<<blocks_for(k), kThreads, 0, st>>>(vs.rank, dseeds, k, seed_rank);
+    check_launch();
+    float *m32 = call.alloc<float>(k * 8);
+    uint8_t *st32 = call.alloc<uint8_t>(k);
+    SYM_CUDA(cudaMemsetAsync(st32, 0, k, st));
+    init_means(call, vs, seed_rank, k, m32);
+    unsigned long long *evals = call.alloc<unsigned long long>(1);
+    SYM_CUDA(cudaMemsetAsync(evals, 0, 8, st));
+    SYM_CUDA(cudaEventRecord(ev[2], st));
+    int bulk = 0, polish = 0;
+    double tc_evals = 0, seed_iterations = 0;
+    const bool tensor =
+        f0.precision == SYM_MS_BF16_REFINED &&
+        meanshift_bf16_bulk(call, vs, m32, st32, k, h2, f0.max_iterations, &bulk, &tc_evals,
+                            nullptr, 0, &stats.tc_kernel_ms, &stats.tc_launches, &seed_iterations);
+    if (!tensor)
+      bulk = shift(call, vs, m32, st32, k, h2, f0.max_iterations, false, &seed_iterations, evals);
+    SYM_CUDA(cudaEventRecord(ev[3], st));
+    polish = shift(call, vs, m32, st32, k, h2, f0.polish_iterations, true, &seed_iterations, evals);
+    std::vector<float> means(k * 8);
+    std::vector<uint8_t> state(k);
+    call.d2h(means.data(), m32, k * 32);
+    call.d2h(state.data(), st32, k);
+    SYM_CUDA(cudaEventRecord(ev[4], st));
+    call.sync();
+    stats.iterations = bulk;
+    stats.polish_iterations = polish;
+    stats.tc_evaluations = tc_evals;
+    stats.seed_iterations = seed_iterations;
+    stats.votes = total;
+    stats.seeds = k;
+    // ---- modes and verification, mesh by mesh
+    for (uint64_t i = 0; i < count; ++i) {
+      Part &pt = parts[i];
+      sym_batch_item &it = items[i];
+      if (!pt.q) continue;
+      sym_fast_result &r = *it.out;
+      try {
+        float off[6];
+        fused_offset(i, off);
+        std::vector<float> mi(pt.k * 8);
+        std::vector<uint8_t> si(state.begin() + pt.seed_base, state.begin() + pt.seed_base + pt.k);
+        for (uint64_t j = 0; j < pt.k; ++j)
+          for (int d = 0; d < 8; ++d)
+            mi[j * 8 + d] = means[(pt.seed_base + j) * 8 + d] - (d < 6 ? off[d] : 0.f);
+        r.iterations = bulk;
+        r.polish_iterations = polish;
+        std::vector<double> mode_pos;
+        std::vector<uint64_t> rank;
+        mode_phase(call, *it.mesh, vs, mi, si, pt.k, h2, it.fast->mode == SYM_REFLECTION, off,
+                   *it.options, r, mode_pos, rank);
+        if (it.fast->verify && r.clusters)
+          verification_fast(call, it.mesh->surface(), r.records, r.clusters,
+                            it.options->verify_threshold * it.mesh->model.box_size,
+                            it.fast->refine, it.mesh->model.center, r.coverage, r.rms, r.patches,
+                            &r.verify_undecided, &r.verify_fp64_rows);
+      } catch (const Error &e) {
+        it.status = e.status;
+        std::snprintf(it.message, sizeof(it.message), "%s", e.what());
+      }
+    }
+  } else {
+    for (int j = 2; j < 5; ++j) SYM_CUDA(cudaEventRecord(ev[j], st));
+  }
+  cudaEvent_t done;
+  SYM_CUDA(cudaEventCreate(&done));
+  SYM_CUDA(cudaEventRecord(done, st));
+  SYM_CUDA(cudaEventSynchronize(done));
+  float t[4] = {0, 0, 0, 0};
+  cudaEventElapsedTime(&t[0], ev[0], ev[1]);
+  cudaEventElapsedTime(&t[1], ev[1], ev[2]);
+  cudaEventElapsedTime(&t[2], ev[2], ev[3]);
+  cudaEventElapsedTime(&t[3], ev[3], ev[4]);
+  float t_rest = 0;
+  cudaEventElapsedTime(&t_rest, ev[4], done);
+  stats.meshes = count;
+  stats.votes_ms = t[0];
+  stats.vote_set_ms = t[1];
+  stats.bulk_ms = t[2];
+  stats.polish_ms = t[3];
+  stats.modes_verification_ms = t_rest;
+  for (auto &e : ev) cudaEventDestroy(e);
+  cudaEventDestroy(done);
 }
 
 }  // namespace sym
@@ -1257,6 +1513,28 @@ sym_status sym_detect_fast_sampled(sym_context *ctx, sym_mesh_handle *mesh,
     sym_rng_seed(&rng, options->seed);  // the engine detect() seeds (pipeline.cpp:25)
     sym::detect_fast(call, *mesh, nullptr, 0, *options, *fast, *out, &rng);
     out->launches = ctx->metrics.current.custom_launches;
+    return SYM_OK;
+  } catch (const sym::Error &e) {
+    sym_error_text = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    sym_error_text = e.what();
+    return SYM_RUNTIME_ERROR;
+  }
+}
+
+sym_status sym_detect_fast_fused(sym_context *ctx, sym_batch_item *items, uint64_t count,
+                                 sym_fused_stats *stats) {
+  if (!ctx || (count && !items) || !stats) return SYM_INVALID_ARGUMENT;
+  try {
+    sym::Call call(ctx, "detect_fast_fused");
+    sym::detect_fast_fused(call, items, count, *stats);
+    stats->launches = ctx->metrics.current.custom_launches;
+    for (uint64_t i = 0; i < count; ++i)
+      if (items[i].status != SYM_OK) {
+        sym_error_text = items[i].message;
+        return items[i].status;
+      }
     return SYM_OK;
   } catch (const sym::Error &e) {
     sym_error_text = e.what();
