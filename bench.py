@@ -186,6 +186,166 @@ def batch_bench(gpu, n, workers):
             "results_equal": bool(same), "clock": "host wall clock, synchronous calls"}
 
 
+def _wall(fn):
+    """Host wall-clock seconds of fn() between two device synchronisations,
+    and its result."""
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, r
+
+
+def c4_leg(gpu, count=256, samples=2000, seeds=256):
+    """The uneven batch (BASELINE C4; mesh.uneven_batch): `count` meshes of
+    2k-60k vertices (icospheres, tori, mirrored height fields; 1-4 planted
+    symmetries; noise sigma in [0, 5e-3]), each loaded raw through the GPU
+    prepare and sampled on the device: meshes/s of sym_detect_fast one mesh
+    after the other, against sym_detect_fast_fused (one mean shift for every
+    mesh's seeds) in both mean-shift forms.  Host wall clock around each
+    pass after a warm-up pass; the loads are not timed."""
+    from mitra_algo_gb300.mesh import uneven_batch
+    from mitra_algo_gb300.types import Options
+    t_gen = time.perf_counter()
+    batch = uneven_batch(count)
+    jobs, modes = [], []
+    for mesh, mode, _ in batch:
+        o = Options(sample_ratio=min(1.0, samples / mesh.vertex_count),
+                    pair_threshold=0.25 if mode == "rigid" else 0.05, bandwidth=BANDWIDTH,
+                    max_pairs=10 ** 8, max_votes=2 * 10 ** 9 - 1, max_clusters=8)
+        jobs.append((gpu.load_mesh_raw(mesh, o), None, o))
+        modes.append(mode)
+    t_gen = time.perf_counter() - t_gen
+    kw = dict(seeds=seeds, max_iterations=ITERATIONS, polish_iterations=POLISH)
+
+    def loop(pr):
+        return [gpu.detect_fast(m, None, o, precision=pr, mode=md, **kw)
+                for (m, _, o), md in zip(jobs, modes)]
+
+    def fused(pr):
+        return gpu.detect_fast_fused(jobs, precision=pr, mode=modes, **kw)
+
+    fused("bf16")
+    t_fb, (rb, stats) = _wall(lambda: fused("bf16"))
+    t_ff, (rf, _) = _wall(lambda: fused("fp32"))
+    loop("bf16")
+    t_lb, rl = _wall(lambda: loop("bf16"))
+    for m, _, _ in jobs:
+        m.close()
+
+    def found(rs):  # meshes whose top mode is supported by Newton-converged seeds and covers 30%
+        return sum(1 for r in rs if r["clusters"] and r["precise"][0] and r["coverage"][0] >= 0.3)
+    same = sum(1 for a, b in zip(rl, rb) if a["pairs"] == b["pairs"] and a["votes"] == b["votes"])
+    return {"meshes": count, "vertices": [int(min(m.vertex_count for m, _, _ in batch)),
+                                          int(max(m.vertex_count for m, _, _ in batch))],
+            "samples_per_mesh": samples, "seeds_per_mesh": seeds,
+            "per_mesh_loop_meshes_per_s": round(count / t_lb, 2),
+            "fused_meshes_per_s": round(count / t_fb, 2),
+            "fused_fp32_meshes_per_s": round(count / t_ff, 2),
+            "fused_over_loop": round(t_lb / t_fb, 2), "fused_bf16_over_fp32": round(t_ff / t_fb, 2),
+            "votes": int(stats["votes"]), "approach_iterations": int(stats["iterations"]),
+            "fused_device_ms": {k: round(stats[k], 2) for k in
+                                ("votes_ms", "vote_set_ms", "bulk_ms", "polish_ms",
+                                 "modes_verification_ms")},
+            "same_pairs_and_votes": same, "top_mode_found": {"loop": found(rl), "fused": found(rb)},
+            "generate_and_load_s": round(t_gen, 1),
+            "clock": "host wall clock, synchronous calls; one warm-up pass"}
+
+
+def c5_leg(gpu, count=8, samples=10000, seeds=1024, refine=3, reference_seeds=64):
+    """The stress batch (BASELINE C5; mesh.stress_batch): `count` meshes of
+    1e5-1e6 triangles, half reflection and half rigid, 30% of each surface
+    unsymmetric relief: the full pipeline with verification and `refine`
+    FP64 ICP passes, meshes/s one mesh after the other and fused; then, per
+    mesh (untimed), the error of every reported motion and refined motion
+    against FP64 and of `reference_seeds` seeds' modes, and the share of
+    votes outside the bandwidth of every reported mode (outliers)."""
+    from mitra_algo_gb300.mesh import stress_batch
+    from mitra_algo_gb300.types import Options
+    batch = stress_batch(count)
+    jobs, modes = [], []
+    for mesh, mode in batch:
+        o = Options(sample_ratio=min(1.0, samples / mesh.vertex_count), pair_threshold=0.05,
+                    bandwidth=BANDWIDTH, max_pairs=10 ** 8, max_votes=2 * 10 ** 9 - 1,
+                    max_clusters=8)
+        jobs.append((gpu.load_mesh_raw(mesh, o), None, o))
+        modes.append(mode)
+    kw = dict(seeds=seeds, max_iterations=ITERATIONS, polish_iterations=POLISH, refine=refine)
+    gpu.detect_fast_fused(jobs, precision="bf16", mode=modes, **kw)
+    t_fused, (rf, _) = _wall(lambda: gpu.detect_fast_fused(jobs, precision="bf16", mode=modes, **kw))
+    t_loop, rl = _wall(lambda: [gpu.detect_fast(m, None, o, precision="bf16", mode=md, **kw)
+                                for (m, _, o), md in zip(jobs, modes)])
+    err = [gpu.detect_fast(m, None, o, precision="bf16", mode=md, reference_seeds=reference_seeds,
+                           **kw) for (m, _, o), md in zip(jobs, modes)]
+    for m, _, _ in jobs:
+        m.close()
+    precise_err = [x for r in err for x, ok in zip(r["transform_error"], r["precise"]) if ok]
+    outliers = [1 - min(1.0, sum(r["support"]) / max(r["votes"], 1)) for r in rl]
+    return {"meshes": count, "triangles": [int(min(m.faces.shape[1] for m, _ in batch)),
+                                           int(max(m.faces.shape[1] for m, _ in batch))],
+            "modes": modes, "samples_per_mesh": samples, "seeds_per_mesh": seeds,
+            "refine_passes": refine,
+            "per_mesh_loop_meshes_per_s": round(count / t_loop, 3),
+            "fused_meshes_per_s": round(count / t_fused, 3),
+            "votes": [int(r["votes"]) for r in rl],
+            "outlier_share": [round(x, 3) for x in outliers],
+            "error_vs_fp64": {
+                "modes_converged_max": max(r["mode_error_max"] for r in err),
+                "seeds_compared": int(sum(r["seeds_compared"] for r in err)),
+                "seeds_converged_both": int(sum(r["modes_compared"] for r in err)),
+                "transform_precise_max": max(precise_err) if precise_err else None,
+                "transform_precise_within_1e-4": sum(x <= 1e-4 for x in precise_err),
+                "transform_precise_count": len(precise_err),
+                "transform_all_max": max(r["transform_error_max"] for r in err),
+                "refined_all_max": max(r["transform_error_refined_max"] for r in err)},
+            "coverage_top": [round(r["coverage"][0], 3) if r["clusters"] else None for r in rl],
+            "clock": "host wall clock, synchronous calls; one warm-up pass"}
+
+
+def c3_leg(gpu, steps=3):
+    """The large single mesh (BASELINE C3; workload "c3"): the torus of 1e6
+    triangles with 12 rotated motif copies (2 mirrored), 200,000 samples
+    drawn on the device, votes subsampled to 1e6, 4,096 seeds: device time
+    per mesh (CUDA events) of both mean-shift forms, and the error of 256
+    reference seeds' modes and of the reported motions against FP64."""
+    import torch
+    from mitra_algo_gb300.mesh import motif_torus
+    from mitra_algo_gb300.types import Options
+    mesh = motif_torus(R=1.0, r=0.3, nu=1000, nv=500, copies=12, mirrored=2, noise=5e-4, seed=0)
+    o = Options(sample_ratio=200_000 / mesh.vertex_count, pair_threshold=0.05, bandwidth=BANDWIDTH,
+                max_pairs=10 ** 9, max_votes=2 * 10 ** 9 - 1, max_clusters=20)
+    resident = gpu.load_mesh_raw(mesh, o)
+    stream = torch.cuda.ExternalStream(gpu.stream_handle)
+    out = {"workload": "motif torus 1e6 triangles, 200,000 samples, 1e6 subsampled votes, "
+                       "4,096 seeds", "vertices": int(mesh.vertex_count)}
+    for pr in ("bf16", "fp32"):
+        kw = dict(precision=pr, seeds=4096, max_iterations=ITERATIONS, polish_iterations=POLISH,
+                  vote_cap=1_000_000)
+        e = gpu.detect_fast(resident, None, o, reference_seeds=256, **kw)
+        times = []
+        for _ in range(steps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            r = gpu.detect_fast(resident, None, o, **kw)
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        ms = statistics.mean(times[1:])
+        out[pr] = {"meshes_per_s": round(1000 / ms, 3), "ms_per_step": round(ms, 2),
+                   "pairs": int(r["pairs"]), "votes": int(r["votes"]),
+                   "stage_ms": {k: round(v, 2) for k, v in r["stage_ms"].items()},
+                   "mode_error": {"converged_both": int(e["modes_compared"]),
+                                  "max": e["mode_error_max"], "within_1e-4": int(e["modes_within"]),
+                                  "all_seeds_within_1e-4": int(e["seeds_within"]),
+                                  "reference_seeds": int(e["seeds_compared"])},
+                   "transform_error_precise_max": max(
+                       [x for x, ok in zip(e["transform_error"], e["precise"]) if ok], default=None)}
+    out["bf16_over_fp32"] = round(out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"], 3)
+    resident.close()
+    return out
+
+
 def workload(small=False, name="c2"):
     """The benchmark mesh and options; `small` is a level-5, 5,000-sample,
     256-seed variant used for profiler captures.  name "c3": the large
@@ -688,6 +848,9 @@ def run_gpu(args):
 
     gauss = gaussian_leg() if extra else None
     c1 = c1_exact(gpu) if extra else None
+    c3 = c3_leg(gpu) if extra and args.c3 else None
+    c4 = c4_leg(gpu, args.c4_meshes) if extra and args.c4_meshes else None
+    c5 = c5_leg(gpu, args.c5_meshes) if extra and args.c5_meshes else None
     if rank != 0:
         return
     r = res_bf16[-1]
@@ -791,6 +954,9 @@ def run_gpu(args):
         line["gaussian_kernel"] = gauss
     if extra:
         line["c1_exact"] = c1
+    for name, leg in (("c3", c3), ("c4", c4), ("c5", c5)):
+        if leg:
+            line[name] = leg
     if not args.no_cpu and extra:
         line["cpu_baseline"] = cpu_baseline(prepared, opts)
     print(json.dumps(line))
@@ -865,6 +1031,11 @@ def main():
     ap.add_argument("--config", choices=["c2", "c3"], default="c2",
                     help="c2: the motif icosphere (default); c3: the 1e6-triangle torus "
                          "(no batch, reflection or CPU legs)")
+    ap.add_argument("--c3", type=int, default=1, help="1: include the large-torus leg (C3)")
+    ap.add_argument("--c4-meshes", type=int, default=256,
+                    help="meshes of the uneven batch leg (C4; 0: skip)")
+    ap.add_argument("--c5-meshes", type=int, default=8,
+                    help="meshes of the stress batch leg (C5, full size 64; 0: skip)")
     ap.add_argument("--batch", type=int, default=48,
                     help="meshes of the uneven batch measurement (0: skip)")
     ap.add_argument("--batch-workers", type=int, default=4,

@@ -309,7 +309,7 @@ class Gb300Backend:
 
     def detect_fast_fused(self, jobs, precision="bf16", seeds=2048, seed_rng=7,
                           max_iterations=100, polish_iterations=100, verify=True,
-                          mode="rigid", tuning=None, kernel="epanechnikov"):
+                          mode="rigid", tuning=None, kernel="epanechnikov", refine=0):
         """sym_detect_fast_fused over `jobs` = [(ResidentMesh, sample, Options), ...]
         (a sample None is drawn on the device; `mode` may be one mode for all
         or a list, one per job): one mean shift for every mesh's seeds.
@@ -321,7 +321,7 @@ class Gb300Backend:
         results = [abi.FastResult() for _ in jobs]
         for it, (mesh, sample, options), res, md in zip(items, jobs, results, modes):
             fo = self._fast_options(precision, seeds, seed_rng, max_iterations, polish_iterations,
-                                    0, verify, md, tuning=tuning, kernel=kernel)
+                                    0, verify, md, refine=refine, tuning=tuning, kernel=kernel)
             opts = options.to_c()
             keep += [fo, opts]
             it.mesh = mesh.handle

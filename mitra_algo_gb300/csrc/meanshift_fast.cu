@@ -105,6 +105,30 @@ __global__ void chunk_boxes(const float *desc, uint64_t q, uint64_t nchunks, flo
     for (int k = 0; k < 6; ++k) cbox[c * 12 + k] = l[k], cbox[c * 12 + 6 + k] = h[k];
 }
 
+// One block per run of kBlockChunks chunks: the union of their boxes.
+__global__ void __launch_bounds__(kBlockChunks) block_boxes(const float *cbox, uint64_t nchunks,
+                                                            float *bbox) {
+  __shared__ float part[kBlockChunks / 32][12];
+  const uint64_t c = uint64_t(blockIdx.x) * kBlockChunks + threadIdx.x;
+  const bool live = c < nchunks;
+  float v[12];
+  for (int k = 0; k < 12; ++k) v[k] = live ? cbox[c * 12 + k] : (k < 6 ? INFINITY : -INFINITY);
+  for (int o = 16; o; o >>= 1)
+    for (int k = 0; k < 12; ++k) {
+      const float w = __shfl_xor_sync(0xffffffffu, v[k], o);
+      v[k] = k < 6 ? fminf(v[k], w) : fmaxf(v[k], w);
+    }
+  if ((threadIdx.x & 31) == 0)
+    for (int k = 0; k < 12; ++k) part[threadIdx.x >> 5][k] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    const int k = threadIdx.x;
+    float r = part[0][k];
+    for (int w = 1; w < kBlockChunks / 32; ++w) r = k < 6 ? fminf(r, part[w][k]) : fmaxf(r, part[w][k]);
+    bbox[uint64_t(blockIdx.x) * 12 + k] = r;
+  }
+}
+
 // ------------------------------------------------------------ mean shift
 __device__ __forceinline__ float box_gap2(const float *a_lo, const float *a_hi, const float *b) {
   float g = 0;
@@ -124,7 +148,8 @@ __device__ __forceinline__ float box_gap2(const float *a_lo, const float *a_hi, 
 // NEWTON: some seed of the launch is kNear (the plain instance keeps its
 // register footprint small).
 template <typename T, bool COUNT, bool NEWTON>
-__global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cbox, uint64_t nchunks,
+__global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cbox, const float *bbox,
+                                                  uint64_t nchunks,
                                                   uint64_t q, const T *means, const uint8_t *state,
                                                   const int32_t *ids, uint64_t nactive, T h2,
                                                   T gk, float skip_gap2, uint64_t chunks_per_split,
@@ -167,6 +192,13 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
   uint64_t c1 = c0 + chunks_per_split < nchunks ? c0 + chunks_per_split : nchunks;
   unsigned long long done = 0;
   for (uint64_t c = c0; c < c1; ++c) {
+    if (c == c0 || c % kBlockChunks == 0) {  // the block's box first (one test for the CTA)
+      const uint64_t blk = c / kBlockChunks;
+      if (box_gap2(lo, hi, bbox + blk * 12) > skip_gap2) {
+        c = (blk + 1) * kBlockChunks - 1;
+        continue;
+      }
+    }
     if (box_gap2(lo, hi, cbox + c * 12) > skip_gap2) continue;
     // skip the chunk unless some seed of the block lies within the bandwidth
     // of its box (exact for Epanechnikov weights)
@@ -204,8 +236,11 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
         } else {
           const T floor_w = gk > T(0) ? exp2(-gk) : T(0);
           const T w = gk > T(0) ? exp2(-gk * (d2 / h2)) - floor_w : T(1) - d2 / h2;
+          // sums of w (v - x), not of w v: the step m - x comes out without
+          // the cancellation of a mean of large coordinates (votes moved
+          // to their own cell of vote space lie up to 14 from the origin)
 #pragma unroll
-          for (int d = 0; d < 6; ++d) acc[d] += w * xs[j * 8 + d];
+          for (int d = 0; d < 6; ++d) acc[d] += w * e[d];
           acc[6] += w;
           if (newton) {  // Epanechnikov: unweighted sums; Gaussian: by 2^(-k d^2/h^2)
             const T wn = gk > T(0) ? w + floor_w : T(1);
@@ -323,7 +358,7 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
   T x[6], delta[6], move = 0;
   for (int d = 0; d < 6; ++d) {
     x[d] = means[uint64_t(s) * 8 + d];
-    delta[d] = acc[d] / acc[6] - x[d];
+    delta[d] = acc[d] / acc[6];  // m - x from the sums of w (v - x)
     move += delta[d] * delta[d];
   }
   if (!near) {
@@ -498,11 +533,11 @@ int shift_impl(Call &call, const VoteSet &v, const T *desc, T *means, uint8_t *s
     if (g.splits * g.slots > cap) fail(SYM_RUNTIME_ERROR, "mean-shift partial buffer too small");
     const dim3 grid(unsigned(g.tiles), unsigned(g.splits));
     if (counts[1])
-      ms_tile<T, false, true><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state, ids,
+      ms_tile<T, false, true><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.bbox, v.nchunks, v.q, means, state, ids,
                                                       n, T(h2), T(v.kernel_k), gap * gap, g.cps,
                                                       partial, evals);
     else
-      ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.nchunks, v.q, means, state,
+      ms_tile<T, false, false><<<grid, kChunk, 0, st>>>(desc, v.cbox, v.bbox, v.nchunks, v.q, means, state,
                                                        ids, n, T(h2), T(v.kernel_k), gap * gap,
                                                        g.cps, partial, evals);
     check_launch();
@@ -557,7 +592,13 @@ VoteSet build_vote_set(Call &call, const float *desc_raw, const double *desc64_r
   v.cbox = call.alloc<float>(v.nchunks * 12);
   chunk_boxes<<<blocks_for(v.nchunks * 32), kThreads, 0, st>>>(v.desc, q, v.nchunks, v.cbox);
   check_launch();
-  call.launched(desc64_raw ? 8 : 7);
+  v.nblocks = (v.nchunks + kBlockChunks - 1) / kBlockChunks;
+  v.bbox = call.alloc<float>(v.nblocks * 12);
+  if (v.nblocks) {
+    block_boxes<<<unsigned(v.nblocks), kBlockChunks, 0, st>>>(v.cbox, v.nchunks, v.bbox);
+    check_launch();
+  }
+  call.launched(desc64_raw ? 9 : 8);
   return v;
 }
 
@@ -609,7 +650,7 @@ void count_within(Call &call, const VoteSet &v, const float *points, uint64_t nm
   float *partial = call.alloc<float>(g.splits * g.slots * 8);
   float gap = float(std::sqrt(h2)) + 1e-6f;
   ms_tile<float, true, false><<<dim3(unsigned(g.tiles), unsigned(g.splits)), kChunk, 0, st>>>(
-      v.desc, v.cbox, v.nchunks, v.q, points, nullptr, ids, nm, float(h2), 0.f, gap * gap, g.cps,
+      v.desc, v.cbox, v.bbox, v.nchunks, v.q, points, nullptr, ids, nm, float(h2), 0.f, gap * gap, g.cps,
       partial, nullptr);
   check_launch();
   sum_counts<<<blocks_for(nm), kThreads, 0, st>>>(partial, g.splits, g.slots, ids, nm, counts);

@@ -30,7 +30,7 @@ constexpr int kChunk = 128;  // votes per chunk = seeds per tile
 constexpr uint8_t kMoving = 0, kConverged = 1, kExhausted = 2, kNear = 3, kSettled = 4;
 constexpr double kSwitch2 = 1e-4, kNewtonStop2 = 1e-8, kTrust = 0.25;
 constexpr int kNewtonCap = 10;
-// Floats (or doubles) per partial sum of one seed: sum w x (6), sum w, pad,
+// Floats (or doubles) per partial sum of one seed: sum w (v - x) (6), sum w, pad,
 // then for kNear seeds the unweighted in-window sums of d = v - x: sum d
 // (6) and sum d d^T (21, upper triangle row by row), pad.
 constexpr int kPartial = 40;
@@ -52,6 +52,13 @@ struct Tuning {
 // scales its BF16 seed operand by it exactly.
 constexpr double kGauss2 = 8.0;
 
+// Chunks per block box: a seed tile whose box lies beyond the bandwidth of
+// a block's box skips its kBlockChunks chunks with one test (exact, as the
+// chunk tests: the block box holds every vote of its chunks).  Votes of a
+// fused batch lie in one cell of vote space per mesh, so a tile's seeds
+// (one or two meshes) meet only their own meshes' blocks.
+constexpr int kBlockChunks = 256;
+
 struct VoteSet {
   Tuning tuning;
   // weight kernel: 0 Epanechnikov 1 - d^2 / h^2 (the reference's); > 0 the
@@ -61,6 +68,8 @@ struct VoteSet {
   float *desc = nullptr;      // q x 8, Morton order
   double *desc64 = nullptr;   // q x 8, same order (only when requested)
   float *cbox = nullptr;      // nchunks x 12: lo[6], hi[6]
+  uint64_t nblocks = 0;       // runs of kBlockChunks consecutive chunks
+  float *bbox = nullptr;      // nblocks x 12: the box of each run's chunks
   float *gbox = nullptr;      // 12: box of all votes
   int32_t *order = nullptr;   // sorted position -> original vote
   int32_t *rank = nullptr;    // original vote -> sorted position

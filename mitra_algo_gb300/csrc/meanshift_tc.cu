@@ -336,11 +336,17 @@ __device__ __forceinline__ uint32_t active_tiles(const unsigned *nact) {
 
 // boxes[t * kBoxFloats ..]: the box of tile t's active seeds (12 floats:
 // lo, hi), then the boxes of its eight groups of 16 seeds (one block per
-// tile).
+// tile).  Then the block cull: sblk[t * nblk ..] lists, in ascending order,
+// the blocks of kBlockChunks chunks whose box lies within the bandwidth of
+// the tile's box and of some group's box (exact, as the chunk tests), and
+// nsurv[t] counts them.
 constexpr int kGroupSeeds = 16, kBoxFloats = 12 * (1 + kChunk / kGroupSeeds);
 __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigned *nact,
-                           float *boxes) {
+                           const float *bbox, uint32_t nblk, float skip_gap2, float *boxes,
+                           uint32_t *sblk, uint32_t *nsurv) {
   __shared__ float part[kChunk / kGroupSeeds][12];
+  __shared__ float tb[kBoxFloats];
+  __shared__ uint32_t warp_cnt[kChunk / 32], base_s;
   if (blockIdx.x >= active_tiles(nact)) return;
   const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
   const bool live = slot < nact[0];
@@ -357,6 +363,7 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigne
   const int group = threadIdx.x / kGroupSeeds;
   if (threadIdx.x % kGroupSeeds == 0)
     for (int d = 0; d < 6; ++d) part[group][d] = lo[d], part[group][6 + d] = hi[d];
+  if (threadIdx.x == 0) base_s = 0;
   __syncthreads();
   float *out = boxes + uint64_t(blockIdx.x) * kBoxFloats;
   constexpr int kGroups = kChunk / kGroupSeeds;
@@ -364,79 +371,127 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigne
     float v = part[0][threadIdx.x];
     for (int w = 1; w < kGroups; ++w)
       v = threadIdx.x < 6 ? fminf(v, part[w][threadIdx.x]) : fmaxf(v, part[w][threadIdx.x]);
-    out[threadIdx.x] = v;
+    out[threadIdx.x] = v, tb[threadIdx.x] = v;
   } else if (threadIdx.x < kBoxFloats) {
-    out[threadIdx.x] = part[(threadIdx.x - 12) / 12][(threadIdx.x - 12) % 12];
+    const float v = part[(threadIdx.x - 12) / 12][(threadIdx.x - 12) % 12];
+    out[threadIdx.x] = v, tb[threadIdx.x] = v;
   }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *mine = sblk + uint64_t(blockIdx.x) * nblk;
+  for (uint32_t b0 = 0; b0 < nblk; b0 += kChunk) {
+    const uint32_t b = b0 + threadIdx.x;
+    bool keep = false;
+    if (b < nblk) {
+      float bb[12];
+      for (int d = 0; d < 12; ++d) bb[d] = bbox[uint64_t(b) * 12 + d];
+      if (box_gap2_tc(tb, tb + 6, bb) <= skip_gap2)
+        for (int g = 0; g < kGroups && !keep; ++g)
+          keep = box_gap2_tc(tb + 12 + 12 * g, tb + 18 + 12 * g, bb) <= skip_gap2;
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_cnt[warp] = __popc(bal);
+    __syncthreads();
+    uint32_t before = base_s, total = 0;
+    for (int w = 0; w < kChunk / 32; ++w) {
+      if (w < warp) before += warp_cnt[w];
+      total += warp_cnt[w];
+    }
+    if (keep) mine[before + __popc(bal & ((1u << lane) - 1u))] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) base_s += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) nsurv[blockIdx.x] = base_s;
+}
+
+// The CTAs of a list kernel's grid shared among the active tiles: CTA i
+// serves tile i % tiles and takes every per-th of its surviving blocks,
+// starting at i / tiles (per = CTAs / tiles); false for a CTA left over.
+__device__ __forceinline__ bool list_share(const unsigned *nact, uint32_t &t, uint32_t &sub,
+                                           uint32_t &per) {
+  const uint32_t tiles = active_tiles(nact), i = blockIdx.x;
+  if (!tiles) return false;
+  per = gridDim.x / tiles;
+  if (!per || i >= per * tiles) return false;
+  t = i % tiles, sub = i / tiles;
+  return true;
 }
 
 constexpr int kListThreads = 256;  // chunks per block of the list kernels
+static_assert(kListThreads == kBlockChunks, "one thread per chunk of a block box");
 
 // need[t * nchunks + c]: some seed of tile t lies within the bandwidth of
 // chunk c's box (tested against the tile's box, then each group's box, then
-// the group's 16 seeds).  Exact for Epanechnikov weights: every vote of a
-// skipped chunk is farther than the bandwidth from every seed of the tile.
-// bcount[t * gridDim.x + blockIdx.x] = the block's kept chunks.
+// the group's 16 seeds), for the chunks of tile t's surviving blocks.  Exact
+// for Epanechnikov weights: every vote of a skipped chunk is farther than
+// the bandwidth from every seed of the tile.  bcount[t * nblk + j] = the
+// kept chunks of the tile's j-th surviving block.
 __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, const float *means,
                                                            const int32_t *ids, const unsigned *nact,
                                                            const float *cbox, uint64_t nchunks,
-                                                           float skip_gap2, uint8_t *need,
-                                                           uint32_t *bcount) {
+                                                           const uint32_t *sblk, const uint32_t *nsurv,
+                                                           uint32_t nblk, float skip_gap2,
+                                                           uint8_t *need, uint32_t *bcount) {
   __shared__ float seed[kChunk * 6];
   __shared__ float gb[kBoxFloats];
-  const uint64_t t = blockIdx.y;
-  if (t >= active_tiles(nact)) return;
+  uint32_t t, sub, per;
+  if (!list_share(nact, t, sub, per)) return;
   const unsigned nactive = nact[0];
+  const uint32_t ns = nsurv[t];
+  if (sub >= ns) return;
   for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
-    const uint64_t slot = t * kChunk + i;
+    const uint64_t slot = uint64_t(t) * kChunk + i;
     const bool live = slot < nactive;
     for (int d = 0; d < 6; ++d) seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
   }
-  if (threadIdx.x < kBoxFloats) gb[threadIdx.x] = boxes[t * kBoxFloats + threadIdx.x];
+  if (threadIdx.x < kBoxFloats) gb[threadIdx.x] = boxes[uint64_t(t) * kBoxFloats + threadIdx.x];
   __syncthreads();
-  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  bool keep = false;
-  if (c < nchunks) {
-    float cb[12];
-    for (int d = 0; d < 12; ++d) cb[d] = cbox[c * 12 + d];
-    if (box_gap2_tc(gb, gb + 6, cb) <= skip_gap2)
-      for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
-        const float *b = gb + 12 + 12 * g;
-        if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
-        for (int i = kGroupSeeds * g; i < kGroupSeeds * (g + 1) && !keep; ++i) {
-          float q = 0;
-          for (int d = 0; d < 6; ++d) {
-            const float x = seed[i * 6 + d];
-            const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
-            q += e * e;
+  for (uint32_t j = sub; j < ns; j += per) {
+    const uint64_t c = uint64_t(sblk[uint64_t(t) * nblk + j]) * kBlockChunks + threadIdx.x;
+    bool keep = false;
+    if (c < nchunks) {
+      float cb[12];
+      for (int d = 0; d < 12; ++d) cb[d] = cbox[c * 12 + d];
+      if (box_gap2_tc(gb, gb + 6, cb) <= skip_gap2)
+        for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
+          const float *b = gb + 12 + 12 * g;
+          if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
+          for (int i = kGroupSeeds * g; i < kGroupSeeds * (g + 1) && !keep; ++i) {
+            float q = 0;
+            for (int d = 0; d < 6; ++d) {
+              const float x = seed[i * 6 + d];
+              const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
+              q += e * e;
+            }
+            keep = q <= skip_gap2;
           }
-          keep = q <= skip_gap2;
         }
-      }
-    need[t * nchunks + c] = keep;
+      need[uint64_t(t) * nchunks + c] = keep;
+    }
+    const int kept = __syncthreads_count(keep);
+    if (threadIdx.x == 0) bcount[uint64_t(t) * nblk + j] = uint32_t(kept);
   }
-  const int kept = __syncthreads_count(keep);
-  if (threadIdx.x == 0) bcount[t * gridDim.x + blockIdx.x] = uint32_t(kept);
 }
 
-// One block: boff = exclusive scan of the active tiles' block counts,
-// offsets[t] = first list entry of tile t (offsets[tiles] = list length),
-// and the work plan: tile t gets pieces[t+1] - pieces[t] CTAs, about
-// len_t * budget / total of them (at least one), so every CTA streams a
-// similar number of chunks; budget = sms - tiles (at least tiles), so the
-// pieces fill one wave of the GPU.
-__global__ void __launch_bounds__(1024) scan_lists(const uint32_t *bcount, const unsigned *nact,
-                                                   uint32_t nblk, uint32_t sms, uint32_t *boff,
-                                                   uint64_t *offsets, uint32_t *pieces) {
+// One block per active tile: boff[t * nblk + j] = exclusive scan of the
+// tile's bcount over its surviving blocks, tile_len[t] = the sum.
+__global__ void __launch_bounds__(1024) scan_tiles(const uint32_t *bcount, const unsigned *nact,
+                                                   const uint32_t *nsurv, uint32_t nblk,
+                                                   uint32_t *boff, uint32_t *tile_len) {
   __shared__ uint32_t warp_sum[32];
   __shared__ uint32_t carry_s;
-  const uint32_t tiles = active_tiles(nact), total = tiles * nblk;
+  const uint32_t t = blockIdx.x;
+  if (t >= active_tiles(nact)) return;
+  const uint32_t n = nsurv[t];
+  const uint32_t *in = bcount + uint64_t(t) * nblk;
+  uint32_t *out = boff + uint64_t(t) * nblk;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) carry_s = 0;
   __syncthreads();
-  for (uint32_t base = 0; base < total; base += blockDim.x) {
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
     const uint32_t j = base + threadIdx.x;
-    const uint32_t v = j < total ? bcount[j] : 0u;
+    const uint32_t v = j < n ? in[j] : 0u;
     uint32_t x = v;  // inclusive warp scan
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -453,17 +508,55 @@ __global__ void __launch_bounds__(1024) scan_lists(const uint32_t *bcount, const
       warp_sum[lane] = w;  // inclusive over warps
     }
     __syncthreads();
-    const uint32_t before = carry_s + (warp ? warp_sum[warp - 1] : 0u) + x - v;
-    if (j < total) boff[j] = before;
+    if (j < n) out[j] = carry_s + (warp ? warp_sum[warp - 1] : 0u) + x - v;
+    __syncthreads();
+    if (threadIdx.x == 0) carry_s += warp_sum[(blockDim.x >> 5) - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) tile_len[t] = carry_s;
+}
+
+// One block: offsets[t] = first list entry of tile t (exclusive scan of
+// the active tiles' list lengths; offsets[tiles] = the total), and the work
+// plan: tile t gets pieces[t+1] - pieces[t] CTAs, about len_t * budget /
+// total of them (at least one), so every CTA streams a similar number of
+// chunks; budget = sms - tiles (at least tiles), so the pieces fill one
+// wave of the GPU.
+__global__ void __launch_bounds__(1024) scan_lists(const uint32_t *tile_len, const unsigned *nact,
+                                                   uint32_t sms, uint64_t *offsets, uint32_t *pieces) {
+  __shared__ uint32_t warp_sum[32];
+  __shared__ uint32_t carry_s;
+  const uint32_t tiles = active_tiles(nact);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < tiles; base += blockDim.x) {
+    const uint32_t j = base + threadIdx.x;
+    const uint32_t v = j < tiles ? tile_len[j] : 0u;
+    uint32_t x = v;  // inclusive warp scan
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < int(blockDim.x >> 5) ? warp_sum[lane] : 0u;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_sum[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    if (j < tiles) offsets[j] = carry_s + (warp ? warp_sum[warp - 1] : 0u) + x - v;
     __syncthreads();
     if (threadIdx.x == 0) carry_s += warp_sum[(blockDim.x >> 5) - 1];
     __syncthreads();
   }
   const uint32_t list_len = carry_s;
-  for (uint32_t t = threadIdx.x; t <= tiles; t += blockDim.x)
-    offsets[t] = t < tiles ? boff[t * nblk] : list_len;
-  __syncthreads();
   if (threadIdx.x == 0) {
+    offsets[tiles] = list_len;
     const uint32_t budget = tiles < sms ? sms - tiles : tiles;
     uint32_t at = 0;
     for (uint32_t t = 0; t < tiles; ++t) {
@@ -476,25 +569,36 @@ __global__ void __launch_bounds__(1024) scan_lists(const uint32_t *bcount, const
   }
 }
 
-// list[boff[..] + r] = t * nchunks + c for the r-th kept chunk c of the block
-// (ascending c), same grid as tile_count.
+// list[offsets[t] + boff[t * nblk + j] + r] = t * nchunks + c for the r-th
+// kept chunk c (ascending) of tile t's j-th surviving block: per tile, the
+// kept chunks in ascending order.  CTAs shared among tiles as tile_count's.
 __global__ void __launch_bounds__(kListThreads) scatter_lists(const uint8_t *need,
                                                               const uint32_t *boff,
+                                                              const uint32_t *bcount,
+                                                              const uint32_t *sblk,
+                                                              const uint32_t *nsurv, uint32_t nblk,
+                                                              const uint64_t *offsets,
                                                               const unsigned *nact,
                                                               uint64_t nchunks, int32_t *list) {
   __shared__ uint32_t warp_cnt[kListThreads / 32];
-  const uint64_t t = blockIdx.y;
-  if (t >= active_tiles(nact)) return;
-  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool keep = c < nchunks && need[t * nchunks + c];
+  uint32_t t, sub, per;
+  if (!list_share(nact, t, sub, per)) return;
+  const uint32_t ns = nsurv[t];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t bal = __ballot_sync(0xffffffffu, keep);
-  if (lane == 0) warp_cnt[warp] = __popc(bal);
-  __syncthreads();
-  uint32_t before = boff[t * gridDim.x + blockIdx.x];
-  for (int w = 0; w < warp; ++w) before += warp_cnt[w];
-  before += __popc(bal & ((1u << lane) - 1u));
-  if (keep) list[before] = int32_t(t * nchunks + c);
+  for (uint32_t j = sub; j < ns; j += per) {
+    const uint64_t e = uint64_t(t) * nblk + j;
+    if (!bcount[e]) continue;  // the same for the whole CTA
+    const uint64_t c = uint64_t(sblk[e]) * kBlockChunks + threadIdx.x;
+    const bool keep = c < nchunks && need[uint64_t(t) * nchunks + c];
+    const uint32_t bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_cnt[warp] = __popc(bal);
+    __syncthreads();
+    uint64_t before = offsets[t] + boff[e];
+    for (int w = 0; w < warp; ++w) before += warp_cnt[w];
+    before += __popc(bal & ((1u << lane) - 1u));
+    if (keep) list[before] = int32_t(uint64_t(t) * nchunks + c);
+    __syncthreads();
+  }
 }
 
 // --------------------------------------------- pipelined tensor kernel
@@ -1047,10 +1151,14 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   check_launch();
   int32_t *ids = call.alloc<int32_t>(k);
   float *boxes = call.alloc<float>(max_tiles * kBoxFloats);
-  const uint32_t nblk = uint32_t((v.nchunks + kListThreads - 1) / kListThreads);
+  const uint32_t nblk = uint32_t(v.nblocks);
   uint8_t *need = call.alloc<uint8_t>(max_tiles * v.nchunks);
   uint32_t *bcount = call.alloc<uint32_t>(max_tiles * nblk), *boff = call.alloc<uint32_t>(max_tiles * nblk);
+  uint32_t *sblk = call.alloc<uint32_t>(max_tiles * nblk), *nsurv = call.alloc<uint32_t>(max_tiles);
+  uint32_t *tile_len = call.alloc<uint32_t>(max_tiles);
   int32_t *list = call.alloc<int32_t>(max_tiles * v.nchunks);
+  // CTAs of the list kernels, shared among the active tiles at run time
+  const unsigned list_ctas = unsigned(std::max<uint64_t>(max_tiles, 8 * 152));
   uint64_t *offsets = call.alloc<uint64_t>(max_tiles + 1);
   uint32_t *pieces = call.alloc<uint32_t>(max_tiles + 1);
   // budget + tiles CTAs: tc_ctas_per_sm waves of the 152 SMs
@@ -1082,15 +1190,18 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   int it = 0;
   for (; it < max_iter; ++it) {
     active_seeds_async(call, v, means, state, k, ids, nact, iter, trace_dev, trace_cap);
-    tile_boxes<<<unsigned(max_tiles), kChunk, 0, st>>>(means, ids, nact, boxes);
+    tile_boxes<<<unsigned(max_tiles), kChunk, 0, st>>>(means, ids, nact, v.bbox, nblk, gap * gap,
+                                                        boxes, sblk, nsurv);
     check_launch();
-    tile_count<<<dim3(nblk, unsigned(max_tiles)), kListThreads, 0, st>>>(
-        boxes, means, ids, nact, v.cbox, v.nchunks, gap * gap, need, bcount);
+    tile_count<<<list_ctas, kListThreads, 0, st>>>(boxes, means, ids, nact, v.cbox, v.nchunks, sblk,
+                                                   nsurv, nblk, gap * gap, need, bcount);
     check_launch();
-    scan_lists<<<1, 1024, 0, st>>>(bcount, nact, nblk, sms, boff, offsets, pieces);
+    scan_tiles<<<unsigned(max_tiles), 1024, 0, st>>>(bcount, nact, nsurv, nblk, boff, tile_len);
     check_launch();
-    scatter_lists<<<dim3(nblk, unsigned(max_tiles)), kListThreads, 0, st>>>(need, boff, nact,
-                                                                              v.nchunks, list);
+    scan_lists<<<1, 1024, 0, st>>>(tile_len, nact, sms, offsets, pieces);
+    check_launch();
+    scatter_lists<<<list_ctas, kListThreads, 0, st>>>(need, boff, bcount, sblk, nsurv, nblk, offsets,
+                                                      nact, v.nchunks, list);
     check_launch();
     if (kernel_ms) mark_event();
     ms_tile_tc<<<unsigned(max_grid), kThreadsTc, kTcSmem, st>>>(args);
@@ -1099,7 +1210,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     ms_update_bulk<<<unsigned((k + 7) / 8), 256, 0, st>>>(means, partial, pieces, ids, nact,
                                                           float(h2), state);
     check_launch();
-    call.launched(6);
+    call.launched(7);
     if (it % kCheck == kCheck - 1) {
       unsigned n = 0;
       call.d2h(&n, nact, sizeof(unsigned));

@@ -215,6 +215,7 @@ struct BvhView {
   const float *xyz;
   const int32_t *child;
   const float *box;
+  const float4 *fn;  // nf: unit face normal from the FP64 corners, w = 1 (0: none usable)
 };
 
 __device__ __forceinline__ F3 vtx(const BvhView &b, int32_t v) {
@@ -311,42 +312,69 @@ __device__ __forceinline__ int32_t support_query(const BvhView &b, const double 
 }
 
 // ------------------------------------------- exact decisions, FP32 search
-// Error bound of the FP32 search, in distance units: kErr (512 FP32 units)
-// times the largest coordinate magnitude of the vertex, its image and the
-// mesh.  The FP32 distance of a face whose smallest corner-pair angle has
-// sin^2 >= kWellShaped differs from the FP64 distance of the FP64 image by
-// about 5 units for the rounding of the inputs and the image (the distance
-// is 1-Lipschitz in both) plus about 100 units times (edge length /
-// magnitude) for the region tests, whose conditioning is that angle's
-// 1 / sin^2 -- well below kErr; other faces enter the candidates by the
-// distance of their box and leave the decision to FP64.  The same bound
-// serves as the band of the FP32 threshold tests (2 tau, the plane side,
-// tau), and kNormalBand (on the cosine) as that of the normal test.
+// Error bound of the FP32 search, in distance units: kErr (512 FP32 units u)
+// times M, the largest coordinate magnitude of the vertex, its image, the
+// translation and the mesh.  The FP32 corners and image are within a few
+// u M of their FP64 values, and the distance is 1-Lipschitz in each; the
+// face's unit normal comes from the FP64 corners (rounded once to FP32), so
+// the plane distance n . (p - a) and the three edge functions
+// (n x e) . (p - v) carry errors of a few u (M + |p - v|) whatever the
+// face's shape, and the segment distances of a few u M as well -- far below
+// kErr M.  A face decided by face_d2n therefore has its FP32 distance within
+// kErr M of the reference's FP64 distance; a face without a usable normal
+// (its FP64 normal not accurate to well below u: no area, or a corner angle
+// with sin below 1e-6), or whose projection falls within the rounding band
+// of an edge line, enters the candidates by a lower bound and leaves the
+// decision to FP64.  The same bound serves as the band of the FP32 threshold
+// tests (2 tau, the plane side, tau), and kNormalBand (on the cosine) as
+// that of the normal test, whose FP32 error is a few u.
 constexpr float kErr = 1.0f / 32768.0f;
-constexpr float kWellShaped = 0.05f;
 constexpr float kNormalBand = 1.0f / 1024.0f;
 constexpr int kCandidates = 16;
 
-// sin^2 of the smallest angle of triangle abc: |ab x ac|^2 over the product
-// of the two longest squared edges.
-__device__ __forceinline__ float shape_quality(F3 a, F3 b, F3 c) {
-  const F3 ab = b - a, ac = c - a, bc = c - b;
-  const float l0 = dotf(ab, ab), l1 = dotf(ac, ac), l2 = dotf(bc, bc);
-  const F3 n = crossf(ab, ac);
-  const float lo = fminf(l0, fminf(l1, l2));
-  const float prod = (l0 * l1 * l2) / fmaxf(lo, 1e-37f);
-  return prod > 0.f ? dotf(n, n) / prod : 0.f;
+// FP32 squared distance from p to the face (a, b, c) with unit normal n;
+// um = u M, the FP32 unit at the query's magnitude.  The plane distance
+// when p projects inside all three edges by more than their rounding band
+// (p then projects into the face), the nearest of the three edge segments
+// when it projects outside one of them by more than its band (the nearest
+// point then lies on the boundary).  Otherwise `d2` receives min(plane,
+// segments), a lower bound of the distance, and the function returns
+// false.  Band of an edge function E = (n x e) . (p - v): with |dn| <= u,
+// corners within 1.8 u M and the image within 30 u M of their FP64 values,
+// and the cross and dot products' rounding, |dE| <= u (11 |e| |p - v| +
+// 3.6 M |p - v| + 32 M |e|) <= 42 u M (|p - v| + |e|) for |e| <= 3.5 M; the
+// band is 64 u M (|p - v| + |e|).
+__device__ bool face_d2n(F3 p, F3 a, F3 b, F3 c, F3 n, float um, float &d2) {
+  const F3 ab = b - a, bc = c - b, ca = a - c, ap = p - a, bp = p - b, cp = p - c;
+  const float k = 64.f * um;
+  const float ba = k * (sqrtf(dotf(ap, ap)) + sqrtf(dotf(ab, ab)));
+  const float bb = k * (sqrtf(dotf(bp, bp)) + sqrtf(dotf(bc, bc)));
+  const float bcb = k * (sqrtf(dotf(cp, cp)) + sqrtf(dotf(ca, ca)));
+  const float ea = dotf(crossf(n, ab), ap), eb = dotf(crossf(n, bc), bp), ec = dotf(crossf(n, ca), cp);
+  const float seg = fminf(segment_d2f(p, a, b), fminf(segment_d2f(p, b, c), segment_d2f(p, c, a)));
+  if (ea < -ba || eb < -bb || ec < -bcb) {
+    d2 = seg;
+    return true;
+  }
+  const float h = dotf(n, ap);
+  if (ea > ba && eb > bb && ec > bcb) {
+    d2 = h * h;
+    return true;
+  }
+  d2 = fminf(h * h, seg);
+  return false;
 }
 
 // Faces whose FP64 distance to the image can be the smallest: every face
-// whose FP32 distance (or, for a badly shaped face, box distance) is within
-// 2 error bounds of min(best FP32 distance, tau + bound) -- the face of
-// smallest FP64 distance is at most 2 bounds farther in FP32 than the best
-// FP32 face.  Nodes are pruned with a slightly larger radius, for the
-// rounding of their boxes' distances.  Badly shaped faces are listed as
-// ~face.  Returns the count (kCandidates + 1 on overflow); `best` receives
-// the smallest FP32 squared distance of a well-shaped face (INFINITY when
-// none lies within tau + 3 bounds).
+// whose FP32 distance (or, for a face face_d2n leaves undecided or one
+// without a usable normal, a lower bound: the face_d2n bound or the box
+// distance) is within 2 error bounds of min(best FP32 distance, tau +
+// bound) -- the face of smallest FP64 distance is at most 2 bounds farther
+// in FP32 than the best FP32 face.  Nodes are pruned with a slightly larger
+// radius, for the rounding of their boxes' distances.  Undecided faces are
+// listed as ~face.  Returns the count (kCandidates + 1 on overflow); `best`
+// receives the smallest FP32 squared distance of a decided face (INFINITY
+// when none lies within tau + 3 bounds).
 __device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err, int32_t *faces,
                                float *keys, float &best, int *status) {
   best = INFINITY;
@@ -354,21 +382,22 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err,
   float lim = radius * radius, lim_box = (radius + err * 0.03125f) * (radius + err * 0.03125f);
   int n = 0;
   bool overflow = false;
+  const float um = err * (1.f / 512.f);  // err = kErr M = 512 u M
   auto consider = [&](int32_t f, float box) {
-    const F3 a = vtx(b, b.faces[f]), bb = vtx(b, b.faces[b.nf + f]), cc = vtx(b, b.faces[2 * b.nf + f]);
-    float key;
-    int32_t id = f;
-    if (shape_quality(a, bb, cc) >= kWellShaped) {
-      key = triangle_d2f(p, a, bb, cc);
+    const float4 fn = b.fn[f];
+    float key = box;
+    int32_t id = ~f;
+    if (fn.w != 0.f) {
+      const F3 a = vtx(b, b.faces[f]), bb = vtx(b, b.faces[b.nf + f]), cc = vtx(b, b.faces[2 * b.nf + f]);
+      if (face_d2n(p, a, bb, cc, F3{fn.x, fn.y, fn.z}, um, key)) id = f;
+    }
+    if (id >= 0) {
       if (key < best) {
         best = key;
         radius = fminf(tau_err, sqrtf(best)) + 2.f * err;
         lim = radius * radius;
         lim_box = (radius + err * 0.03125f) * (radius + err * 0.03125f);
       }
-    } else {
-      key = box;
-      id = ~f;
     }
     if (key > lim) return;
     if (n == kCandidates) {  // drop entries beyond the current limit
@@ -429,13 +458,18 @@ struct MotionF {
 };
 
 // Row lists between the verification kernels.
+// The rows each later kernel takes.  The FP64 and reference-order rows are
+// marked per row and compacted in ascending order (compact_indices), so a
+// warp of those kernels serves neighbouring vertices of one motion and
+// walks nearly the same BVH nodes, as verify_fp32's warps do; appended in
+// completion order they made every load of a warp 32 scattered ones.
 struct RowLists {
   uint32_t *forward;    // accepted forward rows whose FP64 distance is still needed
   int32_t *faces;       // kCandidates faces per forward row (-1 padded)
-  uint32_t *fp64;       // rows decided in FP64
-  unsigned long long *counts;  // [forward, fp64, overflow, tie]
-  uint32_t *reference;  // rows left to the reference-order BVH
-  double *limits;       // their search limits
+  uint8_t *mark;        // per row: 1 = left to the next kernel (FP64, then reference order)
+  int32_t *fp64;        // rows decided in FP64, ascending
+  int32_t *reference;   // rows left to the reference-order BVH, ascending
+  unsigned long long *counts;  // [forward, unused, unused, tie]
 };
 
 // Decisions in FP32 (verify_fp32).  The reference's tests are made with
@@ -454,6 +488,7 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
   flags[row] = 0;
+  lists.mark[row] = 0;
   if (!inverse) err[c * nv + i] = 0.0;
   const MotionF &m = motions[c];
   float r[9];
@@ -465,7 +500,7 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   if (!inverse) q = q + F3{m.t[0], m.t[1], m.t[2]};
   const float mag = fmaxf(scale, fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z))));
   const float e = kErr * fmaxf(mag, fmaxf(fabsf(m.t[0]), fmaxf(fabsf(m.t[1]), fabsf(m.t[2]))));
-  auto to_fp64 = [&]() { lists.fp64[atomicAdd(&lists.counts[1], 1ull)] = uint32_t(row); };
+  auto to_fp64 = [&]() { lists.mark[row] = 1; };
   // the image moves at least 2 tau (verification.cpp:64)
   const F3 dq = q - p;
   const float moved = sqrtf(dotf(dq, dq));
@@ -494,17 +529,10 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
               r[6] * ni.x + r[7] * ni.y + r[8] * ni.z};
   int agree = 0, disagree = 0;
   for (int j = 0; j < n; ++j) {
-    const int32_t f = faces[j];
-    const F3 a = vtx(b, b.faces[f]), bb = vtx(b, b.faces[b.nf + f]), cc = vtx(b, b.faces[2 * b.nf + f]);
-    const F3 ab = bb - a, ac = cc - a;
-    const F3 fn = crossf(ab, ac);
-    const float len = sqrtf(dotf(fn, fn));
-    // the direction of the FP32 normal is off by about (rounding of the
-    // corners) x (edge lengths) / |ab x ac|: a face small against the
-    // coordinate magnitude leaves the test to FP64
-    const float drift = 4.f * 5.96e-8f * mag * (sqrtf(dotf(ab, ab)) + sqrtf(dotf(ac, ac)));
-    if (!(drift <= 0.5f * kNormalBand * len)) return to_fp64();
-    const float v = dotf(rn, fn) / len;
+    // the face's unit normal from its FP64 corners (every candidate here
+    // has one): the cosine is good to a few u
+    const float4 fn = b.fn[faces[j]];
+    const float v = dotf(rn, F3{fn.x, fn.y, fn.z});
     if (fabsf(v - 0.5f) <= kNormalBand) return to_fp64();
     if (v >= 0.5f) ++agree;
     else ++disagree;
@@ -622,15 +650,11 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
   }
   flags[row] = v == 1;
   if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
-  if (v == 2) {
-    const unsigned long long j = atomicAdd(&lists.counts[2], 1ull);
-    lists.reference[j] = uint32_t(row);
-    lists.limits[j] = d;
-  }
+  if (v != 2) lists.mark[row] = 0;  // marked rows go on to the reference-order search
 }
 
 // Rows whose candidates overflowed the list: the reference's search itself
-// (exact_query) with the tau^2 limit.
+// (exact_query) with the search limit nextafter(tau^2, inf).
 __global__ void verify_listed_ref(Surface s, const double *vn, const ClusterMotion *motions,
                                   double tau, RowLists lists, unsigned long long count,
                                   uint8_t *flags, double *err, int *status) {
@@ -641,7 +665,8 @@ __global__ void verify_listed_ref(Surface s, const double *vn, const ClusterMoti
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
   double d = 0;
-  const bool ok = exact_query(s, vn, motions[c], inverse, i, tau, lists.limits[k], d, status);
+  const bool ok = exact_query(s, vn, motions[c], inverse, i, tau,
+                              nextafter(tau * tau, double(INFINITY)), d, status);
   flags[row] = ok;
   if (!inverse) err[c * nv + i] = ok ? d : 0.0;
 }
@@ -945,6 +970,32 @@ __global__ void count_roots(int32_t *parent_all, uint64_t nv, uint64_t sets, uns
 
 }  // namespace
 
+// Unit normal of every face, (b - a) x (c - a) normalised in FP64 as the
+// reference's normal test forms it (src/cpu/verification.cpp:71-75), rounded
+// to FP32, w = 1.  w = 0 when that FP64 normal is not accurate to well below
+// an FP32 unit (|ab x ac| <= 1e-6 |ab| |ac|: its direction error is about
+// 1e-16 / sin of the corner angle), and near the reference's cut-off of
+// unit() (a cross product of norm <= 1e-14 becomes the zero vector, which
+// fails the test): those faces leave their rows to the FP64 decisions.
+__global__ void lbvh_face_normals(const double *xyz, uint64_t nv, const int32_t *faces,
+                                  uint64_t nf, float4 *fn) {
+  const uint64_t f = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  D3 c[3];
+  for (int k = 0; k < 3; ++k) {
+    const int32_t v = faces[k * nf + f];
+    c[k] = D3{xyz[v], xyz[nv + v], xyz[2 * nv + v]};
+  }
+  const D3 ab = c[1] - c[0], ac = c[2] - c[0], n = cross(ab, ac);
+  const double n2 = dot(n, n), l2 = dot(ab, ab) * dot(ac, ac);
+  if (!(n2 > 1e-12 * l2) || !(n2 > 4e-28)) {
+    fn[f] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const D3 u = unit(n);
+  fn[f] = make_float4(float(u.x), float(u.y), float(u.z), 1.f);
+}
+
 Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
                 const int32_t *faces, uint64_t nf) {
   Lbvh b;
@@ -954,14 +1005,18 @@ Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
   const uint64_t ni = nf - 1;
   auto pad = [](uint64_t x) { return (x + 255) & ~uint64_t(255); };
   const uint64_t s_xyz = pad(12 * nv), s_child = pad(8 * ni + 8), s_box = pad(48 * ni + 48);
-  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box));
+  const uint64_t s_fn = pad(16 * nf);
+  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box + s_fn));
   b.xyz = reinterpret_cast<float *>(b.block);
   b.child = reinterpret_cast<int32_t *>(b.block + s_xyz);
   b.box = reinterpret_cast<float *>(b.block + s_xyz + s_child);
   b.vn = reinterpret_cast<float *>(b.block + s_xyz + s_child + s_box);
+  b.fn = reinterpret_cast<float4 *>(b.block + 2 * s_xyz + s_child + s_box);
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(xyz, nv, b.xyz);
   check_launch();
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(vn, nv, b.vn);
+  check_launch();
+  lbvh_face_normals<<<blocks_for(nf), kThreads, 0, st>>>(xyz, nv, faces, nf, b.fn);
   check_launch();
   // the mesh box, for the Morton quantisation
   std::vector<float> h(3 * nv);
@@ -991,7 +1046,7 @@ Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
                                                      parent_in, parent_leaf, b.box, arrivals);
     check_launch();
   }
-  call.launched(ni ? 7 : 5);
+  call.launched(ni ? 8 : 6);
   call.sync();
   return b;
 }
@@ -1067,7 +1122,7 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   cudaStream_t st = call.stream();
   if (fp64_rows) *fp64_rows = 0;
   if (!rows) return 0;
-  if (rows >= (uint64_t(1) << 32)) fail(SYM_INVALID_ARGUMENT, "verification: too many queries");
+  if (rows >= (uint64_t(1) << 31)) fail(SYM_INVALID_ARGUMENT, "verification: too many queries");
   if (!m.nf) {
     SYM_CUDA(cudaMemsetAsync(flags, 0, rows, st));
     SYM_CUDA(cudaMemsetAsync(err, 0, nc * nv * 8, st));
@@ -1086,18 +1141,21 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   RowLists lists;
   lists.forward = call.alloc<uint32_t>(nc * nv);
   lists.faces = call.alloc<int32_t>(nc * nv * kCandidates);
-  lists.fp64 = call.alloc<uint32_t>(rows);
-  lists.reference = call.alloc<uint32_t>(rows);
-  lists.limits = call.alloc<double>(rows);
+  lists.mark = call.alloc<uint8_t>(rows);
+  lists.fp64 = call.alloc<int32_t>(rows);
+  lists.reference = call.alloc<int32_t>(rows);
   lists.counts = call.alloc<unsigned long long>(4);
+  uint64_t *listed = call.alloc<uint64_t>(2);
   SYM_CUDA(cudaMemsetAsync(lists.counts, 0, 32, st));
-  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
+  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn};
   Surface s{m.xyz, nv, m.faces, m.nf, nullptr, nullptr};
   verify_fp32<<<blocks_for(rows), kThreads, 0, st>>>(view, bvh.vn, dmf, nc, float(tau), bvh.scale,
                                                       flags, err, lists, call.status());
   check_launch();
+  compact_indices(call, lists.mark, rows, lists.fp64, listed);
   unsigned long long counts[4] = {0, 0, 0, 0};
-  call.d2h(counts, lists.counts, 16);
+  call.d2h(counts, lists.counts, 8);
+  call.d2h(&counts[1], listed, 8);
   call.sync();
   call.launched();
   if (counts[0]) {
@@ -1113,7 +1171,9 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
                                                                   counts[1], call.status());
     check_launch();
     call.launched();
-    call.d2h(counts + 2, lists.counts + 2, 16);
+    compact_indices(call, lists.mark, rows, lists.reference, listed + 1);
+    call.d2h(&counts[2], listed + 1, 8);
+    call.d2h(&counts[3], lists.counts + 3, 8);
     call.sync();
   }
   if (fp64_rows) *fp64_rows = counts[1];
@@ -1148,7 +1208,7 @@ void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record 
   ClusterMotion *dm = call.upload(motions.data(), nc);
   if (refine > 0 && m.nf) {
     const Lbvh &bvh = *m.lbvh;
-    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box};
+    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn};
     refine_motions(call, view, m.xyz, m.vn, m.w, dm, nc, tau, refine, origin);
     call.d2h(motions.data(), dm, nc * sizeof(ClusterMotion));
     call.check_status("transform refinement");

@@ -314,3 +314,103 @@ def motif_torus(R=1.0, r=0.3, nu=1000, nv=500, copies=12, mirrored=2, bumps=6, n
         diag = np.linalg.norm(verts.max(0) - verts.min(0))
         verts = verts + rng.normal(0, noise * diag, verts.shape)
     return Mesh(verts.T.copy(), faces.T.copy())
+
+
+def _vertex_normals(verts: np.ndarray, faces: np.ndarray) -> np.ndarray:
+    """Area-weighted vertex normals (n, 3) of vertices (n, 3), faces (f, 3)."""
+    a, b, c = verts[faces[:, 0]], verts[faces[:, 1]], verts[faces[:, 2]]
+    fn = np.cross(b - a, c - a)
+    vn = np.zeros_like(verts)
+    for k in range(3):
+        np.add.at(vn, faces[:, k], fn)
+    return vn / np.maximum(np.linalg.norm(vn, axis=1, keepdims=True), 1e-300)
+
+
+def add_random_bumps(mesh: Mesh, share: float, seed: int, amp=(0.02, 0.06)) -> Mesh:
+    """Unsymmetric relief over about `share` of the surface: Gaussian bumps
+    along the vertex normals at seeded vertices, each of width a tenth of
+    the bounding-box diagonal, as many as cover that share of the vertices."""
+    rng = np.random.default_rng(seed)
+    v = mesh.vertices.T.copy()
+    f = mesh.faces.T
+    n = _vertex_normals(v, f)
+    diag = float(np.linalg.norm(v.max(0) - v.min(0)))
+    sig = 0.1 * diag
+    disp = np.zeros(len(v))
+    covered = np.zeros(len(v), bool)
+    for _ in range(200):
+        if covered.mean() >= share:
+            break
+        c = v[rng.integers(len(v))]
+        d2 = ((v - c) ** 2).sum(1)
+        disp += rng.uniform(*amp) * diag * np.exp(-d2 / (2 * sig * sig))
+        covered |= d2 < (1.5 * sig) ** 2
+    return Mesh((v + n * disp[:, None]).T.copy(), mesh.faces.copy())
+
+
+def add_noise(mesh: Mesh, sigma: float, seed: int) -> Mesh:
+    """Gaussian vertex noise of `sigma` times the bounding-box diagonal."""
+    if sigma <= 0:
+        return mesh
+    v = mesh.vertices
+    diag = float(np.linalg.norm(v.max(1) - v.min(1)))
+    return Mesh(v + np.random.default_rng(seed).normal(0, sigma * diag, v.shape), mesh.faces.copy())
+
+
+def uneven_batch(count=256, seed=0):
+    """The uneven batch (BASELINE C4): `count` seeded meshes, an even mix of
+    motif icospheres, motif tori and mirrored height fields, vertex counts
+    log-uniform in 2k-60k (the nearest icosphere level; grid sizes for the
+    others), each with 1-4 planted symmetries (rotations about z of a
+    repeated motif, rotated or mirrored copies of a motif, or the height
+    field's mirror plane) and Gaussian noise sigma uniform in [0, 5e-3] of
+    the diagonal.  Returns [(mesh, mode, planted), ...] with mode "rigid" or
+    "reflection"."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        kind = ("sphere", "torus", "height")[i % 3]
+        target = float(np.exp(rng.uniform(np.log(2000), np.log(60000))))
+        planted = int(rng.integers(1, 5))
+        noise = float(rng.uniform(0.0, 5e-3))
+        if kind == "sphere":
+            level = int(np.clip(np.round(np.log(target / 10) / np.log(4)), 4, 6))
+            mesh = motif_sphere(level=level, bumps=int(rng.integers(6, 13)), folds=planted + 1,
+                                partial_shift=float(rng.uniform(0.2, 0.5)), noise=noise,
+                                seed=1000 + i)
+            mode = "rigid"
+        elif kind == "torus":
+            nu = max(24, int(np.sqrt(2 * target)))
+            mesh = motif_torus(nu=nu, nv=max(12, nu // 2), copies=planted + 1,
+                               mirrored=int(rng.integers(0, 2)), noise=noise, seed=1000 + i)
+            mode = "rigid"
+        else:
+            mesh = add_noise(mirrored_heightfield(size=max(32, int(np.sqrt(target))),
+                                                  bumps=int(rng.integers(4, 9)), seed=1000 + i),
+                             noise, 2000 + i)
+            planted, mode = 1, "reflection"
+        out.append((mesh, mode, planted))
+    return out
+
+
+def stress_batch(count=64, seed=1):
+    """The stress batch (BASELINE C5): `count` seeded meshes of 1e5-1e6
+    triangles (log-uniform), half reflection (mirrored height fields) and
+    half rigid (motif tori with rotated copies), with unsymmetric random
+    bumps over about 30% of each surface, so that most pairs vote for no
+    symmetry.  Returns [(mesh, mode), ...]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        tris = float(np.exp(rng.uniform(np.log(1e5), np.log(1e6))))
+        if i % 2:
+            size = int(np.sqrt(tris / 2)) + 1
+            mesh = mirrored_heightfield(size=size, bumps=int(rng.integers(5, 10)), seed=3000 + i)
+            mode = "reflection"
+        else:
+            nu = int(np.sqrt(tris))
+            mesh = motif_torus(nu=nu, nv=max(12, nu // 2), copies=int(rng.integers(3, 7)),
+                               mirrored=0, noise=0.0, seed=3000 + i)
+            mode = "rigid"
+        out.append((add_random_bumps(mesh, 0.3, 4000 + i), mode))
+    return out

@@ -3,9 +3,10 @@ counterpart): the stages before the mean shift run mesh by mesh, then one
 mean shift serves every mesh's seeds, each mesh's votes moved to their own
 cell of vote space.  Against sym_detect_fast on each mesh alone: the same
 samples, pairs and votes (exact), and every strongly supported mode with a
-well-defined position (Newton-converged seeds) found again within 1e-4
-relative (the mode-error target: the fused run's FP32 sums go in another
-order, its BF16 tiles hold other seeds)."""
+well-defined position (Newton-converged seeds) found again within 2e-4
+relative -- each run's modes are held to 1e-4 of FP64 (the mode-error
+target), so two runs may differ by twice that: the fused run's FP32 sums go
+in another order, its BF16 tiles hold other seeds."""
 import numpy as np
 import pytest
 
@@ -63,7 +64,7 @@ def test_fused_equals_single_mesh_runs(batch, precision):
                 continue
             want = motion(alone, i)
             err = min(np.linalg.norm(m - want) / np.linalg.norm(want) for m in found)
-            assert err <= 1e-4, (mode, i, err)
+            assert err <= 2e-4, (mode, i, err)
 
 
 def test_fused_rejects_mixed_bandwidths(batch):
@@ -72,3 +73,40 @@ def test_fused_rejects_mixed_bandwidths(batch):
     other = Options(**{**o0.__dict__, "bandwidth": BANDWIDTH * 2})
     with pytest.raises(ValueError):
         gpu.detect_fast_fused([(m0, s0, other)] + rest, mode=modes)
+
+
+def test_uneven_batch_fused(batch):
+    """Twelve meshes of the uneven batch (2k-60k vertices, rigid and
+    reflection mixed, samples drawn on the device): the same pairs and votes
+    as the single-mesh runs, and every strongly supported Newton-converged
+    mode found again (12 modes reported, so that the strong ones are not
+    cut by the cap on the reported count).  "Strongly supported" here also
+    means at least 50 votes within the bandwidth: with 1,500 samples some of
+    these meshes' vote sets are so sparse that most seeds end in modes of a
+    handful of votes, whose positions are noise."""
+    from mitra_algo_gb300.mesh import uneven_batch
+    gpu = batch[0]
+    jobs, modes = [], []
+    for mesh, mode, _ in uneven_batch(12, seed=5):
+        o = Options(sample_ratio=min(1.0, 1500 / mesh.vertex_count),
+                    pair_threshold=0.25 if mode == "rigid" else 0.05, bandwidth=BANDWIDTH,
+                    max_pairs=10 ** 7, max_votes=2 * 10 ** 7, max_clusters=12)
+        jobs.append((gpu.load_mesh_raw(mesh, o), None, o))
+        modes.append(mode)
+    try:
+        kw = dict(precision="bf16", seeds=128, max_iterations=300, polish_iterations=30)
+        fused, _ = gpu.detect_fast_fused(jobs, mode=modes, **kw)
+        for (mesh, _, o), mode, f in zip(jobs, modes, fused):
+            alone = gpu.detect_fast(mesh, None, o, mode=mode, **kw)
+            for k in ("sampled", "pruned", "pairs", "votes"):
+                assert f[k] == alone[k], k
+            strong = max(0.5 * max(alone["support"], default=0), 50)
+            found = [motion(f, i) for i in range(f["clusters"]) if f["precise"][i]]
+            for i in range(alone["clusters"]):
+                if alone["precise"][i] and alone["support"][i] >= strong:
+                    want = motion(alone, i)
+                    err = min(np.linalg.norm(m - want) / np.linalg.norm(want) for m in found)
+                    assert err <= 2e-4, (mode, i, err)
+    finally:
+        for m, _, _ in jobs:
+            m.close()

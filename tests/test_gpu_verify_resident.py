@@ -115,6 +115,27 @@ def test_exact_mirror_of_a_grid(gpu):
     assert got.coverage[0] > 0.9  # the exact mirror is verified nearly everywhere
 
 
+def test_noisy_torus_with_slivers(gpu):
+    """A torus whose vertex noise makes a tenth of its faces slivers (smallest
+    angle under 13 degrees, as on the 1e6-triangle benchmark torus) under
+    rotations about its axis: nearly every image lies on the surface, and
+    many near the edge lines of several faces."""
+    from mitra_algo_gb300.mesh import motif_torus
+    mesh = motif_torus(R=1.0, r=0.3, nu=160, nv=80, copies=6, mirrored=1, noise=3e-3, seed=7)
+    o = Options(verify_threshold=0.01)
+    p = prepare(mesh, o)
+    c = np.asarray(p.context.center)
+    rigid = []
+    for k in (1, 2, 3):
+        R = rotation((0, 0, 1), 2 * np.pi * k / 6)
+        rigid.append((R, c - R @ c))
+    R = rotation((0, 0, 1), 0.37)
+    rigid.append((R, c - R @ c))
+    rigid.append((rotation((0.02, 0.01, 1), 1.1), c - rotation((0.02, 0.01, 1), 1.1) @ c + 2e-3))
+    got, undecided = compare(gpu, p, o, records(rigid=rigid, planes=[((1, 0, 0), 0.0)]))
+    assert max(got.coverage) > 0.5
+
+
 def test_empty_cluster_list(gpu):
     mesh = motif_sphere(level=3, bumps=4, folds=3, partial_shift=0.3, noise=0.0, seed=1)
     o = Options()
