@@ -341,28 +341,33 @@ __device__ __forceinline__ uint32_t active_tiles(const unsigned *nact) {
 // the tile's box and of some group's box (exact, as the chunk tests), and
 // nsurv[t] counts them.
 constexpr int kGroupSeeds = 16, kBoxFloats = 12 * (1 + kChunk / kGroupSeeds);
-__global__ void tile_boxes(const float *means, const int32_t *ids, const unsigned *nact,
-                           const float *bbox, uint32_t nblk, float skip_gap2, float *boxes,
-                           uint32_t *sblk, uint32_t *nsurv) {
+constexpr int kCullThreads = 512;  // threads of tile_boxes (the first kChunk hold the seeds)
+__global__ void __launch_bounds__(kCullThreads) tile_boxes(const float *means, const int32_t *ids,
+                                                           const unsigned *nact, const float *bbox,
+                                                           uint32_t nblk, float skip_gap2,
+                                                           float *boxes, uint32_t *sblk,
+                                                           uint32_t *nsurv) {
   __shared__ float part[kChunk / kGroupSeeds][12];
   __shared__ float tb[kBoxFloats];
-  __shared__ uint32_t warp_cnt[kChunk / 32], base_s;
+  __shared__ uint32_t warp_cnt[kCullThreads / 32], base_s;
   if (blockIdx.x >= active_tiles(nact)) return;
-  const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
-  const bool live = slot < nact[0];
-  float lo[6], hi[6];
-  for (int d = 0; d < 6; ++d) {
-    float m = live ? means[uint64_t(ids[slot]) * 8 + d] : 0.f;
-    lo[d] = live ? m : INFINITY, hi[d] = live ? m : -INFINITY;
-  }
-  for (int o = kGroupSeeds / 2; o; o >>= 1)  // within each group of 16 lanes
+  if (threadIdx.x < kChunk) {  // whole warps
+    const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
+    const bool live = slot < nact[0];
+    float lo[6], hi[6];
     for (int d = 0; d < 6; ++d) {
-      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+      float m = live ? means[uint64_t(ids[slot]) * 8 + d] : 0.f;
+      lo[d] = live ? m : INFINITY, hi[d] = live ? m : -INFINITY;
     }
-  const int group = threadIdx.x / kGroupSeeds;
-  if (threadIdx.x % kGroupSeeds == 0)
-    for (int d = 0; d < 6; ++d) part[group][d] = lo[d], part[group][6 + d] = hi[d];
+    for (int o = kGroupSeeds / 2; o; o >>= 1)  // within each group of 16 lanes
+      for (int d = 0; d < 6; ++d) {
+        lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+        hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+      }
+    const int group = threadIdx.x / kGroupSeeds;
+    if (threadIdx.x % kGroupSeeds == 0)
+      for (int d = 0; d < 6; ++d) part[group][d] = lo[d], part[group][6 + d] = hi[d];
+  }
   if (threadIdx.x == 0) base_s = 0;
   __syncthreads();
   float *out = boxes + uint64_t(blockIdx.x) * kBoxFloats;
@@ -379,7 +384,7 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigne
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t *mine = sblk + uint64_t(blockIdx.x) * nblk;
-  for (uint32_t b0 = 0; b0 < nblk; b0 += kChunk) {
+  for (uint32_t b0 = 0; b0 < nblk; b0 += kCullThreads) {
     const uint32_t b = b0 + threadIdx.x;
     bool keep = false;
     if (b < nblk) {
@@ -393,7 +398,7 @@ __global__ void tile_boxes(const float *means, const int32_t *ids, const unsigne
     if (lane == 0) warp_cnt[warp] = __popc(bal);
     __syncthreads();
     uint32_t before = base_s, total = 0;
-    for (int w = 0; w < kChunk / 32; ++w) {
+    for (int w = 0; w < kCullThreads / 32; ++w) {
       if (w < warp) before += warp_cnt[w];
       total += warp_cnt[w];
     }
@@ -474,88 +479,103 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
   }
 }
 
-// One block per active tile: boff[t * nblk + j] = exclusive scan of the
-// tile's bcount over its surviving blocks, tile_len[t] = the sum.
-__global__ void __launch_bounds__(1024) scan_tiles(const uint32_t *bcount, const unsigned *nact,
-                                                   const uint32_t *nsurv, uint32_t nblk,
-                                                   uint32_t *boff, uint32_t *tile_len) {
-  __shared__ uint32_t warp_sum[32];
-  __shared__ uint32_t carry_s;
-  const uint32_t t = blockIdx.x;
-  if (t >= active_tiles(nact)) return;
-  const uint32_t n = nsurv[t];
-  const uint32_t *in = bcount + uint64_t(t) * nblk;
-  uint32_t *out = boff + uint64_t(t) * nblk;
+// Inclusive scan of one value per thread over a block of 1024 threads;
+// `total` receives the block's sum.  Uses warp_sum[32] (shared).
+__device__ __forceinline__ uint32_t block_scan_1024(uint32_t v, uint32_t *warp_sum, uint32_t &total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) carry_s = 0;
-  __syncthreads();
-  for (uint32_t base = 0; base < n; base += blockDim.x) {
-    const uint32_t j = base + threadIdx.x;
-    const uint32_t v = j < n ? in[j] : 0u;
-    uint32_t x = v;  // inclusive warp scan
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sum[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t w = lane < int(blockDim.x >> 5) ? warp_sum[lane] : 0u;
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += y;
-      }
-      warp_sum[lane] = w;  // inclusive over warps
-    }
-    __syncthreads();
-    if (j < n) out[j] = carry_s + (warp ? warp_sum[warp - 1] : 0u) + x - v;
-    __syncthreads();
-    if (threadIdx.x == 0) carry_s += warp_sum[(blockDim.x >> 5) - 1];
-    __syncthreads();
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  if (threadIdx.x == 0) tile_len[t] = carry_s;
+  if (lane == 31) warp_sum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = warp_sum[lane];
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    warp_sum[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  const uint32_t r = (warp ? warp_sum[warp - 1] : 0u) + x;
+  total = warp_sum[31];
+  __syncthreads();
+  return r;
 }
 
-// One block: offsets[t] = first list entry of tile t (exclusive scan of
-// the active tiles' list lengths; offsets[tiles] = the total), and the work
-// plan: tile t gets pieces[t+1] - pieces[t] CTAs, about len_t * budget /
-// total of them (at least one), so every CTA streams a similar number of
-// chunks; budget = sms - tiles (at least tiles), so the pieces fill one
-// wave of the GPU.
-__global__ void __launch_bounds__(1024) scan_lists(const uint32_t *tile_len, const unsigned *nact,
-                                                   uint32_t sms, uint64_t *offsets, uint32_t *pieces) {
+// One block of 1024 threads.  The surviving (tile, block) entries, tile by
+// tile and in block order within a tile, form the list's order: seg[t] =
+// exclusive scan of nsurv over the active tiles; boff[t * nblk + j] = the
+// list position of entry (t, j)'s first kept chunk (exclusive scan of the
+// counts over all entries in that order); offsets[t] = the first list
+// entry of tile t (offsets[tiles] = the list length); and the work plan:
+// tile t gets pieces[t+1] - pieces[t] CTAs, about len_t * budget / total
+// of them (at least one), so every CTA streams a similar number of chunks;
+// budget = sms - tiles (at least tiles), so the pieces fill one wave of the
+// GPU.  seg holds max_tiles + 1 entries.  A list longer than `cap` (which
+// the counts never give) records DS_CAPACITY and leaves an empty plan.
+__global__ void __launch_bounds__(1024) scan_lists(const uint32_t *bcount, const uint32_t *nsurv,
+                                                   const unsigned *nact, uint32_t nblk, uint32_t sms,
+                                                   uint64_t cap, uint32_t *seg, uint32_t *boff,
+                                                   uint64_t *offsets, uint32_t *pieces,
+                                                   int *status) {
   __shared__ uint32_t warp_sum[32];
   __shared__ uint32_t carry_s;
   const uint32_t tiles = active_tiles(nact);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (threadIdx.x == 0) carry_s = 0;
   __syncthreads();
-  for (uint32_t base = 0; base < tiles; base += blockDim.x) {
-    const uint32_t j = base + threadIdx.x;
-    const uint32_t v = j < tiles ? tile_len[j] : 0u;
-    uint32_t x = v;  // inclusive warp scan
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_sum[warp] = x;
+  for (uint32_t base = 0; base < tiles; base += blockDim.x) {  // segment starts
+    const uint32_t t = base + threadIdx.x;
+    const uint32_t v = t < tiles ? nsurv[t] : 0u;
+    uint32_t total;
+    const uint32_t incl = block_scan_1024(v, warp_sum, total);
+    if (t < tiles) seg[t] = carry_s + incl - v;
     __syncthreads();
-    if (warp == 0) {
-      uint32_t w = lane < int(blockDim.x >> 5) ? warp_sum[lane] : 0u;
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += y;
+    if (threadIdx.x == 0) carry_s += total;
+    __syncthreads();
+  }
+  const uint32_t entries = carry_s;
+  __syncthreads();  // every thread has read carry_s before it is reset
+  if (threadIdx.x == 0) seg[tiles] = entries, carry_s = 0;
+  __syncthreads();
+  for (uint32_t base = 0; base < entries; base += blockDim.x) {  // list positions
+    const uint32_t e = base + threadIdx.x;
+    uint32_t t = 0, v = 0;
+    if (e < entries) {  // the tile of entry e: the last t with seg[t] <= e
+      uint32_t lo = 0, hi = tiles;  // seg[lo] <= e < seg[hi]
+      while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (seg[mid] <= e) lo = mid;
+        else hi = mid;
       }
-      warp_sum[lane] = w;  // inclusive over warps
+      t = lo;
+      v = bcount[uint64_t(t) * nblk + (e - seg[t])];
     }
+    uint32_t total;
+    const uint32_t incl = block_scan_1024(v, warp_sum, total);
+    if (e < entries) boff[uint64_t(t) * nblk + (e - seg[t])] = carry_s + incl - v;
     __syncthreads();
-    if (j < tiles) offsets[j] = carry_s + (warp ? warp_sum[warp - 1] : 0u) + x - v;
-    __syncthreads();
-    if (threadIdx.x == 0) carry_s += warp_sum[(blockDim.x >> 5) - 1];
+    if (threadIdx.x == 0) carry_s += total;
     __syncthreads();
   }
   const uint32_t list_len = carry_s;
+  for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x)  // a tile with no entry starts
+    offsets[t] = seg[t] < seg[t + 1] ? boff[uint64_t(t) * nblk] : 0u;  // fixed below
+  __syncthreads();
+  if (threadIdx.x == 0 && list_len > cap) {
+    atomicExch(status, DS_CAPACITY);
+    for (uint32_t t = 0; t <= tiles; ++t) offsets[t] = 0, pieces[t] = 0;
+    return;
+  }
   if (threadIdx.x == 0) {
+    // empty tiles take the position where the next entries start
+    uint64_t next = list_len;
+    for (uint32_t t = tiles; t-- > 0;) {
+      if (seg[t] < seg[t + 1]) next = offsets[t];
+      else offsets[t] = next;
+    }
     offsets[tiles] = list_len;
     const uint32_t budget = tiles < sms ? sms - tiles : tiles;
     uint32_t at = 0;
@@ -569,17 +589,17 @@ __global__ void __launch_bounds__(1024) scan_lists(const uint32_t *tile_len, con
   }
 }
 
-// list[offsets[t] + boff[t * nblk + j] + r] = t * nchunks + c for the r-th
-// kept chunk c (ascending) of tile t's j-th surviving block: per tile, the
-// kept chunks in ascending order.  CTAs shared among tiles as tile_count's.
+// list[boff[t * nblk + j] + r] = t * nchunks + c for the r-th kept chunk c
+// (ascending) of tile t's j-th surviving block: per tile, the kept chunks in
+// ascending order.  CTAs shared among tiles as tile_count's.
 __global__ void __launch_bounds__(kListThreads) scatter_lists(const uint8_t *need,
                                                               const uint32_t *boff,
                                                               const uint32_t *bcount,
                                                               const uint32_t *sblk,
                                                               const uint32_t *nsurv, uint32_t nblk,
-                                                              const uint64_t *offsets,
                                                               const unsigned *nact,
-                                                              uint64_t nchunks, int32_t *list) {
+                                                              uint64_t nchunks, uint64_t cap,
+                                                              int32_t *list, int *status) {
   __shared__ uint32_t warp_cnt[kListThreads / 32];
   uint32_t t, sub, per;
   if (!list_share(nact, t, sub, per)) return;
@@ -593,10 +613,11 @@ __global__ void __launch_bounds__(kListThreads) scatter_lists(const uint8_t *nee
     const uint32_t bal = __ballot_sync(0xffffffffu, keep);
     if (lane == 0) warp_cnt[warp] = __popc(bal);
     __syncthreads();
-    uint64_t before = offsets[t] + boff[e];
+    uint64_t before = boff[e];
     for (int w = 0; w < warp; ++w) before += warp_cnt[w];
     before += __popc(bal & ((1u << lane) - 1u));
-    if (keep) list[before] = int32_t(uint64_t(t) * nchunks + c);
+    if (keep && before < cap) list[before] = int32_t(uint64_t(t) * nchunks + c);
+    else if (keep) atomicExch(status, DS_CAPACITY);
     __syncthreads();
   }
 }
@@ -1155,10 +1176,18 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   uint8_t *need = call.alloc<uint8_t>(max_tiles * v.nchunks);
   uint32_t *bcount = call.alloc<uint32_t>(max_tiles * nblk), *boff = call.alloc<uint32_t>(max_tiles * nblk);
   uint32_t *sblk = call.alloc<uint32_t>(max_tiles * nblk), *nsurv = call.alloc<uint32_t>(max_tiles);
-  uint32_t *tile_len = call.alloc<uint32_t>(max_tiles);
-  int32_t *list = call.alloc<int32_t>(max_tiles * v.nchunks);
-  // CTAs of the list kernels, shared among the active tiles at run time
-  const unsigned list_ctas = unsigned(std::max<uint64_t>(max_tiles, 8 * 152));
+  uint32_t *seg = call.alloc<uint32_t>(max_tiles + 1);
+  const uint64_t list_cap = max_tiles * v.nchunks;
+  int32_t *list = call.alloc<int32_t>(list_cap);
+  // CTAs of the list kernels, shared among the active tiles at run time:
+  // one full wave of the GPU at their occupancy
+  static const int list_per_sm = [] {
+    int a = 0, b = 0;
+    SYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, tile_count, kListThreads, 0));
+    SYM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, scatter_lists, kListThreads, 0));
+    return std::max(1, std::min(a, b));
+  }();
+  const unsigned list_ctas = unsigned(std::max<uint64_t>(max_tiles, uint64_t(152) * list_per_sm));
   uint64_t *offsets = call.alloc<uint64_t>(max_tiles + 1);
   uint32_t *pieces = call.alloc<uint32_t>(max_tiles + 1);
   // budget + tiles CTAs: tc_ctas_per_sm waves of the 152 SMs
@@ -1190,18 +1219,17 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   int it = 0;
   for (; it < max_iter; ++it) {
     active_seeds_async(call, v, means, state, k, ids, nact, iter, trace_dev, trace_cap);
-    tile_boxes<<<unsigned(max_tiles), kChunk, 0, st>>>(means, ids, nact, v.bbox, nblk, gap * gap,
-                                                        boxes, sblk, nsurv);
+    tile_boxes<<<unsigned(max_tiles), kCullThreads, 0, st>>>(means, ids, nact, v.bbox, nblk,
+                                                              gap * gap, boxes, sblk, nsurv);
     check_launch();
     tile_count<<<list_ctas, kListThreads, 0, st>>>(boxes, means, ids, nact, v.cbox, v.nchunks, sblk,
                                                    nsurv, nblk, gap * gap, need, bcount);
     check_launch();
-    scan_tiles<<<unsigned(max_tiles), 1024, 0, st>>>(bcount, nact, nsurv, nblk, boff, tile_len);
+    scan_lists<<<1, 1024, 0, st>>>(bcount, nsurv, nact, nblk, sms, list_cap, seg, boff, offsets,
+                                   pieces, call.status());
     check_launch();
-    scan_lists<<<1, 1024, 0, st>>>(tile_len, nact, sms, offsets, pieces);
-    check_launch();
-    scatter_lists<<<list_ctas, kListThreads, 0, st>>>(need, boff, bcount, sblk, nsurv, nblk, offsets,
-                                                      nact, v.nchunks, list);
+    scatter_lists<<<list_ctas, kListThreads, 0, st>>>(need, boff, bcount, sblk, nsurv, nblk, nact,
+                                                      v.nchunks, list_cap, list, call.status());
     check_launch();
     if (kernel_ms) mark_event();
     ms_tile_tc<<<unsigned(max_grid), kThreadsTc, kTcSmem, st>>>(args);
@@ -1210,7 +1238,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     ms_update_bulk<<<unsigned((k + 7) / 8), 256, 0, st>>>(means, partial, pieces, ids, nact,
                                                           float(h2), state);
     check_launch();
-    call.launched(7);
+    call.launched(6);
     if (it % kCheck == kCheck - 1) {
       unsigned n = 0;
       call.d2h(&n, nact, sizeof(unsigned));

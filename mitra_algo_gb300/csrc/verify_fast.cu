@@ -463,13 +463,22 @@ struct MotionF {
 // warp of those kernels serves neighbouring vertices of one motion and
 // walks nearly the same BVH nodes, as verify_fp32's warps do; appended in
 // completion order they made every load of a warp 32 scattered ones.
+constexpr uint32_t kNoSlot = 0xffffffffu;
+constexpr int32_t kNoFace = INT32_MIN;  // padding of a candidate list (~f marks an undecided face)
+
 struct RowLists {
   uint32_t *forward;    // accepted forward rows whose FP64 distance is still needed
   int32_t *faces;       // kCandidates faces per forward row (-1 padded)
   uint8_t *mark;        // per row: 1 = left to the next kernel (FP64, then reference order)
   int32_t *fp64;        // rows decided in FP64, ascending
   int32_t *reference;   // rows left to the reference-order BVH, ascending
-  unsigned long long *counts;  // [forward, unused, unused, tie]
+  // the FP32 candidates of an FP64 row (kCandidates per slot, kNoFace
+  // padded), so the FP64 decisions need no search of their own; slot_of[row]
+  // = kNoSlot for a row sent on before its candidates were known
+  uint32_t *slot_of;
+  int32_t *cand;
+  unsigned long long slots;    // capacity of cand, in slots
+  unsigned long long *counts;  // [forward, slots used, unused, tie]
 };
 
 // Decisions in FP32 (verify_fp32).  The reference's tests are made with
@@ -500,7 +509,10 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   if (!inverse) q = q + F3{m.t[0], m.t[1], m.t[2]};
   const float mag = fmaxf(scale, fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z))));
   const float e = kErr * fmaxf(mag, fmaxf(fabsf(m.t[0]), fmaxf(fabsf(m.t[1]), fabsf(m.t[2]))));
-  auto to_fp64 = [&]() { lists.mark[row] = 1; };
+  auto to_fp64 = [&]() {
+    lists.mark[row] = 1;
+    lists.slot_of[row] = kNoSlot;
+  };
   // the image moves at least 2 tau (verification.cpp:64)
   const F3 dq = q - p;
   const float moved = sqrtf(dotf(dq, dq));
@@ -517,12 +529,24 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   float best;
   const int n = candidate_faces(b, q, tau + e, e, faces, keys, best, status);
   if (n > kCandidates) return to_fp64();
+  // from here on an FP64 row keeps its candidates: they hold every face at
+  // the FP64 minimum (the window covers the FP32 error of the FP64 image)
+  auto to_fp64_listed = [&]() {
+    lists.mark[row] = 1;
+    const unsigned long long k = atomicAdd(&lists.counts[1], 1ull);
+    if (k >= lists.slots) {
+      lists.slot_of[row] = kNoSlot;
+      return;
+    }
+    lists.slot_of[row] = uint32_t(k);
+    for (int j = 0; j < kCandidates; ++j) lists.cand[k * kCandidates + j] = j < n ? faces[j] : kNoFace;
+  };
   for (int j = 0; j < n; ++j)
-    if (faces[j] < 0) return to_fp64();  // a badly shaped face
+    if (faces[j] < 0) return to_fp64_listed();  // an undecided face
   if (!n) return;                        // no face within tau (all farther than tau + 3e)
   const float dbest = sqrtf(best);
   if (dbest - e > tau) return;           // every face farther than tau
-  if (dbest + e >= tau) return to_fp64();
+  if (dbest + e >= tau) return to_fp64_listed();
   // the normal test of every candidate (verification.cpp:70-73)
   const F3 ni{vn32[i], vn32[nv + i], vn32[2 * nv + i]};
   const F3 rn{r[0] * ni.x + r[1] * ni.y + r[2] * ni.z, r[3] * ni.x + r[4] * ni.y + r[5] * ni.z,
@@ -533,11 +557,11 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
     // has one): the cosine is good to a few u
     const float4 fn = b.fn[faces[j]];
     const float v = dotf(rn, F3{fn.x, fn.y, fn.z});
-    if (fabsf(v - 0.5f) <= kNormalBand) return to_fp64();
+    if (fabsf(v - 0.5f) <= kNormalBand) return to_fp64_listed();
     if (v >= 0.5f) ++agree;
     else ++disagree;
   }
-  if (agree && disagree) return to_fp64();
+  if (agree && disagree) return to_fp64_listed();
   if (!agree) return;
   flags[row] = 1;
   if (!inverse) {
@@ -629,28 +653,98 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
                                  const ClusterMotion *motions, double tau, float scale,
                                  uint8_t *flags, double *err, RowLists lists,
                                  unsigned long long count, int *status) {
-  const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= count) return;
-  const uint64_t row = lists.fp64[k], nv = b.nv;
+  constexpr int kGroup = 8;  // lanes per row: candidates j = sub and sub + 8
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t k = gid / kGroup;
+  const int sub = threadIdx.x % kGroup;
+  const unsigned group_mask = 0xffu << (threadIdx.x & 31 & ~(kGroup - 1));
+  if (k >= count) return;  // whole groups (count rows x 8 lanes)
+  const uint64_t row = uint64_t(lists.fp64[k]), nv = b.nv;
   const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
   const bool inverse = rem >= nv;
   const uint64_t i = rem % nv;
-  double d = 0;
-  int32_t tied[kCandidates];
-  int v = hybrid_query(b, s, vn, motions[c], inverse, i, tau, scale, d, tied, status);
-  if (v == 3) {
-    atomicAdd(&lists.counts[3], 1ull);
-    const M3 r = query_rotation(motions[c], inverse);
-    D3 q;
-    query_skipped(motions[c], r, inverse, vertex(s, int32_t(i)), tau, q);
-    int32_t first = tied[0];
-    for (int x = 1; x < kCandidates && tied[x] >= 0; ++x)
-      first = first_in_reference_order(t, q, first, tied[x]);
-    v = normal_agrees(s, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
+  const uint32_t slot = lists.slot_of[row];
+  if (slot == kNoSlot) {  // no candidates yet: the search, on one lane
+    if (sub) return;
+    double d = 0;
+    int32_t tied[kCandidates];
+    int v = hybrid_query(b, s, vn, motions[c], inverse, i, tau, scale, d, tied, status);
+    if (v == 3) {
+      atomicAdd(&lists.counts[3], 1ull);
+      const M3 r = query_rotation(motions[c], inverse);
+      D3 q;
+      query_skipped(motions[c], r, inverse, vertex(s, int32_t(i)), tau, q);
+      int32_t first = tied[0];
+      for (int x = 1; x < kCandidates && tied[x] >= 0; ++x)
+        first = first_in_reference_order(t, q, first, tied[x]);
+      v = normal_agrees(s, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
+    }
+    flags[row] = v == 1;
+    if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
+    if (v != 2) lists.mark[row] = 0;  // marked rows go on to the reference-order search
+    return;
   }
-  flags[row] = v == 1;
-  if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
-  if (v != 2) lists.mark[row] = 0;  // marked rows go on to the reference-order search
+  const ClusterMotion &m = motions[c];
+  const M3 r = query_rotation(m, inverse);
+  D3 q;
+  const bool skipped = query_skipped(m, r, inverse, vertex(s, int32_t(i)), tau, q);
+  int v = 0;
+  double dmin = INFINITY;
+  if (!skipped) {
+    // the reference's FP64 distance of each candidate, and the minimum
+    const int32_t *cl = lists.cand + uint64_t(slot) * kCandidates;
+    int32_t f[2];
+    double d[2];
+    for (int h = 0; h < 2; ++h) {
+      const int32_t x = cl[sub + kGroup * h];
+      f[h] = x == kNoFace ? -1 : (x < 0 ? ~x : x);
+      d[h] = f[h] < 0 ? INFINITY
+                      : triangle_d2(q, corner(s, f[h], 0), corner(s, f[h], 1), corner(s, f[h], 2));
+      dmin = fmin(dmin, d[h]);
+    }
+    for (int o = kGroup / 2; o; o >>= 1) dmin = fmin(dmin, __shfl_xor_sync(group_mask, dmin, o));
+    if (dmin <= tau * tau) {
+      // the normal test of the faces at exactly the minimum
+      const D3 ni{vn[i], vn[nv + i], vn[2 * nv + i]};
+      int agree = 0, disagree = 0;
+      bool ok[2] = {false, false};
+      int32_t first = -1;  // this lane's face at the minimum the reference visits first
+      for (int h = 0; h < 2; ++h)
+        if (f[h] >= 0 && d[h] == dmin) {
+          ok[h] = normal_agrees(s, f[h], r, ni);
+          if (ok[h]) ++agree;
+          else ++disagree;
+          first = first < 0 ? f[h] : first_in_reference_order(t, q, first, f[h]);
+        }
+      for (int o = kGroup / 2; o; o >>= 1) {
+        agree += __shfl_xor_sync(group_mask, agree, o);
+        disagree += __shfl_xor_sync(group_mask, disagree, o);
+      }
+      if (agree && disagree) {
+        // faces at the minimum disagree: the one the reference visits first
+        // (its visiting order is a total order on the faces for this
+        // query, so the group reduces it like a minimum)
+        for (int o = kGroup / 2; o; o >>= 1) {
+          const int32_t other = __shfl_xor_sync(group_mask, first, o);
+          if (other >= 0) first = first < 0 ? other : first_in_reference_order(t, q, first, other);
+        }
+        const bool mine_agrees = (f[0] == first && first >= 0 && ok[0]) || (f[1] == first && first >= 0 && ok[1]);
+        v = (__ballot_sync(group_mask, mine_agrees) & group_mask) ? 1 : 0;
+        if (sub == 0) {  // one count per converged set of groups
+          const unsigned active = __activemask();
+          const unsigned leaders = active & 0x01010101u;
+          if ((threadIdx.x & 31) == __ffs(leaders) - 1) atomicAdd(&lists.counts[3], __popc(leaders));
+        }
+      } else {
+        v = agree ? 1 : 0;
+      }
+    }
+  }
+  if (sub == 0) {
+    flags[row] = v == 1;
+    if (!inverse) err[c * nv + i] = v == 1 ? dmin : 0.0;
+    lists.mark[row] = 0;
+  }
 }
 
 // Rows whose candidates overflowed the list: the reference's search itself
@@ -1144,6 +1238,9 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   lists.mark = call.alloc<uint8_t>(rows);
   lists.fp64 = call.alloc<int32_t>(rows);
   lists.reference = call.alloc<int32_t>(rows);
+  lists.slot_of = call.alloc<uint32_t>(rows);
+  lists.slots = std::min<uint64_t>(rows, uint64_t(1) << 24);  // at most 1 GiB of candidates
+  lists.cand = call.alloc<int32_t>(lists.slots * kCandidates);
   lists.counts = call.alloc<unsigned long long>(4);
   uint64_t *listed = call.alloc<uint64_t>(2);
   SYM_CUDA(cudaMemsetAsync(lists.counts, 0, 32, st));
@@ -1166,7 +1263,7 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   if (counts[1]) {
     ensure_ref_bvh(call, m);
     s.nodes = m.ref->dev.nodes, s.ids = m.ref->dev.ids;
-    verify_rows_fp64<<<blocks_for(counts[1]), kThreads, 0, st>>>(view, s, m.ref->dev, m.vn, dm, tau,
+    verify_rows_fp64<<<blocks_for(counts[1] * 8), kThreads, 0, st>>>(view, s, m.ref->dev, m.vn, dm, tau,
                                                                   bvh.scale, flags, err, lists,
                                                                   counts[1], call.status());
     check_launch();
