@@ -131,6 +131,8 @@ sym_status sym_context_create(int device, sym_context **out) {
 
 void sym_context_destroy(sym_context *ctx) {
   if (!ctx) return;
+  for (sym_context *h : ctx->helpers) sym_context_destroy(h);
+  ctx->helpers.clear();
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->arena.release();

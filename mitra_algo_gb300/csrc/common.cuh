@@ -100,6 +100,9 @@ struct sym_context {
   int *host_status = nullptr;   // pinned host mirror for cheap reads
   sym::Metrics metrics;
   cudaDeviceProp prop{};
+  // contexts of the same device this one runs independent per-mesh work on
+  // (the fused batch's modes and verification), created on first use
+  std::vector<sym_context *> helpers;
 };
 
 namespace sym {

@@ -339,14 +339,14 @@ __device__ __forceinline__ uint32_t active_tiles(const unsigned *nact) {
 // tile).  Then the block cull: sblk[t * nblk ..] lists, in ascending order,
 // the blocks of kBlockChunks chunks whose box lies within the bandwidth of
 // the tile's box and of some group's box (exact, as the chunk tests), and
-// nsurv[t] counts them.
+// nsurv[t] counts them; their counts bcount[t * nblk + j] are zeroed.
 constexpr int kGroupSeeds = 16, kBoxFloats = 12 * (1 + kChunk / kGroupSeeds);
 constexpr int kCullThreads = 512;  // threads of tile_boxes (the first kChunk hold the seeds)
 __global__ void __launch_bounds__(kCullThreads) tile_boxes(const float *means, const int32_t *ids,
                                                            const unsigned *nact, const float *bbox,
                                                            uint32_t nblk, float skip_gap2,
                                                            float *boxes, uint32_t *sblk,
-                                                           uint32_t *nsurv) {
+                                                           uint32_t *nsurv, uint32_t *bcount) {
   __shared__ float part[kChunk / kGroupSeeds][12];
   __shared__ float tb[kBoxFloats];
   __shared__ uint32_t warp_cnt[kCullThreads / 32], base_s;
@@ -402,7 +402,11 @@ __global__ void __launch_bounds__(kCullThreads) tile_boxes(const float *means, c
       if (w < warp) before += warp_cnt[w];
       total += warp_cnt[w];
     }
-    if (keep) mine[before + __popc(bal & ((1u << lane) - 1u))] = b;
+    if (keep) {
+      const uint32_t at = before + __popc(bal & ((1u << lane) - 1u));
+      mine[at] = b;
+      bcount[uint64_t(blockIdx.x) * nblk + at] = 0;  // tile_count adds the block's kept chunks
+    }
     __syncthreads();
     if (threadIdx.x == 0) base_s += total;
     __syncthreads();
@@ -427,11 +431,16 @@ constexpr int kListThreads = 256;  // chunks per block of the list kernels
 static_assert(kListThreads == kBlockChunks, "one thread per chunk of a block box");
 
 // need[t * nchunks + c]: some seed of tile t lies within the bandwidth of
-// chunk c's box (tested against the tile's box, then each group's box, then
-// the group's 16 seeds), for the chunks of tile t's surviving blocks.  Exact
-// for Epanechnikov weights: every vote of a skipped chunk is farther than
-// the bandwidth from every seed of the tile.  bcount[t * nblk + j] = the
-// kept chunks of the tile's j-th surviving block.
+// chunk c's box, for the chunks of tile t's surviving blocks: tested
+// against the tile's box, each group's box (16 seeds), each quad's box (4
+// consecutive seeds), then the quad's seeds.  Exact for Epanechnikov
+// weights: every vote of a skipped chunk is farther than the bandwidth from
+// every seed of the tile; and a box holds its seeds' coordinates, so in
+// FP32 too its gap (monotone in every operation) is never above a seed's.
+// bcount[t * nblk + j] (zeroed by tile_boxes) gains the kept chunks of the
+// tile's j-th surviving block, one integer atomic per warp: no barrier
+// between blocks, and the counts do not depend on the order.
+constexpr int kQuads = kChunk / 4;
 __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, const float *means,
                                                            const int32_t *ids, const unsigned *nact,
                                                            const float *cbox, uint64_t nchunks,
@@ -440,6 +449,8 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
                                                            uint8_t *need, uint32_t *bcount) {
   __shared__ float seed[kChunk * 6];
   __shared__ float gb[kBoxFloats];
+  __shared__ float qb[kQuads * 12];
+  __shared__ bool alive[kChunk];
   uint32_t t, sub, per;
   if (!list_share(nact, t, sub, per)) return;
   const unsigned nactive = nact[0];
@@ -448,10 +459,22 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
   for (int i = threadIdx.x; i < kChunk; i += blockDim.x) {
     const uint64_t slot = uint64_t(t) * kChunk + i;
     const bool live = slot < nactive;
+    alive[i] = live;
     for (int d = 0; d < 6; ++d) seed[i * 6 + d] = live ? means[uint64_t(ids[slot]) * 8 + d] : 1e30f;
   }
   if (threadIdx.x < kBoxFloats) gb[threadIdx.x] = boxes[uint64_t(t) * kBoxFloats + threadIdx.x];
   __syncthreads();
+  if (threadIdx.x < kQuads) {  // a quad without live seeds gets an empty box (gap infinite)
+    float lo[6], hi[6];
+    for (int d = 0; d < 6; ++d) lo[d] = INFINITY, hi[d] = -INFINITY;
+    for (int i = 4 * threadIdx.x; i < 4 * threadIdx.x + 4; ++i)
+      if (alive[i])
+        for (int d = 0; d < 6; ++d) lo[d] = fminf(lo[d], seed[i * 6 + d]), hi[d] = fmaxf(hi[d], seed[i * 6 + d]);
+    for (int d = 0; d < 6; ++d) qb[threadIdx.x * 12 + d] = lo[d], qb[threadIdx.x * 12 + 6 + d] = hi[d];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  uint32_t *bc = bcount + uint64_t(t) * nblk;
   for (uint32_t j = sub; j < ns; j += per) {
     const uint64_t c = uint64_t(sblk[uint64_t(t) * nblk + j]) * kBlockChunks + threadIdx.x;
     bool keep = false;
@@ -462,20 +485,23 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
         for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
           const float *b = gb + 12 + 12 * g;
           if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
-          for (int i = kGroupSeeds * g; i < kGroupSeeds * (g + 1) && !keep; ++i) {
-            float q = 0;
-            for (int d = 0; d < 6; ++d) {
-              const float x = seed[i * 6 + d];
-              const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
-              q += e * e;
+          for (int qd = 4 * g; qd < 4 * g + 4 && !keep; ++qd) {
+            if (box_gap2_tc(qb + 12 * qd, qb + 12 * qd + 6, cb) > skip_gap2) continue;
+            for (int i = 4 * qd; i < 4 * qd + 4 && !keep; ++i) {
+              float q = 0;
+              for (int d = 0; d < 6; ++d) {
+                const float x = seed[i * 6 + d];
+                const float e = fmaxf(fmaxf(cb[d] - x, x - cb[6 + d]), 0.f);
+                q += e * e;
+              }
+              keep = q <= skip_gap2;
             }
-            keep = q <= skip_gap2;
           }
         }
       need[uint64_t(t) * nchunks + c] = keep;
     }
-    const int kept = __syncthreads_count(keep);
-    if (threadIdx.x == 0) bcount[uint64_t(t) * nblk + j] = uint32_t(kept);
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0 && bal) atomicAdd(&bc[j], unsigned(__popc(bal)));
   }
 }
 
@@ -1220,7 +1246,7 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
   for (; it < max_iter; ++it) {
     active_seeds_async(call, v, means, state, k, ids, nact, iter, trace_dev, trace_cap);
     tile_boxes<<<unsigned(max_tiles), kCullThreads, 0, st>>>(means, ids, nact, v.bbox, nblk,
-                                                              gap * gap, boxes, sblk, nsurv);
+                                                              gap * gap, boxes, sblk, nsurv, bcount);
     check_launch();
     tile_count<<<list_ctas, kListThreads, 0, st>>>(boxes, means, ids, nact, v.cbox, v.nchunks, sblk,
                                                    nsurv, nblk, gap * gap, need, bcount);

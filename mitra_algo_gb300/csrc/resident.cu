@@ -947,6 +947,19 @@ __global__ void place_votes(const float *desc, uint64_t q, float o0, float o1, f
   o[1] = make_float4(x[4], x[5], x[6], x[7]);
 }
 
+// The first n helper contexts of ctx, created on first use.
+const std::vector<sym_context *> &helper_contexts(sym_context *ctx, int n) {
+  while (int(ctx->helpers.size()) < n) {
+    sym_context *h = nullptr;
+    const sym_status st = sym_context_create(ctx->device, &h);
+    if (st != SYM_OK) fail(st, "helper context: " + sym_error_text);
+    ctx->helpers.push_back(h);
+  }
+  return ctx->helpers;
+}
+
+constexpr int kFusedWorkers = 4;  // host threads (helper contexts) for the per-mesh finish
+
 void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fused_stats &stats) {
   stats = sym_fused_stats{};
   if (!count) return;
@@ -1074,13 +1087,21 @@ void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fu
     stats.seed_iterations = seed_iterations;
     stats.votes = total;
     stats.seeds = k;
-    // ---- modes and verification, mesh by mesh
-    for (uint64_t i = 0; i < count; ++i) {
+    // ---- modes and verification, mesh by mesh on helper contexts: the
+    // meshes are independent and the vote set is complete (the stream was
+    // synchronised above), so a few host threads overlap their launches and
+    // host round trips, each mesh in its own workspace
+    const int workers = int(std::min<uint64_t>(count, kFusedWorkers));
+    const std::vector<sym_context *> &helpers = helper_contexts(call.ctx, workers);
+    std::atomic<uint64_t> next{0};
+    auto finish = [&](sym_context *hctx) {
+     for (uint64_t i = next++; i < count; i = next++) {
       Part &pt = parts[i];
       sym_batch_item &it = items[i];
       if (!pt.q) continue;
       sym_fast_result &r = *it.out;
       try {
+        Call hcall(hctx, "detect_fast_fused");
         float off[6];
         fused_offset(i, off);
         std::vector<float> mi(pt.k * 8);
@@ -1092,18 +1113,26 @@ void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fu
         r.polish_iterations = polish;
         std::vector<double> mode_pos;
         std::vector<uint64_t> rank;
-        mode_phase(call, *it.mesh, vs, mi, si, pt.k, h2, it.fast->mode == SYM_REFLECTION, off,
+        mode_phase(hcall, *it.mesh, vs, mi, si, pt.k, h2, it.fast->mode == SYM_REFLECTION, off,
                    *it.options, r, mode_pos, rank);
         if (it.fast->verify && r.clusters)
-          verification_fast(call, it.mesh->surface(), r.records, r.clusters,
+          verification_fast(hcall, it.mesh->surface(), r.records, r.clusters,
                             it.options->verify_threshold * it.mesh->model.box_size,
                             it.fast->refine, it.mesh->model.center, r.coverage, r.rms, r.patches,
                             &r.verify_undecided, &r.verify_fp64_rows);
       } catch (const Error &e) {
         it.status = e.status;
         std::snprintf(it.message, sizeof(it.message), "%s", e.what());
+      } catch (const std::exception &e) {  // nothing may leave a worker thread
+        it.status = SYM_RUNTIME_ERROR;
+        std::snprintf(it.message, sizeof(it.message), "%s", e.what());
       }
-    }
+     }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < workers; ++w) pool.emplace_back(finish, helpers[w]);
+    finish(helpers[0]);
+    for (auto &t : pool) t.join();
   } else {
     for (int j = 2; j < 5; ++j) SYM_CUDA(cudaEventRecord(ev[j], st));
   }
@@ -1116,6 +1145,8 @@ void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fu
   cudaEventElapsedTime(&t[1], ev[1], ev[2]);
   cudaEventElapsedTime(&t[2], ev[2], ev[3]);
   cudaEventElapsedTime(&t[3], ev[3], ev[4]);
+  // ev[4] -> done spans the per-mesh finish: the main stream is idle while
+  // the helper contexts run it, so its events mark the phase's wall time
   float t_rest = 0;
   cudaEventElapsedTime(&t_rest, ev[4], done);
   stats.meshes = count;
