@@ -197,6 +197,49 @@ def _wall(fn):
     return time.perf_counter() - t0, r
 
 
+def batch_cpu_reference(meshes, results, pair_samples=10 ** 9):
+    """The reference's CPU path (the oracle port, bit-exact with the
+    reference's CPU library) on a few meshes of a batch, each on one host
+    core: reference_sample with `pair_samples` pruned samples paired (scaled
+    to all of them by candidate pairs; every sample by default), the clustering's
+    cost per seed-vote evaluation taken on 4,000 of the mesh's votes, and
+    one verification of the mesh's reported top motion (x max_clusters).
+    Returns the per-mesh lower bounds, their mean, and the implied meshes/s
+    on one core and on all host cores at once (meshes are independent),
+    both upper bounds; the reference stops with "Too many mean-shift modes"
+    at MODE_BUDGET trajectories on meshes whose votes need more."""
+    from mitra_algo_gb300.mesh import prepare
+    from mitra_algo_gb300.types import ClusterOutput, Csr
+    per = []
+    for (mesh, o), r in zip(meshes, results):
+        p = prepare(mesh, o)
+        one = ClusterOutput(np.array([int(r["reflection"][0])], np.uint8),
+                            np.asarray(r["rotation"][0], float).reshape(1, 9),
+                            np.asarray(r["translation"][0], float).reshape(1, 3),
+                            np.asarray(r["plane_normal"][0], float).reshape(1, 3),
+                            np.array([r["plane_offset"][0]], float),
+                            Csr(np.zeros(2, np.uint64), np.zeros(0, np.int32)))
+        ref = reference_sample(p, o, pair_samples=pair_samples, cluster=one)
+        per.append(ref)
+    mean_s = statistics.mean(x["per_mesh_s"] for x in per)
+    cores = os.cpu_count() or 1
+    return {"kind": "port", "meshes_sampled": len(per), "cores_one_mesh_each": 1,
+            "per_mesh_s_lower_bound": [round(x["per_mesh_s"], 2) for x in per],
+            "sample_s": round(sum(x["sample_s"] for x in per), 2),
+            "meshes_per_s_one_core": round(1 / mean_s, 4),
+            "meshes_per_s_all_cores": round(cores / mean_s, 3), "host_cores": cores,
+            "mean_shift_s_lower_bound": [round(x["model_s"]["mean_shift_lower_bound"], 2)
+                                         for x in per],
+            "how": "oracle port of the reference's CPU backend, one core per mesh; "
+                   "per-mesh time = measured curvature, selection, pairing and votes + "
+                   "MODE_BUDGET trajectories x votes x measured cost per seed-vote "
+                   "evaluation + one verification x max_clusters; the mean-shift term is "
+                   "the least work before the reference stops with 'Too many mean-shift "
+                   "modes', which it reaches whenever its trajectories' windows hold fewer "
+                   "than votes / MODE_BUDGET votes each, so the per-mesh time is a lower "
+                   "bound and meshes/s an upper bound"}
+
+
 def c4_leg(gpu, count=256, samples=2000, seeds=256):
     """The uneven batch (BASELINE C4; mesh.uneven_batch): `count` meshes of
     2k-60k vertices (icospheres, tori, mirrored height fields; 1-4 planted
@@ -209,13 +252,14 @@ def c4_leg(gpu, count=256, samples=2000, seeds=256):
     from mitra_algo_gb300.types import Options
     t_gen = time.perf_counter()
     batch = uneven_batch(count)
-    jobs, modes = [], []
+    jobs, modes, opts = [], [], []
     for mesh, mode, _ in batch:
         o = Options(sample_ratio=min(1.0, samples / mesh.vertex_count),
                     pair_threshold=0.25 if mode == "rigid" else 0.05, bandwidth=BANDWIDTH,
                     max_pairs=10 ** 8, max_votes=2 * 10 ** 9 - 1, max_clusters=8)
         jobs.append((gpu.load_mesh_raw(mesh, o), None, o))
         modes.append(mode)
+        opts.append(o)
     t_gen = time.perf_counter() - t_gen
     kw = dict(seeds=seeds, max_iterations=ITERATIONS, polish_iterations=POLISH)
 
@@ -237,6 +281,8 @@ def c4_leg(gpu, count=256, samples=2000, seeds=256):
     def found(rs):  # meshes whose top mode is supported by Newton-converged seeds and covers 30%
         return sum(1 for r in rs if r["clusters"] and r["precise"][0] and r["coverage"][0] >= 0.3)
     same = sum(1 for a, b in zip(rl, rb) if a["pairs"] == b["pairs"] and a["votes"] == b["votes"])
+    picks = [i for i in (0, count // 3, 2 * count // 3, count - 1) if rl[i]["clusters"]][:4]
+    cpu_ref = batch_cpu_reference([(batch[i][0], opts[i]) for i in picks], [rl[i] for i in picks])
     return {"meshes": count, "vertices": [int(min(m.vertex_count for m, _, _ in batch)),
                                           int(max(m.vertex_count for m, _, _ in batch))],
             "samples_per_mesh": samples, "seeds_per_mesh": seeds,
@@ -249,7 +295,7 @@ def c4_leg(gpu, count=256, samples=2000, seeds=256):
                                 ("votes_ms", "vote_set_ms", "bulk_ms", "polish_ms",
                                  "modes_verification_ms")},
             "same_pairs_and_votes": same, "top_mode_found": {"loop": found(rl), "fused": found(rb)},
-            "generate_and_load_s": round(t_gen, 1),
+            "generate_and_load_s": round(t_gen, 1), "cpu_reference": cpu_ref,
             "clock": "host wall clock, synchronous calls; one warm-up pass"}
 
 
@@ -266,13 +312,14 @@ def c5_leg(gpu, count=8, samples=10000, seeds=1024, refine=3, reference_seeds=64
     from mitra_algo_gb300.mesh import stress_batch
     from mitra_algo_gb300.types import Options
     batch = stress_batch(count)
-    jobs, modes = [], []
+    jobs, modes, opts = [], [], []
     for mesh, mode in batch:
         o = Options(sample_ratio=min(1.0, samples / mesh.vertex_count), pair_threshold=0.05,
                     bandwidth=BANDWIDTH, max_pairs=10 ** 8, max_votes=2 * 10 ** 9 - 1,
                     max_clusters=8)
         jobs.append((gpu.load_mesh_raw(mesh, o), None, o))
         modes.append(mode)
+        opts.append(o)
     kw = dict(seeds=seeds, max_iterations=ITERATIONS, polish_iterations=POLISH, refine=refine)
     gpu.detect_fast_fused(jobs, precision="bf16", mode=modes, **kw)
     t_fused, (rf, _) = _wall(lambda: gpu.detect_fast_fused(jobs, precision="bf16", mode=modes, **kw))
@@ -283,6 +330,9 @@ def c5_leg(gpu, count=8, samples=10000, seeds=1024, refine=3, reference_seeds=64
     for m, _, _ in jobs:
         m.close()
     precise_err = [x for r in err for x, ok in zip(r["transform_error"], r["precise"]) if ok]
+    picks = [i for i in (0, 1) if i < count and rl[i]["clusters"]]
+    cpu_ref = batch_cpu_reference([(batch[i][0], opts[i]) for i in picks],
+                                  [rl[i] for i in picks], pair_samples=2000)
     outliers = [1 - min(1.0, sum(r["support"]) / max(r["votes"], 1)) for r in rl]
     return {"meshes": count, "triangles": [int(min(m.faces.shape[1] for m, _ in batch)),
                                            int(max(m.faces.shape[1] for m, _ in batch))],
@@ -302,6 +352,7 @@ def c5_leg(gpu, count=8, samples=10000, seeds=1024, refine=3, reference_seeds=64
                 "transform_all_max": max(r["transform_error_max"] for r in err),
                 "refined_all_max": max(r["transform_error_refined_max"] for r in err)},
             "coverage_top": [round(r["coverage"][0], 3) if r["clusters"] else None for r in rl],
+            "cpu_reference": cpu_ref,
             "clock": "host wall clock, synchronous calls; one warm-up pass"}
 
 
@@ -447,14 +498,15 @@ def peaks():
 MODE_BUDGET = 20000  # the reference's mode budget (src/cpu/clustering.cpp:90-95)
 
 
-def reference_sample(prepared, opts, seed=0, pair_samples=2000, cluster_votes=4000):
+def reference_sample(prepared, opts, seed=0, pair_samples=2000, cluster_votes=4000, cluster=None):
     """One bounded sample of the reference's CPU path on this workload,
     timed on one host core with the oracle (the CPU restatement of the
     reference's backend, bit-exact with it): curvature and selection of the
     full mesh, pairing of `pair_samples` pruned samples drawn with `seed`,
     the votes of those pairs, a reference clustering of `cluster_votes` of
     those votes (its cost per seed-vote evaluation), and the verification of
-    one cluster (the planted 5-fold rotation).  Returns the measured times,
+    one cluster (`cluster`, a ClusterOutput of one record; by default the
+    motif sphere's planted 5-fold rotation).  Returns the measured times,
     the counts, and the per-mesh time they imply by the reference's own
     work: pairing and votes scale with the candidate pairs (S (S - 1) / 2)
     and the pairs; the mean shift runs at least MODE_BUDGET trajectories of
@@ -493,9 +545,9 @@ def reference_sample(prepared, opts, seed=0, pair_samples=2000, cluster_votes=40
     c = np.asarray(p.context.center)
     R = np.array([[np.cos(0.4 * np.pi), -np.sin(0.4 * np.pi), 0],
                   [np.sin(0.4 * np.pi), np.cos(0.4 * np.pi), 0], [0, 0, 1]])
-    one = ClusterOutput(np.zeros(1, np.uint8), R.reshape(1, 9), (c - R @ c).reshape(1, 3),
-                        np.zeros((1, 3)), np.zeros(1),
-                        Csr(np.zeros(2, np.uint64), np.zeros(0, np.int32)))
+    one = cluster if cluster is not None else ClusterOutput(
+        np.zeros(1, np.uint8), R.reshape(1, 9), (c - R @ c).reshape(1, 3), np.zeros((1, 3)),
+        np.zeros(1), Csr(np.zeros(2, np.uint64), np.zeros(0, np.int32)))
     t0 = time.perf_counter()
     cpu.verification(p.mesh, p.topology, one, p.context, o)
     t_ver = time.perf_counter() - t0
