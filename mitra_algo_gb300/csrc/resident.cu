@@ -30,6 +30,8 @@
 #include <cmath>
 #include <limits>
 #include <map>
+#include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -983,47 +985,83 @@ void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fu
   }
   if (!(h > 0 && h < 2)) fail(SYM_INVALID_ARGUMENT, "fused detection needs a bandwidth below 2");
   cudaStream_t st = call.stream();
-  StageClock clock(st);
   cudaEvent_t ev[5];
   for (auto &e : ev) SYM_CUDA(cudaEventCreate(&e));
   SYM_CUDA(cudaEventRecord(ev[0], st));
-  // ---- the stages before the mean shift, mesh by mesh
+  // ---- the stages before the mean shift, mesh by mesh on helper contexts:
+  // one Call per helper thread for the whole phase, so each mesh's votes
+  // stay in its helper's workspace (an arena is reset only when the next
+  // Call on that context begins, after the shared mean shift) until the
+  // main stream has gathered them; offsets follow the meshes' order
   struct Part {
     float *desc = nullptr;
     uint64_t q = 0, base = 0, k = 0, seed_base = 0;
-    bool ok = false;
+    bool ok = false, done = false;
   };
   std::vector<Part> parts(count);
-  uint64_t total = 0;
-  for (uint64_t i = 0; i < count; ++i) {
-    sym_batch_item &it = items[i];
-    sym_fast_result &r = *it.out;
-    r = sym_fast_result{};
-    it.status = SYM_OK;
-    it.message[0] = 0;
-    try {
-      sym_rng rng;
-      const bool on_device = !it.sample && it.sample_count == SYM_SAMPLE_ON_DEVICE;
-      if (on_device) {
-        validate_prepare_options(*it.options);
-        sym_rng_seed(&rng, it.options->seed);
-      } else {
-        for (uint64_t j = 0; j < it.sample_count; ++j)
-          if (it.sample[j] < 0 || uint64_t(it.sample[j]) >= it.mesh->nv)
-            fail(SYM_INVALID_ARGUMENT, "sample vertex index out of range");
+  const int workers = int(std::min<uint64_t>(count, kFusedWorkers));
+  const std::vector<sym_context *> &helpers = helper_contexts(call.ctx, workers);
+  {
+    std::atomic<uint64_t> next{0};
+    std::string failure;
+    std::mutex failure_lock;
+    auto prepare_votes = [&](sym_context *hctx) {
+      try {
+        Call hcall(hctx, "detect_fast_fused");
+        StageClock hclock(hcall.stream());
+        for (uint64_t i = next++; i < count; i = next++) {
+          sym_batch_item &it = items[i];
+          sym_fast_result &r = *it.out;
+          r = sym_fast_result{};
+          it.status = SYM_OK;
+          it.message[0] = 0;
+          parts[i].done = true;
+          try {
+            sym_rng rng;
+            const bool on_device = !it.sample && it.sample_count == SYM_SAMPLE_ON_DEVICE;
+            if (on_device) {
+              validate_prepare_options(*it.options);
+              sym_rng_seed(&rng, it.options->seed);
+            } else {
+              for (uint64_t j = 0; j < it.sample_count; ++j)
+                if (it.sample[j] < 0 || uint64_t(it.sample[j]) >= it.mesh->nv)
+                  fail(SYM_INVALID_ARGUMENT, "sample vertex index out of range");
+            }
+            double *unused = nullptr;
+            parts[i].q = vote_phase(hcall, *it.mesh, on_device ? nullptr : it.sample,
+                                    on_device ? 0 : it.sample_count, *it.options, *it.fast, r,
+                                    on_device ? &rng : nullptr, false, hclock, &parts[i].desc,
+                                    &unused);
+            parts[i].ok = true;
+          } catch (const Error &e) {
+            it.status = e.status;
+            std::snprintf(it.message, sizeof(it.message), "%s", e.what());
+          } catch (const std::exception &e) {  // nothing may leave a worker thread
+            it.status = SYM_RUNTIME_ERROR;
+            std::snprintf(it.message, sizeof(it.message), "%s", e.what());
+          }
+        }
+        hcall.sync();  // this helper's votes are complete
+      } catch (const std::exception &e) {
+        std::lock_guard<std::mutex> g(failure_lock);
+        failure = e.what();
       }
-      double *unused = nullptr;
-      parts[i].q = vote_phase(call, *it.mesh, on_device ? nullptr : it.sample,
-                              on_device ? 0 : it.sample_count, *it.options, *it.fast, r,
-                              on_device ? &rng : nullptr, false, clock, &parts[i].desc, &unused);
-      parts[i].ok = true;
-      parts[i].base = total;
-      total += parts[i].q;
-    } catch (const Error &e) {
-      it.status = e.status;
-      std::snprintf(it.message, sizeof(it.message), "%s", e.what());
-    }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < workers; ++w) pool.emplace_back(prepare_votes, helpers[w]);
+    prepare_votes(helpers[0]);
+    for (auto &t : pool) t.join();
+    for (uint64_t i = 0; i < count; ++i)
+      if (!parts[i].done) {  // a helper that could not start left it
+        items[i].status = SYM_RUNTIME_ERROR;
+        *items[i].out = sym_fast_result{};
+        std::snprintf(items[i].message, sizeof(items[i].message), "%s",
+                      failure.empty() ? "not processed" : failure.c_str());
+      }
   }
+  uint64_t total = 0;
+  for (uint64_t i = 0; i < count; ++i)
+    if (parts[i].ok) parts[i].base = total, total += parts[i].q;
   if (total > uint64_t(std::numeric_limits<int32_t>::max()))
     fail(SYM_RUNTIME_ERROR, "Vote budget exceeded; lower --sample-ratio or tighten --pair-threshold");
   SYM_CUDA(cudaEventRecord(ev[1], st));
@@ -1091,8 +1129,6 @@ void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fu
     // meshes are independent and the vote set is complete (the stream was
     // synchronised above), so a few host threads overlap their launches and
     // host round trips, each mesh in its own workspace
-    const int workers = int(std::min<uint64_t>(count, kFusedWorkers));
-    const std::vector<sym_context *> &helpers = helper_contexts(call.ctx, workers);
     std::atomic<uint64_t> next{0};
     auto finish = [&](sym_context *hctx) {
      for (uint64_t i = next++; i < count; i = next++) {

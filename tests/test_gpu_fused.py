@@ -110,3 +110,21 @@ def test_uneven_batch_fused(batch):
     finally:
         for m, _, _ in jobs:
             m.close()
+
+
+def test_fused_reports_a_failing_item(batch):
+    """An item whose sample holds an out-of-range vertex fails with the
+    reference's message while the others are processed, and the context
+    (with its helper contexts) serves the next fused call unchanged."""
+    gpu, jobs, modes = batch
+    kw = dict(precision="bf16", seeds=64, max_iterations=60, polish_iterations=20)
+    (m0, _, o0) = jobs[0]
+    bad = np.array([0, m0.prepared.mesh.vertex_count], np.int32)
+    with pytest.raises(Exception, match="sample vertex index out of range"):
+        gpu.detect_fast_fused([jobs[1], (m0, bad, o0), jobs[2]], mode=[modes[1], modes[0], modes[2]],
+                              **kw)
+    again, _ = gpu.detect_fast_fused(jobs[1:3], mode=modes[1:3], **kw)
+    first, _ = gpu.detect_fast_fused(jobs[1:3], mode=modes[1:3], **kw)
+    for a, b in zip(again, first):
+        for k in ("sampled", "pairs", "votes", "clusters", "support"):
+            assert a[k] == b[k], k
