@@ -241,7 +241,7 @@ def batch_cpu_reference(meshes, results, pair_samples=10 ** 9):
 
 
 def c4_leg(gpu, count=256, samples=2000, seeds=256):
-    """The uneven batch (BASELINE C4; mesh.uneven_batch): `count` meshes of
+    """The uneven batch (mesh.uneven_batch): `count` meshes of
     2k-60k vertices (icospheres, tori, mirrored height fields; 1-4 planted
     symmetries; noise sigma in [0, 5e-3]), each loaded raw through the GPU
     prepare and sampled on the device: meshes/s of sym_detect_fast one mesh
@@ -300,7 +300,7 @@ def c4_leg(gpu, count=256, samples=2000, seeds=256):
 
 
 def c5_leg(gpu, count=8, samples=10000, seeds=1024, refine=3, reference_seeds=64):
-    """The stress batch (BASELINE C5; mesh.stress_batch): `count` meshes of
+    """The stress batch (mesh.stress_batch): `count` meshes of
     1e5-1e6 triangles, half reflection and half rigid, 30% of each surface
     unsymmetric relief: the full pipeline with verification and `refine`
     FP64 ICP passes, meshes/s one mesh after the other and fused; then, per
@@ -357,7 +357,7 @@ def c5_leg(gpu, count=8, samples=10000, seeds=1024, refine=3, reference_seeds=64
 
 
 def c3_leg(gpu, steps=3):
-    """The large single mesh (BASELINE C3; workload "c3"): the torus of 1e6
+    """The large single mesh (workload "c3"): the torus of 1e6
     triangles with 12 rotated motif copies (2 mirrored), 200,000 samples
     drawn on the device, votes subsampled to 1e6, 4,096 seeds: device time
     per mesh (CUDA events) of both mean-shift forms, and the error of 256
@@ -1089,11 +1089,11 @@ def main():
     ap.add_argument("--config", choices=["c2", "c3"], default="c2",
                     help="c2: the motif icosphere (default); c3: the 1e6-triangle torus "
                          "(no batch, reflection or CPU legs)")
-    ap.add_argument("--c3", type=int, default=1, help="1: include the large-torus leg (C3)")
+    ap.add_argument("--c3", type=int, default=1, help="1: include the large-torus leg (the line's c3 field)")
     ap.add_argument("--c4-meshes", type=int, default=256,
-                    help="meshes of the uneven batch leg (C4; 0: skip)")
+                    help="meshes of the uneven batch leg (the c4 field; 0: skip)")
     ap.add_argument("--c5-meshes", type=int, default=8,
-                    help="meshes of the stress batch leg (C5, full size 64; 0: skip)")
+                    help="meshes of the stress batch leg (the c5 field; full size 64; 0: skip)")
     ap.add_argument("--batch", type=int, default=48,
                     help="meshes of the uneven batch measurement (0: skip)")
     ap.add_argument("--batch-workers", type=int, default=4,

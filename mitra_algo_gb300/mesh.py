@@ -358,7 +358,7 @@ def add_noise(mesh: Mesh, sigma: float, seed: int) -> Mesh:
 
 
 def uneven_batch(count=256, seed=0):
-    """The uneven batch (BASELINE C4): `count` seeded meshes, an even mix of
+    """The uneven batch: `count` seeded meshes, an even mix of
     motif icospheres, motif tori and mirrored height fields, vertex counts
     log-uniform in 2k-60k (the nearest icosphere level; grid sizes for the
     others), each with 1-4 planted symmetries (rotations about z of a
@@ -394,7 +394,7 @@ def uneven_batch(count=256, seed=0):
 
 
 def stress_batch(count=64, seed=1):
-    """The stress batch (BASELINE C5): `count` seeded meshes of 1e5-1e6
+    """The stress batch: `count` seeded meshes of 1e5-1e6
     triangles (log-uniform), half reflection (mirrored height fields) and
     half rigid (motif tori with rotated copies), with unsymmetric random
     bumps over about 30% of each surface, so that most pairs vote for no

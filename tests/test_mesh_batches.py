@@ -1,4 +1,4 @@
-"""The seeded C4/C5 batch generators (mesh.uneven_batch, mesh.stress_batch):
+"""The seeded batch generators (mesh.uneven_batch: 2k-60k-vertex meshes; mesh.stress_batch: 1e5-1e6 triangles):
 deterministic, with vertex and triangle counts inside their stated ranges,
 valid faces and the stated mode mix."""
 import numpy as np
