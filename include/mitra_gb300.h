@@ -305,6 +305,9 @@ typedef struct sym_mesh_handle sym_mesh_handle;
 sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh,
                          const sym_topology_view *topology,
                          const sym_model_context *model, sym_mesh_handle **out);
+/* Waits for all work on the mesh's device, then frees the mesh; any
+ * context may have used it, and the loading context may already be
+ * destroyed. */
 void sym_mesh_free(sym_mesh_handle *handle);
 
 enum { SYM_MS_FP32 = 0, SYM_MS_BF16_REFINED = 1 };

@@ -540,6 +540,7 @@ class ResidentMesh:
 
     def __init__(self, backend: Gb300Backend, prepared: Prepared, raw=None):
         self._lib = backend._lib
+        self._backend = backend  # its context outlives the mesh
         self.prepared = prepared
         h = C.c_void_p()
         if raw is not None:  # prepared on the GPU from the raw mesh

@@ -56,7 +56,7 @@ void tc_selftest_host(Call &call, const uint16_t *a1, const uint16_t *b1, const 
 }  // namespace sym
 
 struct sym_mesh_handle {
-  sym_context *ctx = nullptr;
+  int device = 0;  // the device holding its memory (not tied to the loading context)
   sym_mesh_view host{};
   std::vector<sym_edge> host_edges;  // sym_mesh_load only (an edge table in any order)
   sym_model_context model{};
@@ -1272,7 +1272,7 @@ sym_status sym_mesh_load(sym_context *ctx, const sym_mesh_view *mesh, const sym_
           uint64_t(mesh->faces.v2[f]) >= nv)
         sym::fail(SYM_INVALID_ARGUMENT, "Face index out of range");
     auto h = new sym_mesh_handle();
-    h->ctx = ctx;
+    h->device = ctx->device;
     h->host = *mesh;
     h->model = *model;
     h->nv = nv, h->nf = nf, h->ne = ne;
@@ -1349,7 +1349,7 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
     sym::Call call(ctx, "mesh_load_raw");
     const sym::PreparedDevice p = sym::prepare_device(call, *mesh, *options);
     h = new sym_mesh_handle();
-    h->ctx = ctx;
+    h->device = ctx->device;
     h->host = sym_mesh_view{};  // the vertices and faces live on the device only
     h->model = p.context;
     h->nv = p.nv, h->nf = p.nf, h->ne = p.ne, h->nbr_count = p.nbr_count;
@@ -1419,8 +1419,10 @@ sym_status sym_mesh_load_raw(sym_context *ctx, const sym_mesh_view *mesh,
 
 void sym_mesh_free(sym_mesh_handle *h) {
   if (!h) return;
-  cudaSetDevice(h->ctx->device);
-  cudaStreamSynchronize(h->ctx->stream);
+  // every stream of the device may still read the mesh (any context can
+  // use it); the loading context may already be gone
+  cudaSetDevice(h->device);
+  cudaDeviceSynchronize();
   h->release();
   delete h;
 }
