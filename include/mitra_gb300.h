@@ -530,12 +530,13 @@ sym_status sym_detect_fast_fused(sym_context *ctx, sym_batch_item *items, uint64
  * counterpart): K seeds over Q 6-D votes (host, q x 6 doubles), seeds are
  * vote indices.  Approach phase (at most max_iterations, in the requested
  * precision: FP32, BF16 tensor cores, or FP64): plain mean-shift steps until a
- * seed's squared step is below 1e-4 h^2.  Polish phase (at most
+ * seed's squared step is below 4e-4 h^2 (a step under h/50).  Polish phase (at most
  * polish_iterations, FP32; FP64 for SYM_MS_FP64): safeguarded Newton steps on
  * m(x) = x until a Newton step is below 1e-4 h (converged).  A rejected
  * Newton step (singular system, step longer than h/4 or against the plain
- * step: the density is flat along some direction, the mode has no
- * well-defined position) settles the seed after one plain step.  Writes
+ * step) is replaced by the plain step and Newton is tried again; the third
+ * rejection settles the seed (the density is flat along some direction,
+ * the mode has no well-defined position).  Writes
  * the K final means (k x 6), each seed's state (0 still approaching,
  * 1 converged, 2 exhausted, 3 near a mode when the iterations ran out,
  * 4 settled) and the approach / polish iteration counts.  `precision`: SYM_MS_FP32,

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(kChunk) ms_tile(const T *desc, const float *cb
   uint64_t slots = uint64_t(gridDim.x) * kChunk;
   bool live = slot < nactive;
   int32_t seed = live ? ids[slot] : 0;
-  const bool newton = NEWTON && !COUNT && live && state[seed] == kNear;
+  const bool newton = NEWTON && !COUNT && live && is_near(state[seed]);
   T m[6];
   for (int d = 0; d < 6; ++d) m[d] = live ? means[uint64_t(seed) * 8 + d] : T(0);
   float lo[6], hi[6];
@@ -342,7 +342,8 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
   const uint64_t slot = uint64_t(blockIdx.x) * kChunk + threadIdx.x;
   if (slot >= nactive) return;
   const int32_t s = ids[slot];
-  const bool near = state[s] == kNear;
+  const uint8_t st_s = state[s];
+  const bool near = is_near(st_s);
   T acc[7] = {0, 0, 0, 0, 0, 0, 0}, ns[27];
   for (int g = 0; g < kGroups; ++g)
     for (int d = 0; d < 7; ++d) acc[d] += red[(uint64_t(g) * kPartial + d) * slots + slot];
@@ -384,9 +385,10 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
     for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + step[d];
     if (len < T(kNewtonStop2) * h2) state[s] = kConverged;
     else if (polish_it >= kNewtonCap) state[s] = kSettled;
-  } else {
+  } else {  // rejected: the plain step, and Newton again (settled at the third rejection)
     for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + delta[d];
-    state[s] = kSettled;
+    state[s] = polish_it >= kNewtonCap ? kSettled
+             : st_s == kNear ? kNearRetry1 : st_s == kNearRetry1 ? kNearRetry2 : kSettled;
   }
 }
 
@@ -412,7 +414,7 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
   bool sort = k <= kRetile;
   for (uint64_t at = 0; at < k; at += blockDim.x) {
     uint64_t s = at + threadIdx.x;
-    bool act = s < k && (state[s] == kMoving || (include_near && state[s] == kNear));
+    bool act = s < k && (state[s] == kMoving || (include_near && is_near(state[s])));
     unsigned bal = __ballot_sync(0xffffffffu, act);
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) warp_tot[warp] = __popc(bal);
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
       total += warp_tot[w];
     }
     unsigned pos = base_s + before + __popc(bal & ((1u << lane) - 1));
-    if (act && state[s] == kNear) atomicAdd(&near_s, 1u);
+    if (act && is_near(state[s])) atomicAdd(&near_s, 1u);
     if (act) {
       if (sort) {
         float x[6];

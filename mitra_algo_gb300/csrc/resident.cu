@@ -1505,6 +1505,8 @@ sym_status sym_meanshift6(sym_context *ctx, const double *votes, uint64_t q, con
     }
     call.d2h(state_out, state, k);
     call.check_status("mean_shift6");
+    for (uint64_t i = 0; i < k; ++i)  // a seed between Newton retries is near a mode
+      if (sym::is_near(state_out[i])) state_out[i] = sym::kNear;
     for (uint64_t i = 0; i < k; ++i)
       for (int d = 0; d < 6; ++d) means_out[i * 6 + d] = out[i * 8 + d];
     return SYM_OK;

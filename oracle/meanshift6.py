@@ -5,17 +5,17 @@ unpinned).
 Epanechnikov weights w = 1 - d^2/h^2 for d^2 < h^2 (kernel "epanechnikov"),
 or the shifted Gaussian w = 2^(-8 d^2/h^2) - 2^-8 for d^2 < h^2 (kernel
 "gaussian": zero at the cut).  A seed takes plain mean-shift steps m(x) - x until its squared
-step is below 1e-4 h^2, then safeguarded Newton steps on m(x) = x:
+step is below 4e-4 h^2 (a step under h/50), then safeguarded Newton steps on m(x) = x:
     (I - J) s = m(x) - x,   J = 2 / (h^2 sum w) * (sum d d^T - (m - x) (sum d)^T)
 with d = v - x over the votes within the bandwidth (Epanechnikov), or
     J = 2 k ln2 / (h^2 sum w) * (sum g d d^T - (m - x) (sum g d)^T)
 with g = w + 2^-k = 2^(-k d^2/h^2), k = 8 (Gaussian: dw/dx = 2 k ln2 g d / h^2).  A Newton step is taken
 when the 6x6 system is regular (pivots above 1e-12), |s| <= h/4 and
 s.(m - x) > 0 (or the step already meets the convergence test); otherwise the
-density is flat along some direction (a ridge, no well-defined mode
-position): the plain step is taken and the seed stops (settled).  A seed
-whose accepted Newton steps have not converged after 10 polish iterations
-settles too.  Stopping rules: exhausted when the total weight is <= 1e-14
+plain step is taken and Newton is tried again at the next iteration; at the
+third rejection the density is flat along some direction (a ridge, no
+well-defined mode position) and the seed stops (settled).  A seed of the
+polish not converged after 10 polish iterations settles too.  Stopping rules: exhausted when the total weight is <= 1e-14
 (the reference's rule, src/cpu/clustering.cpp:169-181), converged when a
 Newton step's square is below 1e-8 h^2.  States: 0 approaching,
 1 converged, 2 exhausted, 3 near a mode, 4 settled.
@@ -23,7 +23,8 @@ Newton step's square is below 1e-8 h^2.  States: 0 approaching,
 import numpy as np
 
 MOVING, CONVERGED, EXHAUSTED, NEAR, SETTLED = 0, 1, 2, 3, 4
-SWITCH2, NEWTON_STOP2, TRUST, NEWTON_CAP = 1e-4, 1e-8, 0.25, 10
+NEAR1, NEAR2 = 5, 6  # near after one / two rejected Newton steps (reported as NEAR)
+SWITCH2, NEWTON_STOP2, TRUST, NEWTON_CAP = 4e-4, 1e-8, 0.25, 10
 GAUSS_K = 8.0  # base-2 exponent scale of the Gaussian kernel
 
 
@@ -55,9 +56,10 @@ def solve6(M, b, tiny=1e-12):
     return b
 
 
-def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov"):
-    """The kNear step of one seed from its weights w over all votes x
-    (polish_it: the polish iteration, -1 in the approach phase)."""
+def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov", state=NEAR):
+    """The kNear step of one seed (in `state`: NEAR, NEAR1 or NEAR2) from its
+    weights w over all votes x (polish_it: the polish iteration, -1 in the
+    approach phase)."""
     inside = w > 0
     di = x[inside] - m
     if kernel == "gaussian":
@@ -74,8 +76,10 @@ def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov")
             and (s @ delta > 0 or s @ s < NEWTON_STOP2 * h2)):
         if s @ s < NEWTON_STOP2 * h2:
             return m + s, CONVERGED
-        return m + s, SETTLED if polish_it >= NEWTON_CAP else NEAR
-    return m + delta, SETTLED
+        return m + s, SETTLED if polish_it >= NEWTON_CAP else state
+    if polish_it >= NEWTON_CAP:
+        return m + delta, SETTLED
+    return m + delta, {NEAR: NEAR1, NEAR1: NEAR2}.get(int(state), SETTLED)
 
 
 def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=100, block=64,
@@ -91,13 +95,15 @@ def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=10
     counts = []
     for phase, budget in ((False, max_iterations), (True, polish_iterations)):
         counts.append(_phase(x, means, state, h2, budget, phase, block, kernel))
+    state[(state == NEAR1) | (state == NEAR2)] = NEAR
     return means, state, tuple(counts)
 
 
 def _phase(x, means, state, h2, budget, polish, block, kernel):
     iterations = 0
     for it in range(budget):
-        act = np.flatnonzero((state == MOVING) | ((state == NEAR) & polish))
+        near = (state == NEAR) | (state == NEAR1) | (state == NEAR2)
+        act = np.flatnonzero((state == MOVING) | (near & polish))
         if act.size == 0:
             break
         iterations += 1
@@ -119,7 +125,7 @@ def _phase(x, means, state, h2, budget, polish, block, kernel):
                         state[i] = NEAR
                 else:
                     means[i], state[i] = newton_seed(x, m[j], w[j], tot[j], delta[j], move[j], h2,
-                                                     it if polish else -1, kernel)
+                                                     it if polish else -1, kernel, state[i])
     return iterations
 
 

@@ -81,9 +81,10 @@ def test_uneven_batch_fused(batch):
     as the single-mesh runs, and every strongly supported Newton-converged
     mode found again (12 modes reported, so that the strong ones are not
     cut by the cap on the reported count).  "Strongly supported" here also
-    means at least 50 votes within the bandwidth: with 1,500 samples some of
-    these meshes' vote sets are so sparse that most seeds end in modes of a
-    handful of votes, whose positions are noise."""
+    means at least 50 votes within the
+    bandwidth: with 1,500 samples some of these meshes' vote sets are so
+    sparse that most seeds end in modes of a handful of votes, whose
+    positions are noise."""
     from mitra_algo_gb300.mesh import uneven_batch
     gpu = batch[0]
     jobs, modes = [], []
