@@ -534,9 +534,9 @@ sym_status sym_detect_fast_fused(sym_context *ctx, sym_batch_item *items, uint64
  * polish_iterations, FP32; FP64 for SYM_MS_FP64): safeguarded Newton steps on
  * m(x) = x until a Newton step is below 1e-4 h (converged).  A rejected
  * Newton step (singular system, step longer than h/4 or against the plain
- * step) is replaced by the plain step and Newton is tried again; the third
- * rejection settles the seed (the density is flat along some direction,
- * the mode has no well-defined position).  Writes
+ * step) is replaced by the plain step and Newton is tried once more; the
+ * second rejection settles the seed (the density is flat along some
+ * direction, the mode has no well-defined position).  Writes
  * the K final means (k x 6), each seed's state (0 still approaching,
  * 1 converged, 2 exhausted, 3 near a mode when the iterations ran out,
  * 4 settled) and the approach / polish iteration counts.  `precision`: SYM_MS_FP32,

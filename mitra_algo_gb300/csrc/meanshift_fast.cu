@@ -385,10 +385,9 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
     for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + step[d];
     if (len < T(kNewtonStop2) * h2) state[s] = kConverged;
     else if (polish_it >= kNewtonCap) state[s] = kSettled;
-  } else {  // rejected: the plain step, and Newton again (settled at the third rejection)
+  } else {  // rejected: the plain step, and Newton once more (settled at the second rejection)
     for (int d = 0; d < 6; ++d) means[uint64_t(s) * 8 + d] = x[d] + delta[d];
-    state[s] = polish_it >= kNewtonCap ? kSettled
-             : st_s == kNear ? kNearRetry1 : st_s == kNearRetry1 ? kNearRetry2 : kSettled;
+    state[s] = polish_it < kNewtonCap && st_s == kNear ? kNearRetry1 : kSettled;
   }
 }
 

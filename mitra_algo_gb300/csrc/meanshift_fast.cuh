@@ -24,19 +24,17 @@ constexpr int kChunk = 128;  // votes per chunk = seeds per tile
 // singular, the step is longer than kTrust h or points against the plain
 // step (unless it already meets the convergence test): the seed takes the
 // plain step instead and tries Newton again at the next iteration
-// (kNearRetry1, kNearRetry2); a third rejection means the density is flat
-// along some direction there (a ridge), so the mode has no well-defined
-// position and the seed stops (kSettled).  kExhausted: total weight <= 1e-14.
+// (kNearRetry1); a second rejection means the density is flat along some
+// direction there (a ridge), so the mode has no well-defined position and
+// the seed stops (kSettled).  kExhausted: total weight <= 1e-14.
 // A seed of the polish still unconverged after kNewtonCap polish iterations
 // (Newton steps that keep being accepted without shrinking, or rejected)
 // settles too.  The retries matter for the BF16 form, whose approach ends
 // within the rounding of its weights: one rejection decided by that
 // rounding no longer fixes the seed's fate.
 constexpr uint8_t kMoving = 0, kConverged = 1, kExhausted = 2, kNear = 3, kSettled = 4;
-constexpr uint8_t kNearRetry1 = 5, kNearRetry2 = 6;  // kNear after one / two rejected Newton steps
-__host__ __device__ inline bool is_near(uint8_t s) {
-  return s == kNear || s == kNearRetry1 || s == kNearRetry2;
-}
+constexpr uint8_t kNearRetry1 = 5;  // kNear after one rejected Newton step
+__host__ __device__ inline bool is_near(uint8_t s) { return s == kNear || s == kNearRetry1; }
 constexpr double kSwitch2 = 4e-4, kNewtonStop2 = 1e-8, kTrust = 0.25;
 constexpr int kNewtonCap = 10;
 // Floats (or doubles) per partial sum of one seed: sum w (v - x) (6), sum w, pad,

@@ -12,8 +12,8 @@ with d = v - x over the votes within the bandwidth (Epanechnikov), or
 with g = w + 2^-k = 2^(-k d^2/h^2), k = 8 (Gaussian: dw/dx = 2 k ln2 g d / h^2).  A Newton step is taken
 when the 6x6 system is regular (pivots above 1e-12), |s| <= h/4 and
 s.(m - x) > 0 (or the step already meets the convergence test); otherwise the
-plain step is taken and Newton is tried again at the next iteration; at the
-third rejection the density is flat along some direction (a ridge, no
+plain step is taken and Newton is tried once more at the next iteration; at
+the second rejection the density is flat along some direction (a ridge, no
 well-defined mode position) and the seed stops (settled).  A seed of the
 polish not converged after 10 polish iterations settles too.  Stopping rules: exhausted when the total weight is <= 1e-14
 (the reference's rule, src/cpu/clustering.cpp:169-181), converged when a
@@ -23,7 +23,7 @@ Newton step's square is below 1e-8 h^2.  States: 0 approaching,
 import numpy as np
 
 MOVING, CONVERGED, EXHAUSTED, NEAR, SETTLED = 0, 1, 2, 3, 4
-NEAR1, NEAR2 = 5, 6  # near after one / two rejected Newton steps (reported as NEAR)
+NEAR1 = 5  # near after one rejected Newton step (reported as NEAR)
 SWITCH2, NEWTON_STOP2, TRUST, NEWTON_CAP = 4e-4, 1e-8, 0.25, 10
 GAUSS_K = 8.0  # base-2 exponent scale of the Gaussian kernel
 
@@ -57,7 +57,7 @@ def solve6(M, b, tiny=1e-12):
 
 
 def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov", state=NEAR):
-    """The kNear step of one seed (in `state`: NEAR, NEAR1 or NEAR2) from its
+    """The kNear step of one seed (in `state`: NEAR or NEAR1) from its
     weights w over all votes x (polish_it: the polish iteration, -1 in the
     approach phase)."""
     inside = w > 0
@@ -77,9 +77,7 @@ def newton_seed(x, m, w, tot, delta, move, h2, polish_it, kernel="epanechnikov",
         if s @ s < NEWTON_STOP2 * h2:
             return m + s, CONVERGED
         return m + s, SETTLED if polish_it >= NEWTON_CAP else state
-    if polish_it >= NEWTON_CAP:
-        return m + delta, SETTLED
-    return m + delta, {NEAR: NEAR1, NEAR1: NEAR2}.get(int(state), SETTLED)
+    return m + delta, NEAR1 if polish_it < NEWTON_CAP and state == NEAR else SETTLED
 
 
 def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=100, block=64,
@@ -95,14 +93,14 @@ def meanshift6(votes, seeds, bandwidth, max_iterations=100, polish_iterations=10
     counts = []
     for phase, budget in ((False, max_iterations), (True, polish_iterations)):
         counts.append(_phase(x, means, state, h2, budget, phase, block, kernel))
-    state[(state == NEAR1) | (state == NEAR2)] = NEAR
+    state[state == NEAR1] = NEAR
     return means, state, tuple(counts)
 
 
 def _phase(x, means, state, h2, budget, polish, block, kernel):
     iterations = 0
     for it in range(budget):
-        near = (state == NEAR) | (state == NEAR1) | (state == NEAR2)
+        near = (state == NEAR) | (state == NEAR1)
         act = np.flatnonzero((state == MOVING) | (near & polish))
         if act.size == 0:
             break
