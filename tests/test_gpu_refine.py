@@ -152,3 +152,30 @@ def test_refinement_inside_detect_fast(gpu):
     ea = np.abs(np.abs(na) - np.array([1.0, 0, 0])).max() + abs(a["plane_offset"][0])
     eb = np.abs(np.abs(nb) - np.array([1.0, 0, 0])).max() + abs(b["plane_offset"][0])
     assert eb <= ea + 1e-12, (ea, eb)
+
+
+def test_one_pass_with_faces_without_area(gpu):
+    """Faces without area among the correspondences (each repeats a corner
+    of a face of the copy, so its cross product is exactly zero): the
+    device's closest point on such a face is the nearest of its segments,
+    as in the FP64 restatement, and one pass still equals it."""
+    import dataclasses
+    mesh, truth = two_copies("rigid")
+    o = Options()
+    p = prepare(mesh, o)
+    f = p.mesh.faces
+    pick = np.arange(f.shape[1] // 2, f.shape[1], 5)  # faces of the copy
+    extra = np.stack([f[0, pick], f[0, pick], f[1, pick]])
+    faces = np.concatenate([f, extra], axis=1).astype(np.int32)
+    fn = np.concatenate([p.topology.face_normals, np.zeros((3, extra.shape[1]))], axis=1)
+    q = dataclasses.replace(p, mesh=Mesh(p.mesh.vertices, faces),
+                            topology=dataclasses.replace(p.topology, face_normals=fn))
+    start = perturbed(truth, 3e-3)
+    resident = gpu.load_mesh(q)
+    got = gpu.refine_transforms(resident, o, [record(start)], 1)
+    resident.close()
+    tau = o.verify_threshold * p.context.box_size
+    want = refine_pass(q.mesh.vertices, q.topology.normals, q.topology.weights, q.mesh.faces,
+                       start, tau)
+    er, et = motion_error(dict(rotation=got["rotation"][0], translation=got["translation"][0]), want)
+    assert er < 1e-6 and et < 1e-6, (er, et)
