@@ -960,7 +960,7 @@ const std::vector<sym_context *> &helper_contexts(sym_context *ctx, int n) {
   return ctx->helpers;
 }
 
-constexpr int kFusedWorkers = 4;  // host threads (helper contexts) for the per-mesh finish
+constexpr int kFusedWorkers = 8;  // host threads (helper contexts) for the per-mesh finish
 
 void detect_fast_fused(Call &call, sym_batch_item *items, uint64_t count, sym_fused_stats &stats) {
   stats = sym_fused_stats{};
