@@ -66,6 +66,13 @@ constexpr double kGauss2 = 8.0;
 // (one or two meshes) meet only their own meshes' blocks.
 constexpr int kBlockChunks = 256;
 
+// Votes per sub-box: the Newton polish and the support count test each run
+// of kSubVotes consecutive votes of a chunk against the warp's seeds before
+// evaluating it (exact like the chunk test; the approach keeps whole chunks).
+constexpr int kSubVotes = 16, kSubs = kChunk / kSubVotes;
+static_assert(kChunk % kSubVotes == 0 && kSubVotes <= 32 && (kSubVotes & (kSubVotes - 1)) == 0,
+              "sub-boxes cut chunks into runs of lanes");
+
 struct VoteSet {
   Tuning tuning;
   // weight kernel: 0 Epanechnikov 1 - d^2 / h^2 (the reference's); > 0 the
@@ -75,6 +82,7 @@ struct VoteSet {
   float *desc = nullptr;      // q x 8, Morton order
   double *desc64 = nullptr;   // q x 8, same order (only when requested)
   float *cbox = nullptr;      // nchunks x 12: lo[6], hi[6]
+  float *sbox = nullptr;      // nchunks x kSubs x 12: the boxes of each chunk's sub-runs
   uint64_t nblocks = 0;       // runs of kBlockChunks consecutive chunks
   float *bbox = nullptr;      // nblocks x 12: the box of each run's chunks
   float *gbox = nullptr;      // 12: box of all votes
