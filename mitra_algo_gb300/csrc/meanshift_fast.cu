@@ -430,6 +430,72 @@ __global__ void __launch_bounds__(kChunk) ms_update(T *means, const T *red, uint
 
 constexpr int kRetile = 2048;  // seeds sorted in one block (static shared memory)
 
+__device__ __forceinline__ bool pair_less(unsigned long long ka, int32_t va, unsigned long long kb,
+                                          int32_t vb) {
+  return ka < kb || (ka == kb && va < vb);
+}
+
+// Sorts the n (<= kRetile) pairs keys[0..n), vals[0..n) of shared memory by
+// (key, value) and writes the values in that order to out[0..n); one block
+// of kRetile / 2 threads.  A bitonic network over the next power of two (at
+// least 64; padding pairs (~0, INT32_MAX) sort last): thread t holds
+// elements 2t and 2t + 1 in registers, so the stride-1 steps stay in the
+// thread, strides 2-32 are shuffles within a warp, and only the strides of
+// 64 and more go through the shared arrays.  The pairs are distinct (the
+// values are seed ids), so the order is the sorted order whatever the
+// network.
+__device__ void sort_pairs(unsigned long long *keys, int32_t *vals, unsigned n, int32_t *out) {
+  unsigned p2 = 64;
+  while (p2 < n) p2 <<= 1;
+  const unsigned t = threadIdx.x;
+  const bool on = t < p2 / 2;  // whole warps: p2 / 2 is a multiple of 32
+  unsigned long long k[2];
+  int32_t v[2];
+  for (int j = 0; j < 2; ++j) {
+    const unsigned i = 2 * t + j;
+    k[j] = on && i < n ? keys[i] : ~0ull;
+    v[j] = on && i < n ? vals[i] : 0x7fffffff;
+  }
+  __syncthreads();  // every pair read before the shared steps write
+  // element i keeps the smaller of (i, i ^ s) when it is the lower index of
+  // an ascending pair or the upper index of a descending one
+  auto step = [&](int j, unsigned size, unsigned s, unsigned long long pk, int32_t pv) {
+    const unsigned i = 2 * t + j;
+    const bool keep_min = ((i & s) == 0) == ((i & size) == 0);
+    if (pair_less(pk, pv, k[j], v[j]) == keep_min) k[j] = pk, v[j] = pv;
+  };
+  for (unsigned size = 2; size <= p2; size <<= 1)
+    for (unsigned s = size >> 1; s; s >>= 1) {
+      if (s >= 64) {
+        if (on)
+          for (int j = 0; j < 2; ++j) keys[2 * t + j] = k[j], vals[2 * t + j] = v[j];
+        __syncthreads();
+        if (on)
+          for (int j = 0; j < 2; ++j) {
+            const unsigned p = (2 * t + j) ^ s;
+            step(j, size, s, keys[p], vals[p]);
+          }
+        __syncthreads();
+      } else if (on && s == 1) {
+        const bool up = ((2 * t) & size) == 0;
+        if (pair_less(k[1], v[1], k[0], v[0]) == up) {
+          const unsigned long long tk = k[0];
+          const int32_t tv = v[0];
+          k[0] = k[1], v[0] = v[1], k[1] = tk, v[1] = tv;
+        }
+      } else if (on) {  // partner thread t ^ (s / 2), in the same warp
+        for (int j = 0; j < 2; ++j) {
+          const unsigned long long pk = __shfl_xor_sync(0xffffffffu, k[j], s >> 1);
+          const int32_t pv = __shfl_xor_sync(0xffffffffu, v[j], s >> 1);
+          step(j, size, s, pk, pv);
+        }
+      }
+    }
+  if (on)
+    for (int j = 0; j < 2; ++j)
+      if (2 * t + j < n) out[2 * t + j] = v[j];
+}
+
 // Active seeds (kMoving, and kNear when include_near) in seed order, then
 // sorted by the Morton key of
 // their current mean (ties by seed id) when k <= kRetile.  nactive[0] = the
@@ -477,30 +543,7 @@ __global__ void __launch_bounds__(1024) retile(const T *means, const uint8_t *st
     __syncthreads();
   }
   unsigned n = base_s;
-  if (sort) {
-    unsigned p2 = 1;
-    while (p2 < n) p2 <<= 1;
-    for (unsigned i = n + threadIdx.x; i < p2; i += blockDim.x) keys[i] = ~0ull, vals[i] = 0x7fffffff;
-    __syncthreads();
-    for (unsigned size = 2; size <= p2; size <<= 1)
-      for (unsigned stride = size >> 1; stride; stride >>= 1) {
-        for (unsigned i = threadIdx.x; i < p2; i += blockDim.x) {
-          unsigned j = i ^ stride;
-          if (j > i) {
-            bool up = (i & size) == 0;
-            bool gt = keys[i] > keys[j] || (keys[i] == keys[j] && vals[i] > vals[j]);
-            if (gt == up) {
-              unsigned long long tk = keys[i];
-              keys[i] = keys[j], keys[j] = tk;
-              int32_t tv = vals[i];
-              vals[i] = vals[j], vals[j] = tv;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) ids[i] = vals[i];
-  }
+  if (sort) sort_pairs(keys, vals, n, ids);
   __syncthreads();
   if (threadIdx.x == 0) {
     nactive[0] = n, nactive[1] = near_s;
