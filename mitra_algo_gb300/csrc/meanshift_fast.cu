@@ -68,12 +68,19 @@ __global__ void morton_keys(const float *desc, uint64_t q, const float *box, int
   idx[v] = int32_t(v);
 }
 
+// dst row v = src row order[v]; rows of 8 values (32 or 64 bytes, and the
+// buffers 16-byte aligned), moved as 16-byte words.
 template <typename T>
 __global__ void permute(const T *src, const int32_t *order, uint64_t q, T *dst) {
   uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (v >= q) return;
   uint64_t from = uint64_t(uint32_t(order[v]));
-  for (int k = 0; k < 8; ++k) dst[v * 8 + k] = src[from * 8 + k];
+  constexpr int kWords = 8 * sizeof(T) / 16;
+  const uint4 *s = reinterpret_cast<const uint4 *>(src + from * 8);
+  uint4 w[kWords];
+  for (int k = 0; k < kWords; ++k) w[k] = s[k];
+  uint4 *d = reinterpret_cast<uint4 *>(dst + v * 8);
+  for (int k = 0; k < kWords; ++k) d[k] = w[k];
 }
 
 __global__ void invert(const int32_t *order, uint64_t q, int32_t *rank) {
