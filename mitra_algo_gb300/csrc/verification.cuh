@@ -304,6 +304,7 @@ struct Lbvh {
   float *box = nullptr;            // (nf - 1) x 12: the two children's lo[3], hi[3]
   float *vn = nullptr;             // 3 x nv, FP32 copy of the vertex normals
   float4 *fn = nullptr;            // nf: unit face normals from the FP64 corners, w = 1 (0: none)
+  int32_t *order = nullptr;        // nv: the vertices in Morton order of their position
   char *block = nullptr;           // owns every array above (cudaMalloc)
   float scale = 0;                 // largest vertex coordinate magnitude
 };

@@ -125,6 +125,22 @@ __global__ void lbvh_keys(const float *xyz, uint64_t nv, const int32_t *faces, u
   ids[f] = int32_t(f);
 }
 
+// key = Morton code of vertex v (30 bits, the faces' quantisation) << 32 | v.
+__global__ void lbvh_vertex_keys(const float *xyz, uint64_t nv, float3 lo, float3 inv,
+                                 uint64_t *keys, int32_t *ids) {
+  uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  float l[3] = {lo.x, lo.y, lo.z}, s[3] = {inv.x, inv.y, inv.z};
+  uint32_t q[3];
+  for (int a = 0; a < 3; ++a) {
+    float u = (xyz[uint64_t(a) * nv + v] - l[a]) * s[a];
+    q[a] = uint32_t(fminf(fmaxf(u * 1024.f, 0.f), 1023.f));
+  }
+  uint32_t code = (spread3(q[0]) << 2) | (spread3(q[1]) << 1) | spread3(q[2]);
+  keys[v] = (uint64_t(code) << 32) | uint64_t(uint32_t(v));
+  ids[v] = int32_t(v);
+}
+
 __device__ __forceinline__ int lcp(const uint64_t *keys, int64_t n, int64_t i, int64_t j) {
   if (j < 0 || j >= n) return -1;
   return __clzll(keys[i] ^ keys[j]);
@@ -216,6 +232,7 @@ struct BvhView {
   const int32_t *child;
   const float *box;
   const float4 *fn;  // nf: unit face normal from the FP64 corners, w = 1 (0: none usable)
+  const int32_t *order;  // nv: query order of the vertices (Morton order of their position)
 };
 
 __device__ __forceinline__ F3 vtx(const BvhView &b, int32_t v) {
@@ -458,23 +475,27 @@ struct MotionF {
 };
 
 // Row lists between the verification kernels.
-// The rows each later kernel takes.  The FP64 and reference-order rows are
-// marked per row and compacted in ascending order (compact_indices), so a
-// warp of those kernels serves neighbouring vertices of one motion and
-// walks nearly the same BVH nodes, as verify_fp32's warps do; appended in
-// completion order they made every load of a warp 32 scattered ones.
+// A row (c, direction, vertex i) holds the flag and error of one query;
+// the kernels take the queries qid = (c, direction, j) of vertex order[j],
+// the vertices in Morton order of their position, so a warp serves
+// neighbouring vertices of one motion and walks nearly the same BVH nodes
+// (in the mesh's own vertex order the warps of the benchmark mesh spread
+// over 3x more of it).  The FP64 and reference-order queries are marked
+// per query and compacted in ascending order (compact_indices), so their
+// warps keep that locality; appended in completion order they made every
+// load of a warp 32 scattered ones.
 constexpr uint32_t kNoSlot = 0xffffffffu;
 constexpr int32_t kNoFace = INT32_MIN;  // padding of a candidate list (~f marks an undecided face)
 
 struct RowLists {
   uint32_t *forward;    // accepted forward rows whose FP64 distance is still needed
   int32_t *faces;       // kCandidates faces per forward row (-1 padded)
-  uint8_t *mark;        // per row: 1 = left to the next kernel (FP64, then reference order)
-  int32_t *fp64;        // rows decided in FP64, ascending
-  int32_t *reference;   // rows left to the reference-order BVH, ascending
-  // the FP32 candidates of an FP64 row (kCandidates per slot, kNoFace
-  // padded), so the FP64 decisions need no search of their own; slot_of[row]
-  // = kNoSlot for a row sent on before its candidates were known
+  uint8_t *mark;        // per query: 1 = left to the next kernel (FP64, then reference order)
+  int32_t *fp64;        // queries decided in FP64, ascending
+  int32_t *reference;   // queries left to the reference-order BVH, ascending
+  // the FP32 candidates of an FP64 query (kCandidates per slot, kNoFace
+  // padded), so the FP64 decisions need no search of their own; slot_of[qid]
+  // = kNoSlot for a query sent on before its candidates were known
   uint32_t *slot_of;
   int32_t *cand;
   unsigned long long slots;    // capacity of cand, in slots
@@ -490,14 +511,17 @@ struct RowLists {
 __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions, uint64_t nc,
                             float tau, float scale, uint8_t *flags, double *err, RowLists lists,
                             int *status) {
-  const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  // query q = (c, direction, j) takes vertex i = order[j]: the warps walk
+  // neighbouring vertices; flags and errors stay per vertex (row)
+  const uint64_t qid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t nv = b.nv;
-  if (row >= nc * 2 * nv) return;
-  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  if (qid >= nc * 2 * nv) return;
+  const uint64_t c = qid / (2 * nv), rem = qid % (2 * nv);
   const bool inverse = rem >= nv;
-  const uint64_t i = rem % nv;
+  const uint64_t i = uint64_t(b.order[rem % nv]);
+  const uint64_t row = qid - rem % nv + i;
   flags[row] = 0;
-  lists.mark[row] = 0;
+  lists.mark[qid] = 0;
   if (!inverse) err[c * nv + i] = 0.0;
   const MotionF &m = motions[c];
   float r[9];
@@ -510,8 +534,8 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   const float mag = fmaxf(scale, fmaxf(fabsf(q.x), fmaxf(fabsf(q.y), fabsf(q.z))));
   const float e = kErr * fmaxf(mag, fmaxf(fabsf(m.t[0]), fmaxf(fabsf(m.t[1]), fabsf(m.t[2]))));
   auto to_fp64 = [&]() {
-    lists.mark[row] = 1;
-    lists.slot_of[row] = kNoSlot;
+    lists.mark[qid] = 1;
+    lists.slot_of[qid] = kNoSlot;
   };
   // the image moves at least 2 tau (verification.cpp:64)
   const F3 dq = q - p;
@@ -532,13 +556,13 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   // from here on an FP64 row keeps its candidates: they hold every face at
   // the FP64 minimum (the window covers the FP32 error of the FP64 image)
   auto to_fp64_listed = [&]() {
-    lists.mark[row] = 1;
+    lists.mark[qid] = 1;
     const unsigned long long k = atomicAdd(&lists.counts[1], 1ull);
     if (k >= lists.slots) {
-      lists.slot_of[row] = kNoSlot;
+      lists.slot_of[qid] = kNoSlot;
       return;
     }
-    lists.slot_of[row] = uint32_t(k);
+    lists.slot_of[qid] = uint32_t(k);
     for (int j = 0; j < kCandidates; ++j) lists.cand[k * kCandidates + j] = j < n ? faces[j] : kNoFace;
   };
   for (int j = 0; j < n; ++j)
@@ -659,11 +683,12 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
   const int sub = threadIdx.x % kGroup;
   const unsigned group_mask = 0xffu << (threadIdx.x & 31 & ~(kGroup - 1));
   if (k >= count) return;  // whole groups (count rows x 8 lanes)
-  const uint64_t row = uint64_t(lists.fp64[k]), nv = b.nv;
-  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  const uint64_t qid = uint64_t(lists.fp64[k]), nv = b.nv;  // a query, as verify_fp32's
+  const uint64_t c = qid / (2 * nv), rem = qid % (2 * nv);
   const bool inverse = rem >= nv;
-  const uint64_t i = rem % nv;
-  const uint32_t slot = lists.slot_of[row];
+  const uint64_t i = uint64_t(b.order[rem % nv]);
+  const uint64_t row = qid - rem % nv + i;
+  const uint32_t slot = lists.slot_of[qid];
   if (slot == kNoSlot) {  // no candidates yet: the search, on one lane
     if (sub) return;
     double d = 0;
@@ -681,7 +706,7 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
     }
     flags[row] = v == 1;
     if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
-    if (v != 2) lists.mark[row] = 0;  // marked rows go on to the reference-order search
+    if (v != 2) lists.mark[qid] = 0;  // marked queries go on to the reference-order search
     return;
   }
   const ClusterMotion &m = motions[c];
@@ -743,21 +768,23 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
   if (sub == 0) {
     flags[row] = v == 1;
     if (!inverse) err[c * nv + i] = v == 1 ? dmin : 0.0;
-    lists.mark[row] = 0;
+    lists.mark[qid] = 0;
   }
 }
 
 // Rows whose candidates overflowed the list: the reference's search itself
 // (exact_query) with the search limit nextafter(tau^2, inf).
-__global__ void verify_listed_ref(Surface s, const double *vn, const ClusterMotion *motions,
-                                  double tau, RowLists lists, unsigned long long count,
-                                  uint8_t *flags, double *err, int *status) {
+__global__ void verify_listed_ref(Surface s, const double *vn, const int32_t *order,
+                                  const ClusterMotion *motions, double tau, RowLists lists,
+                                  unsigned long long count, uint8_t *flags, double *err,
+                                  int *status) {
   const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k >= count) return;
-  const uint64_t row = lists.reference[k], nv = s.nv;
-  const uint64_t c = row / (2 * nv), rem = row % (2 * nv);
+  const uint64_t qid = lists.reference[k], nv = s.nv;  // a query, as verify_fp32's
+  const uint64_t c = qid / (2 * nv), rem = qid % (2 * nv);
   const bool inverse = rem >= nv;
-  const uint64_t i = rem % nv;
+  const uint64_t i = uint64_t(order[rem % nv]);
+  const uint64_t row = qid - rem % nv + i;
   double d = 0;
   const bool ok = exact_query(s, vn, motions[c], inverse, i, tau,
                               nextafter(tau * tau, double(INFINITY)), d, status);
@@ -1099,13 +1126,14 @@ Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
   const uint64_t ni = nf - 1;
   auto pad = [](uint64_t x) { return (x + 255) & ~uint64_t(255); };
   const uint64_t s_xyz = pad(12 * nv), s_child = pad(8 * ni + 8), s_box = pad(48 * ni + 48);
-  const uint64_t s_fn = pad(16 * nf);
-  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box + s_fn));
+  const uint64_t s_fn = pad(16 * nf), s_order = pad(4 * nv);
+  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box + s_fn + s_order));
   b.xyz = reinterpret_cast<float *>(b.block);
   b.child = reinterpret_cast<int32_t *>(b.block + s_xyz);
   b.box = reinterpret_cast<float *>(b.block + s_xyz + s_child);
   b.vn = reinterpret_cast<float *>(b.block + s_xyz + s_child + s_box);
   b.fn = reinterpret_cast<float4 *>(b.block + 2 * s_xyz + s_child + s_box);
+  b.order = reinterpret_cast<int32_t *>(b.block + 2 * s_xyz + s_child + s_box + s_fn);
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(xyz, nv, b.xyz);
   check_launch();
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(vn, nv, b.vn);
@@ -1129,6 +1157,16 @@ Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
                                                  make_float3(1 / ext, 1 / ext, 1 / ext), keys, ids);
   check_launch();
   radix_sort_pairs(call, keys, ids, skeys, sids, nf, 64);
+  {  // the query order of the verification: neighbouring vertices in a warp
+    uint64_t *vkeys = call.alloc<uint64_t>(nv), *svkeys = call.alloc<uint64_t>(nv);
+    int32_t *vids = call.alloc<int32_t>(nv);
+    lbvh_vertex_keys<<<blocks_for(nv), kThreads, 0, st>>>(
+        b.xyz, nv, make_float3(lo[0], lo[1], lo[2]), make_float3(1 / ext, 1 / ext, 1 / ext), vkeys,
+        vids);
+    check_launch();
+    call.launched();
+    radix_sort_pairs(call, vkeys, vids, svkeys, b.order, nv, 64);
+  }
   if (ni) {
     int32_t *parent_in = call.alloc<int32_t>(ni), *parent_leaf = call.alloc<int32_t>(nf);
     unsigned *arrivals = call.alloc<unsigned>(ni);
@@ -1244,7 +1282,7 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   lists.counts = call.alloc<unsigned long long>(4);
   uint64_t *listed = call.alloc<uint64_t>(2);
   SYM_CUDA(cudaMemsetAsync(lists.counts, 0, 32, st));
-  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn};
+  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn, bvh.order};
   Surface s{m.xyz, nv, m.faces, m.nf, nullptr, nullptr};
   verify_fp32<<<blocks_for(rows), kThreads, 0, st>>>(view, bvh.vn, dmf, nc, float(tau), bvh.scale,
                                                       flags, err, lists, call.status());
@@ -1275,8 +1313,8 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   }
   if (fp64_rows) *fp64_rows = counts[1];
   if (counts[2]) {
-    verify_listed_ref<<<blocks_for(counts[2]), kThreads, 0, st>>>(s, m.vn, dm, tau, lists,
-                                                                   counts[2], flags, err,
+    verify_listed_ref<<<blocks_for(counts[2]), kThreads, 0, st>>>(s, m.vn, bvh.order, dm, tau,
+                                                                   lists, counts[2], flags, err,
                                                                    call.status());
     check_launch();
     call.launched();
@@ -1305,7 +1343,7 @@ void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record 
   ClusterMotion *dm = call.upload(motions.data(), nc);
   if (refine > 0 && m.nf) {
     const Lbvh &bvh = *m.lbvh;
-    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn};
+    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn, bvh.order};
     refine_motions(call, view, m.xyz, m.vn, m.w, dm, nc, tau, refine, origin);
     call.d2h(motions.data(), dm, nc * sizeof(ClusterMotion));
     call.check_status("transform refinement");
