@@ -147,15 +147,18 @@ void RefBvhSource::release() {
 namespace {
 
 // flags[(c * 2 + dir) * nv + i], err[c * nv + i] (forward direction).
-__global__ void verify_vertices(Surface s, const double *vn, const ClusterMotion *clusters,
-                                uint64_t nc, double tau, double limit, uint8_t *flags, double *err,
-                                int *status) {
-  uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  uint64_t nv = s.nv;
-  if (row >= nc * 2 * nv) return;
-  uint64_t c = row / (2 * nv), rem = row % (2 * nv);
-  bool inverse = rem >= nv;
-  uint64_t i = rem % nv;
+// Query (c, direction, j) takes vertex i = order[j], the vertices in Morton
+// order of their position, so a warp walks neighbouring vertices through
+// nearly the same BVH nodes; flags and errors stay per vertex (row).
+__global__ void verify_vertices(Surface s, const double *vn, const int32_t *order,
+                                const ClusterMotion *clusters, uint64_t nc, double tau,
+                                double limit, uint8_t *flags, double *err, int *status) {
+  const uint64_t qid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const uint64_t nv = s.nv;
+  if (qid >= nc * 2 * nv) return;
+  const uint64_t c = qid / (2 * nv), rem = qid % (2 * nv);
+  const bool inverse = rem >= nv;
+  const uint64_t i = uint64_t(order[rem % nv]), row = qid - rem % nv + i;
   flags[row] = 0;
   if (!inverse) err[c * nv + i] = 0;
   double d = 0;
@@ -420,6 +423,34 @@ void finish_verification(Call &call, const uint8_t *flags, const double *err, co
   }
 }
 
+// The vertices in Morton order of their position (10 bits per axis over
+// the mesh's box, ties in index order): the query order of the
+// verification kernels.
+static std::vector<int32_t> morton_order(const sym_mesh_view &m) {
+  const uint64_t nv = m.vertices.count;
+  const double *x[3] = {m.vertices.x, m.vertices.y, m.vertices.z};
+  double lo[3], ext = 0;
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = nv ? *std::min_element(x[a], x[a] + nv) : 0.0;
+    const double hi = nv ? *std::max_element(x[a], x[a] + nv) : 0.0;
+    ext = std::max(ext, hi - lo[a]);
+  }
+  std::vector<uint64_t> key(nv);
+  for (uint64_t v = 0; v < nv; ++v) {
+    uint64_t code = 0;
+    for (int a = 0; a < 3; ++a) {
+      const double u = ext > 0 ? (x[a][v] - lo[a]) / ext * 1024.0 : 0.0;
+      const uint64_t cell = uint64_t(std::min(1023.0, std::max(0.0, u)));
+      for (int bit = 0; bit < 10; ++bit) code |= ((cell >> bit) & 1u) << (3 * bit + (2 - a));
+    }
+    key[v] = code << 32 | v;
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int32_t> order(nv);
+  for (uint64_t j = 0; j < nv; ++j) order[j] = int32_t(uint32_t(key[j]));
+  return order;
+}
+
 // Device core of sym_verification.  Mesh arrays are device pointers; `m` is
 // the host mesh (the BVH is built on the host with the reference's
 // construction order).  Fills per (cluster, side) vertex lists, patches,
@@ -452,8 +483,10 @@ void verification_core(Call &call, const sym_mesh_view &m, const double *xyz, co
   uint8_t *flags = call.alloc<uint8_t>(rows);
   double *err = call.alloc<double>(nc * nv);
   double limit = std::nextafter(tau * tau, std::numeric_limits<double>::infinity());
-  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dm, nc, tau, limit, flags, err,
-                                                         call.status());
+  const std::vector<int32_t> order = morton_order(m);
+  const int32_t *dorder = call.upload(order.data(), order.size());
+  verify_vertices<<<blocks_for(rows), kThreads, 0, st>>>(s, vn, dorder, dm, nc, tau, limit, flags,
+                                                         err, call.status());
   check_launch();
   call.launched();
   finish_verification(call, flags, err, w, nbr_off, nbr, nv, nc, side, patches, coverage, rms);

@@ -905,10 +905,12 @@ struct Origin {
 __global__ void refine_pairs(BvhView b, const double *xyz, const double *vn,
                              const ClusterMotion *motions, uint64_t nc, double tau, float tau2, Origin o,
                              double *target, uint8_t *ok, int *status) {
-  const uint64_t row = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  // query (c, j) takes vertex i = order[j] (neighbouring vertices in a
+  // warp); the pairs stay per vertex (row), so the sums keep their order
+  const uint64_t qid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const uint64_t nv = b.nv;
-  if (row >= nc * nv) return;
-  const uint64_t c = row / nv, i = row % nv;
+  if (qid >= nc * nv) return;
+  const uint64_t c = qid / nv, i = uint64_t(b.order[qid % nv]), row = c * nv + i;
   ok[row] = 0;
   float best = tau2;
   double q[3];
