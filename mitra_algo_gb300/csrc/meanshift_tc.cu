@@ -433,7 +433,8 @@ static_assert(kListThreads == kBlockChunks, "one thread per chunk of a block box
 // need[t * nchunks + c]: some seed of tile t lies within the bandwidth of
 // chunk c's box, for the chunks of tile t's surviving blocks: tested
 // against the tile's box, each group's box (16 seeds), each quad's box (4
-// consecutive seeds), then the quad's seeds.  Exact for Epanechnikov
+// consecutive seeds), then the quad's seeds, among the seeds within the
+// bandwidth of the block's box only (a mask per block).  Exact for Epanechnikov
 // weights: every vote of a skipped chunk is farther than the bandwidth from
 // every seed of the tile; and a box holds its seeds' coordinates, so in
 // FP32 too its gap (monotone in every operation) is never above a seed's.
@@ -443,14 +444,16 @@ static_assert(kListThreads == kBlockChunks, "one thread per chunk of a block box
 constexpr int kQuads = kChunk / 4;
 __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, const float *means,
                                                            const int32_t *ids, const unsigned *nact,
-                                                           const float *cbox, uint64_t nchunks,
-                                                           const uint32_t *sblk, const uint32_t *nsurv,
-                                                           uint32_t nblk, float skip_gap2,
-                                                           uint8_t *need, uint32_t *bcount) {
+                                                           const float *cbox, const float *bbox,
+                                                           uint64_t nchunks, const uint32_t *sblk,
+                                                           const uint32_t *nsurv, uint32_t nblk,
+                                                           float skip_gap2, uint8_t *need,
+                                                           uint32_t *bcount) {
   __shared__ float seed[kChunk * 6];
   __shared__ float gb[kBoxFloats];
   __shared__ float qb[kQuads * 12];
   __shared__ bool alive[kChunk];
+  __shared__ uint32_t reach[kChunk / 32];  // seeds within the bandwidth of the block's box
   uint32_t t, sub, per;
   if (!list_share(nact, t, sub, per)) return;
   const unsigned nactive = nact[0];
@@ -476,18 +479,44 @@ __global__ void __launch_bounds__(kListThreads) tile_count(const float *boxes, c
   const int lane = threadIdx.x & 31;
   uint32_t *bc = bcount + uint64_t(t) * nblk;
   for (uint32_t j = sub; j < ns; j += per) {
-    const uint64_t c = uint64_t(sblk[uint64_t(t) * nblk + j]) * kBlockChunks + threadIdx.x;
+    const uint32_t blk = sblk[uint64_t(t) * nblk + j];
+    // the seeds that can reach the block at all: a seed beyond the
+    // bandwidth of the block's box is beyond it for each of its chunks
+    // (their boxes lie inside it), so the chunk tests skip it
+    __syncthreads();  // the previous block's mask is no longer read
+    if (threadIdx.x < kChunk) {  // whole warps
+      bool ok = false;
+      if (alive[threadIdx.x]) {
+        const float *bb = bbox + uint64_t(blk) * 12;
+        float q = 0;
+        for (int d = 0; d < 6; ++d) {
+          const float x = seed[threadIdx.x * 6 + d];
+          const float e = fmaxf(fmaxf(bb[d] - x, x - bb[6 + d]), 0.f);
+          q += e * e;
+        }
+        ok = q <= skip_gap2;
+      }
+      const unsigned bal = __ballot_sync(0xffffffffu, ok);
+      if (lane == 0) reach[threadIdx.x >> 5] = bal;
+    }
+    __syncthreads();
+    const uint64_t c = uint64_t(blk) * kBlockChunks + threadIdx.x;
     bool keep = false;
     if (c < nchunks) {
       float cb[12];
       for (int d = 0; d < 12; ++d) cb[d] = cbox[c * 12 + d];
       if (box_gap2_tc(gb, gb + 6, cb) <= skip_gap2)
         for (int g = 0; g < kChunk / kGroupSeeds && !keep; ++g) {
+          const uint32_t gm = (reach[g >> 1] >> ((g & 1) * kGroupSeeds)) & 0xffffu;
+          if (!gm) continue;
           const float *b = gb + 12 + 12 * g;
           if (box_gap2_tc(b, b + 6, cb) > skip_gap2) continue;
           for (int qd = 4 * g; qd < 4 * g + 4 && !keep; ++qd) {
+            const uint32_t qm = (gm >> (4 * (qd - 4 * g))) & 0xfu;
+            if (!qm) continue;
             if (box_gap2_tc(qb + 12 * qd, qb + 12 * qd + 6, cb) > skip_gap2) continue;
             for (int i = 4 * qd; i < 4 * qd + 4 && !keep; ++i) {
+              if (!((qm >> (i - 4 * qd)) & 1u)) continue;
               float q = 0;
               for (int d = 0; d < 6; ++d) {
                 const float x = seed[i * 6 + d];
@@ -1248,8 +1277,9 @@ bool meanshift_bf16_bulk(Call &call, const VoteSet &v, float *means, uint8_t *st
     tile_boxes<<<unsigned(max_tiles), kCullThreads, 0, st>>>(means, ids, nact, v.bbox, nblk,
                                                               gap * gap, boxes, sblk, nsurv, bcount);
     check_launch();
-    tile_count<<<list_ctas, kListThreads, 0, st>>>(boxes, means, ids, nact, v.cbox, v.nchunks, sblk,
-                                                   nsurv, nblk, gap * gap, need, bcount);
+    tile_count<<<list_ctas, kListThreads, 0, st>>>(boxes, means, ids, nact, v.cbox, v.bbox,
+                                                   v.nchunks, sblk, nsurv, nblk, gap * gap, need,
+                                                   bcount);
     check_launch();
     scan_lists<<<1, 1024, 0, st>>>(bcount, nsurv, nact, nblk, sms, list_cap, seg, boff, offsets,
                                    pieces, call.status());
