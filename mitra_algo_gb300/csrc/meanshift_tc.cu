@@ -275,6 +275,9 @@ __device__ __forceinline__ uint32_t bf16_pair(const __nv_bfloat16 *p) {
 
 __global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, const float *cbox,
                              const float *gbox, float inv_h, uint8_t *images) {
+  // the image is assembled in shared memory (its 2-byte entries lie 16 or
+  // 128 bytes apart for neighbouring votes) and written out in 16-byte words
+  __shared__ __align__(16) uint8_t img[kImage];
   uint64_t c = blockIdx.x;
   int t = threadIdx.x;  // vote in chunk
   if (c >= nchunks) return;
@@ -286,7 +289,6 @@ __global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, co
   }
   uint64_t v = c * kChunk + t;
   bool live = v < q;
-  uint8_t *img = images + c * kImage;
   __nv_bfloat16 *b1 = reinterpret_cast<__nv_bfloat16 *>(img);
   __nv_bfloat16 *b2 = reinterpret_cast<__nv_bfloat16 *>(img + kB1Bytes);
   float *ce = reinterpret_cast<float *>(img + kB1Bytes + kB2Bytes);
@@ -315,6 +317,10 @@ __global__ void build_images(const float *desc, uint64_t q, uint64_t nchunks, co
   b1[kmajor_offset(t, 15, 128, 256) / 2] = fl;
   b2[kmajor_offset(6, t, 128, 2048) / 2] = __float2bfloat16_rn(live ? 1.f : 0.f);
   for (int k : {7, 14, 15}) b2[kmajor_offset(k, t, 128, 2048) / 2] = zero;
+  __syncthreads();
+  const uint4 *src = reinterpret_cast<const uint4 *>(img);
+  uint4 *dst = reinterpret_cast<uint4 *>(images + c * kImage);
+  for (int w = t; w < int(kImage / 16); w += kChunk) dst[w] = src[w];
 }
 
 __device__ __forceinline__ float box_gap2_tc(const float *lo, const float *hi, const float *b) {
