@@ -389,9 +389,10 @@ __device__ bool face_d2n(F3 p, F3 a, F3 b, F3 c, F3 n, float um, float &d2) {
 // bound) -- the face of smallest FP64 distance is at most 2 bounds farther
 // in FP32 than the best FP32 face.  Nodes are pruned with a slightly larger
 // radius, for the rounding of their boxes' distances.  Undecided faces are
-// listed as ~face.  Returns the count (kCandidates + 1 on overflow); `best`
-// receives the smallest FP32 squared distance of a decided face (INFINITY
-// when none lies within tau + 3 bounds).
+// listed as ~face.  Returns the count (N + 1 on overflow: faces and keys
+// hold N entries); `best` receives the smallest FP32 squared distance of a
+// decided face (INFINITY when none lies within tau + 3 bounds).
+template <int N = kCandidates>
 __device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err, int32_t *faces,
                                float *keys, float &best, int *status) {
   best = INFINITY;
@@ -417,13 +418,13 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err,
       }
     }
     if (key > lim) return;
-    if (n == kCandidates) {  // drop entries beyond the current limit
+    if (n == N) {  // drop entries beyond the current limit
       int m = 0;
       for (int j = 0; j < n; ++j)
         if (keys[j] <= lim) faces[m] = faces[j], keys[m++] = keys[j];
       n = m;
     }
-    if (n == kCandidates) {
+    if (n == N) {
       overflow = true;
       return;
     }
@@ -448,7 +449,7 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err,
       const bool p0 = c0 >= 0 && d0 <= lim_box, p1 = c1 >= 0 && d1 <= lim_box;
       if (top + 2 > kStackFast) {
         atomicExch(status, DS_CAPACITY);
-        return kCandidates + 1;
+        return N + 1;
       }
       if (p0 && p1) {  // the nearer child is popped first
         const bool first0 = d0 <= d1;
@@ -461,7 +462,7 @@ __device__ int candidate_faces(const BvhView &b, F3 p, float tau_err, float err,
       }
     }
   }
-  if (overflow) return kCandidates + 1;
+  if (overflow) return N + 1;
   int m = 0;
   for (int j = 0; j < n; ++j)
     if (keys[j] <= lim) faces[m] = faces[j], keys[m++] = keys[j];
@@ -618,8 +619,8 @@ __global__ void forward_errors(Surface s, const ClusterMotion *motions, RowLists
 // One query of the reference's verification, decided with the FP32
 // candidates and FP64 rechecks.  Returns 1 (supports; `d2` = the reference's
 // FP64 squared distance), 0 (does not), 3 (the faces at the minimum, listed
-// in `tied`, disagree on the normal test; `d2` = the minimum) or 2 (more
-// candidates than the list holds; `d2` = the tau^2 search limit).
+// in `tied`, N entries, -1 padded, disagree on the normal test; `d2` = the
+// minimum) or 2 (more than N candidates; `d2` = the tau^2 search limit).
 //
 // The reference keeps the face of strictly smallest FP64 distance, the first
 // its BVH visits among faces at exactly that distance (surface.h:52-83).
@@ -627,6 +628,7 @@ __global__ void forward_errors(Surface s, const ClusterMotion *motions, RowLists
 // minimum is the reference's distance; the normal test of the faces at
 // exactly that minimum decides when they all give the same outcome; when
 // they do not, the reference's visiting order decides (verify_listed_ref).
+template <int N = kCandidates>
 __device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn,
                             const ClusterMotion &m, bool inverse, uint64_t i, double tau,
                             float scale, double &d2, int32_t *tied, int *status) {
@@ -637,16 +639,16 @@ __device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn
   const F3 qf{float(q.x), float(q.y), float(q.z)};
   const float mag = fmaxf(scale, fmaxf(fabsf(qf.x), fmaxf(fabsf(qf.y), fabsf(qf.z))));
   const float e = kErr * mag;
-  int32_t faces[kCandidates];
-  float keys[kCandidates];
+  int32_t faces[N];
+  float keys[N];
   float best;
-  const int n = candidate_faces(b, qf, float(tau) + e, e, faces, keys, best, status);
-  if (n > kCandidates) {
+  const int n = candidate_faces<N>(b, qf, float(tau) + e, e, faces, keys, best, status);
+  if (n > N) {
     d2 = nextafter(tau * tau, double(INFINITY));
     return 2;
   }
   double dmin = INFINITY;
-  double dist[kCandidates];
+  double dist[N];
   for (int j = 0; j < n; ++j) {
     faces[j] = faces[j] < 0 ? ~faces[j] : faces[j];
     dist[j] = triangle_d2(q, corner(s, faces[j], 0), corner(s, faces[j], 1), corner(s, faces[j], 2));
@@ -663,7 +665,7 @@ __device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn
   }
   d2 = dmin;
   if (agree && disagree) {
-    for (int j = t; j < kCandidates; ++j) tied[j] = -1;
+    for (int j = t; j < N; ++j) tied[j] = -1;
     return 3;
   }
   return agree ? 1 : 0;
@@ -772,8 +774,46 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
   }
 }
 
-// Rows whose candidates overflowed the list: the reference's search itself
-// (exact_query) with the search limit nextafter(tau^2, inf).
+// Queries whose candidates overflowed the list of verify_fp32 and of
+// verify_rows_fp64: the same FP32 search and FP64 decision with room for
+// kWideCandidates faces (one thread per query; such queries are rare, and
+// the reference-order search they would otherwise take walks the
+// reference's BVH one FP64 node at a time).  A query that overflows this
+// list as well stays marked for verify_listed_ref.
+constexpr int kWideCandidates = 64;
+__global__ void verify_rows_wide(BvhView b, Surface s, RefBvh t, const double *vn,
+                                 const ClusterMotion *motions, double tau, float scale,
+                                 uint8_t *flags, double *err, RowLists lists,
+                                 unsigned long long count, int *status) {
+  const uint64_t k = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const uint64_t qid = uint64_t(lists.reference[k]), nv = b.nv;  // a query, as verify_fp32's
+  const uint64_t c = qid / (2 * nv), rem = qid % (2 * nv);
+  const bool inverse = rem >= nv;
+  const uint64_t i = uint64_t(b.order[rem % nv]);
+  const uint64_t row = qid - rem % nv + i;
+  double d = 0;
+  int32_t tied[kWideCandidates];
+  int v = hybrid_query<kWideCandidates>(b, s, vn, motions[c], inverse, i, tau, scale, d, tied,
+                                        status);
+  if (v == 2) return;  // still marked
+  if (v == 3) {
+    atomicAdd(&lists.counts[3], 1ull);
+    const M3 r = query_rotation(motions[c], inverse);
+    D3 q;
+    query_skipped(motions[c], r, inverse, vertex(s, int32_t(i)), tau, q);
+    int32_t first = tied[0];
+    for (int x = 1; x < kWideCandidates && tied[x] >= 0; ++x)
+      first = first_in_reference_order(t, q, first, tied[x]);
+    v = normal_agrees(s, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
+  }
+  flags[row] = v == 1;
+  if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
+  lists.mark[qid] = 0;
+}
+
+// Queries whose candidates overflowed the wide list too: the reference's
+// search itself (exact_query) with the search limit nextafter(tau^2, inf).
 __global__ void verify_listed_ref(Surface s, const double *vn, const int32_t *order,
                                   const ClusterMotion *motions, double tau, RowLists lists,
                                   unsigned long long count, uint8_t *flags, double *err,
@@ -1312,6 +1352,17 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
     call.d2h(&counts[2], listed + 1, 8);
     call.d2h(&counts[3], lists.counts + 3, 8);
     call.sync();
+    if (counts[2]) {  // overflowed lists: the wider list first
+      verify_rows_wide<<<blocks_for(counts[2]), kThreads, 0, st>>>(
+          view, s, m.ref->dev, m.vn, dm, tau, bvh.scale, flags, err, lists, counts[2],
+          call.status());
+      check_launch();
+      call.launched();
+      compact_indices(call, lists.mark, rows, lists.reference, listed + 1);
+      call.d2h(&counts[2], listed + 1, 8);
+      call.d2h(&counts[3], lists.counts + 3, 8);
+      call.sync();
+    }
   }
   if (fp64_rows) *fp64_rows = counts[1];
   if (counts[2]) {
