@@ -486,6 +486,7 @@ struct MotionF {
 // warps keep that locality; appended in completion order they made every
 // load of a warp 32 scattered ones.
 constexpr uint32_t kNoSlot = 0xffffffffu;
+constexpr uint32_t kWideSlot = 0xfffffffeu;  // overflowed the list: for verify_rows_wide
 constexpr int32_t kNoFace = INT32_MIN;  // padding of a candidate list (~f marks an undecided face)
 
 struct RowLists {
@@ -493,10 +494,11 @@ struct RowLists {
   int32_t *faces;       // kCandidates faces per forward row (-1 padded)
   uint8_t *mark;        // per query: 1 = left to the next kernel (FP64, then reference order)
   int32_t *fp64;        // queries decided in FP64, ascending
-  int32_t *reference;   // queries left to the reference-order BVH, ascending
+  int32_t *reference;   // queries left to the wide list, then to the reference-order BVH
   // the FP32 candidates of an FP64 query (kCandidates per slot, kNoFace
   // padded), so the FP64 decisions need no search of their own; slot_of[qid]
-  // = kNoSlot for a query sent on before its candidates were known
+  // = kNoSlot for a query sent on before its candidates were known,
+  // kWideSlot for one whose candidates overflowed the list
   uint32_t *slot_of;
   int32_t *cand;
   unsigned long long slots;    // capacity of cand, in slots
@@ -553,7 +555,11 @@ __global__ void verify_fp32(BvhView b, const float *vn32, const MotionF *motions
   float keys[kCandidates];
   float best;
   const int n = candidate_faces(b, q, tau + e, e, faces, keys, best, status);
-  if (n > kCandidates) return to_fp64();
+  if (n > kCandidates) {  // the same search would overflow again: straight to the wide list
+    lists.mark[qid] = 1;
+    lists.slot_of[qid] = kWideSlot;
+    return;
+  }
   // from here on an FP64 row keeps its candidates: they hold every face at
   // the FP64 minimum (the window covers the FP32 error of the FP64 image)
   auto to_fp64_listed = [&]() {
@@ -691,6 +697,7 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
   const uint64_t i = uint64_t(b.order[rem % nv]);
   const uint64_t row = qid - rem % nv + i;
   const uint32_t slot = lists.slot_of[qid];
+  if (slot == kWideSlot) return;  // left marked for verify_rows_wide
   if (slot == kNoSlot) {  // no candidates yet: the search, on one lane
     if (sub) return;
     double d = 0;
