@@ -284,7 +284,8 @@ __device__ unsigned block_sum(unsigned v) {
 }
 
 // The pair kernels take one source per block and test its candidate runs
-// (source_runs) in srt, the samples in cell order.
+// (source_runs) in srt: the samples in cell order, or in kmin order when
+// there are no cells.
 struct Windows {
   const uint64_t *lo, *hi, *klo, *khi;
 };
