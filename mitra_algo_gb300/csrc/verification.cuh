@@ -305,6 +305,7 @@ struct Lbvh {
   float *vn = nullptr;             // 3 x nv, FP32 copy of the vertex normals
   float4 *fn = nullptr;            // nf: unit face normals from the FP64 corners, w = 1 (0: none)
   int32_t *order = nullptr;        // nv: the vertices in Morton order of their position
+  double *fn64 = nullptr;          // nf x 3: unit(cross(b - a, c - a)) of each face, FP64
   char *block = nullptr;           // owns every array above (cudaMalloc)
   float scale = 0;                 // largest vertex coordinate magnitude
 };

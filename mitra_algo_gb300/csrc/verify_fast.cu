@@ -233,6 +233,7 @@ struct BvhView {
   const float *box;
   const float4 *fn;  // nf: unit face normal from the FP64 corners, w = 1 (0: none usable)
   const int32_t *order;  // nv: query order of the vertices (Morton order of their position)
+  const double *fn64;    // nf x 3: the faces' FP64 unit normals of the normal test
 };
 
 __device__ __forceinline__ F3 vtx(const BvhView &b, int32_t v) {
@@ -622,6 +623,13 @@ __global__ void forward_errors(Surface s, const ClusterMotion *motions, RowLists
   err[c * nv + i] = dmin;
 }
 
+// The reference's normal test (verification.cpp:70-73, normal_agrees) with
+// the face's unit normal from the per-mesh table: the same FP64 values.
+__device__ __forceinline__ bool normal_agrees_t(const BvhView &b, int32_t f, const M3 &r, D3 ni) {
+  const D3 fnorm{b.fn64[3 * uint64_t(f)], b.fn64[3 * uint64_t(f) + 1], b.fn64[3 * uint64_t(f) + 2]};
+  return !(dot(mul(r, ni), fnorm) < 0.5);
+}
+
 // One query of the reference's verification, decided with the FP32
 // candidates and FP64 rechecks.  Returns 1 (supports; `d2` = the reference's
 // FP64 squared distance), 0 (does not), 3 (the faces at the minimum, listed
@@ -666,7 +674,7 @@ __device__ int hybrid_query(const BvhView &b, const Surface &s, const double *vn
   for (int j = 0; j < n; ++j) {
     if (dist[j] != dmin) continue;
     tied[t++] = faces[j];
-    if (normal_agrees(s, faces[j], r, ni)) ++agree;
+    if (normal_agrees_t(b, faces[j], r, ni)) ++agree;
     else ++disagree;
   }
   d2 = dmin;
@@ -711,7 +719,7 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
       int32_t first = tied[0];
       for (int x = 1; x < kCandidates && tied[x] >= 0; ++x)
         first = first_in_reference_order(t, q, first, tied[x]);
-      v = normal_agrees(s, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
+      v = normal_agrees_t(b, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
     }
     flags[row] = v == 1;
     if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
@@ -745,7 +753,7 @@ __global__ void verify_rows_fp64(BvhView b, Surface s, RefBvh t, const double *v
       int32_t first = -1;  // this lane's face at the minimum the reference visits first
       for (int h = 0; h < 2; ++h)
         if (f[h] >= 0 && d[h] == dmin) {
-          ok[h] = normal_agrees(s, f[h], r, ni);
+          ok[h] = normal_agrees_t(b, f[h], r, ni);
           if (ok[h]) ++agree;
           else ++disagree;
           first = first < 0 ? f[h] : first_in_reference_order(t, q, first, f[h]);
@@ -812,7 +820,7 @@ __global__ void verify_rows_wide(BvhView b, Surface s, RefBvh t, const double *v
     int32_t first = tied[0];
     for (int x = 1; x < kWideCandidates && tied[x] >= 0; ++x)
       first = first_in_reference_order(t, q, first, tied[x]);
-    v = normal_agrees(s, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
+    v = normal_agrees_t(b, first, r, D3{vn[i], vn[nv + i], vn[2 * nv + i]}) ? 1 : 0;
   }
   flags[row] = v == 1;
   if (!inverse) err[c * nv + i] = v == 1 ? d : 0.0;
@@ -1148,7 +1156,7 @@ __global__ void count_roots(int32_t *parent_all, uint64_t nv, uint64_t sets, uns
 // unit() (a cross product of norm <= 1e-14 becomes the zero vector, which
 // fails the test): those faces leave their rows to the FP64 decisions.
 __global__ void lbvh_face_normals(const double *xyz, uint64_t nv, const int32_t *faces,
-                                  uint64_t nf, float4 *fn) {
+                                  uint64_t nf, float4 *fn, double *fn64) {
   const uint64_t f = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (f >= nf) return;
   D3 c[3];
@@ -1157,12 +1165,13 @@ __global__ void lbvh_face_normals(const double *xyz, uint64_t nv, const int32_t 
     c[k] = D3{xyz[v], xyz[nv + v], xyz[2 * nv + v]};
   }
   const D3 ab = c[1] - c[0], ac = c[2] - c[0], n = cross(ab, ac);
+  const D3 u = unit(n);  // the normal test's expression (normal_agrees), once per face
+  fn64[3 * f] = u.x, fn64[3 * f + 1] = u.y, fn64[3 * f + 2] = u.z;
   const double n2 = dot(n, n), l2 = dot(ab, ab) * dot(ac, ac);
   if (!(n2 > 1e-12 * l2) || !(n2 > 4e-28)) {
     fn[f] = make_float4(0.f, 0.f, 0.f, 0.f);
     return;
   }
-  const D3 u = unit(n);
   fn[f] = make_float4(float(u.x), float(u.y), float(u.z), 1.f);
 }
 
@@ -1175,19 +1184,20 @@ Lbvh lbvh_build(Call &call, const double *xyz, const double *vn, uint64_t nv,
   const uint64_t ni = nf - 1;
   auto pad = [](uint64_t x) { return (x + 255) & ~uint64_t(255); };
   const uint64_t s_xyz = pad(12 * nv), s_child = pad(8 * ni + 8), s_box = pad(48 * ni + 48);
-  const uint64_t s_fn = pad(16 * nf), s_order = pad(4 * nv);
-  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box + s_fn + s_order));
+  const uint64_t s_fn = pad(16 * nf), s_order = pad(4 * nv), s_fn64 = pad(24 * nf);
+  SYM_CUDA(cudaMalloc(&b.block, 2 * s_xyz + s_child + s_box + s_fn + s_order + s_fn64));
   b.xyz = reinterpret_cast<float *>(b.block);
   b.child = reinterpret_cast<int32_t *>(b.block + s_xyz);
   b.box = reinterpret_cast<float *>(b.block + s_xyz + s_child);
   b.vn = reinterpret_cast<float *>(b.block + s_xyz + s_child + s_box);
   b.fn = reinterpret_cast<float4 *>(b.block + 2 * s_xyz + s_child + s_box);
   b.order = reinterpret_cast<int32_t *>(b.block + 2 * s_xyz + s_child + s_box + s_fn);
+  b.fn64 = reinterpret_cast<double *>(b.block + 2 * s_xyz + s_child + s_box + s_fn + s_order);
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(xyz, nv, b.xyz);
   check_launch();
   lbvh_vertices<<<blocks_for(3 * nv), kThreads, 0, st>>>(vn, nv, b.vn);
   check_launch();
-  lbvh_face_normals<<<blocks_for(nf), kThreads, 0, st>>>(xyz, nv, faces, nf, b.fn);
+  lbvh_face_normals<<<blocks_for(nf), kThreads, 0, st>>>(xyz, nv, faces, nf, b.fn, b.fn64);
   check_launch();
   // the mesh box, for the Morton quantisation
   std::vector<float> h(3 * nv);
@@ -1331,7 +1341,8 @@ uint64_t exact_flags(Call &call, const ResidentSurface &m, const ClusterMotion *
   lists.counts = call.alloc<unsigned long long>(4);
   uint64_t *listed = call.alloc<uint64_t>(2);
   SYM_CUDA(cudaMemsetAsync(lists.counts, 0, 32, st));
-  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn, bvh.order};
+  const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn, bvh.order,
+                     bvh.fn64};
   Surface s{m.xyz, nv, m.faces, m.nf, nullptr, nullptr};
   verify_fp32<<<blocks_for(rows), kThreads, 0, st>>>(view, bvh.vn, dmf, nc, float(tau), bvh.scale,
                                                       flags, err, lists, call.status());
@@ -1403,7 +1414,8 @@ void verification_fast(Call &call, const ResidentSurface &m, sym_cluster_record 
   ClusterMotion *dm = call.upload(motions.data(), nc);
   if (refine > 0 && m.nf) {
     const Lbvh &bvh = *m.lbvh;
-    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn, bvh.order};
+    const BvhView view{bvh.nv, bvh.nf, bvh.faces, bvh.xyz, bvh.child, bvh.box, bvh.fn, bvh.order,
+                     bvh.fn64};
     refine_motions(call, view, m.xyz, m.vn, m.w, dm, nc, tau, refine, origin);
     call.d2h(motions.data(), dm, nc * sizeof(ClusterMotion));
     call.check_status("transform refinement");
