@@ -136,6 +136,39 @@ def test_noisy_torus_with_slivers(gpu):
     assert max(got.coverage) > 0.5
 
 
+def fan_pair_mesh(valences, shift=5.0, gap=4.0):
+    """For each valence N, two identical cones: an apex with N triangles to a
+    rim whose heights alternate, the second cone `shift` along x from the
+    first; cones of different N lie `gap` apart along y."""
+    from mitra_algo_gb300.types import Mesh
+    verts, faces = [], []
+    for row, n in enumerate(valences):
+        for copy in range(2):
+            base = len(verts)
+            o = np.array([shift * copy, gap * row, 0.0])
+            verts.append(o + [0.0, 0.0, 0.3])
+            for k in range(n):
+                a = 2 * np.pi * k / n
+                verts.append(o + [np.cos(a), np.sin(a), 0.25 if k % 2 else -0.25])
+            for k in range(n):
+                faces.append([base, base + 1 + k, base + 1 + (k + 1) % n])
+    return Mesh(np.array(verts).T.copy(), np.array(faces, np.int32).T.copy())
+
+
+def test_high_valence_fans(gpu):
+    """Images landing exactly on a vertex of 24, 40 or 80 faces: every face
+    at the FP64 minimum is a candidate, more than the 16-entry lists hold,
+    so the queries take the 64-entry list (24, 40) or the reference-order
+    search (80); the faces' normals alternate, so the ties are decided by
+    the reference's visiting order."""
+    mesh = fan_pair_mesh((24, 40, 80))
+    o = Options(verify_threshold=0.01)
+    p = prepare(mesh, o)
+    got, undecided = compare(gpu, p, o, records(rigid=[(np.eye(3), (5.0, 0.0, 0.0)),
+                                                       (np.eye(3), (5.0, 1e-9, 0.0))]))
+    assert got.coverage[0] > 0 and undecided > 0
+
+
 def test_empty_cluster_list(gpu):
     mesh = motif_sphere(level=3, bumps=4, folds=3, partial_shift=0.3, noise=0.0, seed=1)
     o = Options()
